@@ -1,0 +1,203 @@
+/*
+ * tcp_gpu.h -- C ABI of libtcpgpu.so, the GB300 (sm_103a) implementation of
+ * the TCP_allpair force-and-integrate step.
+ *
+ * The reference drives this path through Fortran subroutines with implicit
+ * interfaces and derived-type arguments (force.f90, vverlet.f90, init.f90).
+ * Every entry point below replaces one of them; the comment above each
+ * declaration names the routine and its file:line.  A Fortran caller binds
+ * these with ISO_C_BINDING (fortran/tcp_gpu_mod.f90 in the package); other
+ * callers use the same plain C types: no C++ and no CUDA types cross this
+ * boundary.
+ *
+ * State model.  A tcp_ctx owns one system on one GPU: device-resident SoA
+ * FP64 positions, velocities and forces (plus the 32-bit fixed-point position
+ * copy of the FP32 pair kernel), the SPME meshes and cuFFT plans, the RDF/VDF
+ * histograms and a CUDA stream.  Host arrays are authoritative only after
+ * tcp_download().  Particles are ordered as in the reference: species 0
+ * (electrons, "qel") first, then species 1 (ions, "qion").
+ *
+ * Units are the reference's (data.f90:21-24): Angstrom, eV, amu, time in
+ * units of 10.18 fs, eps = 14.399644154020082 eV*A.
+ *
+ * Errors.  Every function returns 0 (TCP_OK) or a TCP_ERR_* code; the
+ * reference STOPs instead (force.f90:19-22, main.f90:222-225).
+ * tcp_last_error() gives a one-line message for the calling thread.
+ * Contexts are not re-entrant: one host thread per context at a time.
+ */
+#ifndef TCP_GPU_H
+#define TCP_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define TCP_OK 0
+#define TCP_ERR_BAD_PARAM 1     /* invalid argument or parameter combination   */
+#define TCP_ERR_CUTOFF 2        /* rc > min(box)/2, force.f90:18-22            */
+#define TCP_ERR_CUDA 3          /* CUDA runtime error (message has details)    */
+#define TCP_ERR_CUFFT 4         /* cuFFT plan or execution failure             */
+#define TCP_ERR_TIMEOUT 5       /* a bounded device-side wait gave up          */
+#define TCP_ERR_NO_DEVICE 6     /* no usable sm_103 device                     */
+#define TCP_ERR_STATE 7         /* call order (e.g. force before ewald_self)   */
+#define TCP_ERR_NOMEM 8         /* device allocation failed                    */
+
+/* ---- enumerations ------------------------------------------------------ */
+#define TCP_PREC_FP64 0         /* plain FP64 pair kernel (the drop-in)        */
+#define TCP_PREC_FP32C 1        /* FP32 pair arithmetic, compensated sums      */
+
+#define TCP_EI_DEUTSCH 0        /* reference e-i term (erfc(ar)-exp(-r/rs))/r, force.f90:135-139 */
+#define TCP_EI_KELBG 1          /* Kelbg e-i potential with length lambda_ei   */
+#define TCP_EI_COULOMB 2        /* bare Coulomb for every pair                 */
+
+#define TCP_THERMO_NOTEMP 0     /* vverlet.f90:174-223 */
+#define TCP_THERMO_ISOKIN 1     /* vverlet.f90:301-372 */
+#define TCP_THERMO_BEREND 2     /* vverlet.f90:227-298 */
+#define TCP_THERMO_STOCH 3      /* vverlet.f90:9-127 (counter-based RNG)       */
+
+#define TCP_RECIP_NONE 0        /* real-space sum only                         */
+#define TCP_RECIP_SPME 1        /* smooth PME, force.f90:652-929               */
+#define TCP_RECIP_EWALD 2       /* plain Ewald k-space sum, |n|^2 <= ewald_nmax2 */
+
+/* tcp_set_flags bits */
+#define TCP_FLAG_RDF 1u         /* accumulate RDF histograms in the pair sum   */
+#define TCP_FLAG_VDF 2u         /* accumulate VDF histograms in the 2nd kick   */
+#define TCP_FLAG_ENERGY 4u      /* compute Ur/Um (default on)                  */
+
+/* Parameters: the fields of TYPE PM (data.f90:68-74), the histogram
+ * spacings of TYPE NM (data.f90:99) and the GPU build's own knobs. */
+typedef struct tcp_params {
+    double xm[2];           /* masses [amu] (PM%xm)                          */
+    double q[2];            /* charges [e] (PM%q)                            */
+    double tau;             /* Berendsen time constant (PM%tau)              */
+    double alpha_lgv;       /* Langevin damping (PM%alpha)                   */
+    double a;               /* Ewald alpha; <= 0 selects 3.1/rc (force.f90:23) */
+    double box[3];          /* box lengths [A] (PM%box)                      */
+    double Te, Ti;          /* target temperatures [eV]                      */
+    double rs;              /* Deutsch length [A] (PM%rs)                    */
+    double rc;              /* real-space cut-off [A] (PM%rc)                */
+    int K[3];               /* SPME mesh (PM%K)                              */
+    int order;              /* B-spline order, 4 (reference) .. 8            */
+    double dx_ee, dx_ei, dx_ii;  /* RDF bin widths (NM%dx_*)                 */
+    double dv_e, dv_i;      /* VDF bin widths (NM%dv_*, main.f90:286-287)    */
+    int ei_model;           /* TCP_EI_*                                      */
+    double lambda_ei;       /* Kelbg length [A]                              */
+    double charge_scale;    /* q -> s q in every energy and force (1 = reference) */
+    int precision;          /* TCP_PREC_*                                    */
+    int reciprocal;         /* TCP_RECIP_*                                   */
+    int ewald_nmax2;        /* plain Ewald: |n|^2 bound                      */
+    int thermo;             /* TCP_THERMO_*                                  */
+    int thermo_period;      /* apply ISOKIN/BEREND every n-th step (1 = reference) */
+    uint64_t seed;          /* STOCH random stream                           */
+} tcp_params;
+
+/* Energies of the last force evaluation / step (TYPE ST, data.f90:89-92). */
+typedef struct tcp_energies {
+    double Ur;              /* real-space energy WITHOUT eps (sys%Ur)        */
+    double Uo;              /* self energy WITHOUT eps (sys%Uo)              */
+    double Um;              /* reciprocal energy WITH eps (sys%Um)           */
+    double Epot;            /* (Ur + Uo) * eps, main.f90:138                 */
+    double mv2el, mv2ion;   /* sum m v^2 per species (sys%mv2el/mv2ion)      */
+} tcp_energies;
+
+typedef struct tcp_ctx tcp_ctx;
+
+/* ---- lifecycle ------------------------------------------------------- */
+/* Allocates the device state for nel electrons + nion ions on `device`.
+ * Replaces the ALLOCATE of main.f90:45 / :335 for the GPU-resident arrays. */
+int tcp_create(const tcp_params *p, int nel, int nion, int device, tcp_ctx **out);
+int tcp_destroy(tcp_ctx *ctx);
+const char *tcp_last_error(void);
+const char *tcp_status_string(int code);
+/* Library version and the compute capability it was built for (103). */
+int tcp_version(int *major, int *minor, int *arch);
+
+/* EWALD_SELF(NS,param,sys,PSI,COMM), force.f90:4-49: checks rc <= L/2,
+ * sets alpha (3.1/rc unless p->a > 0) and rc^2, fills the influence mesh and
+ * returns Uo (no eps).  Must precede every force call. */
+int tcp_ewald_self(tcp_ctx *ctx, double *alpha_out, double *Uo_out);
+
+/* Updates the parameters that may change between steps (temperatures,
+ * thermostat, tau, charge scale, e-i length).  Box, mesh, order, counts and
+ * precision are fixed at tcp_create. */
+int tcp_set_params(tcp_ctx *ctx, const tcp_params *p);
+int tcp_set_flags(tcp_ctx *ctx, unsigned flags);
+
+/* ---- host <-> device ------------------------------------------------- */
+/* Copy one species' records from host memory.  xx, xv, ff point at the first
+ * record's xx(1), xv(1), ff(1) of a PT array (data.f90:32-35); stride_bytes
+ * is the distance between consecutive records (104 for gfortran/ifort), so a
+ * Fortran caller passes C_LOC(qel(1)%xx) and C_LOC(qel(2)) - C_LOC(qel(1)).
+ * A NULL pointer skips that field.  species: 0 = qel, 1 = qion. */
+int tcp_upload(tcp_ctx *ctx, int species, const double *xx, const double *xv,
+               const double *ff, long stride_bytes);
+int tcp_download(tcp_ctx *ctx, int species, double *xx, double *xv, double *ff,
+                 long stride_bytes);
+/* Plain (N,3) row-major arrays for all particles (electrons then ions);
+ * NULL skips a field.  frec: the reciprocal (pme) forces of the last SPME call. */
+int tcp_upload_soa(tcp_ctx *ctx, const double *x, const double *v, const double *f);
+int tcp_download_soa(tcp_ctx *ctx, double *x, double *v, double *f, double *frec);
+
+/* ---- the force evaluation (main.f90:100-141) --------------------------- */
+/* Force_direct_self + Force_direct_ext + Force_direct_sum for the whole
+ * system (force.f90:52-372, main.f90:105-130): f is overwritten with the
+ * real-space forces, *Ur (no eps) returned, RDF accumulated if enabled. */
+int tcp_force_direct(tcp_ctx *ctx, double *Ur);
+/* Force_SPME4(NS,param,sys,COMM,PSI,gsend,pme), force.f90:652-929: the
+ * reciprocal forces (kept on the device, the pme array) and *Um (with eps).
+ * With reciprocal == TCP_RECIP_EWALD the plain Ewald sum is used instead. */
+int tcp_force_spme(tcp_ctx *ctx, double *Um);
+/* SPME_SUM(NS,qel,qion,sys,COMM,pme,grec), force.f90:932-969: f += pme. */
+int tcp_spme_sum(tcp_ctx *ctx);
+/* REMOVE_RIGIDMTN(NS,qel,qion,COMM), force.f90:974-1007: f -= sum(f)/N. */
+int tcp_remove_rigidmtn(tcp_ctx *ctx);
+/* The four calls above in the order of main.f90:100-141, plus
+ * Epot = (Ur+Uo)*eps (main.f90:138). */
+int tcp_force(tcp_ctx *ctx, tcp_energies *e);
+
+/* ---- integration (vverlet.f90) ----------------------------------------- */
+/* VVerletNotemp1(NS,qel,qion,param,dt,gsend), vverlet.f90:132-171 (also the
+ * first half of ISOKIN/BEREND, main.f90:88-92); VVerletStoch1
+ * (vverlet.f90:9-59) when thermo == TCP_THERMO_STOCH. */
+int tcp_vverlet1(tcp_ctx *ctx, double dt);
+/* VVerletNotemp2 / VVerletIsokin2 / VVerletBerend2 / VVerletStoch2
+ * (vverlet.f90:174-223, 301-372, 227-298, 62-127) selected by thermo;
+ * returns sum m v^2 per species. */
+int tcp_vverlet2(tcp_ctx *ctx, double dt, double *mv2el, double *mv2ion);
+/* Finit(...), init.f90:152-239: forces at x - dt v (the reference's quirk),
+ * positions restored. */
+int tcp_finit(tcp_ctx *ctx, double dt, tcp_energies *e);
+
+/* ---- the step (main.f90:81-153) ---------------------------------------- */
+/* nsteps MD steps (vverlet1, SPME, direct sum, SPME_SUM, Epot, net-force
+ * removal, vverlet2+thermostat), captured once as a CUDA graph and replayed.
+ * e receives the energies of the last step (NULL: not read back). */
+int tcp_md_steps(tcp_ctx *ctx, double dt, int nsteps, tcp_energies *e);
+/* Energies of the most recent evaluation without launching anything. */
+int tcp_energies_get(tcp_ctx *ctx, tcp_energies *e);
+
+/* ---- histograms (NS%RDF_*, NS%VDF_*, data.f90:100-101) ----------------- */
+/* rdf: 3*(Ndist+1) doubles ee|ei|ii; vdf: 2*(Ndist+1) doubles e|i.  Counts
+ * follow the reference (+2 per pair, +1 per particle).  reset != 0 zeroes
+ * the device copies afterwards (DUMP does so, result.f90:264-268). */
+int tcp_histograms(tcp_ctx *ctx, double *rdf, double *vdf, int reset);
+
+/* ---- measurement hooks ---------------------------------------------------- */
+/* Runs `reps` launches of one component on the context's stream and returns
+ * the mean device time per launch from CUDA events recorded on that stream.
+ * which: 0 = real-space pair kernel, 1 = SPME chain, 2 = full md step. */
+int tcp_time_component(tcp_ctx *ctx, int which, int reps, double dt, double *ms_per_launch);
+/* Kernel launches issued by the context so far (all kernels of this library). */
+int tcp_launch_count(tcp_ctx *ctx, long long *count);
+/* Measured FP32 FFMA issue rate of the device: a calibration kernel of
+ * dependent-chain-free FFMAs, returned in 1e12 FFMA/s. */
+int tcp_fp32_peak(int device, double *tffma_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

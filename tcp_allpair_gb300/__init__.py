@@ -1,0 +1,216 @@
+"""GB300-native force-and-integrate step of the TCP_allpair two-component
+plasma code, behind the C ABI of libtcpgpu.so (include/tcp_gpu.h).
+
+`Context` mirrors the reference's step routines one to one (force.f90,
+vverlet.f90, init.f90): the method names are the Fortran subroutine names,
+the arrays are the PT records of data.f90:32-35 (numpy structured arrays,
+`system.PT_DTYPE`) and errors raise `TcpError` where the reference STOPs.
+Compute always runs in libtcpgpu.so on the GPU; importing this package
+without the built library, or calling it without a GB300, raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._abi import (EI_COULOMB, EI_DEUTSCH, EI_KELBG, FLAG_ENERGY, FLAG_RDF, FLAG_VDF, PREC_FP32C,
+                   PREC_FP64, RECIP_EWALD, RECIP_NONE, RECIP_SPME, THERMO_BEREND, THERMO_ISOKIN,
+                   THERMO_NOTEMP, THERMO_STOCH, TcpEnergies, TcpError, TcpParams)
+from .system import EPS, NDIST, PT_DTYPE, System, make_config_system, make_system
+
+__all__ = ["Context", "TcpParams", "TcpEnergies", "TcpError", "params_for", "System", "make_system",
+           "make_config_system", "PT_DTYPE", "EPS", "NDIST"]
+
+_THERMO = {"notemp": THERMO_NOTEMP, "isokin": THERMO_ISOKIN, "berend": THERMO_BEREND, "stoch": THERMO_STOCH}
+_EI = {"deutsch": EI_DEUTSCH, "kelbg": EI_KELBG, "coulomb": EI_COULOMB}
+_RECIP = {"none": RECIP_NONE, "spme": RECIP_SPME, "ewald": RECIP_EWALD}
+_PREC = {"fp64": PREC_FP64, "fp32c": PREC_FP32C}
+
+
+def params_for(sys: System, precision="fp32c", ei="kelbg", recip="spme", thermo="notemp",
+               thermo_period=1, nmax2=64, tau=1.0, alpha_lgv=0.0, seed=0, charge_scale=1.0,
+               rdf_dx=None) -> TcpParams:
+    """TcpParams for a generated system (reference units)."""
+    p = TcpParams()
+    p.xm[0], p.xm[1] = sys.xm
+    p.q[0], p.q[1] = sys.q
+    p.tau, p.alpha_lgv = tau, alpha_lgv
+    p.a = sys.alpha
+    for d in range(3):
+        p.box[d] = sys.box
+        p.K[d] = sys.K
+    p.Te, p.Ti = sys.Te, sys.Ti
+    p.rs = sys.lambda_ei
+    p.rc = sys.rc
+    p.order = sys.order
+    dx = rdf_dx if rdf_dx is not None else sys.rc / NDIST
+    p.dx_ee = p.dx_ei = p.dx_ii = dx
+    p.dv_e = sys.Te * 4.0 / NDIST          # main.f90:286-287
+    p.dv_i = sys.Ti * 4.0 / NDIST
+    p.ei_model = _EI[ei]
+    p.lambda_ei = sys.lambda_ei
+    p.charge_scale = charge_scale
+    p.precision = _PREC[precision]
+    p.reciprocal = _RECIP[recip]
+    p.ewald_nmax2 = nmax2
+    p.thermo = _THERMO[thermo]
+    p.thermo_period = thermo_period
+    p.seed = seed
+    return p
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """One system resident on one GB300 (a tcp_ctx of the C ABI)."""
+
+    def __init__(self, params: TcpParams, nel: int, nion: int, device: int = 0):
+        self.lib = _abi.load()
+        self.params = params
+        self.nel, self.nion = nel, nion
+        h = C.c_void_p()
+        _abi.check(self.lib, self.lib.tcp_create(C.byref(params), nel, nion, device, C.byref(h)), "tcp_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.tcp_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _chk(self, code, where):
+        _abi.check(self.lib, code, where)
+
+    @property
+    def n(self):
+        return self.nel + self.nion
+
+    # ---- reference routine names --------------------------------------------
+    def EWALD_SELF(self):
+        """force.f90:4-49 -> (alpha, Uo without eps)."""
+        a, uo = C.c_double(), C.c_double()
+        self._chk(self.lib.tcp_ewald_self(self.h, C.byref(a), C.byref(uo)), "tcp_ewald_self")
+        return a.value, uo.value
+
+    def Force_direct_self(self):
+        """force.f90:52-372 over the whole system -> Ur (no eps); f overwritten."""
+        u = C.c_double()
+        self._chk(self.lib.tcp_force_direct(self.h, C.byref(u)), "tcp_force_direct")
+        return u.value
+
+    def Force_SPME4(self):
+        """force.f90:652-929 -> Um (with eps); reciprocal forces stay on the device."""
+        u = C.c_double()
+        self._chk(self.lib.tcp_force_spme(self.h, C.byref(u)), "tcp_force_spme")
+        return u.value
+
+    def SPME_SUM(self):
+        self._chk(self.lib.tcp_spme_sum(self.h), "tcp_spme_sum")
+
+    def REMOVE_RIGIDMTN(self):
+        self._chk(self.lib.tcp_remove_rigidmtn(self.h), "tcp_remove_rigidmtn")
+
+    def VVerlet1(self, dt):
+        """VVerletNotemp1 / VVerletStoch1 (vverlet.f90:132-171 / 9-59)."""
+        self._chk(self.lib.tcp_vverlet1(self.h, dt), "tcp_vverlet1")
+
+    def VVerlet2(self, dt):
+        """VVerletNotemp2 / Isokin2 / Berend2 / Stoch2 -> (mv2el, mv2ion)."""
+        a, b = C.c_double(), C.c_double()
+        self._chk(self.lib.tcp_vverlet2(self.h, dt, C.byref(a), C.byref(b)), "tcp_vverlet2")
+        return a.value, b.value
+
+    def Finit(self, dt):
+        e = TcpEnergies()
+        self._chk(self.lib.tcp_finit(self.h, dt, C.byref(e)), "tcp_finit")
+        return e.as_dict()
+
+    # ---- composite -------------------------------------------------------------
+    def force(self):
+        e = TcpEnergies()
+        self._chk(self.lib.tcp_force(self.h, C.byref(e)), "tcp_force")
+        return e.as_dict()
+
+    def md_steps(self, dt, nsteps):
+        e = TcpEnergies()
+        self._chk(self.lib.tcp_md_steps(self.h, dt, nsteps, C.byref(e)), "tcp_md_steps")
+        return e.as_dict()
+
+    def set_flags(self, flags):
+        self._chk(self.lib.tcp_set_flags(self.h, flags), "tcp_set_flags")
+
+    def set_params(self, params: TcpParams):
+        self._chk(self.lib.tcp_set_params(self.h, C.byref(params)), "tcp_set_params")
+        self.params = params
+
+    # ---- transfers ---------------------------------------------------------------
+    def upload_pt(self, qel: np.ndarray, qion: np.ndarray, fields=("xx", "xv", "ff")):
+        """Copy PT records (data.f90:32-35) to the device."""
+        for sp, arr in ((0, qel), (1, qion)):
+            if len(arr) == 0:
+                continue
+            base = arr.ctypes.data
+            offs = {k: arr.dtype.fields[k][1] for k in ("xx", "xv", "ff")}
+            ptr = [C.c_void_p(base + offs[k]) if k in fields else None for k in ("xx", "xv", "ff")]
+            self._chk(self.lib.tcp_upload(self.h, sp, *ptr, arr.strides[0]), "tcp_upload")
+
+    def download_pt(self, qel: np.ndarray, qion: np.ndarray, fields=("xx", "xv", "ff")):
+        for sp, arr in ((0, qel), (1, qion)):
+            if len(arr) == 0:
+                continue
+            base = arr.ctypes.data
+            offs = {k: arr.dtype.fields[k][1] for k in ("xx", "xv", "ff")}
+            ptr = [C.c_void_p(base + offs[k]) if k in fields else None for k in ("xx", "xv", "ff")]
+            self._chk(self.lib.tcp_download(self.h, sp, *ptr, arr.strides[0]), "tcp_download")
+
+    def upload(self, x=None, v=None, f=None):
+        """(N,3) float64 arrays, electrons first."""
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (x, v, f)]
+        for a in arrs:
+            if a is not None and a.shape != (self.n, 3):
+                raise ValueError(f"expected shape ({self.n}, 3), got {a.shape}")
+        self._chk(self.lib.tcp_upload_soa(self.h, *[None if a is None else _ptr(a) for a in arrs]),
+                  "tcp_upload_soa")
+
+    def download(self, x=True, v=True, f=True, frec=False):
+        out = [np.empty((self.n, 3)) if w else None for w in (x, v, f, frec)]
+        self._chk(self.lib.tcp_download_soa(self.h, *[None if a is None else _ptr(a) for a in out]),
+                  "tcp_download_soa")
+        return out
+
+    def histograms(self, reset=False):
+        rdf = np.zeros(3 * (NDIST + 1))
+        vdf = np.zeros(2 * (NDIST + 1))
+        self._chk(self.lib.tcp_histograms(self.h, rdf.ctypes.data_as(C.POINTER(C.c_double)),
+                                          vdf.ctypes.data_as(C.POINTER(C.c_double)), int(reset)),
+                  "tcp_histograms")
+        return rdf.reshape(3, NDIST + 1), vdf.reshape(2, NDIST + 1)
+
+    def time_component(self, which, reps, dt=0.0):
+        ms = C.c_double()
+        self._chk(self.lib.tcp_time_component(self.h, which, reps, dt, C.byref(ms)), "tcp_time_component")
+        return ms.value
+
+    def launch_count(self):
+        n = C.c_longlong()
+        self._chk(self.lib.tcp_launch_count(self.h, C.byref(n)), "tcp_launch_count")
+        return n.value
+
+
+def fp32_peak(device: int = 0) -> float:
+    """Measured FP32 FFMA rate of the device in 1e12 FFMA/s."""
+    lib = _abi.load()
+    t = C.c_double()
+    _abi.check(lib, lib.tcp_fp32_peak(device, C.byref(t)), "tcp_fp32_peak")
+    return t.value

@@ -1,0 +1,624 @@
+// ctx.cu -- the C ABI of libtcpgpu.so (include/tcp_gpu.h): context
+// lifecycle, host transfers, the reference-named step routines and the CUDA
+// graph of one MD step.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "tcp_internal.h"
+
+namespace tcp {
+
+static thread_local std::string g_err;
+
+int set_error(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_check(cudaError_t e, const char *what) {
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? TCP_ERR_NOMEM : TCP_ERR_CUDA;
+}
+
+static int validate(const tcp_params *p, int nel, int nion) {
+    if (!p) return set_error(TCP_ERR_BAD_PARAM, "params is NULL");
+    if (nel < 0 || nion < 0 || nel + nion < 2) return set_error(TCP_ERR_BAD_PARAM, "need nel, nion >= 0 and nel+nion >= 2");
+    for (int d = 0; d < 3; ++d)
+        if (!(p->box[d] > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "box lengths must be positive");
+    if (!(p->rc > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "rc must be positive");
+    if (!(p->xm[0] > 0.0) || !(p->xm[1] > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "masses must be positive");
+    if (p->precision != TCP_PREC_FP64 && p->precision != TCP_PREC_FP32C)
+        return set_error(TCP_ERR_BAD_PARAM, "unknown precision");
+    if (p->ei_model < TCP_EI_DEUTSCH || p->ei_model > TCP_EI_COULOMB) return set_error(TCP_ERR_BAD_PARAM, "unknown ei_model");
+    if (p->ei_model == TCP_EI_DEUTSCH && !(p->rs > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "Deutsch model needs rs > 0");
+    if (p->ei_model == TCP_EI_KELBG && !(p->lambda_ei > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "Kelbg model needs lambda_ei > 0");
+    if (p->reciprocal < TCP_RECIP_NONE || p->reciprocal > TCP_RECIP_EWALD) return set_error(TCP_ERR_BAD_PARAM, "unknown reciprocal");
+    if (p->reciprocal == TCP_RECIP_SPME) {
+        if (p->order < 4 || p->order > kMaxOrder) return set_error(TCP_ERR_BAD_PARAM, "SPME order must be in 4..8");
+        for (int d = 0; d < 3; ++d)
+            if (p->K[d] < p->order) return set_error(TCP_ERR_BAD_PARAM, "SPME mesh must be >= order in every dimension");
+    }
+    if (p->reciprocal == TCP_RECIP_EWALD && p->ewald_nmax2 < 0) return set_error(TCP_ERR_BAD_PARAM, "ewald_nmax2 < 0");
+    if (p->thermo < TCP_THERMO_NOTEMP || p->thermo > TCP_THERMO_STOCH) return set_error(TCP_ERR_BAD_PARAM, "unknown thermo");
+    if (p->thermo == TCP_THERMO_BEREND && !(p->tau > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "Berendsen needs tau > 0");
+    return TCP_OK;
+}
+
+static void normalise(tcp_params *p) {
+    if (p->charge_scale == 0.0) p->charge_scale = 1.0;
+    if (p->thermo_period <= 0) p->thermo_period = 1;
+}
+
+static int sync_scalars(tcp_ctx *c) {
+    TCP_CUDA(cudaMemcpyAsync(c->h_scal, c->scal, sizeof(double) * kScalCount, cudaMemcpyDeviceToHost, c->stream));
+    TCP_CUDA(cudaMemcpyAsync(c->h_scal + kScalCount, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    const unsigned st = *reinterpret_cast<unsigned *>(c->h_scal + kScalCount);
+    if (st & kStatusTmaTimeout) {
+        cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream);
+        return set_error(TCP_ERR_TIMEOUT, "a pair-kernel tile wait exceeded its bound");
+    }
+    return TCP_OK;
+}
+
+static void invalidate_graph(tcp_ctx *c) {
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+}
+
+static int ensure_stage(tcp_ctx *c, size_t bytes) {
+    if (c->d_stage_bytes < bytes) {
+        cudaFree(c->d_stage);
+        c->d_stage = nullptr;
+        c->d_stage_bytes = 0;
+        TCP_CUDA(cudaMalloc(&c->d_stage, bytes));
+        c->d_stage_bytes = bytes;
+    }
+    if (c->h_stage_bytes < bytes) {
+        cudaFreeHost(c->h_stage);
+        c->h_stage = nullptr;
+        c->h_stage_bytes = 0;
+        TCP_CUDA(cudaMallocHost(&c->h_stage, bytes));
+        c->h_stage_bytes = bytes;
+    }
+    return TCP_OK;
+}
+
+static bool energy_on(const tcp_ctx *c) { return (c->flags & TCP_FLAG_ENERGY) != 0; }
+
+static int recip_launch(tcp_ctx *c) {
+    if (c->p.reciprocal == TCP_RECIP_SPME) return launch_spme(c, energy_on(c));
+    if (c->p.reciprocal == TCP_RECIP_EWALD) return launch_ewald(c, energy_on(c));
+    return TCP_OK;
+}
+
+// Force evaluation of main.f90:100-141 without host synchronisation.
+static int force_chain(tcp_ctx *c, bool remove_net) {
+    int rc;
+    if ((rc = recip_launch(c))) return rc;
+    if ((rc = launch_pair(c, energy_on(c), (c->flags & TCP_FLAG_RDF) != 0))) return rc;
+    if ((rc = launch_force_finalize(c, c->p.reciprocal != TCP_RECIP_NONE))) return rc;
+    if (remove_net && (rc = launch_remove_rigid(c))) return rc;
+    if (energy_on(c) && (rc = launch_reduce(c, kRedUr, 0))) return rc;
+    return TCP_OK;
+}
+
+static void fill_energies(tcp_ctx *c, tcp_energies *e) {
+    c->last.Ur = c->h_scal[kScalUr];
+    c->last.Um = c->p.reciprocal == TCP_RECIP_NONE ? 0.0 : c->h_scal[kScalUm];
+    c->last.Uo = c->Uo;
+    c->last.Epot = (c->last.Ur + c->Uo) * kEps;      // main.f90:138
+    if (e) *e = c->last;
+}
+
+static bool thermostat_due(const tcp_ctx *c) {
+    return ((c->step_index + 1) % c->p.thermo_period) == 0;
+}
+
+// One MD step (main.f90:81-153) on the stream; *pass = kinetic partial set.
+static int step_chain(tcp_ctx *c, double dt, bool apply, int *pass) {
+    int rc;
+    if ((rc = launch_vverlet1(c, dt, 0.0))) return rc;
+    if ((rc = recip_launch(c))) return rc;
+    if ((rc = launch_pair(c, energy_on(c), (c->flags & TCP_FLAG_RDF) != 0))) return rc;
+    if ((rc = launch_force_finalize(c, c->p.reciprocal != TCP_RECIP_NONE))) return rc;
+    if ((rc = launch_kick2(c, dt, true, apply, (c->flags & TCP_FLAG_VDF) != 0, pass))) return rc;
+    if ((rc = launch_reduce(c, (energy_on(c) ? kRedUr : 0) | kRedMv2, *pass))) return rc;
+    return TCP_OK;
+}
+
+}  // namespace tcp
+
+using namespace tcp;
+
+extern "C" {
+
+const char *tcp_last_error(void) { return g_err.c_str(); }
+
+const char *tcp_status_string(int code) {
+    switch (code) {
+        case TCP_OK: return "ok";
+        case TCP_ERR_BAD_PARAM: return "bad parameter";
+        case TCP_ERR_CUTOFF: return "cut-off radius larger than half the box";
+        case TCP_ERR_CUDA: return "CUDA error";
+        case TCP_ERR_CUFFT: return "cuFFT error";
+        case TCP_ERR_TIMEOUT: return "device wait timed out";
+        case TCP_ERR_NO_DEVICE: return "no usable sm_103 device";
+        case TCP_ERR_STATE: return "call order";
+        case TCP_ERR_NOMEM: return "device allocation failed";
+        default: return "unknown status";
+    }
+}
+
+int tcp_version(int *major, int *minor, int *arch) {
+    if (major) *major = 0;
+    if (minor) *minor = 1;
+    if (arch) *arch = 103;
+    return TCP_OK;
+}
+
+int tcp_create(const tcp_params *p_in, int nel, int nion, int device, tcp_ctx **out) {
+    if (!out) return set_error(TCP_ERR_BAD_PARAM, "out is NULL");
+    *out = nullptr;
+    int rc = validate(p_in, nel, nion);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return set_error(TCP_ERR_NO_DEVICE, "no CUDA device visible");
+    }
+    if (device < 0 || device >= ndev) return set_error(TCP_ERR_BAD_PARAM, "device index out of range");
+    cudaDeviceProp prop;
+    TCP_CUDA(cudaGetDeviceProperties(&prop, device));
+    if (prop.major != 10 || prop.minor != 3)
+        return set_error(TCP_ERR_NO_DEVICE, "libtcpgpu is built for sm_103a (GB300); device is sm_" +
+                                                std::to_string(prop.major) + std::to_string(prop.minor));
+    TCP_CUDA(cudaSetDevice(device));
+    tcp_ctx *c = new tcp_ctx();
+    c->p = *p_in;
+    normalise(&c->p);
+    c->nel = nel;
+    c->nion = nion;
+    c->n = nel + nion;
+    c->device = device;
+    c->num_sms = prop.multiProcessorCount;
+    const size_t n = c->n;
+    auto fail = [&](int code) {
+        tcp_destroy(c);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(cuda_check(cudaGetLastError(), "cudaStreamCreate"));
+#define TCP_ALLOC(ptr, bytes)                                                            \
+    do {                                                                                 \
+        cudaError_t _e = cudaMalloc(&(ptr), (bytes));                                    \
+        if (_e != cudaSuccess) return fail(cuda_check(_e, "cudaMalloc " #ptr));          \
+    } while (0)
+    TCP_ALLOC(c->x, sizeof(double) * 3 * n);
+    TCP_ALLOC(c->v, sizeof(double) * 3 * n);
+    TCP_ALLOC(c->f, sizeof(double) * 3 * n);
+    TCP_ALLOC(c->frec, sizeof(double) * 3 * n);
+    TCP_ALLOC(c->xq, sizeof(int4) * n);
+    TCP_ALLOC(c->xd, sizeof(double4_32a) * n);
+    c->red_cap = red_capacity(c->n, 8192 + 65536);
+    TCP_ALLOC(c->red, sizeof(double) * (size_t)c->red_cap);
+    TCP_ALLOC(c->scal, sizeof(double) * kScalCount);
+    TCP_ALLOC(c->status, sizeof(unsigned));
+    TCP_ALLOC(c->rdf, sizeof(unsigned long long) * 3 * kNbin);
+    TCP_ALLOC(c->vdf, sizeof(unsigned long long) * 2 * kNbin);
+#undef TCP_ALLOC
+    if (cudaMallocHost(&c->h_scal, sizeof(double) * (kScalCount + 1)) != cudaSuccess)
+        return fail(cuda_check(cudaGetLastError(), "cudaMallocHost"));
+    cudaMemsetAsync(c->x, 0, sizeof(double) * 3 * n, c->stream);
+    cudaMemsetAsync(c->v, 0, sizeof(double) * 3 * n, c->stream);
+    cudaMemsetAsync(c->f, 0, sizeof(double) * 3 * n, c->stream);
+    cudaMemsetAsync(c->frec, 0, sizeof(double) * 3 * n, c->stream);
+    cudaMemsetAsync(c->scal, 0, sizeof(double) * kScalCount, c->stream);
+    cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream);
+    cudaMemsetAsync(c->rdf, 0, sizeof(unsigned long long) * 3 * kNbin, c->stream);
+    cudaMemsetAsync(c->vdf, 0, sizeof(unsigned long long) * 2 * kNbin, c->stream);
+    if ((rc = launch_refresh_positions(c))) return fail(rc);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(cuda_check(cudaGetLastError(), "create sync"));
+    *out = c;
+    return TCP_OK;
+}
+
+int tcp_destroy(tcp_ctx *c) {
+    if (!c) return TCP_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    invalidate_graph(c);
+    spme_free(c);
+    cudaFree(c->x);
+    cudaFree(c->v);
+    cudaFree(c->f);
+    cudaFree(c->frec);
+    cudaFree(c->xq);
+    cudaFree(c->xd);
+    cudaFree(c->fpart);
+    cudaFree(c->upart);
+    cudaFree(c->red);
+    cudaFree(c->scal);
+    cudaFree(c->status);
+    cudaFree(c->rdf);
+    cudaFree(c->vdf);
+    cudaFree(c->d_stage);
+    cudaFree(c->kvec);
+    cudaFree(c->ksum);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    if (c->h_scal) cudaFreeHost(c->h_scal);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return TCP_OK;
+}
+
+int tcp_ewald_self(tcp_ctx *c, double *alpha_out, double *Uo_out) {
+    if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
+    cudaSetDevice(c->device);
+    const tcp_params &p = c->p;
+    const double rc_cut = std::min(std::min(p.box[0], p.box[1]), p.box[2]) / 2.0;   // force.f90:18
+    if (p.rc > rc_cut) return set_error(TCP_ERR_CUTOFF, " *** error at cut-off radius *** (rc > min(box)/2)");
+    c->alpha = p.a > 0.0 ? p.a : 3.1 / p.rc;                                       // force.f90:23
+    c->rc2 = p.rc * p.rc;                                                           // force.f90:24
+    c->V = p.box[0] * p.box[1] * p.box[2];
+    const double s = p.charge_scale;
+    c->Uo = (-(double)c->nel * (s * p.q[0]) * (s * p.q[0]) - (double)c->nion * (s * p.q[1]) * (s * p.q[1])) *
+            c->alpha / kSqrtPi;                                                     // force.f90:44-45
+    int rc;
+    if ((rc = pair_setup(c))) return rc;
+    if (p.reciprocal == TCP_RECIP_SPME && (rc = spme_setup(c))) return rc;
+    if (p.reciprocal == TCP_RECIP_EWALD && (rc = ewald_setup(c))) return rc;
+    invalidate_graph(c);
+    c->ewald_ready = true;
+    if (alpha_out) *alpha_out = c->alpha;
+    if (Uo_out) *Uo_out = c->Uo;
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    return TCP_OK;
+}
+
+int tcp_set_params(tcp_ctx *c, const tcp_params *p) {
+    if (!c || !p) return set_error(TCP_ERR_BAD_PARAM, "NULL argument");
+    int rc = validate(p, c->nel, c->nion);
+    if (rc) return rc;
+    tcp_params q = *p;
+    normalise(&q);
+    for (int d = 0; d < 3; ++d)
+        if (q.box[d] != c->p.box[d] || q.K[d] != c->p.K[d])
+            return set_error(TCP_ERR_BAD_PARAM, "box and mesh are fixed at tcp_create");
+    if (q.order != c->p.order || q.precision != c->p.precision || q.reciprocal != c->p.reciprocal ||
+        q.ewald_nmax2 != c->p.ewald_nmax2)
+        return set_error(TCP_ERR_BAD_PARAM, "order, precision and reciprocal method are fixed at tcp_create");
+    const bool alpha_changed = q.a != c->p.a || q.rc != c->p.rc;
+    c->p = q;
+    invalidate_graph(c);
+    if (c->ewald_ready && (alpha_changed || true)) return tcp_ewald_self(c, nullptr, nullptr);
+    return TCP_OK;
+}
+
+int tcp_set_flags(tcp_ctx *c, unsigned flags) {
+    if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
+    if (flags != c->flags) invalidate_graph(c);
+    c->flags = flags;
+    return TCP_OK;
+}
+
+// ---- transfers ---------------------------------------------------------------
+int tcp_upload(tcp_ctx *c, int species, const double *xx, const double *xv, const double *ff, long stride) {
+    if (!c || (species != 0 && species != 1)) return set_error(TCP_ERR_BAD_PARAM, "bad ctx or species");
+    cudaSetDevice(c->device);
+    const int count = species == 0 ? c->nel : c->nion, first = species == 0 ? 0 : c->nel;
+    if (count == 0 || (!xx && !xv && !ff)) return TCP_OK;
+    const double *ptrs[3] = {xx, xv, ff};
+    const char *base = nullptr, *top = nullptr;
+    for (const double *q : ptrs)
+        if (q) {
+            const char *b = reinterpret_cast<const char *>(q);
+            if (!base || b < base) base = b;
+            if (!top || b > top) top = b;
+        }
+    if (stride < 24 || stride % 8 || (top - base) + 24 > (count > 1 ? stride : (top - base) + 24))
+        return set_error(TCP_ERR_BAD_PARAM, "stride must be a multiple of 8 and cover the three fields");
+    long off[3];
+    for (int k = 0; k < 3; ++k) {
+        off[k] = ptrs[k] ? (long)(reinterpret_cast<const char *>(ptrs[k]) - base) : -1;
+        if (off[k] >= 0 && off[k] % 8) return set_error(TCP_ERR_BAD_PARAM, "fields must be 8-byte aligned");
+    }
+    const size_t span = (size_t)(count - 1) * stride + (size_t)(top - base) + 24;
+    int rc;
+    if ((rc = ensure_stage(c, span))) return rc;
+    TCP_CUDA(cudaMemcpyAsync(c->d_stage, base, span, cudaMemcpyHostToDevice, c->stream));
+    if ((rc = launch_extract(c, first, count, stride, off[0], off[1], off[2]))) return rc;
+    if (xx && (rc = launch_refresh_positions(c))) return rc;
+    invalidate_graph(c);   // no-op for correctness; graphs read device memory
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    return TCP_OK;
+}
+
+int tcp_download(tcp_ctx *c, int species, double *xx, double *xv, double *ff, long stride) {
+    if (!c || (species != 0 && species != 1)) return set_error(TCP_ERR_BAD_PARAM, "bad ctx or species");
+    cudaSetDevice(c->device);
+    const int count = species == 0 ? c->nel : c->nion, first = species == 0 ? 0 : c->nel;
+    if (count == 0 || (!xx && !xv && !ff)) return TCP_OK;
+    if (stride < 24 || stride % 8) return set_error(TCP_ERR_BAD_PARAM, "bad stride");
+    int nf = 0, rc;
+    if ((rc = ensure_stage(c, (size_t)count * 4 * 3 * sizeof(double)))) return rc;
+    if ((rc = launch_pack(c, first, count, xx != nullptr, xv != nullptr, ff != nullptr, false, &nf))) return rc;
+    TCP_CUDA(cudaMemcpyAsync(c->h_stage, c->d_stage, (size_t)count * nf * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                             c->stream));
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    double *dst[3] = {xx, xv, ff};
+    int slot = 0;
+    for (int q = 0; q < 3; ++q) {
+        if (!dst[q]) continue;
+        char *b = reinterpret_cast<char *>(dst[q]);
+        for (int r = 0; r < count; ++r)
+            std::memcpy(b + (size_t)r * stride, c->h_stage + ((size_t)r * nf + slot) * 3, 3 * sizeof(double));
+        ++slot;
+    }
+    return TCP_OK;
+}
+
+int tcp_upload_soa(tcp_ctx *c, const double *x, const double *v, const double *f) {
+    if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
+    cudaSetDevice(c->device);
+    int rc;
+    if ((rc = ensure_stage(c, (size_t)c->n * 3 * sizeof(double)))) return rc;
+    const double *src[3] = {x, v, f};
+    for (int q = 0; q < 3; ++q) {
+        if (!src[q]) continue;
+        TCP_CUDA(cudaMemcpyAsync(c->d_stage, src[q], (size_t)c->n * 3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        if ((rc = launch_extract(c, 0, c->n, 24, q == 0 ? 0 : -1, q == 1 ? 0 : -1, q == 2 ? 0 : -1))) return rc;
+    }
+    if (x && (rc = launch_refresh_positions(c))) return rc;
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    return TCP_OK;
+}
+
+int tcp_download_soa(tcp_ctx *c, double *x, double *v, double *f, double *frec) {
+    if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
+    cudaSetDevice(c->device);
+    int nf = 0, rc;
+    if ((rc = ensure_stage(c, (size_t)c->n * 4 * 3 * sizeof(double)))) return rc;
+    if ((rc = launch_pack(c, 0, c->n, x != nullptr, v != nullptr, f != nullptr, frec != nullptr, &nf))) return rc;
+    if (nf == 0) return TCP_OK;
+    TCP_CUDA(cudaMemcpyAsync(c->h_stage, c->d_stage, (size_t)c->n * nf * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                             c->stream));
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    double *dst[4] = {x, v, f, frec};
+    int slot = 0;
+    for (int q = 0; q < 4; ++q) {
+        if (!dst[q]) continue;
+        for (int r = 0; r < c->n; ++r)
+            for (int d = 0; d < 3; ++d) dst[q][3 * (size_t)r + d] = c->h_stage[((size_t)r * nf + slot) * 3 + d];
+        ++slot;
+    }
+    return TCP_OK;
+}
+
+// ---- force routines ------------------------------------------------------------
+#define TCP_REQUIRE_READY(c)                                                                     \
+    do {                                                                                         \
+        if (!(c)) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");                           \
+        if (!(c)->ewald_ready) return set_error(TCP_ERR_STATE, "tcp_ewald_self must be called first"); \
+        cudaSetDevice((c)->device);                                                              \
+    } while (0)
+
+int tcp_force_direct(tcp_ctx *c, double *Ur) {
+    TCP_REQUIRE_READY(c);
+    int rc;
+    if ((rc = launch_pair(c, energy_on(c), (c->flags & TCP_FLAG_RDF) != 0))) return rc;
+    if ((rc = launch_force_finalize(c, false))) return rc;
+    if (energy_on(c) && (rc = launch_reduce(c, kRedUr, 0))) return rc;
+    if ((rc = sync_scalars(c))) return rc;
+    if (Ur) *Ur = energy_on(c) ? c->h_scal[kScalUr] : 0.0;
+    return TCP_OK;
+}
+
+int tcp_force_spme(tcp_ctx *c, double *Um) {
+    TCP_REQUIRE_READY(c);
+    int rc;
+    if (c->p.reciprocal == TCP_RECIP_NONE) {
+        TCP_CUDA(cudaMemsetAsync(c->frec, 0, sizeof(double) * 3 * (size_t)c->n, c->stream));
+        TCP_CUDA(cudaMemsetAsync(c->scal + kScalUm, 0, sizeof(double), c->stream));
+    } else if ((rc = recip_launch(c))) {
+        return rc;
+    }
+    if ((rc = sync_scalars(c))) return rc;
+    if (Um) *Um = c->h_scal[kScalUm];
+    return TCP_OK;
+}
+
+int tcp_spme_sum(tcp_ctx *c) {
+    TCP_REQUIRE_READY(c);
+    int rc;
+    if ((rc = launch_spme_sum(c))) return rc;
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    return TCP_OK;
+}
+
+int tcp_remove_rigidmtn(tcp_ctx *c) {
+    TCP_REQUIRE_READY(c);
+    int rc;
+    if ((rc = launch_fsum(c))) return rc;
+    if ((rc = launch_remove_rigid(c))) return rc;
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    return TCP_OK;
+}
+
+int tcp_force(tcp_ctx *c, tcp_energies *e) {
+    TCP_REQUIRE_READY(c);
+    int rc;
+    if ((rc = force_chain(c, true))) return rc;
+    if ((rc = sync_scalars(c))) return rc;
+    fill_energies(c, e);
+    return TCP_OK;
+}
+
+int tcp_vverlet1(tcp_ctx *c, double dt) {
+    TCP_REQUIRE_READY(c);
+    int rc;
+    if ((rc = launch_vverlet1(c, dt, 0.0))) return rc;
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    return TCP_OK;
+}
+
+int tcp_vverlet2(tcp_ctx *c, double dt, double *mv2el, double *mv2ion) {
+    TCP_REQUIRE_READY(c);
+    int rc, pass = 0;
+    if ((rc = launch_kick2(c, dt, false, thermostat_due(c), (c->flags & TCP_FLAG_VDF) != 0, &pass))) return rc;
+    if ((rc = launch_reduce(c, kRedMv2, pass))) return rc;
+    if ((rc = sync_scalars(c))) return rc;
+    c->step_index++;
+    c->last.mv2el = c->h_scal[kScalMv2e];
+    c->last.mv2ion = c->h_scal[kScalMv2i];
+    if (mv2el) *mv2el = c->last.mv2el;
+    if (mv2ion) *mv2ion = c->last.mv2ion;
+    return TCP_OK;
+}
+
+int tcp_finit(tcp_ctx *c, double dt, tcp_energies *e) {
+    TCP_REQUIRE_READY(c);
+    int rc;
+    if ((rc = launch_shift(c, -dt))) return rc;                  // init.f90:171-185
+    if ((rc = force_chain(c, true))) return rc;                  // init.f90:193-220
+    if ((rc = launch_shift(c, dt))) return rc;                   // init.f90:223-237
+    if ((rc = sync_scalars(c))) return rc;
+    fill_energies(c, e);
+    return TCP_OK;
+}
+
+static int build_graph(tcp_ctx *c, double dt, bool apply, cudaGraphExec_t *out, int *kernels) {
+    cudaGraph_t g;
+    const long long before = c->launches;
+    TCP_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int pass = 0;
+    int rc = step_chain(c, dt, apply, &pass);
+    cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return cuda_check(ce, "cudaStreamEndCapture");
+    ce = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return cuda_check(ce, "cudaGraphInstantiate");
+    *kernels = (int)(c->launches - before);
+    c->launches = before;
+    return TCP_OK;
+}
+
+int tcp_md_steps(tcp_ctx *c, double dt, int nsteps, tcp_energies *e) {
+    TCP_REQUIRE_READY(c);
+    if (nsteps < 0) return set_error(TCP_ERR_BAD_PARAM, "nsteps < 0");
+    int rc;
+    const bool has_thermo = c->p.thermo == TCP_THERMO_ISOKIN || c->p.thermo == TCP_THERMO_BEREND;
+    // c->graph holds the no-rescale step; the rescale step (ISOKIN/BEREND,
+    // every thermo_period-th step) is launched eagerly, it is rare.
+    if (!c->graph || c->graph_dt != dt || c->graph_flags != c->flags) {
+        invalidate_graph(c);
+        if ((rc = build_graph(c, dt, !has_thermo, &c->graph, &c->graph_kernels))) return rc;
+        c->graph_dt = dt;
+        c->graph_flags = c->flags;
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        if (has_thermo && thermostat_due(c)) {
+            int pass = 0;
+            if ((rc = step_chain(c, dt, true, &pass))) return rc;
+        } else {
+            TCP_CUDA(cudaGraphLaunch(c->graph, c->stream));
+            c->launches += c->graph_kernels;
+        }
+        c->step_index++;
+    }
+    if ((rc = sync_scalars(c))) return rc;
+    fill_energies(c, nullptr);
+    c->last.mv2el = c->h_scal[kScalMv2e];
+    c->last.mv2ion = c->h_scal[kScalMv2i];
+    if (e) *e = c->last;
+    return TCP_OK;
+}
+
+int tcp_energies_get(tcp_ctx *c, tcp_energies *e) {
+    if (!c || !e) return set_error(TCP_ERR_BAD_PARAM, "NULL argument");
+    *e = c->last;
+    return TCP_OK;
+}
+
+int tcp_histograms(tcp_ctx *c, double *rdf, double *vdf, int reset) {
+    if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
+    cudaSetDevice(c->device);
+    std::vector<unsigned long long> h(5 * kNbin);
+    TCP_CUDA(cudaMemcpyAsync(h.data(), c->rdf, sizeof(unsigned long long) * 3 * kNbin, cudaMemcpyDeviceToHost, c->stream));
+    TCP_CUDA(cudaMemcpyAsync(h.data() + 3 * kNbin, c->vdf, sizeof(unsigned long long) * 2 * kNbin,
+                             cudaMemcpyDeviceToHost, c->stream));
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    // ordered pairs are counted once each: +2 per unordered pair as force.f90:102
+    if (rdf)
+        for (int k = 0; k < 3 * kNbin; ++k) rdf[k] = (double)h[k];
+    if (vdf)
+        for (int k = 0; k < 2 * kNbin; ++k) vdf[k] = (double)h[3 * kNbin + k];
+    if (reset) {
+        TCP_CUDA(cudaMemsetAsync(c->rdf, 0, sizeof(unsigned long long) * 3 * kNbin, c->stream));
+        TCP_CUDA(cudaMemsetAsync(c->vdf, 0, sizeof(unsigned long long) * 2 * kNbin, c->stream));
+        TCP_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return TCP_OK;
+}
+
+int tcp_time_component(tcp_ctx *c, int which, int reps, double dt, double *ms) {
+    TCP_REQUIRE_READY(c);
+    if (reps <= 0 || !ms) return set_error(TCP_ERR_BAD_PARAM, "reps must be positive");
+    cudaEvent_t e0, e1;
+    TCP_CUDA(cudaEventCreate(&e0));
+    TCP_CUDA(cudaEventCreate(&e1));
+    int rc = TCP_OK;
+    auto one = [&]() -> int {
+        if (which == 0) return launch_pair(c, energy_on(c), false);
+        if (which == 1) return recip_launch(c);
+        return tcp_md_steps(c, dt, 1, nullptr);
+    };
+    if (which == 2) {
+        // build the graph outside the timed region
+        if ((rc = tcp_md_steps(c, dt, 1, nullptr))) return rc;
+    }
+    cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < reps && !rc; ++r) {
+        if (which == 2) {
+            if (c->graph && !(c->p.thermo == TCP_THERMO_ISOKIN || c->p.thermo == TCP_THERMO_BEREND)) {
+                cudaGraphLaunch(c->graph, c->stream);
+                c->launches += c->graph_kernels;
+                c->step_index++;
+            } else {
+                int pass = 0;
+                rc = step_chain(c, dt, thermostat_due(c), &pass);
+                c->step_index++;
+            }
+        } else {
+            rc = one();
+        }
+    }
+    cudaEventRecord(e1, c->stream);
+    cudaEventSynchronize(e1);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if ((rc = sync_scalars(c))) return rc;
+    *ms = (double)t / reps;
+    return TCP_OK;
+}
+
+int tcp_launch_count(tcp_ctx *c, long long *count) {
+    if (!c || !count) return set_error(TCP_ERR_BAD_PARAM, "NULL argument");
+    *count = c->launches;
+    return TCP_OK;
+}
+
+int tcp_fp32_peak(int device, double *tffma) {
+    if (!tffma) return set_error(TCP_ERR_BAD_PARAM, "NULL argument");
+    TCP_CUDA(cudaSetDevice(device));
+    return launch_fp32_peak(device, tffma);
+}
+
+}  // extern "C"

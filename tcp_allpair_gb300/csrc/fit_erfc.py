@@ -1,0 +1,55 @@
+"""Derive the FP32 erfc approximation used by the FP32 pair kernel.
+
+    erfc(x) = exp(-x^2) * t * Q(t),   t = 1 / (1 + P x),   x >= 0
+
+Q is a degree-8 polynomial in t fitted to erfcx(x)/t = erfc(x) exp(x^2)/t by
+Lawson's iteratively reweighted least squares, which converges to the minimax
+fit in relative error, on x in [0, XMAX].  The exp(-x^2) factor is shared with
+the Gaussian term of the Ewald pair force, so a Coulomb pair costs one ex2 and
+one reciprocal on the SFU for both erfc and the Gaussian.
+
+Fit error (FP64 evaluation): 3.8e-8 relative.  Evaluated in FP32 Horner form
+on x in [0, 6]: 3.6e-7 max, 7.8e-8 rms relative (the FP32 rounding of t
+dominates).  Run `python fit_erfc.py` to reproduce the coefficients in
+pair_fp32c.cu (printed highest power first).
+"""
+import numpy as np
+from scipy.special import erfc, erfcx
+
+P = 0.5
+DEG = 8
+XMAX = 8.0
+
+
+def fit(p=P, deg=DEG, xmax=XMAX, iters=200):
+    t = np.linspace(1.0 / (1.0 + p * xmax), 1.0, 20000)
+    x = (1.0 / t - 1.0) / p
+    target = erfcx(x) / t
+    A = np.vander(t, deg + 1)
+    w = np.ones_like(t)
+    for _ in range(iters):
+        sw = np.sqrt(w) / target
+        c, *_ = np.linalg.lstsq(A * sw[:, None], target * sw, rcond=None)
+        err = np.abs(A @ c - target) / target
+        w = w * (err + 1e-300)
+        w /= w.sum()
+    return c, float(np.max(np.abs(A @ c - target) / target))
+
+
+def fp32_error(c, p=P, xmax=6.0):
+    x = np.linspace(0.0, xmax, 200001).astype(np.float32)
+    t = (np.float32(1.0) / (np.float32(1.0) + np.float32(p) * x)).astype(np.float32)
+    q = np.float32(c[0])
+    for ci in c[1:]:
+        q = (q * t + np.float32(ci)).astype(np.float32)
+    approx = np.exp(-x.astype(np.float64) ** 2) * (t * q).astype(np.float64)
+    ref = erfc(x.astype(np.float64))
+    rel = np.abs(approx - ref) / ref
+    return float(rel.max()), float(np.sqrt(np.mean(rel ** 2)))
+
+
+if __name__ == "__main__":
+    c, e = fit()
+    mx, rms = fp32_error(c)
+    print(f"P={P} DEG={DEG} fit max rel {e:.3e}; fp32 max rel {mx:.3e}, rms {rms:.3e}")
+    print(", ".join(f"{v:.9e}f" for v in c))

@@ -1,0 +1,494 @@
+// integrate.cu -- velocity Verlet halves and thermostats (vverlet.f90),
+// net-force removal (REMOVE_RIGIDMTN, force.f90:974-1007), the SPME_SUM add,
+// deterministic FP64 reductions, and the host-record gather/scatter kernels.
+//
+// All state is FP64 SoA [3][n].  Every kernel that moves positions also
+// refreshes the two pair-kernel copies: 32-bit fixed point (int4) and
+// double4_32a.  Reductions write one partial per CTA; a single-CTA kernel sums
+// them in a fixed order, so results do not depend on scheduling.
+#include <cmath>
+
+#include "device_util.cuh"
+#include "tcp_internal.h"
+
+namespace tcp {
+
+constexpr int kIntThreads = 256;
+
+// 2^32 units per box length; the int32 difference of two coordinates is the
+// minimum-image separation.
+__device__ __forceinline__ int fixed_coord(double x, double L) {
+    double t = x / L + 0.5;
+    t -= floor(t);
+    const unsigned long long u = (unsigned long long)llrint(t * 4294967296.0);
+    return (int)(unsigned)(u & 0xffffffffull);
+}
+
+struct IntArgs {
+    double *x, *v, *f;
+    int4 *xq;
+    double4_32a *xd;
+    int nel, n;
+    double xm0, xm1;
+    double L0, L1, L2;
+};
+
+__device__ __forceinline__ void store_pos(const IntArgs &a, int i, double x0, double x1, double x2) {
+    a.x[i] = x0;
+    a.x[(size_t)a.n + i] = x1;
+    a.x[2 * (size_t)a.n + i] = x2;
+    a.xq[i] = make_int4(fixed_coord(x0, a.L0), fixed_coord(x1, a.L1), fixed_coord(x2, a.L2), 0);
+    a.xd[i] = make_double4_32a(x0, x1, x2, 0.0);
+}
+
+// x - L DNINT(x/L) (vverlet.f90:153)
+__device__ __forceinline__ double wrap(double x, double L) { return x - L * round(x / L); }
+
+__global__ void refresh_kernel(const IntArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    store_pos(a, i, a.x[i], a.x[(size_t)a.n + i], a.x[2 * (size_t)a.n + i]);
+}
+
+// Finit's step back / forward, init.f90:171-185 and 223-237
+__global__ void shift_kernel(const IntArgs a, double sdt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    double y[3];
+    const double L[3] = {a.L0, a.L1, a.L2};
+    for (int k = 0; k < 3; ++k) y[k] = wrap(a.x[(size_t)k * a.n + i] + sdt * a.v[(size_t)k * a.n + i], L[k]);
+    store_pos(a, i, y[0], y[1], y[2]);
+}
+
+// VVerletNotemp1 (vverlet.f90:148-167) / VVerletStoch1 (vverlet.f90:34-55)
+__global__ void vverlet1_kernel(const IntArgs a, double dt, double alpha_lgv, int stoch) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const double xm = i < a.nel ? a.xm0 : a.xm1;
+    const double L[3] = {a.L0, a.L1, a.L2};
+    double y[3];
+    for (int k = 0; k < 3; ++k) {
+        const size_t o = (size_t)k * a.n + i;
+        double vk = a.v[o];
+        if (stoch)
+            vk = vk * (1.0 - 0.5 * alpha_lgv * dt / xm) + 0.5 * dt * a.f[o] / xm;
+        else
+            vk = vk + 0.5 * dt * a.f[o] / xm;
+        a.v[o] = vk;
+        y[k] = wrap(a.x[o] + dt * vk, L[k]);
+    }
+    store_pos(a, i, y[0], y[1], y[2]);
+}
+
+// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) ---------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 ctr, uint2 key) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t hi0 = __umulhi(M0, ctr.x), lo0 = M0 * ctr.x;
+        const uint32_t hi1 = __umulhi(M1, ctr.z), lo1 = M1 * ctr.z;
+        ctr = make_uint4(hi1 ^ ctr.y ^ key.x, lo1, hi0 ^ ctr.w ^ key.y, lo0);
+        key.x += W0;
+        key.y += W1;
+    }
+    return ctr;
+}
+
+// Three standard normals for (particle, step): Box-Muller on the words of
+// two Philox blocks (counter = {particle, step lo, step hi, 0|1}).
+__device__ __forceinline__ void gauss3(uint64_t seed, long long step, int i, double g[3]) {
+    const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+    const uint4 r0 = philox4x32_10(make_uint4((uint32_t)i, (uint32_t)step, (uint32_t)((uint64_t)step >> 32), 0u), key);
+    const uint4 r1 = philox4x32_10(make_uint4((uint32_t)i, (uint32_t)step, (uint32_t)((uint64_t)step >> 32), 1u), key);
+    const double s = 2.3283064365386963e-10;  // 2^-32
+    const double u1 = ((double)r0.x + 0.5) * s, u2 = ((double)r0.y + 0.5) * s;
+    const double u3 = ((double)r1.x + 0.5) * s, u4 = ((double)r1.y + 0.5) * s;
+    const double ra = sqrt(-2.0 * log(u1)), rb = sqrt(-2.0 * log(u3));
+    g[0] = ra * cos(2.0 * kPi * u2);
+    g[1] = ra * sin(2.0 * kPi * u2);
+    g[2] = rb * cos(2.0 * kPi * u4);
+}
+
+struct KickArgs {
+    IntArgs a;
+    double dt;
+    int thermo;              // TCP_THERMO_*
+    int remove_net;          // subtract sum(f)/n first (REMOVE_RIGIDMTN fused)
+    const double *fsum_part; // [3][nbf]
+    int nbf;
+    double *mv_part;         // [2][nb] output partials (species)
+    const double *mv_in;     // [2][nb] partials of the first pass (rescale pass)
+    int nb;
+    int vdf;
+    unsigned long long *vdf_counts;
+    double dv0, dv1;
+    double T0, T1, tau, alpha_lgv;
+    uint64_t seed;
+    const double *step;      // device step counter (advanced by the reduction kernel)
+    int rescale;             // 0 kick pass, 1 rescale pass
+};
+
+__device__ __forceinline__ double sum_strided(const double *p, int np) {
+    double s = 0.0;
+    for (int k = 0; k < np; ++k) s += p[k];
+    return s;
+}
+
+__device__ __forceinline__ void vdf_add(const KickArgs &k, int s, double mv2) {
+    const double t = mv2 / 3.0 / (s == 0 ? k.dv0 : k.dv1);   // vverlet.f90:201
+    if (t < (double)kNbin) atomicAdd(&k.vdf_counts[s * kNbin + (int)t], 1ull);
+}
+
+// Second half kick (vverlet.f90:194-219 NOTEMP, :250-255 BEREND/ISOKIN first
+// loop, :91-123 STOCH); per-species sum m v^2 partials; VDF when final.
+__global__ void kick2_kernel(const KickArgs k) {
+    __shared__ double red[32];
+    __shared__ double fbar[3];
+    const IntArgs &a = k.a;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k.remove_net) {
+        if (threadIdx.x < 3) fbar[threadIdx.x] = sum_strided(k.fsum_part + threadIdx.x * k.nbf, k.nbf) / (double)a.n;
+        __syncthreads();
+    }
+    double mv_e = 0.0, mv_i = 0.0;
+    if (i < a.n) {
+        const int s = i < a.nel ? 0 : 1;
+        const double xm = s == 0 ? a.xm0 : a.xm1;
+        double vv[3];
+        double eta[3] = {0.0, 0.0, 0.0};
+        if (k.thermo == TCP_THERMO_STOCH) gauss3(k.seed, (long long)*k.step, i, eta);
+        const double beta = k.thermo == TCP_THERMO_STOCH ? sqrt(2.0 * k.alpha_lgv * (s == 0 ? k.T0 : k.T1) / k.dt) : 0.0;
+        for (int d = 0; d < 3; ++d) {
+            const size_t o = (size_t)d * a.n + i;
+            double fd = a.f[o];
+            if (k.remove_net) fd -= fbar[d];                                 // force.f90:999-1004
+            if (k.thermo == TCP_THERMO_STOCH) {
+                fd = fd + eta[d] * beta;                                     // vverlet.f90:95
+                vv[d] = (a.v[o] + 0.5 * k.dt * fd / xm) / (1.0 + 0.5 * k.alpha_lgv * k.dt / xm);
+            } else {
+                vv[d] = a.v[o] + 0.5 * k.dt * fd / xm;                       // vverlet.f90:197
+            }
+            if (k.remove_net || k.thermo == TCP_THERMO_STOCH) a.f[o] = fd;
+            a.v[o] = vv[d];
+        }
+        const double mv2 = (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]) * xm;   // vverlet.f90:199
+        if (s == 0) mv_e = mv2; else mv_i = mv2;
+        if (k.vdf) vdf_add(k, s, mv2);
+    }
+    const double te = block_sum(mv_e, red);
+    const double ti = block_sum(mv_i, red);
+    if (threadIdx.x == 0) {
+        k.mv_part[blockIdx.x] = te;
+        k.mv_part[k.nb + blockIdx.x] = ti;
+    }
+}
+
+// Rescale pass of VVerletIsokin2 / VVerletBerend2 (vverlet.f90:331-344,
+// 257-270): lambda per species from the first-pass sums, v *= lambda,
+// sum m v^2 and VDF.
+__global__ void rescale_kernel(const KickArgs k) {
+    __shared__ double red[32];
+    __shared__ double lam[2];
+    const IntArgs &a = k.a;
+    if (threadIdx.x < 2) {
+        const int s = threadIdx.x;
+        const double mv2 = sum_strided(k.mv_in + s * k.nb, k.nb);
+        const int cnt = s == 0 ? a.nel : a.n - a.nel;
+        const double T0 = mv2 / (double)(3 * cnt);
+        const double T = s == 0 ? k.T0 : k.T1;
+        lam[s] = k.thermo == TCP_THERMO_ISOKIN ? sqrt(T / T0) : sqrt(1.0 + k.dt * (T / T0 - 1.0) / k.tau);
+    }
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double mv_e = 0.0, mv_i = 0.0;
+    if (i < a.n) {
+        const int s = i < a.nel ? 0 : 1;
+        const double xm = s == 0 ? a.xm0 : a.xm1;
+        double vv[3];
+        for (int d = 0; d < 3; ++d) {
+            const size_t o = (size_t)d * a.n + i;
+            vv[d] = a.v[o] * lam[s];
+            a.v[o] = vv[d];
+        }
+        const double mv2 = (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]) * xm;
+        if (s == 0) mv_e = mv2; else mv_i = mv2;
+        if (k.vdf) vdf_add(k, s, mv2);
+    }
+    const double te = block_sum(mv_e, red);
+    const double ti = block_sum(mv_i, red);
+    if (threadIdx.x == 0) {
+        k.mv_part[blockIdx.x] = te;
+        k.mv_part[k.nb + blockIdx.x] = ti;
+    }
+}
+
+// f += frec (SPME_SUM, force.f90:953-964) with sum(f) partials
+__global__ void add_rec_kernel(double *__restrict__ f, const double *__restrict__ frec, int n,
+                               double *__restrict__ fsum_part) {
+    __shared__ double red[32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double s[3] = {0.0, 0.0, 0.0};
+    if (i < n)
+        for (int d = 0; d < 3; ++d) {
+            const size_t o = (size_t)d * n + i;
+            if (frec) f[o] += frec[o];
+            s[d] = f[o];
+        }
+    for (int d = 0; d < 3; ++d) {
+        const double t = block_sum(s[d], red);
+        if (threadIdx.x == 0) fsum_part[d * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+// f -= sum(f)/n (REMOVE_RIGIDMTN, force.f90:996-1004)
+__global__ void remove_net_kernel(double *__restrict__ f, int n, const double *__restrict__ fsum_part, int nbf) {
+    __shared__ double fbar[3];
+    if (threadIdx.x < 3) fbar[threadIdx.x] = sum_strided(fsum_part + threadIdx.x * nbf, nbf) / (double)n;
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int d = 0; d < 3; ++d) f[(size_t)d * n + i] -= fbar[d];
+}
+
+__global__ void reduce_scalars_kernel(const double *__restrict__ upart, int nu, const double *__restrict__ mv,
+                                      int nb, double *__restrict__ scal, int mask) {
+    __shared__ double red[32];
+    if (mask & kRedUr) {
+        double s = 0.0;
+        for (int k = threadIdx.x; k < nu; k += blockDim.x) s += upart[k];
+        s = block_sum(s, red);
+        if (threadIdx.x == 0) scal[kScalUr] = s;
+    }
+    if (mask & kRedMv2) {
+        double se = 0.0, si = 0.0;
+        for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+            se += mv[k];
+            si += mv[nb + k];
+        }
+        se = block_sum(se, red);
+        si = block_sum(si, red);
+        if (threadIdx.x == 0) {
+            scal[kScalMv2e] = se;
+            scal[kScalMv2i] = si;
+            scal[kScalStep] += 1.0;   // one second half-kick per MD step
+        }
+    }
+}
+
+// ---- host records <-> SoA ------------------------------------------------
+// stage holds `count` records of `stride` bytes; fields at byte offsets
+// off_x/off_v/off_f (or < 0 to skip), 3 doubles each.
+__global__ void extract_kernel(const unsigned char *__restrict__ stage, long stride, long off_x, long off_v,
+                               long off_f, int count, int first, int n, double *x, double *v, double *f) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= count) return;
+    const unsigned char *rec = stage + (size_t)r * stride;
+    const int i = first + r;
+    for (int d = 0; d < 3; ++d) {
+        if (off_x >= 0) x[(size_t)d * n + i] = reinterpret_cast<const double *>(rec + off_x)[d];
+        if (off_v >= 0) v[(size_t)d * n + i] = reinterpret_cast<const double *>(rec + off_v)[d];
+        if (off_f >= 0) f[(size_t)d * n + i] = reinterpret_cast<const double *>(rec + off_f)[d];
+    }
+}
+
+// SoA -> [count][fields][3] packed doubles
+__global__ void pack_kernel(double *__restrict__ out, int count, int first, int n, const double *x,
+                            const double *v, const double *f, const double *f2, int nf) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= count) return;
+    const int i = first + r;
+    const double *src[4] = {x, v, f, f2};
+    int slot = 0;
+    for (int q = 0; q < 4; ++q) {
+        if (!src[q]) continue;
+        for (int d = 0; d < 3; ++d) out[((size_t)r * nf + slot) * 3 + d] = src[q][(size_t)d * n + i];
+        ++slot;
+    }
+}
+
+// FP32 peak: 8 independent FFMA chains per thread
+__global__ void ffma_peak_kernel(float *out, int iters, float a, float b) {
+    float r0 = threadIdx.x, r1 = r0 + 1, r2 = r0 + 2, r3 = r0 + 3, r4 = r0 + 4, r5 = r0 + 5, r6 = r0 + 6,
+          r7 = r0 + 7;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            r0 = fmaf(r0, a, b);
+            r1 = fmaf(r1, a, b);
+            r2 = fmaf(r2, a, b);
+            r3 = fmaf(r3, a, b);
+            r4 = fmaf(r4, a, b);
+            r5 = fmaf(r5, a, b);
+            r6 = fmaf(r6, a, b);
+            r7 = fmaf(r7, a, b);
+        }
+    }
+    const float s = r0 + r1 + r2 + r3 + r4 + r5 + r6 + r7;
+    if (s == 1234.5f) out[0] = s;   // keeps the chains live
+}
+
+// ---------------------------------------------------------------------------
+static IntArgs int_args(tcp_ctx *c) {
+    IntArgs a;
+    a.x = c->x;
+    a.v = c->v;
+    a.f = c->f;
+    a.xq = c->xq;
+    a.xd = c->xd;
+    a.nel = c->nel;
+    a.n = c->n;
+    a.xm0 = c->p.xm[0];
+    a.xm1 = c->p.xm[1];
+    a.L0 = c->p.box[0];
+    a.L1 = c->p.box[1];
+    a.L2 = c->p.box[2];
+    return a;
+}
+
+static int nblocks(int n) { return (n + kIntThreads - 1) / kIntThreads; }
+
+// red[] layout: [3][nb] force sums | [2][nb] kinetic pass 0 | [2][nb] pass 1 | recip energy
+double *fsum_part(tcp_ctx *c) { return c->red; }
+double *mv_part(tcp_ctx *c, int pass) { return c->red + 3 * (size_t)nblocks(c->n) + (size_t)pass * 2 * nblocks(c->n); }
+double *recip_epart(tcp_ctx *c) { return c->red + 7 * (size_t)nblocks(c->n); }
+int red_capacity(int n, int extra) { return 7 * nblocks(n) + extra; }
+int kick_blocks(int n) { return nblocks(n); }
+
+int launch_refresh_positions(tcp_ctx *c) {
+    refresh_kernel<<<nblocks(c->n), kIntThreads, 0, c->stream>>>(int_args(c));
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+int launch_shift(tcp_ctx *c, double sdt) {
+    shift_kernel<<<nblocks(c->n), kIntThreads, 0, c->stream>>>(int_args(c), sdt);
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+int launch_vverlet1(tcp_ctx *c, double dt, double) {
+    vverlet1_kernel<<<nblocks(c->n), kIntThreads, 0, c->stream>>>(int_args(c), dt, c->p.alpha_lgv,
+                                                                  c->p.thermo == TCP_THERMO_STOCH);
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+int launch_spme_sum(tcp_ctx *c) {
+    add_rec_kernel<<<nblocks(c->n), kIntThreads, 0, c->stream>>>(c->f, c->frec, c->n, fsum_part(c));
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+int launch_fsum(tcp_ctx *c) {
+    add_rec_kernel<<<nblocks(c->n), kIntThreads, 0, c->stream>>>(c->f, nullptr, c->n, fsum_part(c));
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+int launch_remove_rigid(tcp_ctx *c) {
+    remove_net_kernel<<<nblocks(c->n), kIntThreads, 0, c->stream>>>(c->f, c->n, fsum_part(c), nblocks(c->n));
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+// Returns the kinetic pass whose partials hold the final sum m v^2.
+int launch_kick2(tcp_ctx *c, double dt, bool remove_net, bool apply_thermo, bool vdf, int *final_pass) {
+    KickArgs k;
+    k.a = int_args(c);
+    k.dt = dt;
+    k.thermo = c->p.thermo;
+    const bool rescale = apply_thermo && (c->p.thermo == TCP_THERMO_ISOKIN || c->p.thermo == TCP_THERMO_BEREND);
+    if (!apply_thermo && k.thermo != TCP_THERMO_STOCH) k.thermo = TCP_THERMO_NOTEMP;
+    k.remove_net = remove_net;
+    k.fsum_part = fsum_part(c);
+    k.nbf = nblocks(c->n);
+    k.nb = nblocks(c->n);
+    k.mv_part = mv_part(c, 0);
+    k.mv_in = nullptr;
+    k.vdf = vdf && !rescale;
+    k.vdf_counts = c->vdf;
+    k.dv0 = c->p.dv_e;
+    k.dv1 = c->p.dv_i;
+    k.T0 = c->p.Te;
+    k.T1 = c->p.Ti;
+    k.tau = c->p.tau;
+    k.alpha_lgv = c->p.alpha_lgv;
+    k.seed = c->p.seed;
+    k.step = c->scal + kScalStep;
+    k.rescale = 0;
+    kick2_kernel<<<k.nb, kIntThreads, 0, c->stream>>>(k);
+    c->launches++;
+    *final_pass = 0;
+    if (rescale) {
+        k.thermo = c->p.thermo;
+        k.remove_net = 0;
+        k.mv_in = mv_part(c, 0);
+        k.mv_part = mv_part(c, 1);
+        k.vdf = vdf;
+        k.rescale = 1;
+        rescale_kernel<<<k.nb, kIntThreads, 0, c->stream>>>(k);
+        c->launches++;
+        *final_pass = 1;
+    }
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+int launch_reduce(tcp_ctx *c, int mask, int pass) {
+    reduce_scalars_kernel<<<1, 1024, 0, c->stream>>>(c->upart, c->n_upart, mv_part(c, pass), nblocks(c->n), c->scal,
+                                                     mask);
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+int launch_extract(tcp_ctx *c, int first, int count, long stride, long off_x, long off_v, long off_f) {
+    extract_kernel<<<nblocks(count), kIntThreads, 0, c->stream>>>(c->d_stage, stride, off_x, off_v, off_f, count,
+                                                                  first, c->n, c->x, c->v, c->f);
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+int launch_pack(tcp_ctx *c, int first, int count, bool x, bool v, bool f, bool frec, int *nf) {
+    *nf = (int)x + (int)v + (int)f + (int)frec;
+    pack_kernel<<<nblocks(count), kIntThreads, 0, c->stream>>>(reinterpret_cast<double *>(c->d_stage), count, first,
+                                                               c->n, x ? c->x : nullptr, v ? c->v : nullptr,
+                                                               f ? c->f : nullptr, frec ? c->frec : nullptr, *nf);
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+int launch_fp32_peak(int device, double *tffma) {
+    cudaDeviceProp prop;
+    TCP_CUDA(cudaGetDeviceProperties(&prop, device));
+    float *out;
+    TCP_CUDA(cudaMalloc(&out, sizeof(float)));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = prop.multiProcessorCount * 8, threads = 256, iters = 4096;
+    ffma_peak_kernel<<<blocks, threads>>>(out, 16, 1.0000001f, 1e-7f);   // warm-up
+    cudaEventRecord(e0);
+    ffma_peak_kernel<<<blocks, threads>>>(out, iters, 1.0000001f, 1e-7f);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    const double ffma = (double)blocks * threads * iters * 16.0 * 8.0;
+    *tffma = ffma / (ms * 1e-3) / 1e12;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+}  // namespace tcp

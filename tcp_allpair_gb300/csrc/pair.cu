@@ -1,0 +1,600 @@
+// pair.cu -- the all-pair Ewald real-space sum (Force_direct_self /
+// Force_direct_ext / Force_direct_sum of force.f90:52-372 for the whole
+// system on one GPU).
+//
+// Layout.  Particles are species-ordered (electrons, then ions).  A CTA owns
+// a block of i-particles of one species and walks a range of j-tiles; each
+// j-tile holds particles of one species, so the pair type (e-e, e-i, i-i)
+// and the charge product are uniform per (CTA, tile).  j-tiles are copied
+// into shared memory by the bulk-copy engine (cp.async.bulk + mbarrier,
+// kStages-deep ring), released by a CTA barrier per tile.  Every ordered
+// pair (i, j) is evaluated (no Newton-3 reactions, so no atomics); TPP
+// threads share one i-particle and split the tile, and are reduced with
+// warp shuffles at the end.  The j-range of the system is split over
+// gridDim.y CTAs; their per-particle partial forces go to fpart[split][3][n]
+// and are summed in a fixed order by force_finalize (deterministic).
+//
+// FP32C kernel: positions are 32-bit fixed point (2^32 units per box
+// length), so the int32 difference is the minimum image (the DNINT of
+// force.f90:92) exactly and converts to FP32 with relative error 6e-8.
+// rsqrt / reciprocal / exp2 run on the SFU; erfc(x) = exp(-x^2) t Q(t)
+// shares its exponential with the Gaussian force term (fit_erfc.py).  Each
+// thread sums a tile's pair forces in FP32 (<= kTjF/kTppF terms) and folds the
+// tile partial into a (hi, lo) TwoSum accumulator; the final value is
+// hi + lo in FP64.
+//
+// FP64 kernel: the reference's expressions (force.f90:99-110, 130-144,
+// 163-175) in double precision with CUDA's erf/erfc/exp/sqrt.
+#include <algorithm>
+#include <cstdio>
+
+#include "device_util.cuh"
+#include "tcp_internal.h"
+
+namespace tcp {
+
+constexpr int kPairThreads = 256;
+constexpr int kTppF = 4;      // threads per i-particle (FP32)
+constexpr int kTjF = 512;     // particles per j-tile (16 B each)
+constexpr int kStagesF = 3;
+constexpr int kTppD = 2;      // FP64
+constexpr int kTjD = 256;     // 32 B each
+constexpr int kStagesD = 3;
+
+struct PairArgs {
+    const int4 *xq;
+    const double4_32a *xd;
+    int nel, n;
+    int bi;                 // i-particles per CTA
+    int nblk_e, nblk;       // i-blocks (electron blocks first)
+    int tj;                 // particles per j-tile
+    int ntile_e, ntile;     // j-tiles (electron tiles first)
+    int tiles_per_split;
+    double *fpart;          // [gridDim.y][3][n]
+    double *upart;          // [gridDim.y * gridDim.x]
+    unsigned long long *rdf;
+    unsigned *status;
+    PairConsts c;
+};
+
+__device__ __forceinline__ void tile_range(const PairArgs &a, int t, int &j0, int &cnt, int &sj) {
+    if (t < a.ntile_e) {
+        sj = 0;
+        j0 = t * a.tj;
+        cnt = min(a.tj, a.nel - j0);
+    } else {
+        sj = 1;
+        j0 = a.nel + (t - a.ntile_e) * a.tj;
+        cnt = min(a.tj, a.n - j0);
+    }
+}
+
+// t Q(t) with the coefficients printed by fit_erfc.py (P = 0.5, degree 8).
+__device__ __forceinline__ float erfc_poly(float t) {
+    float q = -5.783473762e-02f;
+    q = fmaf(q, t, 2.784859768e-01f);
+    q = fmaf(q, t, -4.744286455e-01f);
+    q = fmaf(q, t, 2.632348585e-01f);
+    q = fmaf(q, t, -1.622527577e-02f);
+    q = fmaf(q, t, 1.981928108e-01f);
+    q = fmaf(q, t, 2.442685012e-01f);
+    q = fmaf(q, t, 2.822102988e-01f);
+    q = fmaf(q, t, 2.820961743e-01f);
+    return q * t;
+}
+
+// One j-tile for one i-particle (FP32).  KIND: 0 Coulomb erfc (e-e, i-i and
+// TCP_EI_COULOMB), 1 Deutsch e-i, 2 Kelbg e-i.  Accumulates sum_j w dx (the
+// force divided by eps q_i q_j) and sum_j u/r (energy / q_i q_j).
+template <int KIND, bool ENERGY, bool RDF, int TPP>
+__device__ __forceinline__ void tile_f32(const int4 *__restrict__ tj, int cnt, int sub, int4 xi,
+                                         const PairConsts &c, float &px, float &py, float &pz,
+                                         float &pe, unsigned *hist, float inv_dx) {
+    const int cnt_up = (cnt + TPP - 1) / TPP * TPP;   // uniform trip count per warp
+#pragma unroll 4
+    for (int jj = sub; jj < cnt_up; jj += TPP) {
+        const int4 xj = tj[jj];
+        const float dx = (float)(xi.x - xj.x) * c.sx;
+        const float dy = (float)(xi.y - xj.y) * c.sy;
+        const float dz = (float)(xi.z - xj.z) * c.sz;
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const bool ok = (jj < cnt) && (r2 < c.rc2f) && (r2 > 0.0f);
+        const float rinv = rsqrt_approx(r2);
+        const float r = r2 * rinv;
+        const float t = rcp_approx(fmaf(c.p_alpha, r, 1.0f));
+        const float e = ex2_approx(c.c_exp * r2);
+        const float erfc_ar = e * erfc_poly(t);
+        float s = fmaf(c.c_gauss * r, e, erfc_ar);      // erfc(ar) + 2ar/sqrt(pi) exp(-a^2r^2)
+        float u = erfc_ar;
+        if (KIND == 1) {                                 // Deutsch, force.f90:136-139
+            const float y = ex2_approx(c.c_rs * r);      // exp(-r/rs)
+            s = fmaf(-y, fmaf(r, c.inv_rs, 1.0f), s);
+            u -= y;
+        }
+        if (KIND == 2) {                                 // Kelbg
+            const bool near = ok && (r2 < c.rshort2);
+            if (__any_sync(0xffffffffu, near)) {
+                const float g = ex2_approx(c.c_lam * r2);      // exp(-r^2/lambda^2)
+                s -= near ? g : 0.0f;
+                if (ENERGY) {
+                    const float t2 = rcp_approx(fmaf(c.p_lam, r, 1.0f));
+                    const float erfc_rl = g * erfc_poly(t2);   // erfc(r/lambda)
+                    u += near ? fmaf(c.sqrtpi_lam * r, erfc_rl, -g) : 0.0f;
+                }
+            }
+        }
+        float w = s * (rinv * rinv) * rinv;
+        w = ok ? w : 0.0f;
+        px = fmaf(w, dx, px);
+        py = fmaf(w, dy, py);
+        pz = fmaf(w, dz, pz);
+        if (ENERGY) pe += ok ? u * rinv : 0.0f;
+        if (RDF) {
+            if (ok) {
+                const int bin = (int)(r * inv_dx);
+                if (bin <= kNdist) atomicAdd(&hist[bin], 1u);
+            }
+        }
+    }
+}
+
+template <int EIKIND, bool ENERGY, bool RDF>
+__global__ void __launch_bounds__(kPairThreads) pair_fp32c_kernel(const PairArgs a) {
+    constexpr int TPP = kTppF;
+    __shared__ __align__(128) int4 tiles[kStagesF][kTjF];
+    __shared__ __align__(8) uint64_t bars[kStagesF];
+    __shared__ unsigned hist[RDF ? 3 * kNbin : 1];
+    __shared__ double red[32];
+
+    const int tid = threadIdx.x;
+    const int b = blockIdx.x;
+    int si, i0, iend;
+    if (b < a.nblk_e) {
+        si = 0;
+        i0 = b * a.bi;
+        iend = a.nel;
+    } else {
+        si = 1;
+        i0 = a.nel + (b - a.nblk_e) * a.bi;
+        iend = a.n;
+    }
+    const int i = i0 + tid / TPP;
+    const int sub = tid % TPP;
+    const bool vi = i < iend;
+    const int4 xi = a.xq[vi ? i : i0];
+
+    const int t0 = blockIdx.y * a.tiles_per_split;
+    const int nt = max(0, min(a.tiles_per_split, a.ntile - t0));
+
+    if (tid == 0) {
+        for (int s = 0; s < kStagesF; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    if (RDF)
+        for (int k = tid; k < 3 * kNbin; k += blockDim.x) hist[k] = 0u;
+    __syncthreads();
+    if (tid == 0) {
+        for (int k = 0; k < min(kStagesF, nt); ++k) {
+            int j0, cnt, sj;
+            tile_range(a, t0 + k, j0, cnt, sj);
+            const uint32_t bytes = (uint32_t)cnt * sizeof(int4);
+            mbar_arrive_expect_tx(&bars[k], bytes);
+            bulk_g2s(tiles[k], a.xq + j0, bytes, &bars[k]);
+        }
+    }
+
+    float fxh = 0.f, fxl = 0.f, fyh = 0.f, fyl = 0.f, fzh = 0.f, fzl = 0.f, eh = 0.f, el = 0.f;
+    int k = 0;
+    for (; k < nt; ++k) {
+        const int stage = k % kStagesF;
+        const bool ok = mbar_wait_bounded(&bars[stage], (uint32_t)((k / kStagesF) & 1), kWaitLimitCycles);
+        int j0, cnt, sj;
+        tile_range(a, t0 + k, j0, cnt, sj);
+        const int pt = si + sj;   // 0 e-e, 1 e-i, 2 i-i
+        float px = 0.f, py = 0.f, pz = 0.f, pe = 0.f;
+        unsigned *h = RDF ? hist + pt * kNbin : nullptr;
+        const float inv_dx = RDF ? a.c.inv_dx[pt] : 0.f;
+        if (pt == 1 && EIKIND == 1)
+            tile_f32<1, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, px, py, pz, pe, h, inv_dx);
+        else if (pt == 1 && EIKIND == 2)
+            tile_f32<2, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, px, py, pz, pe, h, inv_dx);
+        else
+            tile_f32<0, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, px, py, pz, pe, h, inv_dx);
+        const float qq = a.c.qqf[pt];
+        acc2(fxh, fxl, px * qq);
+        acc2(fyh, fyl, py * qq);
+        acc2(fzh, fzl, pz * qq);
+        if (ENERGY) acc2(eh, el, pe * qq);
+        // every thread has finished reading this stage: refill it
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicOr(a.status, kStatusTmaTimeout);
+            break;
+        }
+        if (tid == 0 && k + kStagesF < nt) {
+            int j1, c1, s1;
+            tile_range(a, t0 + k + kStagesF, j1, c1, s1);
+            const uint32_t bytes = (uint32_t)c1 * sizeof(int4);
+            mbar_arrive_expect_tx(&bars[stage], bytes);
+            bulk_g2s(tiles[stage], a.xq + j1, bytes, &bars[stage]);
+        }
+    }
+    if (k < nt) {
+        // timed out: wait (bounded) for the copies still in flight, then leave
+        if (tid == 0)
+            for (int kk = k; kk < min(nt, k + kStagesF); ++kk)
+                mbar_wait_bounded(&bars[kk % kStagesF], (uint32_t)((kk / kStagesF) & 1), kWaitLimitCycles);
+        __syncthreads();
+        return;
+    }
+
+    // reduce the TPP threads of one i-particle
+#pragma unroll
+    for (int o = TPP / 2; o > 0; o >>= 1) {
+        float s, e, h2, l2;
+        h2 = __shfl_xor_sync(0xffffffffu, fxh, o);
+        l2 = __shfl_xor_sync(0xffffffffu, fxl, o);
+        two_sum(fxh, h2, s, e);
+        fxh = s;
+        fxl = fxl + l2 + e;
+        h2 = __shfl_xor_sync(0xffffffffu, fyh, o);
+        l2 = __shfl_xor_sync(0xffffffffu, fyl, o);
+        two_sum(fyh, h2, s, e);
+        fyh = s;
+        fyl = fyl + l2 + e;
+        h2 = __shfl_xor_sync(0xffffffffu, fzh, o);
+        l2 = __shfl_xor_sync(0xffffffffu, fzl, o);
+        two_sum(fzh, h2, s, e);
+        fzh = s;
+        fzl = fzl + l2 + e;
+    }
+    if (vi && sub == 0) {
+        double *fp = a.fpart + (size_t)blockIdx.y * 3 * a.n;
+        fp[i] = kEps * ((double)fxh + (double)fxl);
+        fp[a.n + i] = kEps * ((double)fyh + (double)fyl);
+        fp[2 * a.n + i] = kEps * ((double)fzh + (double)fzl);
+    }
+    if (ENERGY) {
+        const double ed = vi ? (double)eh + (double)el : 0.0;
+        const double tot = block_sum(ed, red);
+        if (tid == 0) a.upart[blockIdx.y * gridDim.x + blockIdx.x] = 0.5 * tot;
+    }
+    if (RDF) {
+        __syncthreads();
+        for (int q = tid; q < 3 * kNbin; q += blockDim.x)
+            if (hist[q]) atomicAdd(&a.rdf[q], (unsigned long long)hist[q]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 kernel
+template <int KIND, bool ENERGY, bool RDF, int TPP>
+__device__ __forceinline__ void tile_f64(const double4_32a *__restrict__ tj, int cnt, int sub, double4_32a xi,
+                                         const PairConsts &c, double qq, double &fx, double &fy,
+                                         double &fz, double &ue, unsigned *hist, double inv_dx) {
+    const double a = c.alpha;
+    for (int jj = sub; jj < cnt; jj += TPP) {
+        const double4_32a xj = tj[jj];
+        double xr0 = xi.x - xj.x, xr1 = xi.y - xj.y, xr2 = xi.z - xj.z;
+        xr0 = xr0 - c.box[0] * round(xr0 / c.box[0]);    // force.f90:92 (DNINT)
+        xr1 = xr1 - c.box[1] * round(xr1 / c.box[1]);
+        xr2 = xr2 - c.box[2] * round(xr2 / c.box[2]);
+        const double r2 = xr0 * xr0 + xr1 * xr1 + xr2 * xr2;
+        if (r2 < c.rc2 && r2 > 0.0) {
+            const double r = sqrt(r2);
+            double df, u;
+            if (KIND == 0) {                                   // force.f90:104-106
+                const double x = 1.0 - erf(a * r);
+                df = kEps * qq * (2.0 * exp(-a * a * r2) * a * r / kSqrtPi + x) / r2 / r;
+                u = qq * x / r;
+            } else if (KIND == 1) {                            // force.f90:135-139
+                const double x = 1.0 - erf(a * r);
+                const double y = exp(-r / c.rs);
+                df = kEps * qq * ((2.0 * exp(-a * a * r2) * a * r / kSqrtPi + x - y) / r2 / r - y / r2 / c.rs);
+                u = qq * (x - y) / r;
+            } else {                                           // Kelbg
+                const double x = erfc(a * r);
+                const double g = exp(-r2 / (c.lambda * c.lambda));
+                df = kEps * qq * (x + 2.0 * a * r / kSqrtPi * exp(-a * a * r2) - g) / (r2 * r);
+                u = qq * (x / r - g / r + kSqrtPi * erfc(r / c.lambda) / c.lambda);
+            }
+            fx += df * xr0;
+            fy += df * xr1;
+            fz += df * xr2;
+            if (ENERGY) ue += u;
+            if (RDF) {
+                const double tb = r * inv_dx;
+                if (tb < (double)kNbin) atomicAdd(&hist[(int)tb], 1u);
+            }
+        }
+    }
+}
+
+template <int EIKIND, bool ENERGY, bool RDF>
+__global__ void __launch_bounds__(kPairThreads) pair_fp64_kernel(const PairArgs a) {
+    constexpr int TPP = kTppD;
+    __shared__ __align__(128) double4_32a tiles[kStagesD][kTjD];
+    __shared__ __align__(8) uint64_t bars[kStagesD];
+    __shared__ unsigned hist[RDF ? 3 * kNbin : 1];
+    __shared__ double red[32];
+
+    const int tid = threadIdx.x;
+    const int b = blockIdx.x;
+    int si, i0, iend;
+    if (b < a.nblk_e) {
+        si = 0;
+        i0 = b * a.bi;
+        iend = a.nel;
+    } else {
+        si = 1;
+        i0 = a.nel + (b - a.nblk_e) * a.bi;
+        iend = a.n;
+    }
+    const int i = i0 + tid / TPP;
+    const int sub = tid % TPP;
+    const bool vi = i < iend;
+    const double4_32a xi = a.xd[vi ? i : i0];
+    const int t0 = blockIdx.y * a.tiles_per_split;
+    const int nt = max(0, min(a.tiles_per_split, a.ntile - t0));
+
+    if (tid == 0) {
+        for (int s = 0; s < kStagesD; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    if (RDF)
+        for (int k = tid; k < 3 * kNbin; k += blockDim.x) hist[k] = 0u;
+    __syncthreads();
+    if (tid == 0) {
+        for (int k = 0; k < min(kStagesD, nt); ++k) {
+            int j0, cnt, sj;
+            tile_range(a, t0 + k, j0, cnt, sj);
+            const uint32_t bytes = (uint32_t)cnt * sizeof(double4_32a);
+            mbar_arrive_expect_tx(&bars[k], bytes);
+            bulk_g2s(tiles[k], a.xd + j0, bytes, &bars[k]);
+        }
+    }
+    double fx = 0.0, fy = 0.0, fz = 0.0, ue = 0.0;
+    int k = 0;
+    for (; k < nt; ++k) {
+        const int stage = k % kStagesD;
+        const bool ok = mbar_wait_bounded(&bars[stage], (uint32_t)((k / kStagesD) & 1), kWaitLimitCycles);
+        int j0, cnt, sj;
+        tile_range(a, t0 + k, j0, cnt, sj);
+        const int pt = si + sj;
+        unsigned *h = RDF ? hist + pt * kNbin : nullptr;
+        const double inv_dx = RDF ? a.c.inv_dxd[pt] : 0.0;
+        const double qq = a.c.qq[pt];
+        if (pt == 1 && EIKIND == 1)
+            tile_f64<1, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx);
+        else if (pt == 1 && EIKIND == 2)
+            tile_f64<2, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx);
+        else
+            tile_f64<0, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicOr(a.status, kStatusTmaTimeout);
+            break;
+        }
+        if (tid == 0 && k + kStagesD < nt) {
+            int j1, c1, s1;
+            tile_range(a, t0 + k + kStagesD, j1, c1, s1);
+            const uint32_t bytes = (uint32_t)c1 * sizeof(double4_32a);
+            mbar_arrive_expect_tx(&bars[stage], bytes);
+            bulk_g2s(tiles[stage], a.xd + j1, bytes, &bars[stage]);
+        }
+    }
+    if (k < nt) {
+        if (tid == 0)
+            for (int kk = k; kk < min(nt, k + kStagesD); ++kk)
+                mbar_wait_bounded(&bars[kk % kStagesD], (uint32_t)((kk / kStagesD) & 1), kWaitLimitCycles);
+        __syncthreads();
+        return;
+    }
+#pragma unroll
+    for (int o = TPP / 2; o > 0; o >>= 1) {
+        fx += __shfl_xor_sync(0xffffffffu, fx, o);
+        fy += __shfl_xor_sync(0xffffffffu, fy, o);
+        fz += __shfl_xor_sync(0xffffffffu, fz, o);
+    }
+    if (vi && sub == 0) {
+        double *fp = a.fpart + (size_t)blockIdx.y * 3 * a.n;
+        fp[i] = fx;
+        fp[a.n + i] = fy;
+        fp[2 * a.n + i] = fz;
+    }
+    if (ENERGY) {
+        const double tot = block_sum(vi ? ue : 0.0, red);
+        if (tid == 0) a.upart[blockIdx.y * gridDim.x + blockIdx.x] = 0.5 * tot;
+    }
+    if (RDF) {
+        __syncthreads();
+        for (int q = tid; q < 3 * kNbin; q += blockDim.x)
+            if (hist[q]) atomicAdd(&a.rdf[q], (unsigned long long)hist[q]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// f = sum over splits of fpart (+ frec: the SPME_SUM add of force.f90:953-964
+// fused); per-block partial sums of f for REMOVE_RIGIDMTN (force.f90:986-993).
+__global__ void force_finalize_kernel(const double *__restrict__ fpart, int nsplit,
+                                      const double *__restrict__ frec, double *__restrict__ f, int n,
+                                      double *__restrict__ fsum_part) {
+    __shared__ double red[32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double s[3] = {0.0, 0.0, 0.0};
+    if (i < n) {
+        for (int k = 0; k < 3; ++k) {
+            double acc = 0.0;
+            for (int sp = 0; sp < nsplit; ++sp) acc += fpart[((size_t)sp * 3 + k) * n + i];
+            if (frec) acc += frec[(size_t)k * n + i];
+            f[(size_t)k * n + i] = acc;
+            s[k] = acc;
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        const double t = block_sum(s[k], red);
+        if (threadIdx.x == 0) fsum_part[k * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+static void make_consts(tcp_ctx *c) {
+    PairConsts &k = c->pc;
+    const tcp_params &p = c->p;
+    const double two32 = 4294967296.0;
+    k.sx = (float)(p.box[0] / two32);
+    k.sy = (float)(p.box[1] / two32);
+    k.sz = (float)(p.box[2] / two32);
+    k.rc2f = (float)c->rc2;
+    const double log2e = 1.4426950408889634;
+    k.c_exp = (float)(-c->alpha * c->alpha * log2e);
+    k.p_alpha = (float)(0.5 * c->alpha);
+    k.c_gauss = (float)(2.0 * c->alpha / kSqrtPi);
+    const double rs = p.rs > 0 ? p.rs : 1.0;
+    k.c_rs = (float)(-log2e / rs);
+    k.inv_rs = (float)(1.0 / rs);
+    const double lam = p.lambda_ei > 0 ? p.lambda_ei : 1.0;
+    k.c_lam = (float)(-log2e / (lam * lam));
+    k.p_lam = (float)(0.5 / lam);
+    k.sqrtpi_lam = (float)(kSqrtPi / lam);
+    k.rshort2 = (float)(36.0 * lam * lam);
+    const double dxs[3] = {p.dx_ee, p.dx_ei, p.dx_ii};
+    const double s = p.charge_scale;
+    const double qq[3] = {s * p.q[0] * s * p.q[0], s * p.q[0] * s * p.q[1], s * p.q[1] * s * p.q[1]};
+    for (int t = 0; t < 3; ++t) {
+        k.inv_dx[t] = dxs[t] > 0 ? (float)(1.0 / dxs[t]) : 0.f;
+        k.inv_dxd[t] = dxs[t] > 0 ? 1.0 / dxs[t] : 0.0;
+        k.qqf[t] = (float)qq[t];
+        k.qq[t] = qq[t];
+    }
+    for (int d = 0; d < 3; ++d) k.box[d] = p.box[d];
+    k.rc2 = c->rc2;
+    k.alpha = c->alpha;
+    k.rs = rs;
+    k.lambda = lam;
+    k.ei_model = p.ei_model;
+}
+
+static int ceil_div(int a, int b) { return (a + b - 1) / b; }
+
+struct Geometry {
+    int bi, tj, nblk_e, nblk, ntile_e, ntile;
+};
+
+static Geometry geometry(const tcp_ctx *c, bool fp64) {
+    Geometry g;
+    g.bi = kPairThreads / (fp64 ? kTppD : kTppF);
+    g.tj = fp64 ? kTjD : kTjF;
+    g.nblk_e = ceil_div(c->nel, g.bi);
+    g.nblk = g.nblk_e + ceil_div(c->nion, g.bi);
+    g.ntile_e = ceil_div(c->nel, g.tj);
+    g.ntile = g.ntile_e + ceil_div(c->nion, g.tj);
+    return g;
+}
+
+// Number of j-splits: fill the GPU with whole waves of CTAs.
+static int choose_jsplit(const tcp_ctx *c, const Geometry &g, int blocks_per_sm) {
+    const int slots = std::max(1, c->num_sms * std::max(1, blocks_per_sm));
+    int best = 1;
+    double best_eff = -1.0;
+    for (int s = 1; s <= std::min(g.ntile, 64); ++s) {
+        const int tps = ceil_div(g.ntile, s);
+        const int s_eff = ceil_div(g.ntile, tps);
+        const double waves = (double)g.nblk * s_eff / slots;
+        // efficiency: wave quantisation times tile-split balance
+        const double eff = waves / std::ceil(waves) * ((double)g.ntile / (double)(tps * s_eff));
+        if (eff > best_eff + 0.02) {
+            best_eff = eff;
+            best = s_eff;
+        }
+    }
+    return best;
+}
+
+int pair_setup(tcp_ctx *c) {
+    make_consts(c);
+    const bool fp64 = c->p.precision == TCP_PREC_FP64;
+    Geometry g = geometry(c, fp64);
+    int bps = 1;
+    if (fp64)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp64_kernel<0, true, false>, kPairThreads, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp32c_kernel<2, true, false>, kPairThreads, 0);
+    const char *env = getenv("TCP_JSPLIT");
+    int js = env ? atoi(env) : choose_jsplit(c, g, bps);
+    js = std::max(1, std::min(js, g.ntile));
+    const int tps = ceil_div(g.ntile, js);
+    js = ceil_div(g.ntile, tps);
+    if (c->fpart) cudaFree(c->fpart);
+    if (c->upart) cudaFree(c->upart);
+    c->fpart = nullptr;
+    c->upart = nullptr;
+    c->jsplit = js;
+    c->n_upart = g.nblk * js;
+    TCP_CUDA(cudaMalloc(&c->fpart, sizeof(double) * 3 * (size_t)c->n * js));
+    TCP_CUDA(cudaMalloc(&c->upart, sizeof(double) * (size_t)c->n_upart));
+    TCP_CUDA(cudaMemsetAsync(c->upart, 0, sizeof(double) * (size_t)c->n_upart, c->stream));
+    return TCP_OK;
+}
+
+int launch_pair(tcp_ctx *c, bool energy, bool rdf) {
+    const bool fp64 = c->p.precision == TCP_PREC_FP64;
+    Geometry g = geometry(c, fp64);
+    PairArgs a;
+    a.xq = c->xq;
+    a.xd = c->xd;
+    a.nel = c->nel;
+    a.n = c->n;
+    a.bi = g.bi;
+    a.nblk_e = g.nblk_e;
+    a.nblk = g.nblk;
+    a.tj = g.tj;
+    a.ntile_e = g.ntile_e;
+    a.ntile = g.ntile;
+    a.tiles_per_split = ceil_div(g.ntile, c->jsplit);
+    a.fpart = c->fpart;
+    a.upart = c->upart;
+    a.rdf = c->rdf;
+    a.status = c->status;
+    a.c = c->pc;
+    dim3 grid(g.nblk, c->jsplit);
+    const int ei = c->p.ei_model == TCP_EI_DEUTSCH ? 1 : (c->p.ei_model == TCP_EI_KELBG ? 2 : 0);
+#define TCP_PAIR_DISPATCH(KERNEL)                                                                \
+    do {                                                                                         \
+        if (ei == 0) {                                                                           \
+            if (energy && rdf) KERNEL<0, true, true><<<grid, kPairThreads, 0, c->stream>>>(a);   \
+            else if (energy) KERNEL<0, true, false><<<grid, kPairThreads, 0, c->stream>>>(a);    \
+            else if (rdf) KERNEL<0, false, true><<<grid, kPairThreads, 0, c->stream>>>(a);       \
+            else KERNEL<0, false, false><<<grid, kPairThreads, 0, c->stream>>>(a);               \
+        } else if (ei == 1) {                                                                    \
+            if (energy && rdf) KERNEL<1, true, true><<<grid, kPairThreads, 0, c->stream>>>(a);   \
+            else if (energy) KERNEL<1, true, false><<<grid, kPairThreads, 0, c->stream>>>(a);    \
+            else if (rdf) KERNEL<1, false, true><<<grid, kPairThreads, 0, c->stream>>>(a);       \
+            else KERNEL<1, false, false><<<grid, kPairThreads, 0, c->stream>>>(a);               \
+        } else {                                                                                 \
+            if (energy && rdf) KERNEL<2, true, true><<<grid, kPairThreads, 0, c->stream>>>(a);   \
+            else if (energy) KERNEL<2, true, false><<<grid, kPairThreads, 0, c->stream>>>(a);    \
+            else if (rdf) KERNEL<2, false, true><<<grid, kPairThreads, 0, c->stream>>>(a);       \
+            else KERNEL<2, false, false><<<grid, kPairThreads, 0, c->stream>>>(a);               \
+        }                                                                                        \
+    } while (0)
+    if (fp64)
+        TCP_PAIR_DISPATCH(pair_fp64_kernel);
+    else
+        TCP_PAIR_DISPATCH(pair_fp32c_kernel);
+#undef TCP_PAIR_DISPATCH
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+int launch_force_finalize(tcp_ctx *c, bool add_rec) {
+    const int threads = 256;
+    const int blocks = ceil_div(c->n, threads);
+    force_finalize_kernel<<<blocks, threads, 0, c->stream>>>(c->fpart, c->jsplit, add_rec ? c->frec : nullptr,
+                                                             c->f, c->n, c->red);
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+}  // namespace tcp

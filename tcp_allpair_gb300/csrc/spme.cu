@@ -1,0 +1,452 @@
+// spme.cu -- reciprocal-space sums: smooth PME (Force_SPME4, force.f90:652-929,
+// generalised to B-spline order 4..8) and the plain Ewald k-sum.
+//
+// Mesh layout: Q[iz][iy][ix] (ix fastest, the Fortran order of Q(ix,iy,iz)),
+// FP64.  The 3-D FFT is cuFFT D2Z / Z2D on that layout (the only library
+// call of the path); spreading, the influence-function multiply fused with
+// the energy reduction, and the force gather are kernels of this file.
+//
+// Normalisation: both transforms are unnormalised, so the real mesh after the
+// inverse transform is phi = K^3 Qfin of the reference; its 1/K^3 (FFTE
+// iopt=+1) and K^3 (force.f90:864-865) cancel, giving
+//   Um = eps/(2 pi V) sum_m theta(m) B(m) |S(m)|^2          (force.f90:921)
+//   F_i = -eps/(pi V) sum_k dQ(k)/dx_i phi(k)              (force.f90:882-887)
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "device_util.cuh"
+#include "tcp_internal.h"
+
+namespace tcp {
+
+struct SpmeArgs {
+    const double *x;     // SoA [3][n]
+    int nel, n;
+    double q0, q1;       // scaled charges per species
+    double box0, box1, box2;
+    int K1, K2, K3;
+};
+
+// B-spline weights W[j] = M_P(w + P-1-j) and dW[j] = dM_P/du on the grid
+// points INT(u) + j - (P-3).  Order 4 uses the reference's explicit cubics
+// (force.f90:703-738); other orders the Cox-de Boor recursion run upward on
+// the P nonzero values.
+template <int P>
+__device__ __forceinline__ void spline_w(double u, double *W, double *dW) {
+    if (P == 4) {
+        double z = trunc(u) - u + 1.0;
+        W[0] = z * z * z / 6.0;
+        dW[0] = -3. * z * z / 6.0;
+        z += 1.0;
+        W[1] = (-3. * z * z * z + 12. * z * z - 12. * z + 4.) / 6.0;
+        dW[1] = (9. * z * z - 24. * z + 12.) / 6.0;
+        z += 1.0;
+        W[2] = (3. * z * z * z - 24. * z * z + 60. * z - 44.) / 6.0;
+        dW[2] = (-9. * z * z + 48. * z - 60.) / 6.0;
+        z += 1.0;
+        W[3] = (-z * z * z + 12. * z * z - 48. * z + 64.) / 6.0;
+        dW[3] = (3. * z * z - 24. * z + 48.) / 6.0;
+        return;
+    }
+    const double w = u - trunc(u);
+    double a[P];
+    a[0] = 1.0;
+#pragma unroll
+    for (int j = 1; j < P; ++j) a[j] = 0.0;
+    // a_n[j] = ((w+n-1-j) a_{n-1}[j-1] + (1-w+j) a_{n-1}[j]) / (n-1)
+#pragma unroll
+    for (int nn = 2; nn <= P; ++nn) {
+        if (nn == P) {
+#pragma unroll
+            for (int j = 0; j < P; ++j) dW[j] = (j > 0 ? a[j - 1] : 0.0) - (j < P - 1 ? a[j] : 0.0);
+        }
+        const double inv = 1.0 / (double)(nn - 1);
+#pragma unroll
+        for (int j = nn - 1; j >= 0; --j) {
+            const double left = j > 0 ? a[j - 1] : 0.0;
+            const double right = j < nn - 1 ? a[j] : 0.0;
+            a[j] = ((w + nn - 1 - j) * left + (1.0 - w + j) * right) * inv;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < P; ++j) W[j] = a[j];
+}
+
+__device__ __forceinline__ int wrapi(int i, int K) {
+    i %= K;
+    return i < 0 ? i + K : i;
+}
+
+// charge spreading, force.f90:697-820 (atomic FP64 adds into the mesh)
+template <int P>
+__global__ void spme_spread_kernel(const SpmeArgs a, double *__restrict__ Q) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= a.n) return;
+    const double q = m < a.nel ? a.q0 : a.q1;
+    const double L[3] = {a.box0, a.box1, a.box2};
+    const int K[3] = {a.K1, a.K2, a.K3};
+    double W[3][P], dW[3][P];
+    int base[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];   // :700-702
+        spline_w<P>(u, W[d], dW[d]);
+        base[d] = (int)trunc(u) - (P - 3);
+    }
+#pragma unroll 1
+    for (int k = 0; k < P; ++k) {
+        const int iz = wrapi(base[2] + k, a.K3);
+#pragma unroll 1
+        for (int j = 0; j < P; ++j) {
+            const int iy = wrapi(base[1] + j, a.K2);
+            const double qyz = q * W[1][j] * W[2][k];
+            double *row = Q + (size_t)a.K1 * (iy + (size_t)a.K2 * iz);
+#pragma unroll
+            for (int i = 0; i < P; ++i) atomicAdd(row + wrapi(base[0] + i, a.K1), qyz * W[0][i]);
+        }
+    }
+}
+
+// Qk *= theta B; energy partial sum_m w_m theta B |Qk|^2 (w = 2 for the
+// kx columns that stand for a conjugate pair in the half spectrum).
+__global__ void spme_influence_kernel(cufftDoubleComplex *__restrict__ Qk, const double *__restrict__ infl,
+                                      long total, int Kh, int K1, double *__restrict__ epart, bool energy) {
+    __shared__ double red[32];
+    double e = 0.0;
+    for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+        const double g = infl[idx];
+        cufftDoubleComplex z = Qk[idx];
+        if (energy) {
+            const int kx = (int)(idx % Kh);
+            const double wgt = (kx == 0 || (2 * kx == K1)) ? 1.0 : 2.0;
+            e += wgt * g * (z.x * z.x + z.y * z.y);
+        }
+        z.x *= g;
+        z.y *= g;
+        Qk[idx] = z;
+    }
+    if (energy) {
+        const double t = block_sum(e, red);
+        if (threadIdx.x == 0) epart[blockIdx.x] = t;
+    }
+}
+
+// force gather, force.f90:868-919
+template <int P>
+__global__ void spme_gather_kernel(const SpmeArgs a, const double *__restrict__ phi, double coef,
+                                   double *__restrict__ frec) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= a.n) return;
+    const double q = m < a.nel ? a.q0 : a.q1;
+    const double L[3] = {a.box0, a.box1, a.box2};
+    const int K[3] = {a.K1, a.K2, a.K3};
+    double W[3][P], dW[3][P];
+    int base[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];
+        spline_w<P>(u, W[d], dW[d]);
+        base[d] = (int)trunc(u) - (P - 3);
+    }
+    double gx = 0.0, gy = 0.0, gz = 0.0;
+#pragma unroll 1
+    for (int k = 0; k < P; ++k) {
+        const int iz = wrapi(base[2] + k, a.K3);
+#pragma unroll 1
+        for (int j = 0; j < P; ++j) {
+            const int iy = wrapi(base[1] + j, a.K2);
+            const double *row = phi + (size_t)a.K1 * (iy + (size_t)a.K2 * iz);
+            double sx = 0.0, sd = 0.0;
+#pragma unroll
+            for (int i = 0; i < P; ++i) {
+                const double ph = row[wrapi(base[0] + i, a.K1)];
+                sx += dW[0][i] * ph;
+                sd += W[0][i] * ph;
+            }
+            gx += sx * W[1][j] * W[2][k];
+            gy += sd * dW[1][j] * W[2][k];
+            gz += sd * W[1][j] * dW[2][k];
+        }
+    }
+    // F = -eps/(pi V) q (K_d/L_d) sum dW W W phi
+    frec[m] = -coef * q * gx * ((double)a.K1 / a.box0);
+    frec[(size_t)a.n + m] = -coef * q * gy * ((double)a.K2 / a.box1);
+    frec[2 * (size_t)a.n + m] = -coef * q * gz * ((double)a.K3 / a.box2);
+}
+
+__global__ void sum_partials_kernel(const double *__restrict__ part, int np, double scale,
+                                    double *__restrict__ out) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) *out = s * scale;
+}
+
+// ---- plain Ewald k-sum ------------------------------------------------------
+// S(m) = sum_j q_j exp(2 pi i m.x_j) per k-vector (one CTA per vector)
+__global__ void ewald_sfac_kernel(const double *__restrict__ x, int nel, int n, double q0, double q1,
+                                  const double *__restrict__ kvec, double *__restrict__ ksum,
+                                  double *__restrict__ epart) {
+    __shared__ double red[32];
+    const double mx = kvec[4 * blockIdx.x], my = kvec[4 * blockIdx.x + 1], mz = kvec[4 * blockIdx.x + 2];
+    double sr = 0.0, si = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double q = j < nel ? q0 : q1;
+        const double ph = 2.0 * kPi * (mx * x[j] + my * x[(size_t)n + j] + mz * x[2 * (size_t)n + j]);
+        double s, c;
+        sincos(ph, &s, &c);
+        sr += q * c;
+        si += q * s;
+    }
+    sr = block_sum(sr, red);
+    si = block_sum(si, red);
+    if (threadIdx.x == 0) {
+        ksum[2 * blockIdx.x] = sr;
+        ksum[2 * blockIdx.x + 1] = si;
+        epart[blockIdx.x] = kvec[4 * blockIdx.x + 3] * (sr * sr + si * si);
+    }
+}
+
+// F_i = (2 eps q_i / V) sum_m theta m Im(conj(S) e^{i phase})
+__global__ void ewald_force_kernel(const double *__restrict__ x, int nel, int n, double q0, double q1,
+                                   const double *__restrict__ kvec, const double *__restrict__ ksum, int nk,
+                                   double coef, double *__restrict__ frec) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double q = i < nel ? q0 : q1;
+    const double xi = x[i], yi = x[(size_t)n + i], zi = x[2 * (size_t)n + i];
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    for (int k = 0; k < nk; ++k) {
+        const double mx = kvec[4 * k], my = kvec[4 * k + 1], mz = kvec[4 * k + 2], th = kvec[4 * k + 3];
+        double s, c;
+        sincos(2.0 * kPi * (mx * xi + my * yi + mz * zi), &s, &c);
+        const double im = (ksum[2 * k] * s - ksum[2 * k + 1] * c) * th;
+        fx += im * mx;
+        fy += im * my;
+        fz += im * mz;
+    }
+    frec[i] = coef * q * fx;
+    frec[(size_t)n + i] = coef * q * fy;
+    frec[2 * (size_t)n + i] = coef * q * fz;
+}
+
+// ---------------------------------------------------------------------------
+static double bspline_M(int n, double y) {
+    if (y <= 0.0 || y >= (double)n) return 0.0;
+    if (n == 2) return 1.0 - std::fabs(y - 1.0);
+    return (y * bspline_M(n - 1, y) + ((double)n - y) * bspline_M(n - 1, y - 1.0)) / (double)(n - 1);
+}
+
+// |b(m)|^-2 per axis (36/(4+2cos)^2 for order 4, force.f90:834-839); odd
+// orders vanish at the Nyquist index, where the mean of the neighbours is used.
+static std::vector<double> bspline_moduli(int order, int K) {
+    std::vector<double> den(K), out(K);
+    for (int m = 0; m < K; ++m) {
+        if (order == 4) {
+            const double z = 4.0 + 2.0 * std::cos(2.0 * kPi * m / K);
+            den[m] = z * z / 36.0;
+            continue;
+        }
+        double re = 0.0, im = 0.0;
+        for (int k = 0; k <= order - 2; ++k) {
+            const double mk = bspline_M(order, (double)(k + 1));
+            re += mk * std::cos(2.0 * kPi * m * k / K);
+            im += mk * std::sin(2.0 * kPi * m * k / K);
+        }
+        den[m] = re * re + im * im;
+    }
+    for (int m = 0; m < K; ++m)
+        if (den[m] < 1e-7) den[m] = 0.5 * (den[(m - 1 + K) % K] + den[(m + 1) % K]);
+    for (int m = 0; m < K; ++m) out[m] = 1.0 / den[m];
+    return out;
+}
+
+int spme_free(tcp_ctx *c) {
+    if (c->plans) {
+        cufftDestroy(c->plan_f);
+        cufftDestroy(c->plan_b);
+        c->plans = false;
+    }
+    cudaFree(c->Q);
+    cudaFree(c->Qk);
+    cudaFree(c->infl);
+    c->Q = nullptr;
+    c->Qk = nullptr;
+    c->infl = nullptr;
+    return TCP_OK;
+}
+
+static int spme_energy_blocks(const tcp_ctx *c) {
+    const long total = (long)c->K3 * c->K2 * c->Kh;
+    return (int)std::min<long>((total + 255) / 256, 4096);
+}
+
+int spme_setup(tcp_ctx *c) {
+    const tcp_params &p = c->p;
+    c->K1 = p.K[0];
+    c->K2 = p.K[1];
+    c->K3 = p.K[2];
+    c->Kh = c->K1 / 2 + 1;
+    const size_t nreal = (size_t)c->K1 * c->K2 * c->K3;
+    const size_t nhalf = (size_t)c->Kh * c->K2 * c->K3;
+    if (!c->Q) {
+        if (cudaMalloc(&c->Q, sizeof(double) * nreal) != cudaSuccess ||
+            cudaMalloc(&c->Qk, sizeof(cufftDoubleComplex) * nhalf) != cudaSuccess ||
+            cudaMalloc(&c->infl, sizeof(double) * nhalf) != cudaSuccess)
+            return set_error(TCP_ERR_NOMEM, "SPME mesh allocation failed");
+    }
+    if (!c->plans) {
+        if (cufftPlan3d(&c->plan_f, c->K3, c->K2, c->K1, CUFFT_D2Z) != CUFFT_SUCCESS)
+            return set_error(TCP_ERR_CUFFT, "cufftPlan3d D2Z failed");
+        if (cufftPlan3d(&c->plan_b, c->K3, c->K2, c->K1, CUFFT_Z2D) != CUFFT_SUCCESS) {
+            cufftDestroy(c->plan_f);
+            return set_error(TCP_ERR_CUFFT, "cufftPlan3d Z2D failed");
+        }
+        cufftSetStream(c->plan_f, c->stream);
+        cufftSetStream(c->plan_b, c->stream);
+        c->plans = true;
+    }
+    // theta(m) = exp(-pi^2 m^2/a^2)/m^2 (EWALD_SELF, force.f90:27-42) times
+    // the B-spline moduli, on the half spectrum; theta(0) = 0.
+    std::vector<double> bx = bspline_moduli(p.order, c->K1), by = bspline_moduli(p.order, c->K2),
+                        bz = bspline_moduli(p.order, c->K3);
+    std::vector<double> h(nhalf);
+    const double a2 = c->alpha * c->alpha;
+    for (int k = 0; k < c->K3; ++k) {
+        const int iz = (k + c->K3 / 2) % c->K3 - c->K3 / 2;
+        for (int j = 0; j < c->K2; ++j) {
+            const int iy = (j + c->K2 / 2) % c->K2 - c->K2 / 2;
+            for (int i = 0; i < c->Kh; ++i) {
+                const int ix = (i + c->K1 / 2) % c->K1 - c->K1 / 2;
+                const size_t idx = i + (size_t)c->Kh * (j + (size_t)c->K2 * k);
+                if (ix == 0 && iy == 0 && iz == 0) {
+                    h[idx] = 0.0;
+                    continue;
+                }
+                const double m2 = (double)ix * ix / (p.box[0] * p.box[0]) + (double)iy * iy / (p.box[1] * p.box[1]) +
+                                  (double)iz * iz / (p.box[2] * p.box[2]);
+                h[idx] = std::exp(-m2 * kPi * kPi / a2) / m2 * bx[i] * by[j] * bz[k];
+            }
+        }
+    }
+    TCP_CUDA(cudaMemcpyAsync(c->infl, h.data(), sizeof(double) * nhalf, cudaMemcpyHostToDevice, c->stream));
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    return TCP_OK;
+}
+
+static SpmeArgs spme_args(const tcp_ctx *c) {
+    SpmeArgs a;
+    a.x = c->x;
+    a.nel = c->nel;
+    a.n = c->n;
+    a.q0 = c->p.charge_scale * c->p.q[0];
+    a.q1 = c->p.charge_scale * c->p.q[1];
+    a.box0 = c->p.box[0];
+    a.box1 = c->p.box[1];
+    a.box2 = c->p.box[2];
+    a.K1 = c->K1;
+    a.K2 = c->K2;
+    a.K3 = c->K3;
+    return a;
+}
+
+template <int P>
+static void launch_spread_gather(tcp_ctx *c, const SpmeArgs &a, bool gather, double coef) {
+    const int threads = 128, blocks = (c->n + threads - 1) / threads;
+    if (!gather)
+        spme_spread_kernel<P><<<blocks, threads, 0, c->stream>>>(a, c->Q);
+    else
+        spme_gather_kernel<P><<<blocks, threads, 0, c->stream>>>(a, c->Q, coef, c->frec);
+}
+
+static void spread_gather(tcp_ctx *c, const SpmeArgs &a, bool gather, double coef) {
+    switch (c->p.order) {
+        case 4: launch_spread_gather<4>(c, a, gather, coef); break;
+        case 5: launch_spread_gather<5>(c, a, gather, coef); break;
+        case 6: launch_spread_gather<6>(c, a, gather, coef); break;
+        case 7: launch_spread_gather<7>(c, a, gather, coef); break;
+        default: launch_spread_gather<8>(c, a, gather, coef); break;
+    }
+}
+
+// the red[] region after the force and kinetic partials holds the energy partials
+double *recip_epart(tcp_ctx *c);
+
+int launch_spme(tcp_ctx *c, bool energy) {
+    const SpmeArgs a = spme_args(c);
+    const size_t nreal = (size_t)c->K1 * c->K2 * c->K3;
+    TCP_CUDA(cudaMemsetAsync(c->Q, 0, sizeof(double) * nreal, c->stream));
+    spread_gather(c, a, false, 0.0);
+    c->launches++;
+    if (cufftExecD2Z(c->plan_f, c->Q, c->Qk) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecD2Z failed");
+    const long total = (long)c->K3 * c->K2 * c->Kh;
+    const int eb = spme_energy_blocks(c);
+    double *epart = recip_epart(c);
+    spme_influence_kernel<<<eb, 256, 0, c->stream>>>(c->Qk, c->infl, total, c->Kh, c->K1, epart, energy);
+    c->launches++;
+    if (cufftExecZ2D(c->plan_b, c->Qk, c->Q) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecZ2D failed");
+    spread_gather(c, a, true, kEps / (kPi * c->V));
+    c->launches++;
+    if (energy) {
+        sum_partials_kernel<<<1, 1024, 0, c->stream>>>(epart, eb, kEps / (2.0 * kPi * c->V), c->scal + kScalUm);
+        c->launches++;
+    }
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+int ewald_setup(tcp_ctx *c) {
+    const tcp_params &p = c->p;
+    const int nmax2 = p.ewald_nmax2;
+    const int nm = (int)std::floor(std::sqrt((double)nmax2));
+    std::vector<double> kv;
+    for (int n3 = -nm; n3 <= nm; ++n3)
+        for (int n2 = -nm; n2 <= nm; ++n2)
+            for (int n1 = -nm; n1 <= nm; ++n1) {
+                const int nn = n1 * n1 + n2 * n2 + n3 * n3;
+                if (nn == 0 || nn > nmax2) continue;
+                const double m[3] = {n1 / p.box[0], n2 / p.box[1], n3 / p.box[2]};
+                const double m2 = m[0] * m[0] + m[1] * m[1] + m[2] * m[2];
+                kv.push_back(m[0]);
+                kv.push_back(m[1]);
+                kv.push_back(m[2]);
+                kv.push_back(std::exp(-m2 * kPi * kPi / (c->alpha * c->alpha)) / m2);
+            }
+    c->nk = (int)(kv.size() / 4);
+    if (c->nk > c->red_cap - 7 * kick_blocks(c->n))
+        return set_error(TCP_ERR_BAD_PARAM, "ewald_nmax2 too large: more k-vectors than the energy buffer holds");
+    cudaFree(c->kvec);
+    cudaFree(c->ksum);
+    c->kvec = nullptr;
+    c->ksum = nullptr;
+    if (c->nk == 0) return TCP_OK;
+    TCP_CUDA(cudaMalloc(&c->kvec, sizeof(double) * kv.size()));
+    TCP_CUDA(cudaMalloc(&c->ksum, sizeof(double) * 2 * (size_t)c->nk));
+    TCP_CUDA(cudaMemcpyAsync(c->kvec, kv.data(), sizeof(double) * kv.size(), cudaMemcpyHostToDevice, c->stream));
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    return TCP_OK;
+}
+
+int launch_ewald(tcp_ctx *c, bool energy) {
+    if (c->nk == 0) {
+        TCP_CUDA(cudaMemsetAsync(c->frec, 0, sizeof(double) * 3 * (size_t)c->n, c->stream));
+        TCP_CUDA(cudaMemsetAsync(c->scal + kScalUm, 0, sizeof(double), c->stream));
+        return TCP_OK;
+    }
+    const double q0 = c->p.charge_scale * c->p.q[0], q1 = c->p.charge_scale * c->p.q[1];
+    double *epart = recip_epart(c);
+    ewald_sfac_kernel<<<c->nk, 256, 0, c->stream>>>(c->x, c->nel, c->n, q0, q1, c->kvec, c->ksum, epart);
+    ewald_force_kernel<<<(c->n + 127) / 128, 128, 0, c->stream>>>(c->x, c->nel, c->n, q0, q1, c->kvec, c->ksum,
+                                                                  c->nk, 2.0 * kEps / c->V, c->frec);
+    c->launches += 2;
+    if (energy) {
+        sum_partials_kernel<<<1, 1024, 0, c->stream>>>(epart, c->nk, kEps / (2.0 * kPi * c->V), c->scal + kScalUm);
+        c->launches++;
+    }
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+}  // namespace tcp

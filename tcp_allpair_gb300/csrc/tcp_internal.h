@@ -1,0 +1,157 @@
+// tcp_internal.h -- device data layout, context and kernel interfaces of
+// libtcpgpu.so (not part of the public ABI; see include/tcp_gpu.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "tcp_gpu.h"
+
+namespace tcp {
+
+constexpr double kEps = 14.399644154020082;     // data.f90:21
+constexpr double kPi = 3.1415926535897931;       // data.f90:23
+constexpr double kSqrtPi = 1.7724538509055159;   // data.f90:24
+constexpr int kNdist = 500;                      // data.f90:16
+constexpr int kNbin = kNdist + 1;
+constexpr int kMaxOrder = 8;
+
+// status word bits written by kernels (ctx->d_status)
+constexpr unsigned kStatusTmaTimeout = 1u;
+
+// ---------------------------------------------------------------------------
+// Pair-kernel constants (host-computed once per parameter change).
+struct PairConsts {
+    // FP32 path: fixed-point positions are 2^32 units per box length
+    float sx, sy, sz;          // box / 2^32
+    float rc2f;                // cut-off^2
+    float c_exp;               // -alpha^2 log2(e): exp(-a^2 r^2) = ex2(c_exp r^2)
+    float p_alpha;             // 0.5 alpha: t = 1/(1 + 0.5 alpha r)
+    float c_gauss;             // 2 alpha / sqrt(pi)
+    float c_rs;                // Deutsch: -log2(e)/rs
+    float inv_rs;              // 1/rs
+    float c_lam;               // Kelbg: -log2(e)/lambda^2
+    float p_lam;               // 0.5/lambda
+    float sqrtpi_lam;          // sqrt(pi)/lambda
+    float rshort2;             // (6 lambda)^2: Kelbg Gaussian terms below FP64 resolution beyond
+    float inv_dx[3];           // RDF 1/dx per pair type ee|ei|ii
+    float qqf[3];              // q_i q_j s^2 per pair type (energy/force sign and scale)
+    // FP64 path
+    double box[3];
+    double rc2, alpha, rs, lambda;
+    double inv_dxd[3];
+    double qq[3];
+    int ei_model;
+};
+
+// ---------------------------------------------------------------------------
+struct Ctx;
+
+}  // namespace tcp
+
+struct tcp_ctx {
+    tcp_params p;
+    int nel = 0, nion = 0, n = 0;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    unsigned flags = TCP_FLAG_ENERGY;
+    bool ewald_ready = false;
+    double alpha = 0, rc2 = 0, Uo = 0, V = 0;
+    tcp::PairConsts pc{};
+
+    // particle state, SoA [3][n]
+    double *x = nullptr, *v = nullptr, *f = nullptr, *frec = nullptr;
+    int4 *xq = nullptr;        // fixed-point positions for the FP32 pair kernel
+    double4_32a *xd = nullptr;     // FP64 positions for the FP64 pair kernel
+    // pair-kernel partials
+    int jsplit = 1;
+    double *fpart = nullptr;   // [jsplit][3][n]
+    double *upart = nullptr;   // energy partial per pair block
+    int n_upart = 0;
+    // reductions
+    double *red = nullptr;     // block partials (size red_cap)
+    int red_cap = 0;
+    double *scal = nullptr;    // device scalars, see kScal* below
+    double *h_scal = nullptr;  // pinned host copy
+    unsigned *status = nullptr;
+    unsigned long long *rdf = nullptr;  // [3][kNbin]
+    unsigned long long *vdf = nullptr;  // [2][kNbin]
+    // staging for host transfers
+    unsigned char *d_stage = nullptr;
+    size_t d_stage_bytes = 0;
+    double *h_stage = nullptr;          // pinned
+    size_t h_stage_bytes = 0;
+    // SPME
+    int K1 = 0, K2 = 0, K3 = 0, Kh = 0; // Kh = K1/2+1
+    double *Q = nullptr;                // real mesh [K3][K2][K1]
+    cufftDoubleComplex *Qk = nullptr;   // [K3][K2][Kh]
+    double *infl = nullptr;             // theta * |b|^-2 on the half mesh
+    cufftHandle plan_f = 0, plan_b = 0;
+    bool plans = false;
+    // plain Ewald
+    int nk = 0;
+    double *kvec = nullptr;             // [nk][4]: m_x, m_y, m_z, theta
+    double *ksum = nullptr;             // [nk][2]: S re, im
+    // graph of one md step
+    cudaGraphExec_t graph = nullptr;
+    double graph_dt = 0.0;
+    unsigned graph_flags = 0;
+    int graph_kernels = 0;
+    long long launches = 0;
+    long long step_index = 0;
+    tcp_energies last{};
+};
+
+namespace tcp {
+
+// indices into ctx->scal
+enum {
+    kScalUr = 0, kScalUm = 1, kScalMv2e = 2, kScalMv2i = 3,
+    kScalFx = 4, kScalFy = 5, kScalFz = 6, kScalLamE = 7, kScalLamI = 8, kScalStep = 9,
+    kScalCount = 16
+};
+
+int set_error(int code, const std::string &msg);
+int cuda_check(cudaError_t e, const char *what);
+#define TCP_CUDA(call)                                        \
+    do {                                                      \
+        cudaError_t _e = (call);                              \
+        if (_e != cudaSuccess) return tcp::cuda_check(_e, #call); \
+    } while (0)
+
+// pair.cu
+int pair_setup(tcp_ctx *c);                        // constants, jsplit, partial buffers
+int launch_pair(tcp_ctx *c, bool energy, bool rdf);
+int launch_force_finalize(tcp_ctx *c, bool add_rec);
+// spme.cu
+int spme_setup(tcp_ctx *c);                        // meshes, plans, influence function
+int spme_free(tcp_ctx *c);
+int launch_spme(tcp_ctx *c, bool energy);
+int ewald_setup(tcp_ctx *c);
+int launch_ewald(tcp_ctx *c, bool energy);
+// integrate.cu
+double *fsum_part(tcp_ctx *c);
+double *mv_part(tcp_ctx *c, int pass);
+double *recip_epart(tcp_ctx *c);
+int red_capacity(int n, int extra);
+int kick_blocks(int n);
+int launch_refresh_positions(tcp_ctx *c);
+int launch_shift(tcp_ctx *c, double sdt);
+int launch_vverlet1(tcp_ctx *c, double dt, double unused);
+int launch_spme_sum(tcp_ctx *c);
+int launch_fsum(tcp_ctx *c);
+int launch_remove_rigid(tcp_ctx *c);
+int launch_kick2(tcp_ctx *c, double dt, bool remove_net, bool apply_thermo, bool vdf, int *final_pass);
+int launch_reduce(tcp_ctx *c, int mask, int pass);
+int launch_extract(tcp_ctx *c, int first, int count, long stride, long off_x, long off_v, long off_f);
+int launch_pack(tcp_ctx *c, int first, int count, bool x, bool v, bool f, bool frec, int *nf);
+int launch_fp32_peak(int device, double *tffma);
+
+// reduce targets for launch_reduce
+enum { kRedUr = 1, kRedMv2 = 4 };
+
+}  // namespace tcp

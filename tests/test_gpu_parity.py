@@ -1,0 +1,226 @@
+"""CUDA library (through the C ABI) vs the FP64 oracle on identical seeded inputs.
+
+Tolerances: the FP64 kernels agree with the oracle to summation-order
+rounding (1e-11 relative); the compensated-FP32 pair kernel meets the
+RMS relative force error bound 2e-6 of the FP32 path.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import tcp_allpair_gb300 as T
+
+pytestmark = pytest.mark.gpu
+
+FP32_FORCE_RMS = 2e-6       # RMS relative force error bound of the FP32C path
+FP64_REL = 1e-11
+
+
+def make(n, seed=1, K=16, order=4, lam=0.5, gamma=1.0, alpha_rc=3.1, **kw):
+    return T.make_system(n, gamma=gamma, lam=lam, seed=seed, alpha_rc=alpha_rc, K=K, order=order, **kw)
+
+
+def ctx_for(s, **kw):
+    p = T.params_for(s, **kw)
+    c = T.Context(p, s.nel, s.nion)
+    c.EWALD_SELF()
+    c.upload(x=s.x, v=s.v)
+    return c
+
+
+@pytest.mark.parametrize("ei", ["deutsch", "kelbg", "coulomb"])
+@pytest.mark.parametrize("n", [1024, 1000])
+def test_direct_fp64(ei, n):
+    s = make(n, seed=2)
+    o = oracle.Oracle.from_system(s, ei=ei)
+    fo, uo = o.force_direct(s.x)
+    with ctx_for(s, precision="fp64", ei=ei, recip="none") as c:
+        ur = c.Force_direct_self()
+        _, _, f, _ = c.download(x=False, v=False, f=True)
+    assert ur == pytest.approx(uo, rel=FP64_REL)
+    assert oracle.rms_rel(f, fo) < FP64_REL
+
+
+@pytest.mark.parametrize("ei", ["deutsch", "kelbg", "coulomb"])
+@pytest.mark.parametrize("n", [1024, 4096, 777])
+def test_direct_fp32c(ei, n):
+    s = make(n, seed=3)
+    o = oracle.Oracle.from_system(s, ei=ei)
+    fo, uo = o.force_direct(s.x)
+    with ctx_for(s, precision="fp32c", ei=ei, recip="none") as c:
+        ur = c.Force_direct_self()
+        _, _, f, _ = c.download(x=False, v=False, f=True)
+    err = oracle.rms_rel(f, fo)
+    assert err < FP32_FORCE_RMS, err
+    assert ur == pytest.approx(uo, rel=2e-5)
+
+
+@pytest.mark.parametrize("order,K", [(4, 16), (5, 32), (6, 24), (4, 30)])
+def test_spme_vs_oracle(order, K):
+    s = make(2000, seed=4, K=K, order=order)
+    o = oracle.Oracle.from_system(s, ei="kelbg")
+    fo, umo = o.force_spme(s.x)
+    with ctx_for(s, precision="fp64", ei="kelbg", recip="spme") as c:
+        um = c.Force_SPME4()
+        _, _, _, fr = c.download(x=False, v=False, f=False, frec=True)
+    assert um == pytest.approx(umo, rel=1e-11)
+    assert oracle.rms_rel(fr, fo) < 1e-10
+
+
+def test_ewald_ksum_vs_oracle():
+    s = make(1024, seed=5, alpha_rc=2.8)   # alpha = 5.6/L
+    o = oracle.Oracle.from_system(s, ei="kelbg")
+    fo, uko = o.ewald_ksum(s.x, 64)
+    with ctx_for(s, precision="fp64", ei="kelbg", recip="ewald", nmax2=64) as c:
+        uk = c.Force_SPME4()
+        _, _, _, fr = c.download(x=False, v=False, f=False, frec=True)
+    assert uk == pytest.approx(uko, rel=1e-11)
+    assert oracle.rms_rel(fr, fo) < 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_total_force_and_energies(precision):
+    s = make(2048, seed=6, K=32, order=5)
+    o = oracle.Oracle.from_system(s, ei="kelbg")
+    fo, uro, umo = o.force_total(s.x, recip="spme")
+    with ctx_for(s, precision=precision, ei="kelbg", recip="spme") as c:
+        e = c.force()
+        _, _, f, _ = c.download(x=False, v=False, f=True)
+    tol = FP64_REL if precision == "fp64" else FP32_FORCE_RMS
+    assert oracle.rms_rel(f, fo) < tol
+    assert e["Um"] == pytest.approx(umo, rel=1e-11)
+    assert e["Ur"] == pytest.approx(uro, rel=1e-11 if precision == "fp64" else 2e-5)
+    assert e["Uo"] == pytest.approx(o.Uo, rel=1e-14)
+    assert e["Epot"] == pytest.approx((e["Ur"] + e["Uo"]) * T.EPS, rel=1e-14)
+    assert np.linalg.norm(f.sum(0)) < 1e-9 * np.abs(f).sum()       # REMOVE_RIGIDMTN applied
+
+
+def test_granular_routines_compose_like_force():
+    s = make(1536, seed=7, K=16, order=4)
+    with ctx_for(s, precision="fp64", ei="deutsch", recip="spme") as c:
+        um = c.Force_SPME4()
+        ur = c.Force_direct_self()
+        c.SPME_SUM()
+        c.REMOVE_RIGIDMTN()
+        _, _, f1, _ = c.download(x=False, v=False, f=True)
+        e = c.force()
+        _, _, f2, _ = c.download(x=False, v=False, f=True)
+    assert np.allclose(f1, f2, rtol=1e-13, atol=1e-13 * np.abs(f2).max())
+    assert e["Ur"] == pytest.approx(ur, rel=1e-13) and e["Um"] == pytest.approx(um, rel=1e-13)
+
+
+@pytest.mark.parametrize("thermo", ["notemp", "isokin", "berend"])
+def test_verlet_halves_vs_oracle(thermo):
+    s = make(1000, seed=8, K=16)
+    rng = np.random.default_rng(0)
+    f0 = rng.normal(size=(s.n, 3))
+    o = oracle.Oracle.from_system(s, ei="kelbg", Te=0.7, Ti=0.3, tau=2.0)
+    p = T.params_for(s, precision="fp64", ei="kelbg", recip="spme", thermo=thermo, tau=2.0)
+    p.Te, p.Ti = 0.7, 0.3
+    x, v = s.x.copy(), s.v.copy()
+    with T.Context(p, s.nel, s.nion) as c:
+        c.EWALD_SELF()
+        c.upload(x=x, v=v, f=f0)
+        c.VVerlet1(s.dt)
+        me, mi = c.VVerlet2(s.dt)
+        gx, gv, _, _ = c.download(x=True, v=True, f=False)
+    f = f0.copy()
+    o.vverlet1(x, v, f, s.dt)
+    me_o, mi_o = o.vverlet2(v, f, s.dt, thermo=thermo)
+    assert np.allclose(gx, x, rtol=0, atol=1e-12 * s.box)
+    assert np.allclose(gv, v, rtol=1e-13, atol=1e-15)
+    assert me == pytest.approx(me_o, rel=1e-12) and mi == pytest.approx(mi_o, rel=1e-12)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32c", 1e-5)])
+def test_md_steps_graph_vs_oracle(precision, tol):
+    s = make(1024, seed=9, K=16, order=4)
+    o = oracle.Oracle.from_system(s, ei="kelbg")
+    x, v = s.x.copy(), s.v.copy()
+    f, _, _ = o.force_total(x)
+    with ctx_for(s, precision=precision, ei="kelbg", recip="spme") as c:
+        c.upload(f=f)
+        e = c.md_steps(s.dt, 5)
+        gx, gv, gf, _ = c.download()
+    for _ in range(5):
+        eo = o.md_step(x, v, f, s.dt)
+    assert np.max(np.abs(gx - x)) < tol * s.box
+    assert oracle.rms_rel(gv, v) < tol
+    assert e["Epot"] == pytest.approx(eo["Epot"], rel=10 * tol)
+    assert e["mv2el"] == pytest.approx(eo["mv2el"], rel=tol)
+
+
+def test_finit_vs_oracle():
+    s = make(1024, seed=10, K=16)
+    o = oracle.Oracle.from_system(s, ei="deutsch")
+    x = s.x.copy()
+    fo, uro, umo = o.finit(x, s.v, s.dt)
+    with ctx_for(s, precision="fp64", ei="deutsch", recip="spme") as c:
+        e = c.Finit(s.dt)
+        gx, _, gf, _ = c.download(v=False)
+    assert oracle.rms_rel(gf, fo) < FP64_REL
+    assert np.max(np.abs(gx - x)) < 1e-12 * s.box
+    assert e["Ur"] == pytest.approx(uro, rel=FP64_REL)
+
+
+def test_rdf_vdf_histograms():
+    s = make(1024, seed=12, K=16)
+    o = oracle.Oracle.from_system(s, ei="deutsch")
+    _, _, h = o.force_direct(s.x, rdf=True)
+    with ctx_for(s, precision="fp64", ei="deutsch", recip="none") as c:
+        c.set_flags(T.FLAG_ENERGY | T.FLAG_RDF | T.FLAG_VDF)
+        c.Force_direct_self()
+        _, _, gf, _ = c.download(x=False, v=False, f=True)
+        c.VVerlet2(s.dt)
+        rdf, vdf = c.histograms(reset=True)
+        rdf2, vdf2 = c.histograms()
+    assert np.array_equal(rdf, h)                 # +2 per pair inside rc, force.f90:99-103
+    assert rdf2.sum() == 0 and vdf2.sum() == 0    # reset as DUMP does, result.f90:264-268
+    v, f = s.v.copy(), gf.copy()
+    _, _, hv = o.vverlet2(v, f, s.dt, vdf=True)
+    assert np.array_equal(vdf, hv)                # vverlet.f90:201-204
+
+
+def test_pt_roundtrip_and_stride():
+    s = make(300, seed=13, K=16)
+    qel, qion = s.to_pt()
+    qel["ff"] = np.random.default_rng(1).normal(size=(s.nel, 3))
+    qion["ff"] = np.random.default_rng(2).normal(size=(s.nion, 3))
+    p = T.params_for(s, precision="fp64", recip="spme")
+    with T.Context(p, s.nel, s.nion) as c:
+        c.upload_pt(qel, qion)
+        a = np.zeros_like(qel)
+        b = np.zeros_like(qion)
+        a["id"], b["id"] = 7, 9
+        c.download_pt(a, b)
+    for k in ("xx", "xv", "ff"):
+        assert np.array_equal(a[k], qel[k]) and np.array_equal(b[k], qion[k])
+    assert np.all(a["id"] == 7) and np.all(b["id"] == 9)     # other fields untouched
+
+
+def test_errors():
+    s = make(64, seed=14, K=16)
+    p = T.params_for(s, precision="fp64", recip="spme")
+    p.rc = 0.6 * s.box
+    with T.Context(p, s.nel, s.nion) as c:
+        with pytest.raises(T.TcpError) as ei:
+            c.EWALD_SELF()
+        assert ei.value.code == 2            # TCP_ERR_CUTOFF, force.f90:18-22
+        with pytest.raises(T.TcpError) as ei:
+            c.Force_direct_self()
+        assert ei.value.code == 7            # TCP_ERR_STATE
+
+
+def test_large_fp32c_rows_sample():
+    """N = 65536 (the headline size): sampled rows of the real-space sum vs
+    the oracle, and size-independent properties of the full sum."""
+    s = T.make_config_system("n65536_spme128", seed=0)
+    o = oracle.Oracle.from_system(s, ei="kelbg")
+    rows = np.r_[0:256, 32768:33024]
+    with ctx_for(s, precision="fp32c", ei="kelbg", recip="none") as c:
+        c.Force_direct_self()
+        _, _, f, _ = c.download(x=False, v=False, f=True)
+    fo = np.concatenate([o.force_direct_rows(s.x, 0, 256)[0], o.force_direct_rows(s.x, 32768, 33024)[0]])
+    assert oracle.rms_rel(f[rows], fo) < FP32_FORCE_RMS
+    # ordered-pair sums without reactions: Newton's third law holds only to rounding
+    assert np.linalg.norm(f.sum(0)) < 1e-6 * np.abs(f).sum()
