@@ -1,0 +1,389 @@
+"""Benchmark of the TCP_allpair force-and-integrate step on GB300.
+
+Headline workload (the largest single-GPU configuration): N = 65,536
+(32,768 electrons + 32,768 ions), Gamma = 1, Kelbg e-i lambda = 0.5 a,
+Ewald alpha from erfc(alpha rc) = 1e-6 with rc = L/2, SPME 128^3 order 5,
+NVE velocity Verlet, seeded synthetic inputs.  A "step" is one MD step
+(first half kick + drift, SPME, all-pair real-space sum, net-force removal,
+second half kick, energy and kinetic reductions).
+
+value      pair-int/s = N(N-1)/2 * steps / time of the compensated-FP32 step,
+           state resident in HBM, CUDA events per step on the library's stream,
+           L2 flushed (2x L2 written) between timed steps.
+e2e        the same metric through the C ABI with host PT records: every step
+           uploads x, v, f (tcp_upload), runs one step, downloads x, v, f.
+fp64       the plain FP64 drop-in step at the same configuration.
+roofline   the real-space pair kernel against the measured FP32 FFMA issue rate.
+cpu_baseline / --impl reference
+           the FP64 CPU restatement (oracle/, OpenMP on all host cores; the
+           Fortran/MPI reference cannot be built on this machine) on a bounded
+           sample: R i-rows of the direct sum against all j, one full SPME and
+           one integrator pass, the direct-sum time scaled to N(N-1)/2 pairs.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import pathlib
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "pair-int/s, steps/s @N=65536: FP32-comp vs FP64 on 1 GB300, ≤2e-6 force err"
+WORKLOAD = "n65536_spme128"
+# FP32-pipe issue slots per ordered pair of the pair kernel, counted from the
+# source of tile_f32 (pair.cu) for a Coulomb pair with energy: 3 FMUL (scale),
+# 3 (r^2), 1 (r), 1 (t), 1 (exp arg), 9 (erfc poly), 1 (erfc), 2 (Gaussian),
+# 3 (r^-3 weight), 3 (force FFMA), 2 (energy), 5 (compares/selects) = 34;
+# plus 3 int->float conversions and 3 SFU ops (rsqrt, rcp, ex2).
+RECIPE_FP32_OPS = 34
+RECIPE_SFU_OPS = 3
+SFU_RATE = 16.0 / 128.0       # SFU lanes per SM relative to FP32 lanes
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.device = device
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc:
+            return None
+        self.f.flush()
+        rows = [r.split(",") for r in pathlib.Path(self.f.name).read_text().splitlines() if r.strip()]
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip().lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # plumbing only: barrier and max over ranks
+        dist.init_process_group(backend="gloo")
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist:
+        dist.barrier()
+
+
+def reduce_max(dist, x: float) -> float:
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(dist, x: float) -> float:
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the pair kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "pair_fp32c_kelbg_n32768.md"
+    if not p.exists():
+        return None
+    m = re.search(r"dram_bytes_per_launch_full_size:\s*([0-9.eE+]+)", p.read_text())
+    return float(m.group(1)) if m else None
+
+
+# ---------------------------------------------------------------------------
+# CPU leg: the FP64 restatement on a bounded sample
+def cpu_sample(s, rows_per_species: int, threads: int):
+    import oracle
+    o = oracle.Oracle.from_system(s, ei="kelbg", nthreads=threads)
+    n = s.n
+    t0 = time.perf_counter()
+    fa, _ = o.force_direct_rows(s.x, 0, rows_per_species)
+    fb, _ = o.force_direct_rows(s.x, s.nel, s.nel + rows_per_species)
+    t_rows = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    frec, um = o.force_spme(s.x)
+    t_spme = time.perf_counter() - t0
+    x, v = s.x.copy(), s.v.copy()
+    f = np.zeros_like(x)
+    t0 = time.perf_counter()
+    o.vverlet1(x, v, f, s.dt)
+    o.vverlet2(v, f, s.dt)
+    t_int = time.perf_counter() - t0
+    rows = 2 * rows_per_species
+    pairs = n * (n - 1) / 2
+    t_step = t_rows / (rows * (n - 1)) * pairs + t_spme + t_int
+    sample_rows = np.r_[0:rows_per_species, s.nel:s.nel + rows_per_species]
+    f_rows = np.concatenate([fa, fb]) + frec[sample_rows]
+    return dict(t_step=t_step, value=pairs / t_step, t_rows=t_rows, t_spme=t_spme, t_int=t_int,
+                rows=rows, f_rows=f_rows, sample_rows=sample_rows, um=um)
+
+
+def run_reference(args, world, rank, dist):
+    """--impl reference: the CPU restatement (the reference itself cannot be built)."""
+    if rank != 0:
+        return 0
+    import oracle
+    from tcp_allpair_gb300.system import make_config_system
+    oracle.build()
+    s = make_config_system(WORKLOAD, seed=0)
+    threads = os.cpu_count() or 1
+    R = args.ref_rows
+    for _ in range(args.warmup):
+        cpu_sample(s, R // 2, threads)
+    t0 = time.perf_counter()
+    est = []
+    for _ in range(args.steps):
+        est.append(cpu_sample(s, R // 2, threads)["t_step"])
+    wall = time.perf_counter() - t0
+    t_step = float(np.mean(est))
+    n = s.n
+    value = n * (n - 1) / 2 / t_step
+    sample = (f"{R} of {n} i-rows x all j (FP64, OpenMP) + one SPME 128^3 p5 + one integrator pass per step; "
+              f"direct-sum time scaled to N(N-1)/2 pairs")
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "pair-int/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "steps_per_s": 1.0 / t_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded uniform positions (0.1a rejection), Maxwell-Boltzmann velocities",
+        "config": config_dict(s),
+        "reference_note": "the Fortran 90 + MPI + FFTE reference cannot be built here or on the GPU box "
+                          "(no Fortran compiler, no MPI, FFTE not vendored); timed is the FP64 C restatement "
+                          "of force.f90/vverlet.f90 in oracle/",
+        "cpu_baseline": {"value": value, "unit": "pair-int/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "pair-int/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(out))
+    return 0
+
+
+def config_dict(s):
+    return {"workload": "n65536_spme128_kelbg_nve", "N": s.n, "nel": s.nel, "nion": s.nion, "gamma": 1.0,
+            "lambda_ei_over_a": 0.5, "ei_model": "kelbg", "box_A": s.box, "rc": "L/2",
+            "ewald_alpha_rc": s.alpha * s.rc, "spme_mesh": s.K, "spline_order": s.order, "ensemble": "NVE",
+            "dt_over_wpe": 0.01, "units": "reference (A, eV, amu, 10.18 fs)",
+            "precision": "FP32 pair arithmetic with compensated accumulation; FP64 integration, SPME, reductions",
+            "l2": "flushed between timed steps (a 2x L2 buffer is written outside the timed spans)"}
+
+
+def run_gpu(args, world, rank, local, dist):
+    import oracle
+    import tcp_allpair_gb300 as T
+    from tcp_allpair_gb300.system import make_config_system
+
+    s = make_config_system(WORKLOAD, seed=rank)
+    n = s.n
+    pairs = n * (n - 1) / 2
+    p32 = T.params_for(s, precision="fp32c", ei="kelbg", recip="spme", thermo="notemp")
+    p64 = T.params_for(s, precision="fp64", ei="kelbg", recip="spme", thermo="notemp")
+    ctx = T.Context(p32, s.nel, s.nion, device=local)
+    ctx.EWALD_SELF()
+    ctx.upload(x=s.x, v=s.v)
+    e0 = ctx.force()                        # initial forces (restart-style start, main.f90:49-54)
+    _, _, f32, _ = ctx.download(x=False, v=False, f=True)
+
+    ctx64 = T.Context(p64, s.nel, s.nion, device=local)
+    ctx64.EWALD_SELF()
+    ctx64.upload(x=s.x, v=s.v)
+    ctx64.force()
+    _, _, f64, _ = ctx64.download(x=False, v=False, f=True)
+    err_vs_fp64 = oracle.rms_rel(f32, f64)
+
+    # warm-up, then the timed steps (device-resident)
+    ctx.md_steps(s.dt, args.warmup)
+    launches0 = ctx.launch_count()
+    barrier(dist)
+    with Clocks(local) as clk:
+        t = ctx.time_steps(s.dt, args.steps, flush_l2=True)
+    launches = ctx.launch_count() - launches0
+    barrier(dist)
+    step_ms = t["step"] / t["nsteps"]
+    step_ms_max = reduce_max(dist, step_ms)
+    value = reduce_sum(dist, pairs) * args.steps / (step_ms_max * args.steps * 1e-3)
+    pair_ms = t["pair"] / t["nsteps"]
+
+    # FP64 drop-in step (few steps: FP64 issue rate of GB300 is ~1/64 of FP32)
+    ctx64.md_steps(s.dt, 1)
+    t64 = ctx64.time_steps(s.dt, args.fp64_steps, flush_l2=True)
+    step64_ms = t64["step"] / t64["nsteps"]
+    ctx64.close()
+
+    # e2e through the C ABI with host PT records
+    qel, qion = s.to_pt()
+    ctx_e = T.Context(p32, s.nel, s.nion, device=local)
+    ctx_e.EWALD_SELF()
+    ctx_e.upload_pt(qel, qion, fields=("xx", "xv"))
+    ctx_e.force()
+    ctx_e.download_pt(qel, qion)
+    ctx_e.md_steps(s.dt, 1)
+    barrier(dist)
+    te0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx_e.upload_pt(qel, qion)
+        ctx_e.md_steps(s.dt, 1)
+        ctx_e.download_pt(qel, qion)
+    te = time.perf_counter() - te0
+    te = reduce_max(dist, te)
+    ctx_e.close()
+    e2e_value = reduce_sum(dist, pairs) * args.steps / te
+    stride = qel.strides[0]
+    h2d = sum((len(a) - 1) * stride + 72 for a in (qel, qion) if len(a))   # span xx(1)..ff(3) per species
+    d2h = n * 3 * 3 * 8
+
+    # roofline of the pair kernel (live timing inside the timed steps)
+    peak = T.fp32_peak(local) * 1e12            # FFMA/s
+    ordered = float(n) * (n - 1)
+    achieved = RECIPE_FP32_OPS * ordered / (pair_ms * 1e-3)
+    sfu_frac = RECIPE_SFU_OPS * ordered / (pair_ms * 1e-3) / (peak * SFU_RATE)
+    traffic = profile_traffic()
+    roof = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "Top/s",
+            "frac": achieved / peak, "traffic": traffic,
+            "kernel": "pair_fp32c_kernel (real-space all-pair sum)",
+            "recipe": f"{RECIPE_FP32_OPS} FP32-pipe ops + {RECIPE_SFU_OPS} SFU ops per ordered pair",
+            "peak_source": "measured FFMA issue rate (tcp_fp32_peak) on this GPU, not MEASURED_PEAKS.json "
+                           "(which has HBM and bf16 only)",
+            "sfu_frac": sfu_frac, "pair_kernel_ms": pair_ms}
+
+    # CPU baseline (rank 0, N = 1 only) and the FP32C force error vs the oracle
+    cpu = None
+    err_vs_oracle = None
+    if rank == 0 and world == 1:
+        threads = os.cpu_count() or 1
+        cs = cpu_sample(s, args.ref_rows // 2, threads)
+        cpu = {"value": cs["value"], "unit": "pair-int/s", "cores": threads, "kind": "port",
+               "sample": f"{cs['rows']} of {n} i-rows x all j (FP64, OpenMP) + one SPME + one integrator pass, "
+                         f"direct-sum time scaled to N(N-1)/2 pairs ({cs['t_rows'] + cs['t_spme']:.1f} s CPU)",
+               "ms_per_step": cs["t_step"] * 1e3}
+        # FP32C total force vs the FP64 oracle on the sampled rows
+        err_vs_oracle = oracle.rms_rel(f32[cs["sample_rows"]], cs["f_rows"])
+
+    ctx.close()
+    clocks = clk.summary()
+    out = {
+        "metric": METRIC, "value": value, "unit": "pair-int/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms_max, "steps_per_s": 1e3 / step_ms_max,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded uniform positions (0.1a rejection), Maxwell-Boltzmann velocities",
+        "config": config_dict(s),
+        "breakdown_ms_per_step": {k: t[k] / t["nsteps"] for k in ("vverlet1", "recip", "pair", "epilogue")},
+        "fp64": {"ms_per_step": step64_ms, "value": pairs / (step64_ms * 1e-3), "steps": args.fp64_steps,
+                 "speedup_fp32c_over_fp64": step64_ms / step_ms},
+        "force_error": {"rms_rel_fp32c_vs_fp64_gpu": err_vs_fp64, "rms_rel_fp32c_vs_fp64_oracle_rows": err_vs_oracle,
+                        "bound": 2e-6},
+        "energies_initial": {"Ur": e0["Ur"], "Um": e0["Um"], "Uo": e0["Uo"]},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "pair-int/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ms_per_step": te / args.steps * 1e3,
+                "path": "tcp_upload (PT records x,v,f) + tcp_md_steps(1) + tcp_download (x,v,f), pageable host memory"},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
+def run_pair_only(args):
+    """Launch the real-space pair kernel alone on an N-particle version of the
+    headline system (profiling target: `ncu -k regex:pair_ ... python bench.py
+    --pair-only N`)."""
+    import tcp_allpair_gb300 as T
+    n = args.pair_only
+    s = T.make_system(n, gamma=1.0, lam=0.5, seed=0, ewald_rel_err=1e-6, K=64, order=5)
+    p = T.params_for(s, precision=args.precision, ei="kelbg", recip="none")
+    with T.Context(p, s.nel, s.nion) as c:
+        c.EWALD_SELF()
+        c.upload(x=s.x, v=s.v)
+        for _ in range(3):
+            c.Force_direct_self()
+        ms = c.time_component(0, 5)
+    print(json.dumps({"pair_only": n, "precision": args.precision, "pair_kernel_ms": ms}))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--ref-rows", type=int, default=4096)
+    ap.add_argument("--pair-only", type=int, default=0, help="profile target: pair kernel alone at this N")
+    ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
+    args = ap.parse_args()
+    if args.pair_only:
+        return run_pair_only(args)
+    args.warmup = max(args.warmup, 3)
+    world, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        rc = run_reference(args, world, rank, dist)
+    else:
+        rc = run_gpu(args, world, rank, local, dist)
+    if dist:
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

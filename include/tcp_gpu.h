@@ -191,6 +191,13 @@ int tcp_histograms(tcp_ctx *ctx, double *rdf, double *vdf, int reset);
  * the mean device time per launch from CUDA events recorded on that stream.
  * which: 0 = real-space pair kernel, 1 = SPME chain, 2 = full md step. */
 int tcp_time_component(tcp_ctx *ctx, int which, int reps, double dt, double *ms_per_launch);
+/* Times nsteps MD steps one by one with CUDA events recorded on the
+ * context's stream (also inside the captured step graph), optionally writing
+ * a buffer of twice the L2 size between steps (outside the timed spans).
+ * out[6] receives the summed milliseconds of: whole steps, first half kick,
+ * reciprocal sum, real-space pair kernel, force epilogue + second half kick,
+ * and the number of steps timed. */
+int tcp_time_steps(tcp_ctx *ctx, double dt, int nsteps, int flush_l2, double *out);
 /* Kernel launches issued by the context so far (all kernels of this library). */
 int tcp_launch_count(tcp_ctx *ctx, long long *count);
 /* Measured FP32 FFMA issue rate of the device: a calibration kernel of

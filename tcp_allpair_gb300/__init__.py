@@ -202,6 +202,14 @@ class Context:
         self._chk(self.lib.tcp_time_component(self.h, which, reps, dt, C.byref(ms)), "tcp_time_component")
         return ms.value
 
+    def time_steps(self, dt, nsteps, flush_l2=True):
+        """Per-step CUDA-event timing: dict of summed ms per phase."""
+        out = np.zeros(6)
+        self._chk(self.lib.tcp_time_steps(self.h, dt, nsteps, int(flush_l2),
+                                          out.ctypes.data_as(C.POINTER(C.c_double))), "tcp_time_steps")
+        keys = ("step", "vverlet1", "recip", "pair", "epilogue", "nsteps")
+        return dict(zip(keys, out.tolist()))
+
     def launch_count(self):
         n = C.c_longlong()
         self._chk(self.lib.tcp_launch_count(self.h, C.byref(n)), "tcp_launch_count")

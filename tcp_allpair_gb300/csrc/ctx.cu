@@ -120,14 +120,20 @@ static bool thermostat_due(const tcp_ctx *c) {
 }
 
 // One MD step (main.f90:81-153) on the stream; *pass = kinetic partial set.
+// Phase marks ev[0..4] are recorded on the stream (event nodes in the graph).
 static int step_chain(tcp_ctx *c, double dt, bool apply, int *pass) {
     int rc;
+    TCP_CUDA(cudaEventRecordWithFlags(c->ev[0], c->stream, cudaEventRecordExternal));
     if ((rc = launch_vverlet1(c, dt, 0.0))) return rc;
+    TCP_CUDA(cudaEventRecordWithFlags(c->ev[1], c->stream, cudaEventRecordExternal));
     if ((rc = recip_launch(c))) return rc;
+    TCP_CUDA(cudaEventRecordWithFlags(c->ev[2], c->stream, cudaEventRecordExternal));
     if ((rc = launch_pair(c, energy_on(c), (c->flags & TCP_FLAG_RDF) != 0))) return rc;
+    TCP_CUDA(cudaEventRecordWithFlags(c->ev[3], c->stream, cudaEventRecordExternal));
     if ((rc = launch_force_finalize(c, c->p.reciprocal != TCP_RECIP_NONE))) return rc;
     if ((rc = launch_kick2(c, dt, true, apply, (c->flags & TCP_FLAG_VDF) != 0, pass))) return rc;
     if ((rc = launch_reduce(c, (energy_on(c) ? kRedUr : 0) | kRedMv2, *pass))) return rc;
+    TCP_CUDA(cudaEventRecordWithFlags(c->ev[4], c->stream, cudaEventRecordExternal));
     return TCP_OK;
 }
 
@@ -192,6 +198,8 @@ int tcp_create(const tcp_params *p_in, int nel, int nion, int device, tcp_ctx **
         return code;
     };
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(cuda_check(cudaGetLastError(), "cudaStreamCreate"));
+    for (auto &e : c->ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return fail(cuda_check(cudaGetLastError(), "cudaEventCreate"));
 #define TCP_ALLOC(ptr, bytes)                                                            \
     do {                                                                                 \
         cudaError_t _e = cudaMalloc(&(ptr), (bytes));                                    \
@@ -250,6 +258,9 @@ int tcp_destroy(tcp_ctx *c) {
     cudaFree(c->ksum);
     if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->h_scal) cudaFreeHost(c->h_scal);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    cudaFree(c->l2_flush);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return TCP_OK;
@@ -507,29 +518,41 @@ static int build_graph(tcp_ctx *c, double dt, bool apply, cudaGraphExec_t *out, 
     return TCP_OK;
 }
 
+static int ensure_graph(tcp_ctx *c, double dt) {
+    const bool has_thermo = c->p.thermo == TCP_THERMO_ISOKIN || c->p.thermo == TCP_THERMO_BEREND;
+    // c->graph holds the step without the thermostat rescale; the rescale step
+    // (ISOKIN/BEREND, every thermo_period-th step) is launched eagerly.
+    if (!c->graph || c->graph_dt != dt || c->graph_flags != c->flags) {
+        invalidate_graph(c);
+        int rc = build_graph(c, dt, !has_thermo, &c->graph, &c->graph_kernels);
+        if (rc) return rc;
+        c->graph_dt = dt;
+        c->graph_flags = c->flags;
+    }
+    return TCP_OK;
+}
+
+static int launch_step(tcp_ctx *c, double dt) {
+    const bool has_thermo = c->p.thermo == TCP_THERMO_ISOKIN || c->p.thermo == TCP_THERMO_BEREND;
+    int rc;
+    if (has_thermo && thermostat_due(c)) {
+        int pass = 0;
+        if ((rc = step_chain(c, dt, true, &pass))) return rc;
+    } else {
+        TCP_CUDA(cudaGraphLaunch(c->graph, c->stream));
+        c->launches += c->graph_kernels;
+    }
+    c->step_index++;
+    return TCP_OK;
+}
+
 int tcp_md_steps(tcp_ctx *c, double dt, int nsteps, tcp_energies *e) {
     TCP_REQUIRE_READY(c);
     if (nsteps < 0) return set_error(TCP_ERR_BAD_PARAM, "nsteps < 0");
     int rc;
-    const bool has_thermo = c->p.thermo == TCP_THERMO_ISOKIN || c->p.thermo == TCP_THERMO_BEREND;
-    // c->graph holds the no-rescale step; the rescale step (ISOKIN/BEREND,
-    // every thermo_period-th step) is launched eagerly, it is rare.
-    if (!c->graph || c->graph_dt != dt || c->graph_flags != c->flags) {
-        invalidate_graph(c);
-        if ((rc = build_graph(c, dt, !has_thermo, &c->graph, &c->graph_kernels))) return rc;
-        c->graph_dt = dt;
-        c->graph_flags = c->flags;
-    }
-    for (int s = 0; s < nsteps; ++s) {
-        if (has_thermo && thermostat_due(c)) {
-            int pass = 0;
-            if ((rc = step_chain(c, dt, true, &pass))) return rc;
-        } else {
-            TCP_CUDA(cudaGraphLaunch(c->graph, c->stream));
-            c->launches += c->graph_kernels;
-        }
-        c->step_index++;
-    }
+    if ((rc = ensure_graph(c, dt))) return rc;
+    for (int s = 0; s < nsteps; ++s)
+        if ((rc = launch_step(c, dt))) return rc;
     if ((rc = sync_scalars(c))) return rc;
     fill_energies(c, nullptr);
     c->last.mv2el = c->h_scal[kScalMv2e];
@@ -574,29 +597,11 @@ int tcp_time_component(tcp_ctx *c, int which, int reps, double dt, double *ms) {
     int rc = TCP_OK;
     auto one = [&]() -> int {
         if (which == 0) return launch_pair(c, energy_on(c), false);
-        if (which == 1) return recip_launch(c);
-        return tcp_md_steps(c, dt, 1, nullptr);
+        return recip_launch(c);
     };
-    if (which == 2) {
-        // build the graph outside the timed region
-        if ((rc = tcp_md_steps(c, dt, 1, nullptr))) return rc;
-    }
+    if (which == 2 && (rc = ensure_graph(c, dt))) return rc;
     cudaEventRecord(e0, c->stream);
-    for (int r = 0; r < reps && !rc; ++r) {
-        if (which == 2) {
-            if (c->graph && !(c->p.thermo == TCP_THERMO_ISOKIN || c->p.thermo == TCP_THERMO_BEREND)) {
-                cudaGraphLaunch(c->graph, c->stream);
-                c->launches += c->graph_kernels;
-                c->step_index++;
-            } else {
-                int pass = 0;
-                rc = step_chain(c, dt, thermostat_due(c), &pass);
-                c->step_index++;
-            }
-        } else {
-            rc = one();
-        }
-    }
+    for (int r = 0; r < reps && !rc; ++r) rc = which == 2 ? launch_step(c, dt) : one();
     cudaEventRecord(e1, c->stream);
     cudaEventSynchronize(e1);
     float t = 0.f;
@@ -606,6 +611,35 @@ int tcp_time_component(tcp_ctx *c, int which, int reps, double dt, double *ms) {
     if (rc) return rc;
     if ((rc = sync_scalars(c))) return rc;
     *ms = (double)t / reps;
+    return TCP_OK;
+}
+
+int tcp_time_steps(tcp_ctx *c, double dt, int nsteps, int flush_l2, double *out) {
+    TCP_REQUIRE_READY(c);
+    if (nsteps <= 0 || !out) return set_error(TCP_ERR_BAD_PARAM, "nsteps must be positive");
+    int rc;
+    if (flush_l2 && !c->l2_flush) {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device);
+        c->l2_flush_bytes = 2 * (size_t)std::max(l2, 64 << 20);
+        TCP_CUDA(cudaMalloc(&c->l2_flush, c->l2_flush_bytes));
+    }
+    for (int k = 0; k < 6; ++k) out[k] = 0.0;
+    if ((rc = ensure_graph(c, dt))) return rc;
+    for (int s = 0; s < nsteps; ++s) {
+        if (flush_l2) TCP_CUDA(cudaMemsetAsync(c->l2_flush, s & 0xff, c->l2_flush_bytes, c->stream));
+        if ((rc = launch_step(c, dt))) return rc;
+        TCP_CUDA(cudaEventSynchronize(c->ev[4]));
+        float t[5];
+        cudaEventElapsedTime(&t[0], c->ev[0], c->ev[4]);
+        for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&t[k + 1], c->ev[k], c->ev[k + 1]);
+        for (int k = 0; k < 5; ++k) out[k] += t[k];
+        out[5] += 1.0;
+    }
+    if ((rc = sync_scalars(c))) return rc;
+    fill_energies(c, nullptr);
+    c->last.mv2el = c->h_scal[kScalMv2e];
+    c->last.mv2ion = c->h_scal[kScalMv2i];
     return TCP_OK;
 }
 

@@ -102,6 +102,9 @@ struct tcp_ctx {
     unsigned graph_flags = 0;
     int graph_kernels = 0;
     long long launches = 0;
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // step phase marks
+    void *l2_flush = nullptr;
+    size_t l2_flush_bytes = 0;
     long long step_index = 0;
     tcp_energies last{};
 };
