@@ -142,6 +142,23 @@ int tcp_download(tcp_ctx *ctx, int species, double *xx, double *xv, double *ff,
 int tcp_upload_soa(tcp_ctx *ctx, const double *x, const double *v, const double *f);
 int tcp_download_soa(tcp_ctx *ctx, double *x, double *v, double *f, double *frec);
 
+/* No counterpart in the reference.  The real-space sum of tcp_force_direct
+ * for callers that cannot allocate device memory: programs whose device
+ * memory belongs to another allocator (a pool that reserved the free HBM at
+ * start-up) and step loops that forbid allocation after set-up because
+ * cudaMalloc/cudaFree can synchronise the whole device.  No context and no
+ * allocation: every temporary lives in one static 8 MiB device array that each
+ * GPU loading the library holds until exit, so n is limited to what fits
+ * (about 200,000 particles for TCP_PREC_FP32C, 140,000 for TCP_PREC_FP64);
+ * larger n returns TCP_ERR_BAD_PARAM.  x and f are device arrays, SoA [3][n]
+ * (electrons first); *Ur (host, may be NULL) gets Ur without eps.  Runs on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) and returns when the
+ * forces are written.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current.  Calls share the
+ * array: calls that overlap on the GPU race and must be serialised. */
+int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, const double *x, double *f,
+                             double *Ur, void *stream);
+
 /* ---- the force evaluation (main.f90:100-141) --------------------------- */
 /* Force_direct_self + Force_direct_ext + Force_direct_sum for the whole
  * system (force.f90:52-372, main.f90:105-130): f is overwritten with the

@@ -65,6 +65,8 @@ SIGNATURES = {
     "tcp_upload_soa": (C.c_int, [_CTX, C.c_void_p, C.c_void_p, C.c_void_p]),
     "tcp_download_soa": (C.c_int, [_CTX, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "tcp_force_direct": (C.c_int, [_CTX, _P]),
+    "tcp_force_direct_noalloc": (C.c_int, [C.POINTER(TcpParams), C.c_int, C.c_int, C.c_void_p, C.c_void_p, _P,
+                                           C.c_void_p]),
     "tcp_force_spme": (C.c_int, [_CTX, _P]),
     "tcp_spme_sum": (C.c_int, [_CTX]),
     "tcp_remove_rigidmtn": (C.c_int, [_CTX]),

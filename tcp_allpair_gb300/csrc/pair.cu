@@ -27,6 +27,8 @@
 // 163-175) in double precision with CUDA's erf/erfc/exp/sqrt.
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
+#include <string>
 
 #include "device_util.cuh"
 #include "tcp_internal.h"
@@ -598,3 +600,181 @@ int launch_force_finalize(tcp_ctx *c, bool add_rec) {
 }
 
 }  // namespace tcp
+
+// ---------------------------------------------------------------------------
+// tcp_force_direct_noalloc: the real-space sum of tcp_force_direct for callers
+// that cannot allocate device memory.
+//
+// Some programs that call this library may not allocate at the point where
+// they need forces: a host code whose device memory is owned by another
+// allocator (for example a framework pool that reserved the free HBM at
+// start-up, so a cudaMalloc here would fail or fragment it), or a time-step
+// loop that forbids allocation after set-up because cudaMalloc and cudaFree
+// can synchronise the whole device and stall the other streams of the
+// process.  This variant allocates nothing: every temporary (fixed-point or
+// FP64 positions, per-split partial forces, energy and force-sum partials, the
+// status word) lives in one file-scope device array of kNoAllocBytes, which
+// every GPU that loads the library holds until the process exits.  The caller
+// passes the positions and the force array (device memory, SoA [3][n]) and a
+// host double for Ur.
+//
+// The array is shared by all calls and keeps the last call's contents; this
+// function clears what must start at zero (the status word) and overwrites
+// everything else before reading it.  Calls that overlap on the GPU (from two
+// host threads, or on two streams) race on the array: serialise them.
+namespace tcp {
+
+constexpr size_t kNoAllocBytes = 8u << 20;   // 8 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+__global__ void noalloc_positions_kernel(const double *__restrict__ x, int n, double L0, double L1, double L2,
+                                         int4 *xq, double4_32a *xd) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double L[3] = {L0, L1, L2};
+    double y[3];
+    int q[3];
+    for (int d = 0; d < 3; ++d) {
+        y[d] = x[(size_t)d * n + i];
+        double t = y[d] / L[d] + 0.5;
+        t -= floor(t);
+        q[d] = (int)(unsigned)((unsigned long long)llrint(t * 4294967296.0) & 0xffffffffull);
+    }
+    if (xq) xq[i] = make_int4(q[0], q[1], q[2], 0);
+    if (xd) xd[i] = make_double4_32a(y[0], y[1], y[2], 0.0);
+}
+
+__global__ void noalloc_sum_kernel(const double *__restrict__ part, int np, double *out) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int k = threadIdx.x; k < np; k += blockDim.x) s += part[k];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) *out = s;
+}
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace tcp
+
+extern "C" int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, const double *x, double *f,
+                                        double *Ur, void *stream) {
+    using namespace tcp;
+    static std::mutex mu;
+    static void *scratch_of_device[64] = {nullptr};
+    if (!p || !x || !f) return set_error(TCP_ERR_BAD_PARAM, "NULL argument");
+    if (nel < 0 || nion < 0 || nel + nion < 2) return set_error(TCP_ERR_BAD_PARAM, "need nel, nion >= 0 and nel+nion >= 2");
+    for (int d = 0; d < 3; ++d)
+        if (!(p->box[d] > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "box lengths must be positive");
+    if (!(p->rc > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "rc must be positive");
+    if (p->rc > std::min(std::min(p->box[0], p->box[1]), p->box[2]) / 2.0)
+        return set_error(TCP_ERR_CUTOFF, " *** error at cut-off radius *** (rc > min(box)/2)");
+    if (p->precision != TCP_PREC_FP64 && p->precision != TCP_PREC_FP32C)
+        return set_error(TCP_ERR_BAD_PARAM, "unknown precision");
+    if (p->ei_model < TCP_EI_DEUTSCH || p->ei_model > TCP_EI_COULOMB) return set_error(TCP_ERR_BAD_PARAM, "unknown ei_model");
+    if (p->ei_model == TCP_EI_DEUTSCH && !(p->rs > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "Deutsch model needs rs > 0");
+    if (p->ei_model == TCP_EI_KELBG && !(p->lambda_ei > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "Kelbg model needs lambda_ei > 0");
+
+    // once per device, with that device current: the device address of the array
+    int dev = 0;
+    TCP_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(TCP_ERR_BAD_PARAM, "device index >= 64");
+    void *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!scratch_of_device[dev]) {
+            void *ptr = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+            if (e != cudaSuccess) return cuda_check(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+            scratch_of_device[dev] = ptr;
+        }
+        base = scratch_of_device[dev];
+    }
+
+    // the same constants and geometry as tcp_force_direct (host-side copy only)
+    tcp_ctx tmp;
+    tmp.p = *p;
+    if (tmp.p.charge_scale == 0.0) tmp.p.charge_scale = 1.0;
+    tmp.nel = nel;
+    tmp.nion = nion;
+    tmp.n = nel + nion;
+    tmp.alpha = p->a > 0.0 ? p->a : 3.1 / p->rc;
+    tmp.rc2 = p->rc * p->rc;
+    TCP_CUDA(cudaDeviceGetAttribute(&tmp.num_sms, cudaDevAttrMultiProcessorCount, dev));
+    make_consts(&tmp);
+    const bool fp64 = p->precision == TCP_PREC_FP64;
+    const Geometry g = geometry(&tmp, fp64);
+    int bps = 1;
+    if (fp64)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp64_kernel<0, true, false>, kPairThreads, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp32c_kernel<2, true, false>, kPairThreads, 0);
+    const size_t n = (size_t)tmp.n;
+    const int nbf = ceil_div(tmp.n, 256);
+    auto need = [&](int js) {
+        return align256(16) + align256(n * (fp64 ? sizeof(double4_32a) : sizeof(int4))) +
+               align256(sizeof(double) * 3 * (size_t)nbf) + align256(sizeof(double) * (size_t)g.nblk * js) +
+               align256(sizeof(double) * 3 * n * js);
+    };
+    int js = choose_jsplit(&tmp, g, bps);
+    js = ceil_div(g.ntile, ceil_div(g.ntile, std::max(1, std::min(js, g.ntile))));
+    while (js > 1 && need(js) > kNoAllocBytes) js = ceil_div(g.ntile, ceil_div(g.ntile, js - 1));
+    if (need(js) > kNoAllocBytes)
+        return set_error(TCP_ERR_BAD_PARAM, "n = " + std::to_string(n) + " needs " + std::to_string(need(1)) +
+                                                " bytes of scratch; the static array holds " +
+                                                std::to_string(kNoAllocBytes) + " (8 MiB): use tcp_force_direct");
+    unsigned char *b = static_cast<unsigned char *>(base);
+    unsigned *status = reinterpret_cast<unsigned *>(b);
+    b += align256(16);
+    void *pos = b;
+    b += align256(n * (fp64 ? sizeof(double4_32a) : sizeof(int4)));
+    double *fsum = reinterpret_cast<double *>(b);
+    b += align256(sizeof(double) * 3 * (size_t)nbf);
+    double *upart = reinterpret_cast<double *>(b);
+    b += align256(sizeof(double) * (size_t)g.nblk * js);
+    double *fpart = reinterpret_cast<double *>(b);
+
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    TCP_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
+    noalloc_positions_kernel<<<ceil_div(tmp.n, 256), 256, 0, st>>>(
+        x, tmp.n, p->box[0], p->box[1], p->box[2], fp64 ? nullptr : static_cast<int4 *>(pos),
+        fp64 ? static_cast<double4_32a *>(pos) : nullptr);
+    PairArgs a;
+    a.xq = fp64 ? nullptr : static_cast<const int4 *>(pos);
+    a.xd = fp64 ? static_cast<const double4_32a *>(pos) : nullptr;
+    a.nel = nel;
+    a.n = tmp.n;
+    a.bi = g.bi;
+    a.nblk_e = g.nblk_e;
+    a.nblk = g.nblk;
+    a.tj = g.tj;
+    a.ntile_e = g.ntile_e;
+    a.ntile = g.ntile;
+    a.tiles_per_split = ceil_div(g.ntile, js);
+    a.fpart = fpart;
+    a.upart = upart;
+    a.rdf = nullptr;
+    a.status = status;
+    a.c = tmp.pc;
+    dim3 grid(g.nblk, js);
+    const int ei = p->ei_model == TCP_EI_DEUTSCH ? 1 : (p->ei_model == TCP_EI_KELBG ? 2 : 0);
+    if (fp64) {
+        if (ei == 0) pair_fp64_kernel<0, true, false><<<grid, kPairThreads, 0, st>>>(a);
+        else if (ei == 1) pair_fp64_kernel<1, true, false><<<grid, kPairThreads, 0, st>>>(a);
+        else pair_fp64_kernel<2, true, false><<<grid, kPairThreads, 0, st>>>(a);
+    } else {
+        if (ei == 0) pair_fp32c_kernel<0, true, false><<<grid, kPairThreads, 0, st>>>(a);
+        else if (ei == 1) pair_fp32c_kernel<1, true, false><<<grid, kPairThreads, 0, st>>>(a);
+        else pair_fp32c_kernel<2, true, false><<<grid, kPairThreads, 0, st>>>(a);
+    }
+    force_finalize_kernel<<<nbf, 256, 0, st>>>(fpart, js, nullptr, f, tmp.n, fsum);
+    noalloc_sum_kernel<<<1, 1024, 0, st>>>(upart, g.nblk * js, fsum);   // Ur into fsum[0]
+    TCP_CUDA(cudaGetLastError());
+    double ur = 0.0;
+    unsigned h_status = 0;
+    TCP_CUDA(cudaMemcpyAsync(&ur, fsum, sizeof(double), cudaMemcpyDeviceToHost, st));
+    TCP_CUDA(cudaMemcpyAsync(&h_status, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    TCP_CUDA(cudaStreamSynchronize(st));
+    if (h_status & kStatusTmaTimeout) return set_error(TCP_ERR_TIMEOUT, "a pair-kernel tile wait exceeded its bound");
+    if (Ur) *Ur = ur;
+    return TCP_OK;
+}
