@@ -43,12 +43,16 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "pair-int/s, steps/s @N=65536: FP32-comp vs FP64 on 1 GB300, ≤2e-6 force err"
 WORKLOAD = "n65536_spme128"
-# FP32-pipe issue slots per ordered pair of the pair kernel, counted from the
-# source of tile_f32 (pair.cu) for a Coulomb pair with energy: 3 FMUL (scale),
-# 3 (r^2), 1 (r), 1 (t), 1 (exp arg), 9 (erfc poly), 1 (erfc), 2 (Gaussian),
-# 3 (r^-3 weight), 3 (force FFMA), 2 (energy), 5 (compares/selects) = 34;
-# plus 3 int->float conversions and 3 SFU ops (rsqrt, rcp, ex2).
-RECIPE_FP32_OPS = 34
+# Source-level op recipe of the FP32C real-space kernels (pair.cu tile_f32,
+# pair_n3.cu n3_pair/n3_item), Coulomb pair with energy, cubic box: 3 integer
+# subtractions + 3 int->float conversions (minimum image), r^2 (3), cut-off
+# test (1), r (1), rcp argument (1), exp argument (1), erfc polynomial and
+# products (11), force numerator (1), r^-2 weight and select (3), force
+# accumulation (3), energy select+add (2) = 33 per ordered pair; the Newton-3
+# kernel adds the reaction accumulation (3) = 36 per unique pair.  SFU: rsqrt,
+# rcp, ex2 (3) per pair in both.
+RECIPE_ORDERED = 33
+RECIPE_N3 = 36
 RECIPE_SFU_OPS = 3
 SFU_RATE = 16.0 / 128.0       # SFU lanes per SM relative to FP32 lanes
 
@@ -239,6 +243,7 @@ def run_gpu(args, world, rank, local, dist):
     ctx.EWALD_SELF()
     ctx.upload(x=s.x, v=s.v)
     e0 = ctx.force()                        # initial forces (restart-style start, main.f90:49-54)
+    tune = ctx.autotune_report()
     _, _, f32, _ = ctx.download(x=False, v=False, f=True)
 
     ctx64 = T.Context(p64, s.nel, s.nion, device=local)
@@ -290,15 +295,21 @@ def run_gpu(args, world, rank, local, dist):
     d2h = n * 3 * 3 * 8
 
     # roofline of the pair kernel (live timing inside the timed steps)
-    peak = T.fp32_peak(local) * 1e12            # FFMA/s
-    ordered = float(n) * (n - 1)
-    achieved = RECIPE_FP32_OPS * ordered / (pair_ms * 1e-3)
-    sfu_frac = RECIPE_SFU_OPS * ordered / (pair_ms * 1e-3) / (peak * SFU_RATE)
+    peak = T.fp32_peak(local) * 1e12            # FFMA/s = lane instructions/s
+    variant, variant_ms = tune
+    if variant >= 1:
+        units, recipe, kname = float(n) * (n - 1) / 2, RECIPE_N3, f"pair_n3_kernel (Newton-3 variant {variant})"
+        runit = "unique pair"
+    else:
+        units, recipe, kname = float(n) * (n - 1), RECIPE_ORDERED, "pair_fp32c_kernel (ordered pairs)"
+        runit = "ordered pair"
+    achieved = recipe * units / (pair_ms * 1e-3)
+    sfu_frac = RECIPE_SFU_OPS * units / (pair_ms * 1e-3) / (peak * SFU_RATE)
     traffic = profile_traffic()
     roof = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "Top/s",
             "frac": achieved / peak, "traffic": traffic,
-            "kernel": "pair_fp32c_kernel (real-space all-pair sum)",
-            "recipe": f"{RECIPE_FP32_OPS} FP32-pipe ops + {RECIPE_SFU_OPS} SFU ops per ordered pair",
+            "kernel": kname, "autotune_ms": [round(x, 4) for x in variant_ms[:5].tolist()],
+            "recipe": f"{recipe} FP32/ALU-pipe ops + {RECIPE_SFU_OPS} SFU ops per {runit}",
             "peak_source": "measured FFMA issue rate (tcp_fp32_peak) on this GPU, not MEASURED_PEAKS.json "
                            "(which has HBM and bf16 only)",
             "sfu_frac": sfu_frac, "pair_kernel_ms": pair_ms}

@@ -215,6 +215,10 @@ int tcp_time_component(tcp_ctx *ctx, int which, int reps, double dt, double *ms_
  * reciprocal sum, real-space pair kernel, force epilogue + second half kick,
  * and the number of steps timed. */
 int tcp_time_steps(tcp_ctx *ctx, double dt, int nsteps, int flush_l2, double *out);
+/* The FP32C real-space kernel the autotuner picked for this context (0 =
+ * ordered pairs, >= 1 = Newton-3 variants) and the per-candidate times in ms
+ * (ms[k] for variant k, 0 when not timed), up to nmax entries. */
+int tcp_autotune_report(tcp_ctx *ctx, int *variant, double *ms, int nmax);
 /* Kernel launches issued by the context so far (all kernels of this library). */
 int tcp_launch_count(tcp_ctx *ctx, long long *count);
 /* Measured FP32 FFMA issue rate of the device: a calibration kernel of

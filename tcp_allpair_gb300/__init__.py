@@ -210,6 +210,14 @@ class Context:
         keys = ("step", "vverlet1", "recip", "pair", "epilogue", "nsteps")
         return dict(zip(keys, out.tolist()))
 
+    def autotune_report(self):
+        """(chosen FP32C pair-kernel variant, per-variant ms measured by the autotuner)."""
+        v = C.c_int()
+        ms = np.zeros(8)
+        self._chk(self.lib.tcp_autotune_report(self.h, C.byref(v), ms.ctypes.data_as(C.POINTER(C.c_double)), 8),
+                  "tcp_autotune_report")
+        return v.value, ms
+
     def launch_count(self):
         n = C.c_longlong()
         self._chk(self.lib.tcp_launch_count(self.h, C.byref(n)), "tcp_launch_count")

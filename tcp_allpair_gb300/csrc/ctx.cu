@@ -283,6 +283,7 @@ int tcp_ewald_self(tcp_ctx *c, double *alpha_out, double *Uo_out) {
     if (p.reciprocal == TCP_RECIP_SPME && (rc = spme_setup(c))) return rc;
     if (p.reciprocal == TCP_RECIP_EWALD && (rc = ewald_setup(c))) return rc;
     invalidate_graph(c);
+    c->tuned = false;
     c->ewald_ready = true;
     if (alpha_out) *alpha_out = c->alpha;
     if (Uo_out) *Uo_out = c->Uo;
@@ -420,6 +421,7 @@ int tcp_download_soa(tcp_ctx *c, double *x, double *v, double *f, double *frec) 
 int tcp_force_direct(tcp_ctx *c, double *Ur) {
     TCP_REQUIRE_READY(c);
     int rc;
+    if ((rc = autotune_pair(c))) return rc;
     if ((rc = launch_pair(c, energy_on(c), (c->flags & TCP_FLAG_RDF) != 0))) return rc;
     if ((rc = launch_force_finalize(c, false))) return rc;
     if (energy_on(c) && (rc = launch_reduce(c, kRedUr, 0))) return rc;
@@ -462,6 +464,7 @@ int tcp_remove_rigidmtn(tcp_ctx *c) {
 int tcp_force(tcp_ctx *c, tcp_energies *e) {
     TCP_REQUIRE_READY(c);
     int rc;
+    if ((rc = autotune_pair(c))) return rc;
     if ((rc = force_chain(c, true))) return rc;
     if ((rc = sync_scalars(c))) return rc;
     fill_energies(c, e);
@@ -493,6 +496,7 @@ int tcp_vverlet2(tcp_ctx *c, double dt, double *mv2el, double *mv2ion) {
 int tcp_finit(tcp_ctx *c, double dt, tcp_energies *e) {
     TCP_REQUIRE_READY(c);
     int rc;
+    if ((rc = autotune_pair(c))) return rc;
     if ((rc = launch_shift(c, -dt))) return rc;                  // init.f90:171-185
     if ((rc = force_chain(c, true))) return rc;                  // init.f90:193-220
     if ((rc = launch_shift(c, dt))) return rc;                   // init.f90:223-237
@@ -519,6 +523,8 @@ static int build_graph(tcp_ctx *c, double dt, bool apply, cudaGraphExec_t *out, 
 }
 
 static int ensure_graph(tcp_ctx *c, double dt) {
+    int arc = autotune_pair(c);   // timing launches cannot run inside a capture
+    if (arc) return arc;
     const bool has_thermo = c->p.thermo == TCP_THERMO_ISOKIN || c->p.thermo == TCP_THERMO_BEREND;
     // c->graph holds the step without the thermostat rescale; the rescale step
     // (ISOKIN/BEREND, every thermo_period-th step) is launched eagerly.
@@ -595,6 +601,7 @@ int tcp_time_component(tcp_ctx *c, int which, int reps, double dt, double *ms) {
     TCP_CUDA(cudaEventCreate(&e0));
     TCP_CUDA(cudaEventCreate(&e1));
     int rc = TCP_OK;
+    if ((rc = autotune_pair(c))) return rc;
     auto one = [&]() -> int {
         if (which == 0) return launch_pair(c, energy_on(c), false);
         return recip_launch(c);

@@ -31,6 +31,7 @@
 #include <string>
 
 #include "device_util.cuh"
+#include "pair_math.cuh"
 #include "tcp_internal.h"
 
 namespace tcp {
@@ -71,66 +72,75 @@ __device__ __forceinline__ void tile_range(const PairArgs &a, int t, int &j0, in
     }
 }
 
-// t Q(t) with the coefficients printed by fit_erfc.py (P = 0.5, degree 8).
-__device__ __forceinline__ float erfc_poly(float t) {
-    float q = -5.783473762e-02f;
-    q = fmaf(q, t, 2.784859768e-01f);
-    q = fmaf(q, t, -4.744286455e-01f);
-    q = fmaf(q, t, 2.632348585e-01f);
-    q = fmaf(q, t, -1.622527577e-02f);
-    q = fmaf(q, t, 1.981928108e-01f);
-    q = fmaf(q, t, 2.442685012e-01f);
-    q = fmaf(q, t, 2.822102988e-01f);
-    q = fmaf(q, t, 2.820961743e-01f);
-    return q * t;
-}
-
 // One j-tile for one i-particle (FP32).  KIND: 0 Coulomb erfc (e-e, i-i and
 // TCP_EI_COULOMB), 1 Deutsch e-i, 2 Kelbg e-i.  Accumulates sum_j w dx (the
 // force divided by eps q_i q_j) and sum_j u/r (energy / q_i q_j).
-template <int KIND, bool ENERGY, bool RDF, int TPP>
+// FULL: the tile holds kTjF particles (no tail test).  DIAG: the tile may
+// contain the i-particle itself (r^2 > 0 test).  CUBIC: all box lengths are
+// equal, so the fixed-point difference is used unscaled (lengths in units of
+// L/2^32) and the scale is folded into the constants and the per-tile factor
+// applied when the tile partial is folded.
+template <int KIND, bool ENERGY, bool RDF, int TPP, bool FULL, bool DIAG, bool CUBIC>
 __device__ __forceinline__ void tile_f32(const int4 *__restrict__ tj, int cnt, int sub, int4 xi,
                                          const PairConsts &c, float &px, float &py, float &pz,
                                          float &pe, unsigned *hist, float inv_dx) {
-    const int cnt_up = (cnt + TPP - 1) / TPP * TPP;   // uniform trip count per warp
-#pragma unroll 4
+    const int cnt_up = FULL ? kTjF : (cnt + TPP - 1) / TPP * TPP;   // uniform trip count per warp
+    // constants in the units of this path
+    const float rc2 = CUBIC ? c.u_rc2 : c.rc2f;
+    const float p_alpha = CUBIC ? c.u_p_alpha : c.p_alpha;
+    const float c_exp = CUBIC ? c.u_c_exp : c.c_exp;
+    const float c_gauss = CUBIC ? c.u_c_gauss : c.c_gauss;
+    const float c_rs = CUBIC ? c.u_c_rs : c.c_rs;
+    const float inv_rs = CUBIC ? c.u_inv_rs : c.inv_rs;
+    const float c_lam = CUBIC ? c.u_c_lam : c.c_lam;
+    const float p_lam = CUBIC ? c.u_p_lam : c.p_lam;
+    const float sqrtpi_lam = CUBIC ? c.u_sqrtpi_lam : c.sqrtpi_lam;
+    const float rshort2 = CUBIC ? c.u_rshort2 : c.rshort2;
+#pragma unroll 8
     for (int jj = sub; jj < cnt_up; jj += TPP) {
         const int4 xj = tj[jj];
-        const float dx = (float)(xi.x - xj.x) * c.sx;
-        const float dy = (float)(xi.y - xj.y) * c.sy;
-        const float dz = (float)(xi.z - xj.z) * c.sz;
+        float dx = (float)(xi.x - xj.x);
+        float dy = (float)(xi.y - xj.y);
+        float dz = (float)(xi.z - xj.z);
+        if (!CUBIC) {
+            dx *= c.sx;
+            dy *= c.sy;
+            dz *= c.sz;
+        }
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const bool ok = (jj < cnt) && (r2 < c.rc2f) && (r2 > 0.0f);
+        bool ok = r2 < rc2;
+        if (DIAG) ok = ok && (r2 > 0.0f);
+        if (!FULL) ok = ok && (jj < cnt);
         const float rinv = rsqrt_approx(r2);
         const float r = r2 * rinv;
-        const float t = rcp_approx(fmaf(c.p_alpha, r, 1.0f));
-        const float e = ex2_approx(c.c_exp * r2);
-        const float erfc_ar = e * erfc_poly(t);
-        float s = fmaf(c.c_gauss * r, e, erfc_ar);      // erfc(ar) + 2ar/sqrt(pi) exp(-a^2r^2)
-        float u = erfc_ar;
+        const float t = rcp_approx(fmaf(p_alpha, r, 1.0f));
+        const float e = ex2_approx(c_exp * r2);
+        const float er = (e * erfc_poly(t)) * rinv;     // erfc(ar)/r, shared by energy and force
+        float s = fmaf(c_gauss, e, er);                  // (erfc(ar) + 2ar/sqrt(pi) exp(-a^2r^2)) / r
+        float u = er;
         if (KIND == 1) {                                 // Deutsch, force.f90:136-139
-            const float y = ex2_approx(c.c_rs * r);      // exp(-r/rs)
-            s = fmaf(-y, fmaf(r, c.inv_rs, 1.0f), s);
-            u -= y;
+            const float y = ex2_approx(c_rs * r);        // exp(-r/rs)
+            s = fmaf(-y, rinv + inv_rs, s);
+            if (ENERGY) u = fmaf(-y, rinv, u);
         }
         if (KIND == 2) {                                 // Kelbg
-            const bool near = ok && (r2 < c.rshort2);
+            const bool near = ok && (r2 < rshort2);
             if (__any_sync(0xffffffffu, near)) {
-                const float g = ex2_approx(c.c_lam * r2);      // exp(-r^2/lambda^2)
-                s -= near ? g : 0.0f;
+                const float g = near ? ex2_approx(c_lam * r2) : 0.0f;   // exp(-r^2/lambda^2)
+                s = fmaf(-g, rinv, s);
                 if (ENERGY) {
-                    const float t2 = rcp_approx(fmaf(c.p_lam, r, 1.0f));
+                    const float t2 = rcp_approx(fmaf(p_lam, r, 1.0f));
                     const float erfc_rl = g * erfc_poly(t2);   // erfc(r/lambda)
-                    u += near ? fmaf(c.sqrtpi_lam * r, erfc_rl, -g) : 0.0f;
+                    u += fmaf(sqrtpi_lam, erfc_rl, -g * rinv);
                 }
             }
         }
-        float w = s * (rinv * rinv) * rinv;
+        float w = s * (rinv * rinv);
         w = ok ? w : 0.0f;
         px = fmaf(w, dx, px);
         py = fmaf(w, dy, py);
         pz = fmaf(w, dz, pz);
-        if (ENERGY) pe += ok ? u * rinv : 0.0f;
+        if (ENERGY) pe += ok ? u : 0.0f;                 // select: r = 0 gives inf/NaN
         if (RDF) {
             if (ok) {
                 const int bin = (int)(r * inv_dx);
@@ -140,7 +150,23 @@ __device__ __forceinline__ void tile_f32(const int4 *__restrict__ tj, int cnt, i
     }
 }
 
-template <int EIKIND, bool ENERGY, bool RDF>
+// Dispatch one tile to the specialised loop (uniform per CTA and tile).
+template <int KIND, bool ENERGY, bool RDF, bool CUBIC>
+__device__ __forceinline__ void tile_f32_any(const int4 *__restrict__ tj, int cnt, bool diag, int sub, int4 xi,
+                                             const PairConsts &c, float &px, float &py, float &pz, float &pe,
+                                             unsigned *hist, float inv_dx) {
+    constexpr int TPP = kTppF;
+    if (RDF) {
+        tile_f32<KIND, ENERGY, RDF, TPP, false, true, CUBIC>(tj, cnt, sub, xi, c, px, py, pz, pe, hist, inv_dx);
+    } else if (cnt == kTjF) {
+        if (diag) tile_f32<KIND, ENERGY, false, TPP, true, true, CUBIC>(tj, cnt, sub, xi, c, px, py, pz, pe, hist, inv_dx);
+        else tile_f32<KIND, ENERGY, false, TPP, true, false, CUBIC>(tj, cnt, sub, xi, c, px, py, pz, pe, hist, inv_dx);
+    } else {
+        tile_f32<KIND, ENERGY, false, TPP, false, true, CUBIC>(tj, cnt, sub, xi, c, px, py, pz, pe, hist, inv_dx);
+    }
+}
+
+template <int EIKIND, bool ENERGY, bool RDF, bool CUBIC>
 __global__ void __launch_bounds__(kPairThreads) pair_fp32c_kernel(const PairArgs a) {
     constexpr int TPP = kTppF;
     __shared__ __align__(128) int4 tiles[kStagesF][kTjF];
@@ -195,18 +221,21 @@ __global__ void __launch_bounds__(kPairThreads) pair_fp32c_kernel(const PairArgs
         const int pt = si + sj;   // 0 e-e, 1 e-i, 2 i-i
         float px = 0.f, py = 0.f, pz = 0.f, pe = 0.f;
         unsigned *h = RDF ? hist + pt * kNbin : nullptr;
-        const float inv_dx = RDF ? a.c.inv_dx[pt] : 0.f;
+        const float inv_dx = RDF ? (CUBIC ? a.c.u_inv_dx[pt] : a.c.inv_dx[pt]) : 0.f;
+        // the tile can hold the i-particles of this CTA only on the diagonal
+        const bool diag = (j0 < i0 + a.bi) && (i0 < j0 + cnt);
         if (pt == 1 && EIKIND == 1)
-            tile_f32<1, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, px, py, pz, pe, h, inv_dx);
+            tile_f32_any<1, ENERGY, RDF, CUBIC>(tiles[stage], cnt, diag, sub, xi, a.c, px, py, pz, pe, h, inv_dx);
         else if (pt == 1 && EIKIND == 2)
-            tile_f32<2, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, px, py, pz, pe, h, inv_dx);
+            tile_f32_any<2, ENERGY, RDF, CUBIC>(tiles[stage], cnt, diag, sub, xi, a.c, px, py, pz, pe, h, inv_dx);
         else
-            tile_f32<0, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, px, py, pz, pe, h, inv_dx);
-        const float qq = a.c.qqf[pt];
-        acc2(fxh, fxl, px * qq);
-        acc2(fyh, fyl, py * qq);
-        acc2(fzh, fzl, pz * qq);
-        if (ENERGY) acc2(eh, el, pe * qq);
+            tile_f32_any<0, ENERGY, RDF, CUBIC>(tiles[stage], cnt, diag, sub, xi, a.c, px, py, pz, pe, h, inv_dx);
+        const float qf = CUBIC ? a.c.u_qq_force[pt] : a.c.qqf[pt];
+        const float qe = CUBIC ? a.c.u_qq_energy[pt] : a.c.qqf[pt];
+        acc2(fxh, fxl, px * qf);
+        acc2(fyh, fyl, py * qf);
+        acc2(fzh, fzl, pz * qf);
+        if (ENERGY) acc2(eh, el, pe * qe);
         // every thread has finished reading this stage: refill it
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicOr(a.status, kStatusTmaTimeout);
@@ -468,6 +497,24 @@ static void make_consts(tcp_ctx *c) {
         k.qqf[t] = (float)qq[t];
         k.qq[t] = qq[t];
     }
+    // cubic-box constants in units of u = L/2^32
+    k.cubic = (p.box[0] == p.box[1] && p.box[1] == p.box[2]) ? 1 : 0;
+    const double u = p.box[0] / two32;
+    k.u_rc2 = (float)(c->rc2 / (u * u));
+    k.u_p_alpha = (float)(0.5 * c->alpha * u);
+    k.u_c_exp = (float)(-c->alpha * c->alpha * log2e * u * u);
+    k.u_c_gauss = (float)(2.0 * c->alpha / kSqrtPi * u);
+    k.u_c_rs = (float)(-log2e / rs * u);
+    k.u_inv_rs = (float)(u / rs);
+    k.u_c_lam = (float)(-log2e / (lam * lam) * u * u);
+    k.u_p_lam = (float)(0.5 / lam * u);
+    k.u_sqrtpi_lam = (float)(kSqrtPi / lam * u);
+    k.u_rshort2 = (float)(36.0 * lam * lam / (u * u));
+    for (int t = 0; t < 3; ++t) {
+        k.u_inv_dx[t] = dxs[t] > 0 ? (float)(u / dxs[t]) : 0.f;
+        k.u_qq_force[t] = (float)(qq[t] / (u * u));
+        k.u_qq_energy[t] = (float)(qq[t] / u);
+    }
     for (int d = 0; d < 3; ++d) k.box[d] = p.box[d];
     k.rc2 = c->rc2;
     k.alpha = c->alpha;
@@ -520,7 +567,7 @@ int pair_setup(tcp_ctx *c) {
     if (fp64)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp64_kernel<0, true, false>, kPairThreads, 0);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp32c_kernel<2, true, false>, kPairThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp32c_kernel<2, true, false, true>, kPairThreads, 0);
     const char *env = getenv("TCP_JSPLIT");
     int js = env ? atoi(env) : choose_jsplit(c, g, bps);
     js = std::max(1, std::min(js, g.ntile));
@@ -531,7 +578,7 @@ int pair_setup(tcp_ctx *c) {
     c->fpart = nullptr;
     c->upart = nullptr;
     c->jsplit = js;
-    c->n_upart = g.nblk * js;
+    c->n_upart = std::max(g.nblk * js, fp64 ? 1 : n3_grid(c));
     TCP_CUDA(cudaMalloc(&c->fpart, sizeof(double) * 3 * (size_t)c->n * js));
     TCP_CUDA(cudaMalloc(&c->upart, sizeof(double) * (size_t)c->n_upart));
     TCP_CUDA(cudaMemsetAsync(c->upart, 0, sizeof(double) * (size_t)c->n_upart, c->stream));
@@ -540,6 +587,11 @@ int pair_setup(tcp_ctx *c) {
 
 int launch_pair(tcp_ctx *c, bool energy, bool rdf) {
     const bool fp64 = c->p.precision == TCP_PREC_FP64;
+    if (!rdf && n3_applicable(c)) {
+        c->fpart_splits = 1;
+        return launch_pair_n3(c, energy);
+    }
+    c->fpart_splits = c->jsplit;
     Geometry g = geometry(c, fp64);
     PairArgs a;
     a.xq = c->xq;
@@ -560,29 +612,31 @@ int launch_pair(tcp_ctx *c, bool energy, bool rdf) {
     a.c = c->pc;
     dim3 grid(g.nblk, c->jsplit);
     const int ei = c->p.ei_model == TCP_EI_DEUTSCH ? 1 : (c->p.ei_model == TCP_EI_KELBG ? 2 : 0);
-#define TCP_PAIR_DISPATCH(KERNEL)                                                                \
-    do {                                                                                         \
-        if (ei == 0) {                                                                           \
-            if (energy && rdf) KERNEL<0, true, true><<<grid, kPairThreads, 0, c->stream>>>(a);   \
-            else if (energy) KERNEL<0, true, false><<<grid, kPairThreads, 0, c->stream>>>(a);    \
-            else if (rdf) KERNEL<0, false, true><<<grid, kPairThreads, 0, c->stream>>>(a);       \
-            else KERNEL<0, false, false><<<grid, kPairThreads, 0, c->stream>>>(a);               \
-        } else if (ei == 1) {                                                                    \
-            if (energy && rdf) KERNEL<1, true, true><<<grid, kPairThreads, 0, c->stream>>>(a);   \
-            else if (energy) KERNEL<1, true, false><<<grid, kPairThreads, 0, c->stream>>>(a);    \
-            else if (rdf) KERNEL<1, false, true><<<grid, kPairThreads, 0, c->stream>>>(a);       \
-            else KERNEL<1, false, false><<<grid, kPairThreads, 0, c->stream>>>(a);               \
-        } else {                                                                                 \
-            if (energy && rdf) KERNEL<2, true, true><<<grid, kPairThreads, 0, c->stream>>>(a);   \
-            else if (energy) KERNEL<2, true, false><<<grid, kPairThreads, 0, c->stream>>>(a);    \
-            else if (rdf) KERNEL<2, false, true><<<grid, kPairThreads, 0, c->stream>>>(a);       \
-            else KERNEL<2, false, false><<<grid, kPairThreads, 0, c->stream>>>(a);               \
-        }                                                                                        \
+#define TCP_PAIR_DISPATCH(KERNEL, ...)                                                                   \
+    do {                                                                                                 \
+        if (ei == 0) {                                                                                   \
+            if (energy && rdf) KERNEL<0, true, true __VA_ARGS__><<<grid, kPairThreads, 0, c->stream>>>(a);   \
+            else if (energy) KERNEL<0, true, false __VA_ARGS__><<<grid, kPairThreads, 0, c->stream>>>(a);    \
+            else if (rdf) KERNEL<0, false, true __VA_ARGS__><<<grid, kPairThreads, 0, c->stream>>>(a);       \
+            else KERNEL<0, false, false __VA_ARGS__><<<grid, kPairThreads, 0, c->stream>>>(a);               \
+        } else if (ei == 1) {                                                                            \
+            if (energy && rdf) KERNEL<1, true, true __VA_ARGS__><<<grid, kPairThreads, 0, c->stream>>>(a);   \
+            else if (energy) KERNEL<1, true, false __VA_ARGS__><<<grid, kPairThreads, 0, c->stream>>>(a);    \
+            else if (rdf) KERNEL<1, false, true __VA_ARGS__><<<grid, kPairThreads, 0, c->stream>>>(a);       \
+            else KERNEL<1, false, false __VA_ARGS__><<<grid, kPairThreads, 0, c->stream>>>(a);               \
+        } else {                                                                                         \
+            if (energy && rdf) KERNEL<2, true, true __VA_ARGS__><<<grid, kPairThreads, 0, c->stream>>>(a);   \
+            else if (energy) KERNEL<2, true, false __VA_ARGS__><<<grid, kPairThreads, 0, c->stream>>>(a);    \
+            else if (rdf) KERNEL<2, false, true __VA_ARGS__><<<grid, kPairThreads, 0, c->stream>>>(a);       \
+            else KERNEL<2, false, false __VA_ARGS__><<<grid, kPairThreads, 0, c->stream>>>(a);               \
+        }                                                                                                \
     } while (0)
     if (fp64)
         TCP_PAIR_DISPATCH(pair_fp64_kernel);
+    else if (c->pc.cubic)
+        TCP_PAIR_DISPATCH(pair_fp32c_kernel, , true);
     else
-        TCP_PAIR_DISPATCH(pair_fp32c_kernel);
+        TCP_PAIR_DISPATCH(pair_fp32c_kernel, , false);
 #undef TCP_PAIR_DISPATCH
     c->launches++;
     TCP_CUDA(cudaGetLastError());
@@ -592,7 +646,7 @@ int launch_pair(tcp_ctx *c, bool energy, bool rdf) {
 int launch_force_finalize(tcp_ctx *c, bool add_rec) {
     const int threads = 256;
     const int blocks = ceil_div(c->n, threads);
-    force_finalize_kernel<<<blocks, threads, 0, c->stream>>>(c->fpart, c->jsplit, add_rec ? c->frec : nullptr,
+    force_finalize_kernel<<<blocks, threads, 0, c->stream>>>(c->fpart, c->fpart_splits, add_rec ? c->frec : nullptr,
                                                              c->f, c->n, c->red);
     c->launches++;
     TCP_CUDA(cudaGetLastError());
@@ -707,7 +761,7 @@ extern "C" int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, 
     if (fp64)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp64_kernel<0, true, false>, kPairThreads, 0);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp32c_kernel<2, true, false>, kPairThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp32c_kernel<2, true, false, true>, kPairThreads, 0);
     const size_t n = (size_t)tmp.n;
     const int nbf = ceil_div(tmp.n, 256);
     auto need = [&](int js) {
@@ -762,9 +816,15 @@ extern "C" int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, 
         else if (ei == 1) pair_fp64_kernel<1, true, false><<<grid, kPairThreads, 0, st>>>(a);
         else pair_fp64_kernel<2, true, false><<<grid, kPairThreads, 0, st>>>(a);
     } else {
-        if (ei == 0) pair_fp32c_kernel<0, true, false><<<grid, kPairThreads, 0, st>>>(a);
-        else if (ei == 1) pair_fp32c_kernel<1, true, false><<<grid, kPairThreads, 0, st>>>(a);
-        else pair_fp32c_kernel<2, true, false><<<grid, kPairThreads, 0, st>>>(a);
+        if (tmp.pc.cubic) {
+            if (ei == 0) pair_fp32c_kernel<0, true, false, true><<<grid, kPairThreads, 0, st>>>(a);
+            else if (ei == 1) pair_fp32c_kernel<1, true, false, true><<<grid, kPairThreads, 0, st>>>(a);
+            else pair_fp32c_kernel<2, true, false, true><<<grid, kPairThreads, 0, st>>>(a);
+        } else {
+            if (ei == 0) pair_fp32c_kernel<0, true, false, false><<<grid, kPairThreads, 0, st>>>(a);
+            else if (ei == 1) pair_fp32c_kernel<1, true, false, false><<<grid, kPairThreads, 0, st>>>(a);
+            else pair_fp32c_kernel<2, true, false, false><<<grid, kPairThreads, 0, st>>>(a);
+        }
     }
     force_finalize_kernel<<<nbf, 256, 0, st>>>(fpart, js, nullptr, f, tmp.n, fsum);
     noalloc_sum_kernel<<<1, 1024, 0, st>>>(upart, g.nblk * js, fsum);   // Ur into fsum[0]
@@ -776,5 +836,104 @@ extern "C" int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, 
     TCP_CUDA(cudaStreamSynchronize(st));
     if (h_status & kStatusTmaTimeout) return set_error(TCP_ERR_TIMEOUT, "a pair-kernel tile wait exceeded its bound");
     if (Ur) *Ur = ur;
+    return TCP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner of the FP32C real-space kernel.  Candidates: the ordered-pair
+// kernel (variant 0, any box) and the Newton-3 kernels (variants 1..V, cubic
+// boxes: unroll depth of the rotation loop x CTAs per SM).  Each candidate is
+// launched once to warm up and timed over two launches with CUDA events on the
+// context's stream, on the positions currently on the device; the fastest is
+// kept.  TCP_PAIR_VARIANT=k forces variant k; TCP_AUTOTUNE=0 keeps the default
+// (Newton-3 variant 1 for cubic boxes); TCP_AUTOTUNE_CACHE=<file> stores the
+// choice per (device, n, nel, e-i model) and reuses it without timing.
+namespace tcp {
+
+static std::string tune_key(const tcp_ctx *c) {
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, c->device);
+    return std::string(prop.name) + "|" + std::to_string(c->n) + "|" + std::to_string(c->nel) + "|" +
+           std::to_string(c->p.ei_model);
+}
+
+static int cache_lookup(const char *path, const std::string &key) {
+    FILE *f = fopen(path, "r");
+    if (!f) return -1;
+    char line[512];
+    int v = -1;
+    while (fgets(line, sizeof line, f)) {
+        std::string s(line);
+        const size_t sp = s.rfind(' ');
+        if (sp != std::string::npos && s.substr(0, sp) == key) v = atoi(s.c_str() + sp + 1);
+    }
+    fclose(f);
+    return v;
+}
+
+int autotune_pair(tcp_ctx *c) {
+    if (c->p.precision != TCP_PREC_FP32C || c->tuned) return TCP_OK;
+    c->tuned = true;
+    const int nv = c->pc.cubic ? n3_variant_count() : 0;
+    c->pair_variant = c->pc.cubic ? 1 : 0;
+    if (const char *forced = getenv("TCP_PAIR_VARIANT")) {
+        c->pair_variant = std::min(std::max(atoi(forced), 0), nv);
+        return TCP_OK;
+    }
+    if (const char *off = getenv("TCP_AUTOTUNE"))
+        if (atoi(off) == 0) return TCP_OK;
+    const char *cache = getenv("TCP_AUTOTUNE_CACHE");
+    const std::string key = tune_key(c);
+    if (cache) {
+        const int v = cache_lookup(cache, key);
+        if (v >= 0 && v <= nv) {
+            c->pair_variant = v;
+            return TCP_OK;
+        }
+    }
+    cudaEvent_t e0, e1;
+    TCP_CUDA(cudaEventCreate(&e0));
+    TCP_CUDA(cudaEventCreate(&e1));
+    double best = 1e300;
+    int best_v = c->pair_variant;
+    int rc = TCP_OK;
+    for (int v = 0; v <= nv && !rc; ++v) {
+        c->pair_variant = v;
+        const long long before = c->launches;
+        rc = launch_pair(c, true, false);
+        cudaEventRecord(e0, c->stream);
+        for (int r = 0; r < 2 && !rc; ++r) rc = launch_pair(c, true, false);
+        cudaEventRecord(e1, c->stream);
+        cudaEventSynchronize(e1);
+        c->launches = before;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        c->pair_variant_ms[v] = ms / 2;
+        if (ms / 2 < best) {
+            best = ms / 2;
+            best_v = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    c->pair_variant = best_v;
+    if (cache) {
+        if (FILE *f = fopen(cache, "a")) {
+            fprintf(f, "%s %d\n", key.c_str(), best_v);
+            fclose(f);
+        }
+    }
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+}  // namespace tcp
+
+extern "C" int tcp_autotune_report(tcp_ctx *c, int *variant, double *ms, int nmax) {
+    using namespace tcp;
+    if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
+    if (variant) *variant = c->pair_variant;
+    for (int k = 0; ms && k < nmax && k < 8; ++k) ms[k] = c->pair_variant_ms[k];
     return TCP_OK;
 }

@@ -5,6 +5,11 @@
 // FP64.  The 3-D FFT is cuFFT D2Z / Z2D on that layout (the only library
 // call of the path); spreading, the influence-function multiply fused with
 // the energy reduction, and the force gather are kernels of this file.
+// In the compensated-FP32 mode the charges are still accumulated in FP64
+// (the structure-factor accumulation) and the mesh is then rounded to FP32
+// for R2C / C2R transforms, the influence multiply (energy summed in FP64)
+// and the force gather: on GB300 FP64 runs at 1/64 of the FP32 rate, which
+// makes a 128^3 FP64 transform compute-bound.
 //
 // Normalisation: both transforms are unnormalised, so the real mesh after the
 // inverse transform is phi = K^3 Qfin of the reference; its 1/K^3 (FFTE
@@ -32,41 +37,41 @@ struct SpmeArgs {
 // points INT(u) + j - (P-3).  Order 4 uses the reference's explicit cubics
 // (force.f90:703-738); other orders the Cox-de Boor recursion run upward on
 // the P nonzero values.
-template <int P>
-__device__ __forceinline__ void spline_w(double u, double *W, double *dW) {
+template <int P, typename T>
+__device__ __forceinline__ void spline_w(double u, T *W, T *dW) {
     if (P == 4) {
-        double z = trunc(u) - u + 1.0;
-        W[0] = z * z * z / 6.0;
-        dW[0] = -3. * z * z / 6.0;
-        z += 1.0;
-        W[1] = (-3. * z * z * z + 12. * z * z - 12. * z + 4.) / 6.0;
-        dW[1] = (9. * z * z - 24. * z + 12.) / 6.0;
-        z += 1.0;
-        W[2] = (3. * z * z * z - 24. * z * z + 60. * z - 44.) / 6.0;
-        dW[2] = (-9. * z * z + 48. * z - 60.) / 6.0;
-        z += 1.0;
-        W[3] = (-z * z * z + 12. * z * z - 48. * z + 64.) / 6.0;
-        dW[3] = (3. * z * z - 24. * z + 48.) / 6.0;
+        T z = (T)(trunc(u) - u + 1.0);
+        W[0] = z * z * z / (T)6;
+        dW[0] = (T)-3. * z * z / (T)6;
+        z += (T)1;
+        W[1] = ((T)-3. * z * z * z + (T)12. * z * z - (T)12. * z + (T)4.) / (T)6;
+        dW[1] = ((T)9. * z * z - (T)24. * z + (T)12.) / (T)6;
+        z += (T)1;
+        W[2] = ((T)3. * z * z * z - (T)24. * z * z + (T)60. * z - (T)44.) / (T)6;
+        dW[2] = ((T)-9. * z * z + (T)48. * z - (T)60.) / (T)6;
+        z += (T)1;
+        W[3] = (-z * z * z + (T)12. * z * z - (T)48. * z + (T)64.) / (T)6;
+        dW[3] = ((T)3. * z * z - (T)24. * z + (T)48.) / (T)6;
         return;
     }
-    const double w = u - trunc(u);
-    double a[P];
-    a[0] = 1.0;
+    const T w = (T)(u - trunc(u));
+    T a[P];
+    a[0] = (T)1;
 #pragma unroll
-    for (int j = 1; j < P; ++j) a[j] = 0.0;
+    for (int j = 1; j < P; ++j) a[j] = (T)0;
     // a_n[j] = ((w+n-1-j) a_{n-1}[j-1] + (1-w+j) a_{n-1}[j]) / (n-1)
 #pragma unroll
     for (int nn = 2; nn <= P; ++nn) {
         if (nn == P) {
 #pragma unroll
-            for (int j = 0; j < P; ++j) dW[j] = (j > 0 ? a[j - 1] : 0.0) - (j < P - 1 ? a[j] : 0.0);
+            for (int j = 0; j < P; ++j) dW[j] = (j > 0 ? a[j - 1] : (T)0) - (j < P - 1 ? a[j] : (T)0);
         }
-        const double inv = 1.0 / (double)(nn - 1);
+        const T inv = (T)1 / (T)(nn - 1);
 #pragma unroll
         for (int j = nn - 1; j >= 0; --j) {
-            const double left = j > 0 ? a[j - 1] : 0.0;
-            const double right = j < nn - 1 ? a[j] : 0.0;
-            a[j] = ((w + nn - 1 - j) * left + (1.0 - w + j) * right) * inv;
+            const T left = j > 0 ? a[j - 1] : (T)0;
+            const T right = j < nn - 1 ? a[j] : (T)0;
+            a[j] = ((w + (T)(nn - 1 - j)) * left + ((T)1 - w + (T)j) * right) * inv;
         }
     }
 #pragma unroll
@@ -91,7 +96,7 @@ __global__ void spme_spread_kernel(const SpmeArgs a, double *__restrict__ Q) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];   // :700-702
-        spline_w<P>(u, W[d], dW[d]);
+        spline_w<P, double>(u, W[d], dW[d]);
         base[d] = (int)trunc(u) - (P - 3);
     }
 #pragma unroll 1
@@ -132,35 +137,36 @@ __global__ void spme_influence_kernel(cufftDoubleComplex *__restrict__ Qk, const
     }
 }
 
-// force gather, force.f90:868-919
-template <int P>
-__global__ void spme_gather_kernel(const SpmeArgs a, const double *__restrict__ phi, double coef,
+// force gather, force.f90:868-919.  T = double (FP64 mode) or float (FP32C
+// mode: FP32 mesh and weights, the per-particle sum in FP32, force in FP64).
+template <int P, typename T>
+__global__ void spme_gather_kernel(const SpmeArgs a, const T *__restrict__ phi, double coef,
                                    double *__restrict__ frec) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= a.n) return;
     const double q = m < a.nel ? a.q0 : a.q1;
     const double L[3] = {a.box0, a.box1, a.box2};
     const int K[3] = {a.K1, a.K2, a.K3};
-    double W[3][P], dW[3][P];
+    T W[3][P], dW[3][P];
     int base[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];
-        spline_w<P>(u, W[d], dW[d]);
+        spline_w<P, T>(u, W[d], dW[d]);
         base[d] = (int)trunc(u) - (P - 3);
     }
-    double gx = 0.0, gy = 0.0, gz = 0.0;
+    T gx = 0, gy = 0, gz = 0;
 #pragma unroll 1
     for (int k = 0; k < P; ++k) {
         const int iz = wrapi(base[2] + k, a.K3);
 #pragma unroll 1
         for (int j = 0; j < P; ++j) {
             const int iy = wrapi(base[1] + j, a.K2);
-            const double *row = phi + (size_t)a.K1 * (iy + (size_t)a.K2 * iz);
-            double sx = 0.0, sd = 0.0;
+            const T *row = phi + (size_t)a.K1 * (iy + (size_t)a.K2 * iz);
+            T sx = 0, sd = 0;
 #pragma unroll
             for (int i = 0; i < P; ++i) {
-                const double ph = row[wrapi(base[0] + i, a.K1)];
+                const T ph = row[wrapi(base[0] + i, a.K1)];
                 sx += dW[0][i] * ph;
                 sd += W[0][i] * ph;
             }
@@ -170,9 +176,38 @@ __global__ void spme_gather_kernel(const SpmeArgs a, const double *__restrict__ 
         }
     }
     // F = -eps/(pi V) q (K_d/L_d) sum dW W W phi
-    frec[m] = -coef * q * gx * ((double)a.K1 / a.box0);
-    frec[(size_t)a.n + m] = -coef * q * gy * ((double)a.K2 / a.box1);
-    frec[2 * (size_t)a.n + m] = -coef * q * gz * ((double)a.K3 / a.box2);
+    frec[m] = -coef * q * (double)gx * ((double)a.K1 / a.box0);
+    frec[(size_t)a.n + m] = -coef * q * (double)gy * ((double)a.K2 / a.box1);
+    frec[2 * (size_t)a.n + m] = -coef * q * (double)gz * ((double)a.K3 / a.box2);
+}
+
+// FP32C mode: the FP64 charge mesh rounded to FP32 for the transforms
+__global__ void mesh_to_float_kernel(const double *__restrict__ q, float *__restrict__ qf, long n) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        qf[i] = (float)q[i];
+}
+
+// FP32C influence multiply; the energy sum is kept in FP64
+__global__ void spme_influence_f_kernel(cufftComplex *__restrict__ Qk, const float *__restrict__ infl, long total,
+                                        int Kh, int K1, double *__restrict__ epart, bool energy) {
+    __shared__ double red[32];
+    double e = 0.0;
+    for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+        const float g = infl[idx];
+        cufftComplex z = Qk[idx];
+        if (energy) {
+            const int kx = (int)(idx % Kh);
+            const double wgt = (kx == 0 || (2 * kx == K1)) ? 1.0 : 2.0;
+            e += wgt * (double)g * ((double)z.x * z.x + (double)z.y * z.y);
+        }
+        z.x *= g;
+        z.y *= g;
+        Qk[idx] = z;
+    }
+    if (energy) {
+        const double t = block_sum(e, red);
+        if (threadIdx.x == 0) epart[blockIdx.x] = t;
+    }
 }
 
 __global__ void sum_partials_kernel(const double *__restrict__ part, int np, double scale,
@@ -272,9 +307,15 @@ int spme_free(tcp_ctx *c) {
     cudaFree(c->Q);
     cudaFree(c->Qk);
     cudaFree(c->infl);
+    cudaFree(c->Qf);
+    cudaFree(c->Qkf);
+    cudaFree(c->infl_f);
     c->Q = nullptr;
     c->Qk = nullptr;
     c->infl = nullptr;
+    c->Qf = nullptr;
+    c->Qkf = nullptr;
+    c->infl_f = nullptr;
     return TCP_OK;
 }
 
@@ -291,18 +332,25 @@ int spme_setup(tcp_ctx *c) {
     c->Kh = c->K1 / 2 + 1;
     const size_t nreal = (size_t)c->K1 * c->K2 * c->K3;
     const size_t nhalf = (size_t)c->Kh * c->K2 * c->K3;
+    c->spme_fp32 = c->p.precision == TCP_PREC_FP32C;
     if (!c->Q) {
         if (cudaMalloc(&c->Q, sizeof(double) * nreal) != cudaSuccess ||
             cudaMalloc(&c->Qk, sizeof(cufftDoubleComplex) * nhalf) != cudaSuccess ||
             cudaMalloc(&c->infl, sizeof(double) * nhalf) != cudaSuccess)
             return set_error(TCP_ERR_NOMEM, "SPME mesh allocation failed");
+        if (c->spme_fp32 && (cudaMalloc(&c->Qf, sizeof(float) * nreal) != cudaSuccess ||
+                             cudaMalloc(&c->Qkf, sizeof(cufftComplex) * nhalf) != cudaSuccess ||
+                             cudaMalloc(&c->infl_f, sizeof(float) * nhalf) != cudaSuccess))
+            return set_error(TCP_ERR_NOMEM, "SPME FP32 mesh allocation failed");
     }
     if (!c->plans) {
-        if (cufftPlan3d(&c->plan_f, c->K3, c->K2, c->K1, CUFFT_D2Z) != CUFFT_SUCCESS)
-            return set_error(TCP_ERR_CUFFT, "cufftPlan3d D2Z failed");
-        if (cufftPlan3d(&c->plan_b, c->K3, c->K2, c->K1, CUFFT_Z2D) != CUFFT_SUCCESS) {
+        const cufftType tf = c->spme_fp32 ? CUFFT_R2C : CUFFT_D2Z;
+        const cufftType tb = c->spme_fp32 ? CUFFT_C2R : CUFFT_Z2D;
+        if (cufftPlan3d(&c->plan_f, c->K3, c->K2, c->K1, tf) != CUFFT_SUCCESS)
+            return set_error(TCP_ERR_CUFFT, "cufftPlan3d forward failed");
+        if (cufftPlan3d(&c->plan_b, c->K3, c->K2, c->K1, tb) != CUFFT_SUCCESS) {
             cufftDestroy(c->plan_f);
-            return set_error(TCP_ERR_CUFFT, "cufftPlan3d Z2D failed");
+            return set_error(TCP_ERR_CUFFT, "cufftPlan3d inverse failed");
         }
         cufftSetStream(c->plan_f, c->stream);
         cufftSetStream(c->plan_b, c->stream);
@@ -332,6 +380,11 @@ int spme_setup(tcp_ctx *c) {
         }
     }
     TCP_CUDA(cudaMemcpyAsync(c->infl, h.data(), sizeof(double) * nhalf, cudaMemcpyHostToDevice, c->stream));
+    if (c->spme_fp32) {
+        std::vector<float> hf(h.begin(), h.end());
+        TCP_CUDA(cudaMemcpyAsync(c->infl_f, hf.data(), sizeof(float) * nhalf, cudaMemcpyHostToDevice, c->stream));
+        TCP_CUDA(cudaStreamSynchronize(c->stream));
+    }
     TCP_CUDA(cudaStreamSynchronize(c->stream));
     return TCP_OK;
 }
@@ -357,8 +410,10 @@ static void launch_spread_gather(tcp_ctx *c, const SpmeArgs &a, bool gather, dou
     const int threads = 128, blocks = (c->n + threads - 1) / threads;
     if (!gather)
         spme_spread_kernel<P><<<blocks, threads, 0, c->stream>>>(a, c->Q);
+    else if (c->spme_fp32)
+        spme_gather_kernel<P, float><<<blocks, threads, 0, c->stream>>>(a, c->Qf, coef, c->frec);
     else
-        spme_gather_kernel<P><<<blocks, threads, 0, c->stream>>>(a, c->Q, coef, c->frec);
+        spme_gather_kernel<P, double><<<blocks, threads, 0, c->stream>>>(a, c->Q, coef, c->frec);
 }
 
 static void spread_gather(tcp_ctx *c, const SpmeArgs &a, bool gather, double coef) {
@@ -378,15 +433,24 @@ int launch_spme(tcp_ctx *c, bool energy) {
     const SpmeArgs a = spme_args(c);
     const size_t nreal = (size_t)c->K1 * c->K2 * c->K3;
     TCP_CUDA(cudaMemsetAsync(c->Q, 0, sizeof(double) * nreal, c->stream));
-    spread_gather(c, a, false, 0.0);
+    spread_gather(c, a, false, 0.0);                       // FP64 charge accumulation
     c->launches++;
-    if (cufftExecD2Z(c->plan_f, c->Q, c->Qk) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecD2Z failed");
     const long total = (long)c->K3 * c->K2 * c->Kh;
     const int eb = spme_energy_blocks(c);
     double *epart = recip_epart(c);
-    spme_influence_kernel<<<eb, 256, 0, c->stream>>>(c->Qk, c->infl, total, c->Kh, c->K1, epart, energy);
-    c->launches++;
-    if (cufftExecZ2D(c->plan_b, c->Qk, c->Q) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecZ2D failed");
+    if (c->spme_fp32) {
+        mesh_to_float_kernel<<<std::min<long>((nreal + 255) / 256, 4096), 256, 0, c->stream>>>(c->Q, c->Qf, (long)nreal);
+        c->launches++;
+        if (cufftExecR2C(c->plan_f, c->Qf, c->Qkf) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecR2C failed");
+        spme_influence_f_kernel<<<eb, 256, 0, c->stream>>>(c->Qkf, c->infl_f, total, c->Kh, c->K1, epart, energy);
+        c->launches++;
+        if (cufftExecC2R(c->plan_b, c->Qkf, c->Qf) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecC2R failed");
+    } else {
+        if (cufftExecD2Z(c->plan_f, c->Q, c->Qk) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecD2Z failed");
+        spme_influence_kernel<<<eb, 256, 0, c->stream>>>(c->Qk, c->infl, total, c->Kh, c->K1, epart, energy);
+        c->launches++;
+        if (cufftExecZ2D(c->plan_b, c->Qk, c->Q) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecZ2D failed");
+    }
     spread_gather(c, a, true, kEps / (kPi * c->V));
     c->launches++;
     if (energy) {

@@ -39,6 +39,12 @@ struct PairConsts {
     float rshort2;             // (6 lambda)^2: Kelbg Gaussian terms below FP64 resolution beyond
     float inv_dx[3];           // RDF 1/dx per pair type ee|ei|ii
     float qqf[3];              // q_i q_j s^2 per pair type (energy/force sign and scale)
+    // the same constants for cubic boxes in units of u = L/2^32 (the fixed-point
+    // difference used unscaled): lengths / u, and the per-tile factors q_i q_j / u^2
+    // (force) and q_i q_j / u (energy)
+    int cubic;
+    float u_rc2, u_p_alpha, u_c_exp, u_c_gauss, u_c_rs, u_inv_rs, u_c_lam, u_p_lam, u_sqrtpi_lam, u_rshort2;
+    float u_inv_dx[3], u_qq_force[3], u_qq_energy[3];
     // FP64 path
     double box[3];
     double rc2, alpha, rs, lambda;
@@ -69,6 +75,10 @@ struct tcp_ctx {
     double4_32a *xd = nullptr;     // FP64 positions for the FP64 pair kernel
     // pair-kernel partials
     int jsplit = 1;
+    int fpart_splits = 1;      // splits written by the last pair launch
+    int pair_variant = 1;      // FP32C real-space kernel: 0 ordered pairs, >= 1 Newton-3 variant
+    bool tuned = false;        // autotuner ran for the current parameters
+    double pair_variant_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // autotuner timings
     double *fpart = nullptr;   // [jsplit][3][n]
     double *upart = nullptr;   // energy partial per pair block
     int n_upart = 0;
@@ -90,6 +100,10 @@ struct tcp_ctx {
     double *Q = nullptr;                // real mesh [K3][K2][K1]
     cufftDoubleComplex *Qk = nullptr;   // [K3][K2][Kh]
     double *infl = nullptr;             // theta * |b|^-2 on the half mesh
+    bool spme_fp32 = false;             // FP32C mode: FP32 transforms, influence and gather
+    float *Qf = nullptr;                // FP32 real mesh [K3][K2][K1]
+    cufftComplex *Qkf = nullptr;        // FP32 half spectrum
+    float *infl_f = nullptr;
     cufftHandle plan_f = 0, plan_b = 0;
     bool plans = false;
     // plain Ewald
@@ -130,6 +144,13 @@ int cuda_check(cudaError_t e, const char *what);
 int pair_setup(tcp_ctx *c);                        // constants, jsplit, partial buffers
 int launch_pair(tcp_ctx *c, bool energy, bool rdf);
 int launch_force_finalize(tcp_ctx *c, bool add_rec);
+// pair_n3.cu
+bool n3_applicable(const tcp_ctx *c);
+int n3_grid(const tcp_ctx *c);
+int n3_variant_count();
+const char *n3_variant_name(int v);
+int autotune_pair(tcp_ctx *c);
+int launch_pair_n3(tcp_ctx *c, bool energy);
 // spme.cu
 int spme_setup(tcp_ctx *c);                        // meshes, plans, influence function
 int spme_free(tcp_ctx *c);
