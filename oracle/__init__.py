@@ -68,7 +68,7 @@ def lib():
             "orc_force_total": (C.c_int, [P, C.c_int, C.c_int, D, D, C.c_int, C.c_int, D, D, D, D, C.c_int]),
             "orc_finit": (C.c_int, [P, C.c_int, C.c_int, C.c_double, D, D, D, D, D, D, C.c_int]),
             "orc_md_step": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, D, D, D, D, C.c_double,
-                                      D, D, D, C.c_int]),
+                                      C.c_int, C.c_int, D, D, D, C.c_int]),
             "orc_max_threads": (C.c_int, []),
         }
         for k, (r, a) in sig.items():
@@ -194,10 +194,11 @@ class Oracle:
                          C.byref(ur), C.byref(um), self.nthreads)
         return f, ur.value, um.value
 
-    def md_step(self, x, v, f, dt, thermo="notemp", apply=True):
+    def md_step(self, x, v, f, dt, thermo="notemp", apply=True, recip="spme", nmax2=64):
         e = np.zeros(5)
+        r = {"none": 0, "spme": 1, "ewald": 2}[recip]
         self.L.orc_md_step(C.byref(self.p), THERMO[thermo], int(apply), self.nel, self.nion, dt, _d(x), _d(v),
-                           _d(f), _d(self.psi), self.Uo, _d(e), None, None, self.nthreads)
+                           _d(f), _d(self.psi), self.Uo, r, nmax2, _d(e), None, None, self.nthreads)
         return dict(Ur=e[0], Um=e[1], Epot=e[2], mv2el=e[3], mv2ion=e[4])
 
 

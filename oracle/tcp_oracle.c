@@ -606,10 +606,10 @@ int orc_finit(const orc_params *p, int nel, int nion, double dt, double *x, cons
 
 int orc_md_step(const orc_params *p, int thermo, int apply_thermostat, int nel, int nion,
                 double dt, double *x, double *v, double *f, const double *psi, double Uo,
-                double *energies, double *rdf, double *vdf, int nthreads) {
+                int reciprocal, int nmax2, double *energies, double *rdf, double *vdf, int nthreads) {
     double Ur, Um, mv2el, mv2ion;
     orc_vverlet1(p, nel, nion, dt, x, v, f);                                    /* main.f90:91 */
-    orc_force_total(p, nel, nion, x, psi, 1, 0, f, &Ur, &Um, rdf, nthreads);   /* main.f90:100-141 */
+    orc_force_total(p, nel, nion, x, psi, reciprocal, nmax2, f, &Ur, &Um, rdf, nthreads); /* main.f90:100-141 */
     orc_vverlet2(p, thermo, apply_thermostat, nel, nion, dt, v, f, NULL, &mv2el, &mv2ion, vdf); /* main.f90:145-153 */
     energies[0] = Ur;
     energies[1] = Um;

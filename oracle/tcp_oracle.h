@@ -141,12 +141,13 @@ int orc_finit(const orc_params *p, int nel, int nion, double dt, double *x,
               const double *v, const double *psi, double *f, double *Ur,
               double *Um, int nthreads);
 
-/* One MD step in the order of main.f90:81-153 (NOTEMP/ISOKIN/BEREND).
+/* One MD step in the order of main.f90:81-153 (NOTEMP/ISOKIN/BEREND);
+ * reciprocal as in orc_force_total.
  * energies[5] = {Ur, Um, Epot=(Ur+Uo)*eps, mv2el, mv2ion}. */
 int orc_md_step(const orc_params *p, int thermo, int apply_thermostat,
                 int nel, int nion, double dt, double *x, double *v, double *f,
-                const double *psi, double Uo, double *energies, double *rdf,
-                double *vdf, int nthreads);
+                const double *psi, double Uo, int reciprocal, int nmax2,
+                double *energies, double *rdf, double *vdf, int nthreads);
 
 int orc_max_threads(void);
 

@@ -120,20 +120,32 @@ static bool thermostat_due(const tcp_ctx *c) {
 }
 
 // One MD step (main.f90:81-153) on the stream; *pass = kinetic partial set.
+// Phase mark k: an event-record node when the stream is being captured, a
+// plain record otherwise (the External flag is only valid during capture).
+static int mark(tcp_ctx *c, int k) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    TCP_CUDA(cudaStreamIsCapturing(c->stream, &st));
+    if (st == cudaStreamCaptureStatusActive)
+        TCP_CUDA(cudaEventRecordWithFlags(c->ev[k], c->stream, cudaEventRecordExternal));
+    else
+        TCP_CUDA(cudaEventRecord(c->ev[k], c->stream));
+    return TCP_OK;
+}
+
 // Phase marks ev[0..4] are recorded on the stream (event nodes in the graph).
 static int step_chain(tcp_ctx *c, double dt, bool apply, int *pass) {
     int rc;
-    TCP_CUDA(cudaEventRecordWithFlags(c->ev[0], c->stream, cudaEventRecordExternal));
+    if ((rc = mark(c, 0))) return rc;
     if ((rc = launch_vverlet1(c, dt, 0.0))) return rc;
-    TCP_CUDA(cudaEventRecordWithFlags(c->ev[1], c->stream, cudaEventRecordExternal));
+    if ((rc = mark(c, 1))) return rc;
     if ((rc = recip_launch(c))) return rc;
-    TCP_CUDA(cudaEventRecordWithFlags(c->ev[2], c->stream, cudaEventRecordExternal));
+    if ((rc = mark(c, 2))) return rc;
     if ((rc = launch_pair(c, energy_on(c), (c->flags & TCP_FLAG_RDF) != 0))) return rc;
-    TCP_CUDA(cudaEventRecordWithFlags(c->ev[3], c->stream, cudaEventRecordExternal));
+    if ((rc = mark(c, 3))) return rc;
     if ((rc = launch_force_finalize(c, c->p.reciprocal != TCP_RECIP_NONE))) return rc;
     if ((rc = launch_kick2(c, dt, true, apply, (c->flags & TCP_FLAG_VDF) != 0, pass))) return rc;
     if ((rc = launch_reduce(c, (energy_on(c) ? kRedUr : 0) | kRedMv2, *pass))) return rc;
-    TCP_CUDA(cudaEventRecordWithFlags(c->ev[4], c->stream, cudaEventRecordExternal));
+    if ((rc = mark(c, 4))) return rc;
     return TCP_OK;
 }
 
@@ -215,6 +227,7 @@ int tcp_create(const tcp_params *p_in, int nel, int nion, int device, tcp_ctx **
     TCP_ALLOC(c->red, sizeof(double) * (size_t)c->red_cap);
     TCP_ALLOC(c->scal, sizeof(double) * kScalCount);
     TCP_ALLOC(c->status, sizeof(unsigned));
+    TCP_ALLOC(c->counter, sizeof(unsigned));
     TCP_ALLOC(c->rdf, sizeof(unsigned long long) * 3 * kNbin);
     TCP_ALLOC(c->vdf, sizeof(unsigned long long) * 2 * kNbin);
 #undef TCP_ALLOC
@@ -251,6 +264,7 @@ int tcp_destroy(tcp_ctx *c) {
     cudaFree(c->red);
     cudaFree(c->scal);
     cudaFree(c->status);
+    cudaFree(c->counter);
     cudaFree(c->rdf);
     cudaFree(c->vdf);
     cudaFree(c->d_stage);

@@ -88,6 +88,7 @@ struct tcp_ctx {
     double *scal = nullptr;    // device scalars, see kScal* below
     double *h_scal = nullptr;  // pinned host copy
     unsigned *status = nullptr;
+    unsigned *counter = nullptr;        // dynamic work counter of the Newton-3 kernel
     unsigned long long *rdf = nullptr;  // [3][kNbin]
     unsigned long long *vdf = nullptr;  // [2][kNbin]
     // staging for host transfers
