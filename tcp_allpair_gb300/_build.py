@@ -18,6 +18,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libtcpgpu.so"
+DRIVE = OUT / "tcp_drive"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "177",
               f"-I{ROOT / 'include'}", f"-I{CSRC}"]
@@ -63,6 +64,12 @@ def build(verbose: bool = False, extra_flags=()) -> pathlib.Path:
     objs = [str(OUT / (s.stem + ".o")) for s in sources()]
     if jobs or not LIB.exists():
         run([cc, *ARCH, "-shared", "-cudart", "shared", "-o", str(LIB), *objs, "-lcufft"])
+    # host driver replaying main.f90 on the C ABI
+    drive_src = CSRC / "host" / "tcp_drive.cpp"
+    if not DRIVE.exists() or DRIVE.stat().st_mtime < max(drive_src.stat().st_mtime, LIB.stat().st_mtime):
+        cxx = os.environ.get("CXX", "g++")
+        run([cxx, "-O2", "-std=c++17", f"-I{ROOT / 'include'}", str(drive_src), "-o", str(DRIVE),
+             f"-L{OUT}", "-ltcpgpu", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 
