@@ -203,6 +203,30 @@ int tcp_energies_get(tcp_ctx *ctx, tcp_energies *e);
  * the device copies afterwards (DUMP does so, result.f90:264-268). */
 int tcp_histograms(tcp_ctx *ctx, double *rdf, double *vdf, int reset);
 
+/* ---- many independent systems in one context ---------------------------------- */
+/* No single counterpart in the reference, which runs one system per job
+ * (main.f90): a batch steps nrep independent replicas, each exactly as
+ * main.f90:81-153 steps one system, with one persistent real-space launch
+ * over all replicas, batched SPME transforms per mesh size and one CUDA graph
+ * per step.  params[r], nel[r], nion[r] describe replica r; all replicas use
+ * TCP_PREC_FP32C, TCP_RECIP_SPME, cubic boxes, one B-spline order, and a
+ * NOTEMP / ISOKIN / BEREND thermostat applied every step. */
+typedef struct tcp_batch tcp_batch;
+int tcp_batch_create(const tcp_params *params, const int *nel, const int *nion, int nrep, int device,
+                     tcp_batch **out);
+int tcp_batch_destroy(tcp_batch *b);
+/* EWALD_SELF for every replica; Uo[nrep] (no eps) may be NULL. */
+int tcp_batch_ewald_self(tcp_batch *b, double *Uo);
+/* (n_r, 3) row-major host arrays of replica r; NULL skips a field. */
+int tcp_batch_upload(tcp_batch *b, int rep, const double *x, const double *v, const double *f);
+int tcp_batch_download(tcp_batch *b, int rep, double *x, double *v, double *f);
+/* Forces and energies (e[nrep], may be NULL) of all replicas at the current positions. */
+int tcp_batch_force(tcp_batch *b, tcp_energies *e);
+/* nsteps MD steps of every replica with time step dt; e[nrep] may be NULL. */
+int tcp_batch_md_steps(tcp_batch *b, double dt, int nsteps, tcp_energies *e);
+/* Mean device time of one batched step over nsteps graph replays (CUDA events). */
+int tcp_batch_time_steps(tcp_batch *b, double dt, int nsteps, double *ms_per_step);
+
 /* ---- measurement hooks ---------------------------------------------------- */
 /* Runs `reps` launches of one component on the context's stream and returns
  * the mean device time per launch from CUDA events recorded on that stream.

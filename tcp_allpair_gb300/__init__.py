@@ -20,7 +20,7 @@ from ._abi import (EI_COULOMB, EI_DEUTSCH, EI_KELBG, FLAG_ENERGY, FLAG_RDF, FLAG
                    THERMO_NOTEMP, THERMO_STOCH, TcpEnergies, TcpError, TcpParams)
 from .system import EPS, NDIST, PT_DTYPE, System, make_config_system, make_system
 
-__all__ = ["Context", "TcpParams", "TcpEnergies", "TcpError", "params_for", "System", "make_system",
+__all__ = ["Context", "Batch", "TcpParams", "TcpEnergies", "TcpError", "params_for", "System", "make_system",
            "make_config_system", "PT_DTYPE", "EPS", "NDIST"]
 
 _THERMO = {"notemp": THERMO_NOTEMP, "isokin": THERMO_ISOKIN, "berend": THERMO_BEREND, "stoch": THERMO_STOCH}
@@ -222,6 +222,71 @@ class Context:
         n = C.c_longlong()
         self._chk(self.lib.tcp_launch_count(self.h, C.byref(n)), "tcp_launch_count")
         return n.value
+
+
+class Batch:
+    """Many independent systems stepped together (tcp_batch_* of the C ABI)."""
+
+    def __init__(self, params: list, nel: list, nion: list, device: int = 0):
+        self.lib = _abi.load()
+        self.nrep = len(params)
+        self._params = (TcpParams * self.nrep)(*params)
+        self._nel = (C.c_int * self.nrep)(*nel)
+        self._nion = (C.c_int * self.nrep)(*nion)
+        self.n = [a + b for a, b in zip(nel, nion)]
+        h = C.c_void_p()
+        _abi.check(self.lib, self.lib.tcp_batch_create(self._params, self._nel, self._nion, self.nrep, device,
+                                                       C.byref(h)), "tcp_batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.tcp_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _chk(self, code, where):
+        _abi.check(self.lib, code, where)
+
+    def EWALD_SELF(self):
+        uo = np.zeros(self.nrep)
+        self._chk(self.lib.tcp_batch_ewald_self(self.h, uo.ctypes.data_as(C.POINTER(C.c_double))),
+                  "tcp_batch_ewald_self")
+        return uo
+
+    def upload(self, rep, x=None, v=None, f=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (x, v, f)]
+        self._chk(self.lib.tcp_batch_upload(self.h, rep, *[None if a is None else _ptr(a) for a in arrs]),
+                  "tcp_batch_upload")
+
+    def download(self, rep, x=True, v=True, f=True):
+        out = [np.empty((self.n[rep], 3)) if w else None for w in (x, v, f)]
+        self._chk(self.lib.tcp_batch_download(self.h, rep, *[None if a is None else _ptr(a) for a in out]),
+                  "tcp_batch_download")
+        return out
+
+    def _energies(self, call, *args):
+        e = (TcpEnergies * self.nrep)()
+        self._chk(call(self.h, *args, e), call.__name__)
+        return [x.as_dict() for x in e]
+
+    def force(self):
+        return self._energies(self.lib.tcp_batch_force)
+
+    def md_steps(self, dt, nsteps):
+        return self._energies(self.lib.tcp_batch_md_steps, C.c_double(dt), C.c_int(nsteps))
+
+    def time_steps(self, dt, nsteps):
+        ms = C.c_double()
+        self._chk(self.lib.tcp_batch_time_steps(self.h, dt, nsteps, C.byref(ms)), "tcp_batch_time_steps")
+        return ms.value
 
 
 def fp32_peak(device: int = 0) -> float:

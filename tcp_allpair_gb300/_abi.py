@@ -82,6 +82,15 @@ SIGNATURES = {
     "tcp_autotune_report": (C.c_int, [_CTX, C.POINTER(C.c_int), _P, C.c_int]),
     "tcp_launch_count": (C.c_int, [_CTX, C.POINTER(C.c_longlong)]),
     "tcp_fp32_peak": (C.c_int, [C.c_int, _P]),
+    "tcp_batch_create": (C.c_int, [C.POINTER(TcpParams), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int,
+                                   C.POINTER(C.c_void_p)]),
+    "tcp_batch_destroy": (C.c_int, [C.c_void_p]),
+    "tcp_batch_ewald_self": (C.c_int, [C.c_void_p, _P]),
+    "tcp_batch_upload": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "tcp_batch_download": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "tcp_batch_force": (C.c_int, [C.c_void_p, C.POINTER(TcpEnergies)]),
+    "tcp_batch_md_steps": (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.POINTER(TcpEnergies)]),
+    "tcp_batch_time_steps": (C.c_int, [C.c_void_p, C.c_double, C.c_int, _P]),
 }
 
 _lib = None

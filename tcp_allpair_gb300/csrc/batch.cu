@@ -1,0 +1,772 @@
+// batch.cu -- many independent systems (replicas) in one context: one
+// persistent Newton-3 pair launch over the items of all replicas, SPME with
+// one batched cuFFT plan per distinct mesh, and replica-aware integrator and
+// reduction kernels, captured together as one CUDA graph per MD step.
+//
+// Each replica is a complete system of the reference (its own box, charges,
+// masses, Ewald alpha, e-i model and length, SPME mesh, thermostat target),
+// stepped exactly as main.f90:81-153 steps one system.  Particles of all
+// replicas are concatenated (replica r at [off_r, off_r + n_r), electrons
+// first inside it) in SoA FP64 arrays; rep_of[i] maps a particle to its
+// replica.  Requirements: compensated-FP32 precision, SPME, cubic boxes, one
+// B-spline order for the batch, NOTEMP / ISOKIN / BEREND thermostats applied
+// every step, one time step for all replicas.
+//
+// Per-replica sums (Ur, Um, sum m v^2, sum f) are accumulated with FP64
+// atomics, warp-reduced first when a warp holds one replica.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "device_util.cuh"
+#include "spme_math.cuh"
+#include "tcp_internal.h"
+
+namespace tcp {
+
+struct BRep {
+    int off, n, nel;
+    double L[3];
+    double xm[2], q[2];      // masses, scaled charges
+    int K[3], Kh;
+    long long mesh_off, half_off;
+    double V;
+    double Te, Ti, tau;
+    int thermo;
+};
+
+constexpr int kBThreads = 256;
+
+// accumulator block: ur[nrep] | um[nrep] | mv0[2 nrep] | mv1[2 nrep] | fsum[3 nrep]
+struct BAcc {
+    double *ur, *um, *mv0, *mv1, *fsum;
+};
+
+__device__ __forceinline__ int fixed_coord_b(double x, double L) {
+    double t = x / L + 0.5;
+    t -= floor(t);
+    return (int)(unsigned)((unsigned long long)llrint(t * 4294967296.0) & 0xffffffffull);
+}
+
+__device__ __forceinline__ double wrap_b(double x, double L) { return x - L * round(x / L); }
+
+// add v to acc[key] with one atomic per warp when the warp shares the key
+__device__ __forceinline__ void keyed_add(double *acc, int key, double v) {
+    const unsigned all = __activemask();
+    const int k0 = __shfl_sync(all, key, __ffs(all) - 1);
+    if (__all_sync(all, key == k0) && all == 0xffffffffu) {
+        v = warp_sum(v);
+        if ((threadIdx.x & 31) == 0) atomicAdd(acc + key, v);
+    } else {
+        atomicAdd(acc + key, v);
+    }
+}
+
+struct BParticles {
+    double *x, *v, *f, *frec, *facc;
+    int4 *xq;
+    const int *rep_of;
+    const BRep *reps;
+    int ntot;
+};
+
+// VVerletNotemp1 (vverlet.f90:148-167) per replica
+__global__ void b_vverlet1_kernel(const BParticles a, double dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.ntot) return;
+    const BRep &R = a.reps[a.rep_of[i]];
+    const double xm = (i - R.off) < R.nel ? R.xm[0] : R.xm[1];
+    int q[3];
+    for (int k = 0; k < 3; ++k) {
+        const size_t o = (size_t)k * a.ntot + i;
+        const double vk = a.v[o] + 0.5 * dt * a.f[o] / xm;
+        a.v[o] = vk;
+        const double y = wrap_b(a.x[o] + dt * vk, R.L[k]);
+        a.x[o] = y;
+        q[k] = fixed_coord_b(y, R.L[k]);
+    }
+    a.xq[i] = make_int4(q[0], q[1], q[2], 0);
+}
+
+__global__ void b_refresh_kernel(const BParticles a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.ntot) return;
+    const BRep &R = a.reps[a.rep_of[i]];
+    a.xq[i] = make_int4(fixed_coord_b(a.x[i], R.L[0]), fixed_coord_b(a.x[(size_t)a.ntot + i], R.L[1]),
+                        fixed_coord_b(a.x[2 * (size_t)a.ntot + i], R.L[2]), 0);
+}
+
+template <int P>
+__global__ void b_spread_kernel(const BParticles a, double *__restrict__ Q) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.ntot) return;
+    const BRep &R = a.reps[a.rep_of[i]];
+    const double q = (i - R.off) < R.nel ? R.q[0] : R.q[1];
+    double W[3][P], dW[3][P];
+    int base[3];
+    for (int d = 0; d < 3; ++d) {
+        const double u = (double)R.K[d] * (a.x[(size_t)d * a.ntot + i] + R.L[d] * .5) / R.L[d];
+        spline_w<P, double>(u, W[d], dW[d]);
+        base[d] = (int)trunc(u) - (P - 3);
+    }
+    double *mesh = Q + R.mesh_off;
+#pragma unroll 1
+    for (int k = 0; k < P; ++k) {
+        const int iz = wrapi(base[2] + k, R.K[2]);
+#pragma unroll 1
+        for (int j = 0; j < P; ++j) {
+            const int iy = wrapi(base[1] + j, R.K[1]);
+            const double qyz = q * W[1][j] * W[2][k];
+            double *row = mesh + (size_t)R.K[0] * (iy + (size_t)R.K[1] * iz);
+#pragma unroll
+            for (int ii = 0; ii < P; ++ii) atomicAdd(row + wrapi(base[0] + ii, R.K[0]), qyz * W[0][ii]);
+        }
+    }
+}
+
+__global__ void b_to_float_kernel(const double *__restrict__ q, float *__restrict__ qf, long n) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        qf[i] = (float)q[i];
+}
+
+// influence multiply; blocks [blk0[r], blk0[r+1]) belong to replica r
+__global__ void b_influence_kernel(cufftComplex *__restrict__ Qk, const float *__restrict__ infl,
+                                   const BRep *__restrict__ reps, const int *__restrict__ blk0, int nrep,
+                                   double *__restrict__ um) {
+    __shared__ double red[32];
+    int lo = 0, hi = nrep - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (blk0[mid] <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+    }
+    const BRep &R = reps[lo];
+    const int nb = blk0[lo + 1] - blk0[lo], lb = blockIdx.x - blk0[lo];
+    const long total = (long)R.K[2] * R.K[1] * R.Kh;
+    double e = 0.0;
+    for (long idx = (long)lb * blockDim.x + threadIdx.x; idx < total; idx += (long)nb * blockDim.x) {
+        const float g = infl[R.half_off + idx];
+        cufftComplex z = Qk[R.half_off + idx];
+        const int kx = (int)(idx % R.Kh);
+        const double wgt = (kx == 0 || (2 * kx == R.K[0])) ? 1.0 : 2.0;
+        e += wgt * (double)g * ((double)z.x * z.x + (double)z.y * z.y);
+        z.x *= g;
+        z.y *= g;
+        Qk[R.half_off + idx] = z;
+    }
+    const double t = block_sum(e, red);
+    if (threadIdx.x == 0) atomicAdd(&um[lo], t * kEps / (2.0 * kPi * R.V));
+}
+
+template <int P>
+__global__ void b_gather_kernel(const BParticles a, const float *__restrict__ phi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.ntot) return;
+    const BRep &R = a.reps[a.rep_of[i]];
+    const double q = (i - R.off) < R.nel ? R.q[0] : R.q[1];
+    float W[3][P], dW[3][P];
+    int base[3];
+    for (int d = 0; d < 3; ++d) {
+        const double u = (double)R.K[d] * (a.x[(size_t)d * a.ntot + i] + R.L[d] * .5) / R.L[d];
+        spline_w<P, float>(u, W[d], dW[d]);
+        base[d] = (int)trunc(u) - (P - 3);
+    }
+    const float *mesh = phi + R.mesh_off;
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+#pragma unroll 1
+    for (int k = 0; k < P; ++k) {
+        const int iz = wrapi(base[2] + k, R.K[2]);
+#pragma unroll 1
+        for (int j = 0; j < P; ++j) {
+            const int iy = wrapi(base[1] + j, R.K[1]);
+            const float *row = mesh + (size_t)R.K[0] * (iy + (size_t)R.K[1] * iz);
+            float sx = 0.f, sd = 0.f;
+#pragma unroll
+            for (int ii = 0; ii < P; ++ii) {
+                const float ph = row[wrapi(base[0] + ii, R.K[0])];
+                sx += dW[0][ii] * ph;
+                sd += W[0][ii] * ph;
+            }
+            gx += sx * W[1][j] * W[2][k];
+            gy += sd * dW[1][j] * W[2][k];
+            gz += sd * W[1][j] * dW[2][k];
+        }
+    }
+    const double coef = kEps / (kPi * R.V);
+    a.frec[i] = -coef * q * (double)gx * ((double)R.K[0] / R.L[0]);
+    a.frec[(size_t)a.ntot + i] = -coef * q * (double)gy * ((double)R.K[1] / R.L[1]);
+    a.frec[2 * (size_t)a.ntot + i] = -coef * q * (double)gz * ((double)R.K[2] / R.L[2]);
+}
+
+// f = real-space + reciprocal (SPME_SUM); per-replica sum f (REMOVE_RIGIDMTN)
+__global__ void b_finalize_kernel(const BParticles a, double *__restrict__ fsum) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < a.ntot;
+    const int r = valid ? a.rep_of[i] : a.rep_of[a.ntot - 1];
+    for (int k = 0; k < 3; ++k) {
+        double fk = 0.0;
+        if (valid) {
+            const size_t o = (size_t)k * a.ntot + i;
+            fk = a.facc[o] + a.frec[o];
+            a.f[o] = fk;
+        }
+        keyed_add(fsum, 3 * r + k, fk);
+    }
+}
+
+// second half kick with the net force removed (vverlet.f90:194-219,
+// force.f90:996-1004); sum m v^2 per replica and species into mv
+__global__ void b_kick2_kernel(const BParticles a, double dt, const double *__restrict__ fsum,
+                               double *__restrict__ mv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < a.ntot;
+    const int ic = valid ? i : a.ntot - 1;
+    const int r = a.rep_of[ic];
+    const BRep &R = a.reps[r];
+    const int s = (ic - R.off) < R.nel ? 0 : 1;
+    double mv2 = 0.0;
+    if (valid) {
+        const double xm = R.xm[s];
+        double vv[3];
+        for (int k = 0; k < 3; ++k) {
+            const size_t o = (size_t)k * a.ntot + i;
+            const double fk = a.f[o] - fsum[3 * r + k] / (double)R.n;
+            a.f[o] = fk;
+            vv[k] = a.v[o] + 0.5 * dt * fk / xm;
+            a.v[o] = vv[k];
+        }
+        mv2 = (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]) * xm;
+    }
+    keyed_add(mv, 2 * r + s, mv2);
+}
+
+// ISOKIN / BEREND rescale (vverlet.f90:331-344, 257-270); lambda = 1 for NOTEMP
+__global__ void b_rescale_kernel(const BParticles a, double dt, const double *__restrict__ mv_in,
+                                 double *__restrict__ mv_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < a.ntot;
+    const int ic = valid ? i : a.ntot - 1;
+    const int r = a.rep_of[ic];
+    const BRep &R = a.reps[r];
+    const int s = (ic - R.off) < R.nel ? 0 : 1;
+    const int cnt = s == 0 ? R.nel : R.n - R.nel;
+    double lam = 1.0;
+    if (R.thermo == TCP_THERMO_ISOKIN || R.thermo == TCP_THERMO_BEREND) {
+        const double T0 = mv_in[2 * r + s] / (double)(3 * cnt);
+        const double T = s == 0 ? R.Te : R.Ti;
+        lam = R.thermo == TCP_THERMO_ISOKIN ? sqrt(T / T0) : sqrt(1.0 + dt * (T / T0 - 1.0) / R.tau);
+    }
+    double mv2 = 0.0;
+    if (valid) {
+        double vv[3];
+        for (int k = 0; k < 3; ++k) {
+            const size_t o = (size_t)k * a.ntot + i;
+            vv[k] = a.v[o] * lam;
+            a.v[o] = vv[k];
+        }
+        mv2 = (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]) * R.xm[s];
+    }
+    keyed_add(mv_out, 2 * r + s, mv2);
+}
+
+}  // namespace tcp
+
+// ---------------------------------------------------------------------------
+struct tcp_batch {
+    int nrep = 0, ntot = 0, device = 0, num_sms = 0, order = 4;
+    std::vector<tcp_params> p;
+    std::vector<int> nel, nion, off;
+    std::vector<double> alpha, Uo;
+    cudaStream_t stream = nullptr;
+    double *x = nullptr, *v = nullptr, *f = nullptr, *frec = nullptr, *facc = nullptr;
+    int4 *xq = nullptr;
+    int *rep_of = nullptr;
+    tcp::BRep *reps = nullptr;          // device table
+    std::vector<tcp::BRep> h_reps;
+    void *n3reps = nullptr;             // device Newton-3 table
+    long long n3_items = 0;
+    double *acc = nullptr;              // accumulator block
+    double *h_acc = nullptr;            // pinned copy
+    unsigned *status = nullptr, *counter = nullptr;
+    // SPME
+    double *Q = nullptr;
+    float *Qf = nullptr, *infl = nullptr;
+    cufftComplex *Qk = nullptr;
+    long long mesh_total = 0, half_total = 0;
+    int *blk0 = nullptr;
+    int infl_blocks = 0;
+    struct Group {
+        int K[3];
+        long long mesh_off, half_off;
+        int count;
+        cufftHandle fwd, inv;
+    };
+    std::vector<Group> groups;
+    bool ready = false;
+    cudaGraphExec_t graph = nullptr;
+    double graph_dt = 0;
+    int graph_kernels = 0;
+    long long launches = 0;
+};
+
+namespace tcp {
+
+static BAcc acc_of(tcp_batch *b) {
+    BAcc a;
+    a.ur = b->acc;
+    a.um = b->acc + b->nrep;
+    a.mv0 = b->acc + 2 * b->nrep;
+    a.mv1 = b->acc + 4 * b->nrep;
+    a.fsum = b->acc + 6 * b->nrep;
+    return a;
+}
+
+static BParticles parts(tcp_batch *b) {
+    BParticles a;
+    a.x = b->x;
+    a.v = b->v;
+    a.f = b->f;
+    a.frec = b->frec;
+    a.facc = b->facc;
+    a.xq = b->xq;
+    a.rep_of = b->rep_of;
+    a.reps = b->reps;
+    a.ntot = b->ntot;
+    return a;
+}
+
+template <int P>
+static void b_spme_launch(tcp_batch *b, bool gather) {
+    const int blocks = (b->ntot + 127) / 128;
+    if (!gather)
+        b_spread_kernel<P><<<blocks, 128, 0, b->stream>>>(parts(b), b->Q);
+    else
+        b_gather_kernel<P><<<blocks, 128, 0, b->stream>>>(parts(b), b->Qf);
+}
+
+static void b_spme(tcp_batch *b, bool gather) {
+    switch (b->order) {
+        case 4: b_spme_launch<4>(b, gather); break;
+        case 5: b_spme_launch<5>(b, gather); break;
+        case 6: b_spme_launch<6>(b, gather); break;
+        case 7: b_spme_launch<7>(b, gather); break;
+        default: b_spme_launch<8>(b, gather); break;
+    }
+}
+
+// One batched MD step (main.f90:81-153 for every replica) on b->stream.
+static int b_step(tcp_batch *b, double dt) {
+    const BAcc A = acc_of(b);
+    const int nb = (b->ntot + kBThreads - 1) / kBThreads;
+    const int launches_before = 0;
+    (void)launches_before;
+    TCP_CUDA(cudaMemsetAsync(A.um, 0, sizeof(double) * 8 * (size_t)b->nrep, b->stream));   // um, mv0, mv1, fsum
+    b_vverlet1_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), dt);
+    TCP_CUDA(cudaMemsetAsync(b->Q, 0, sizeof(double) * (size_t)b->mesh_total, b->stream));
+    b_spme(b, false);
+    b_to_float_kernel<<<(int)std::min<long long>((b->mesh_total + 255) / 256, 8192), 256, 0, b->stream>>>(
+        b->Q, b->Qf, (long)b->mesh_total);
+    for (auto &g : b->groups)
+        if (cufftExecR2C(g.fwd, b->Qf + g.mesh_off, b->Qk + g.half_off) != CUFFT_SUCCESS)
+            return set_error(TCP_ERR_CUFFT, "batched cufftExecR2C failed");
+    b_influence_kernel<<<b->infl_blocks, 256, 0, b->stream>>>(b->Qk, b->infl, b->reps, b->blk0, b->nrep, A.um);
+    for (auto &g : b->groups)
+        if (cufftExecC2R(g.inv, b->Qk + g.half_off, b->Qf + g.mesh_off) != CUFFT_SUCCESS)
+            return set_error(TCP_ERR_CUFFT, "batched cufftExecC2R failed");
+    b_spme(b, true);
+    int rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
+                                  b->status, b->counter, b->num_sms, true);
+    if (rc) return rc;
+    b_finalize_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), A.fsum);
+    b_kick2_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), dt, A.fsum, A.mv0);
+    b_rescale_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), dt, A.mv0, A.mv1);
+    b->launches += 9;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+static int b_sync(tcp_batch *b) {
+    TCP_CUDA(cudaMemcpyAsync(b->h_acc, b->acc, sizeof(double) * 9 * (size_t)b->nrep, cudaMemcpyDeviceToHost,
+                             b->stream));
+    unsigned st = 0;
+    TCP_CUDA(cudaMemcpyAsync(&st, b->status, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
+    TCP_CUDA(cudaStreamSynchronize(b->stream));
+    if (st & kStatusTmaTimeout) {
+        cudaMemsetAsync(b->status, 0, sizeof(unsigned), b->stream);
+        return set_error(TCP_ERR_TIMEOUT, "a pair-kernel tile wait exceeded its bound");
+    }
+    return TCP_OK;
+}
+
+static void b_energies(tcp_batch *b, tcp_energies *e) {
+    if (!e) return;
+    for (int r = 0; r < b->nrep; ++r) {
+        e[r].Ur = b->h_acc[r];
+        e[r].Um = b->h_acc[b->nrep + r];
+        e[r].Uo = b->Uo[r];
+        e[r].Epot = (e[r].Ur + e[r].Uo) * kEps;
+        e[r].mv2el = b->h_acc[4 * b->nrep + 2 * r];
+        e[r].mv2ion = b->h_acc[4 * b->nrep + 2 * r + 1];
+    }
+}
+
+}  // namespace tcp
+
+using namespace tcp;
+
+extern "C" {
+
+int tcp_batch_destroy(tcp_batch *b) {
+    if (!b) return TCP_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (auto &g : b->groups) {
+        cufftDestroy(g.fwd);
+        cufftDestroy(g.inv);
+    }
+    for (void *ptr : {(void *)b->x, (void *)b->v, (void *)b->f, (void *)b->frec, (void *)b->facc, (void *)b->xq,
+                      (void *)b->rep_of, (void *)b->reps, b->n3reps, (void *)b->acc, (void *)b->status,
+                      (void *)b->counter, (void *)b->Q, (void *)b->Qf, (void *)b->infl, (void *)b->Qk,
+                      (void *)b->blk0})
+        cudaFree(ptr);
+    if (b->h_acc) cudaFreeHost(b->h_acc);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return TCP_OK;
+}
+
+int tcp_batch_create(const tcp_params *params, const int *nel, const int *nion, int nrep, int device,
+                     tcp_batch **out) {
+    if (!out || !params || !nel || !nion || nrep <= 0) return set_error(TCP_ERR_BAD_PARAM, "bad arguments");
+    *out = nullptr;
+    for (int r = 0; r < nrep; ++r) {
+        const tcp_params &p = params[r];
+        if (p.precision != TCP_PREC_FP32C || p.reciprocal != TCP_RECIP_SPME)
+            return set_error(TCP_ERR_BAD_PARAM, "batch replicas need TCP_PREC_FP32C and TCP_RECIP_SPME");
+        if (!(p.box[0] > 0) || p.box[0] != p.box[1] || p.box[1] != p.box[2])
+            return set_error(TCP_ERR_BAD_PARAM, "batch replicas need cubic boxes");
+        if (p.order != params[0].order || p.order < 4 || p.order > kMaxOrder)
+            return set_error(TCP_ERR_BAD_PARAM, "batch replicas need one B-spline order in 4..8");
+        for (int d = 0; d < 3; ++d)
+            if (p.K[d] < p.order) return set_error(TCP_ERR_BAD_PARAM, "SPME mesh must be >= order");
+        if (nel[r] < 0 || nion[r] < 0 || nel[r] + nion[r] < 2) return set_error(TCP_ERR_BAD_PARAM, "bad particle counts");
+        if (p.thermo == TCP_THERMO_STOCH) return set_error(TCP_ERR_BAD_PARAM, "STOCH is not batched");
+        if (!(p.rc > 0.0) || !(p.xm[0] > 0) || !(p.xm[1] > 0)) return set_error(TCP_ERR_BAD_PARAM, "bad rc or masses");
+        if (p.ei_model == TCP_EI_KELBG && !(p.lambda_ei > 0)) return set_error(TCP_ERR_BAD_PARAM, "Kelbg needs lambda_ei > 0");
+        if (p.ei_model == TCP_EI_DEUTSCH && !(p.rs > 0)) return set_error(TCP_ERR_BAD_PARAM, "Deutsch needs rs > 0");
+    }
+    cudaDeviceProp prop;
+    TCP_CUDA(cudaGetDeviceProperties(&prop, device));
+    if (prop.major != 10 || prop.minor != 3) return set_error(TCP_ERR_NO_DEVICE, "libtcpgpu is built for sm_103a");
+    TCP_CUDA(cudaSetDevice(device));
+    tcp_batch *b = new tcp_batch();
+    b->nrep = nrep;
+    b->device = device;
+    b->num_sms = prop.multiProcessorCount;
+    b->order = params[0].order;
+    b->p.assign(params, params + nrep);
+    for (auto &p : b->p)
+        if (p.charge_scale == 0.0) p.charge_scale = 1.0;
+    b->nel.assign(nel, nel + nrep);
+    b->nion.assign(nion, nion + nrep);
+    b->off.resize(nrep);
+    for (int r = 0; r < nrep; ++r) {
+        b->off[r] = b->ntot;
+        b->ntot += nel[r] + nion[r];
+    }
+    auto fail = [&](int code) {
+        tcp_batch_destroy(b);
+        return code;
+    };
+    const size_t n = b->ntot;
+#define TCP_BALLOC(ptr, bytes)                                                      \
+    do {                                                                            \
+        cudaError_t _e = cudaMalloc(&(ptr), (bytes));                               \
+        if (_e != cudaSuccess) return fail(cuda_check(_e, "cudaMalloc " #ptr));     \
+    } while (0)
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(cuda_check(cudaGetLastError(), "cudaStreamCreate"));
+    TCP_BALLOC(b->x, sizeof(double) * 3 * n);
+    TCP_BALLOC(b->v, sizeof(double) * 3 * n);
+    TCP_BALLOC(b->f, sizeof(double) * 3 * n);
+    TCP_BALLOC(b->frec, sizeof(double) * 3 * n);
+    TCP_BALLOC(b->facc, sizeof(double) * 3 * n);
+    TCP_BALLOC(b->xq, sizeof(int4) * n);
+    TCP_BALLOC(b->rep_of, sizeof(int) * n);
+    TCP_BALLOC(b->reps, sizeof(BRep) * nrep);
+    TCP_BALLOC(b->n3reps, n3_rep_bytes() * nrep);
+    TCP_BALLOC(b->acc, sizeof(double) * 9 * nrep);
+    TCP_BALLOC(b->status, sizeof(unsigned));
+    TCP_BALLOC(b->counter, sizeof(unsigned));
+    if (cudaMallocHost(&b->h_acc, sizeof(double) * 9 * nrep) != cudaSuccess)
+        return fail(cuda_check(cudaGetLastError(), "cudaMallocHost"));
+    std::vector<int> rep_of(n);
+    for (int r = 0; r < nrep; ++r)
+        for (int i = 0; i < nel[r] + nion[r]; ++i) rep_of[b->off[r] + i] = r;
+    TCP_CUDA(cudaMemcpyAsync(b->rep_of, rep_of.data(), sizeof(int) * n, cudaMemcpyHostToDevice, b->stream));
+    for (double *ptr : {b->x, b->v, b->f, b->frec, b->facc})
+        cudaMemsetAsync(ptr, 0, sizeof(double) * 3 * n, b->stream);
+    cudaMemsetAsync(b->acc, 0, sizeof(double) * 9 * nrep, b->stream);
+    cudaMemsetAsync(b->status, 0, sizeof(unsigned), b->stream);
+    // SPME meshes grouped by size: replicas of one group are contiguous so that
+    // one batched plan transforms them all
+    std::map<std::tuple<int, int, int>, std::vector<int>> by_mesh;
+    for (int r = 0; r < nrep; ++r) by_mesh[{params[r].K[0], params[r].K[1], params[r].K[2]}].push_back(r);
+    b->h_reps.resize(nrep);
+    for (auto &kv : by_mesh) {
+        tcp_batch::Group g;
+        g.K[0] = std::get<0>(kv.first);
+        g.K[1] = std::get<1>(kv.first);
+        g.K[2] = std::get<2>(kv.first);
+        g.mesh_off = b->mesh_total;
+        g.half_off = b->half_total;
+        g.count = (int)kv.second.size();
+        const long long nreal = (long long)g.K[0] * g.K[1] * g.K[2];
+        const long long nhalf = (long long)(g.K[0] / 2 + 1) * g.K[1] * g.K[2];
+        for (int k = 0; k < g.count; ++k) {
+            BRep &R = b->h_reps[kv.second[k]];
+            R.mesh_off = b->mesh_total + k * nreal;
+            R.half_off = b->half_total + k * nhalf;
+        }
+        b->mesh_total += nreal * g.count;
+        b->half_total += nhalf * g.count;
+        int nfwd[3] = {g.K[2], g.K[1], g.K[0]};
+        if (cufftPlanMany(&g.fwd, 3, nfwd, nullptr, 1, (int)nreal, nullptr, 1, (int)nhalf, CUFFT_R2C, g.count) !=
+                CUFFT_SUCCESS ||
+            cufftPlanMany(&g.inv, 3, nfwd, nullptr, 1, (int)nhalf, nullptr, 1, (int)nreal, CUFFT_C2R, g.count) !=
+                CUFFT_SUCCESS)
+            return fail(set_error(TCP_ERR_CUFFT, "cufftPlanMany failed"));
+        cufftSetStream(g.fwd, b->stream);
+        cufftSetStream(g.inv, b->stream);
+        b->groups.push_back(g);
+    }
+    TCP_BALLOC(b->Q, sizeof(double) * (size_t)b->mesh_total);
+    TCP_BALLOC(b->Qf, sizeof(float) * (size_t)b->mesh_total);
+    TCP_BALLOC(b->infl, sizeof(float) * (size_t)b->half_total);
+    TCP_BALLOC(b->Qk, sizeof(cufftComplex) * (size_t)b->half_total);
+    TCP_BALLOC(b->blk0, sizeof(int) * (nrep + 1));
+#undef TCP_BALLOC
+    TCP_CUDA(cudaStreamSynchronize(b->stream));
+    *out = b;
+    return TCP_OK;
+}
+
+int tcp_batch_ewald_self(tcp_batch *b, double *Uo) {
+    if (!b) return set_error(TCP_ERR_BAD_PARAM, "batch is NULL");
+    cudaSetDevice(b->device);
+    const int nrep = b->nrep;
+    b->alpha.assign(nrep, 0.0);
+    b->Uo.assign(nrep, 0.0);
+    std::vector<PairConsts> pcs(nrep);
+    std::vector<int> blk0(nrep + 1, 0);
+    std::vector<float> infl((size_t)b->half_total);
+    for (int r = 0; r < nrep; ++r) {
+        const tcp_params &p = b->p[r];
+        if (p.rc > p.box[0] / 2.0) return set_error(TCP_ERR_CUTOFF, "replica " + std::to_string(r) + ": rc > L/2");
+        const double alpha = p.a > 0.0 ? p.a : 3.1 / p.rc;                     // force.f90:23
+        b->alpha[r] = alpha;
+        const double s = p.charge_scale;
+        b->Uo[r] = (-(double)b->nel[r] * (s * p.q[0]) * (s * p.q[0]) - (double)b->nion[r] * (s * p.q[1]) * (s * p.q[1])) *
+                   alpha / kSqrtPi;                                            // force.f90:44-45
+        tcp_ctx tmp;
+        tmp.p = p;
+        tmp.nel = b->nel[r];
+        tmp.nion = b->nion[r];
+        tmp.n = tmp.nel + tmp.nion;
+        tmp.alpha = alpha;
+        tmp.rc2 = p.rc * p.rc;
+        make_pair_consts(&tmp);
+        pcs[r] = tmp.pc;
+        BRep &R = b->h_reps[r];
+        R.off = b->off[r];
+        R.n = b->nel[r] + b->nion[r];
+        R.nel = b->nel[r];
+        for (int d = 0; d < 3; ++d) {
+            R.L[d] = p.box[d];
+            R.K[d] = p.K[d];
+        }
+        R.Kh = p.K[0] / 2 + 1;
+        R.xm[0] = p.xm[0];
+        R.xm[1] = p.xm[1];
+        R.q[0] = s * p.q[0];
+        R.q[1] = s * p.q[1];
+        R.V = p.box[0] * p.box[1] * p.box[2];
+        R.Te = p.Te;
+        R.Ti = p.Ti;
+        R.tau = p.tau;
+        R.thermo = p.thermo;
+        // influence function theta(m) |b(m)|^-2 on the half spectrum (EWALD_SELF, force.f90:27-42)
+        std::vector<double> bx = bspline_moduli(p.order, p.K[0]), by = bspline_moduli(p.order, p.K[1]),
+                            bz = bspline_moduli(p.order, p.K[2]);
+        for (int k = 0; k < p.K[2]; ++k) {
+            const int iz = (k + p.K[2] / 2) % p.K[2] - p.K[2] / 2;
+            for (int j = 0; j < p.K[1]; ++j) {
+                const int iy = (j + p.K[1] / 2) % p.K[1] - p.K[1] / 2;
+                for (int i = 0; i < R.Kh; ++i) {
+                    const int ix = (i + p.K[0] / 2) % p.K[0] - p.K[0] / 2;
+                    const size_t idx = R.half_off + i + (size_t)R.Kh * (j + (size_t)p.K[1] * k);
+                    if (ix == 0 && iy == 0 && iz == 0) {
+                        infl[idx] = 0.f;
+                        continue;
+                    }
+                    const double m2 = (double)ix * ix / (p.box[0] * p.box[0]) + (double)iy * iy / (p.box[1] * p.box[1]) +
+                                      (double)iz * iz / (p.box[2] * p.box[2]);
+                    infl[idx] = (float)(std::exp(-m2 * kPi * kPi / (alpha * alpha)) / m2 * bx[i] * by[j] * bz[k]);
+                }
+            }
+        }
+        const long long half = (long long)R.Kh * p.K[1] * p.K[2];
+        blk0[r + 1] = blk0[r] + (int)std::max<long long>(1, std::min<long long>((half + 255) / 256, 512));
+    }
+    b->infl_blocks = blk0[nrep];
+    std::vector<unsigned char> n3h(n3_rep_bytes() * nrep);
+    b->n3_items = n3_batch_fill(n3h.data(), nrep, b->off.data(), b->nel.data(), b->nion.data(), pcs.data());
+    TCP_CUDA(cudaMemcpyAsync(b->reps, b->h_reps.data(), sizeof(BRep) * nrep, cudaMemcpyHostToDevice, b->stream));
+    TCP_CUDA(cudaMemcpyAsync(b->n3reps, n3h.data(), n3h.size(), cudaMemcpyHostToDevice, b->stream));
+    TCP_CUDA(cudaMemcpyAsync(b->blk0, blk0.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice, b->stream));
+    TCP_CUDA(cudaMemcpyAsync(b->infl, infl.data(), sizeof(float) * infl.size(), cudaMemcpyHostToDevice, b->stream));
+    TCP_CUDA(cudaStreamSynchronize(b->stream));
+    if (Uo)
+        for (int r = 0; r < nrep; ++r) Uo[r] = b->Uo[r];
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    b->ready = true;
+    return TCP_OK;
+}
+
+int tcp_batch_upload(tcp_batch *b, int rep, const double *x, const double *v, const double *f) {
+    if (!b || rep < 0 || rep >= b->nrep) return set_error(TCP_ERR_BAD_PARAM, "bad batch or replica");
+    cudaSetDevice(b->device);
+    const int n = b->nel[rep] + b->nion[rep];
+    std::vector<double> soa(3 * (size_t)n);
+    double *dst[3] = {b->x, b->v, b->f};
+    const double *src[3] = {x, v, f};
+    for (int q = 0; q < 3; ++q) {
+        if (!src[q]) continue;
+        for (int i = 0; i < n; ++i)
+            for (int k = 0; k < 3; ++k) soa[(size_t)k * n + i] = src[q][3 * (size_t)i + k];
+        for (int k = 0; k < 3; ++k)
+            TCP_CUDA(cudaMemcpyAsync(dst[q] + (size_t)k * b->ntot + b->off[rep], soa.data() + (size_t)k * n,
+                                     sizeof(double) * n, cudaMemcpyHostToDevice, b->stream));
+        TCP_CUDA(cudaStreamSynchronize(b->stream));
+    }
+    if (x && b->ready) {
+        b_refresh_kernel<<<(b->ntot + 255) / 256, 256, 0, b->stream>>>(parts(b));
+        TCP_CUDA(cudaGetLastError());
+    }
+    TCP_CUDA(cudaStreamSynchronize(b->stream));
+    return TCP_OK;
+}
+
+int tcp_batch_download(tcp_batch *b, int rep, double *x, double *v, double *f) {
+    if (!b || rep < 0 || rep >= b->nrep) return set_error(TCP_ERR_BAD_PARAM, "bad batch or replica");
+    cudaSetDevice(b->device);
+    const int n = b->nel[rep] + b->nion[rep];
+    std::vector<double> soa(3 * (size_t)n);
+    const double *src[3] = {b->x, b->v, b->f};
+    double *dst[3] = {x, v, f};
+    for (int q = 0; q < 3; ++q) {
+        if (!dst[q]) continue;
+        for (int k = 0; k < 3; ++k)
+            TCP_CUDA(cudaMemcpyAsync(soa.data() + (size_t)k * n, src[q] + (size_t)k * b->ntot + b->off[rep],
+                                     sizeof(double) * n, cudaMemcpyDeviceToHost, b->stream));
+        TCP_CUDA(cudaStreamSynchronize(b->stream));
+        for (int i = 0; i < n; ++i)
+            for (int k = 0; k < 3; ++k) dst[q][3 * (size_t)i + k] = soa[(size_t)k * n + i];
+    }
+    return TCP_OK;
+}
+
+// Forces of all replicas at the current positions (main.f90:100-141 per
+// replica): SPME, real-space sum, SPME_SUM and REMOVE_RIGIDMTN.
+int tcp_batch_force(tcp_batch *b, tcp_energies *e) {
+    if (!b || !b->ready) return set_error(TCP_ERR_STATE, "tcp_batch_ewald_self must be called first");
+    cudaSetDevice(b->device);
+    const BAcc A = acc_of(b);
+    const int nb = (b->ntot + kBThreads - 1) / kBThreads;
+    b_refresh_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b));
+    TCP_CUDA(cudaMemsetAsync(A.um, 0, sizeof(double) * 8 * (size_t)b->nrep, b->stream));
+    TCP_CUDA(cudaMemsetAsync(b->Q, 0, sizeof(double) * (size_t)b->mesh_total, b->stream));
+    b_spme(b, false);
+    b_to_float_kernel<<<(int)std::min<long long>((b->mesh_total + 255) / 256, 8192), 256, 0, b->stream>>>(
+        b->Q, b->Qf, (long)b->mesh_total);
+    for (auto &g : b->groups)
+        if (cufftExecR2C(g.fwd, b->Qf + g.mesh_off, b->Qk + g.half_off) != CUFFT_SUCCESS)
+            return set_error(TCP_ERR_CUFFT, "batched cufftExecR2C failed");
+    b_influence_kernel<<<b->infl_blocks, 256, 0, b->stream>>>(b->Qk, b->infl, b->reps, b->blk0, b->nrep, A.um);
+    for (auto &g : b->groups)
+        if (cufftExecC2R(g.inv, b->Qk + g.half_off, b->Qf + g.mesh_off) != CUFFT_SUCCESS)
+            return set_error(TCP_ERR_CUFFT, "batched cufftExecC2R failed");
+    b_spme(b, true);
+    int rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
+                                  b->status, b->counter, b->num_sms, true);
+    if (rc) return rc;
+    b_finalize_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), A.fsum);
+    // the net-force removal of the step is fused into the kick; here apply it alone
+    b_kick2_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), 0.0, A.fsum, A.mv0);
+    TCP_CUDA(cudaGetLastError());
+    if ((rc = b_sync(b))) return rc;
+    b_energies(b, e);
+    return TCP_OK;
+}
+
+// nsteps MD steps of every replica, one CUDA graph per step.
+int tcp_batch_md_steps(tcp_batch *b, double dt, int nsteps, tcp_energies *e) {
+    if (!b || !b->ready) return set_error(TCP_ERR_STATE, "tcp_batch_ewald_self must be called first");
+    if (nsteps < 0) return set_error(TCP_ERR_BAD_PARAM, "nsteps < 0");
+    cudaSetDevice(b->device);
+    int rc;
+    if (!b->graph || b->graph_dt != dt) {
+        if (b->graph) cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        cudaGraph_t g;
+        const long long before = b->launches;
+        TCP_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        rc = b_step(b, dt);
+        cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+        if (rc) return rc;
+        if (ce != cudaSuccess) return cuda_check(ce, "cudaStreamEndCapture");
+        ce = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) return cuda_check(ce, "cudaGraphInstantiate");
+        b->graph_kernels = (int)(b->launches - before);
+        b->launches = before;
+        b->graph_dt = dt;
+    }
+    for (int s = 0; s < nsteps; ++s) {
+        TCP_CUDA(cudaGraphLaunch(b->graph, b->stream));
+        b->launches += b->graph_kernels;
+    }
+    if ((rc = b_sync(b))) return rc;
+    b_energies(b, e);
+    return TCP_OK;
+}
+
+int tcp_batch_time_steps(tcp_batch *b, double dt, int nsteps, double *ms_per_step) {
+    if (!b || !ms_per_step || nsteps <= 0) return set_error(TCP_ERR_BAD_PARAM, "bad arguments");
+    int rc = tcp_batch_md_steps(b, dt, 1, nullptr);   // builds the graph
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    TCP_CUDA(cudaEventCreate(&e0));
+    TCP_CUDA(cudaEventCreate(&e1));
+    cudaEventRecord(e0, b->stream);
+    for (int s = 0; s < nsteps; ++s) {
+        TCP_CUDA(cudaGraphLaunch(b->graph, b->stream));
+        b->launches += b->graph_kernels;
+    }
+    cudaEventRecord(e1, b->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if ((rc = b_sync(b))) return rc;
+    *ms_per_step = (double)ms / nsteps;
+    return TCP_OK;
+}
+
+}  // extern "C"

@@ -468,7 +468,7 @@ __global__ void force_finalize_kernel(const double *__restrict__ fpart, int nspl
 
 // ---------------------------------------------------------------------------
 // host side
-static void make_consts(tcp_ctx *c) {
+void make_pair_consts(tcp_ctx *c) {
     PairConsts &k = c->pc;
     const tcp_params &p = c->p;
     const double two32 = 4294967296.0;
@@ -560,7 +560,7 @@ static int choose_jsplit(const tcp_ctx *c, const Geometry &g, int blocks_per_sm)
 }
 
 int pair_setup(tcp_ctx *c) {
-    make_consts(c);
+    make_pair_consts(c);
     const bool fp64 = c->p.precision == TCP_PREC_FP64;
     Geometry g = geometry(c, fp64);
     int bps = 1;
@@ -754,7 +754,7 @@ extern "C" int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, 
     tmp.alpha = p->a > 0.0 ? p->a : 3.1 / p->rc;
     tmp.rc2 = p->rc * p->rc;
     TCP_CUDA(cudaDeviceGetAttribute(&tmp.num_sms, cudaDevAttrMultiProcessorCount, dev));
-    make_consts(&tmp);
+    make_pair_consts(&tmp);
     const bool fp64 = p->precision == TCP_PREC_FP64;
     const Geometry g = geometry(&tmp, fp64);
     int bps = 1;

@@ -29,6 +29,7 @@
 // units of L/2^32, SFU rsqrt/rcp/ex2, erfc = exp(-x^2) t Q(t)).  Cubic boxes
 // only; other boxes use the ordered-pair kernel.
 #include <algorithm>
+#include <cstring>
 
 #include "device_util.cuh"
 #include "pair_math.cuh"
@@ -42,22 +43,38 @@ constexpr int kN3Sub = 128;                // j-subtile
 constexpr int kN3Stages = 3;
 constexpr int kN3DynPercent = 10;          // share of the items handed out dynamically
 
-struct N3Args {
-    const int4 *xq;
-    int nel, n;
+// Tile geometry of one system (a replica of a batch, or the only system).
+struct N3Geom {
+    int off;              // first particle in the global arrays
+    int nel, n;           // electrons, particles
     int nIe, nI;          // i-tiles, electron tiles first
     int nSe, nS;          // j-subtiles, electron subtiles first
-    long long total;      // items
-    long long nstatic;    // items [0, nstatic) split statically
-    double *facc;         // [3][n], zeroed before the launch
-    double *upart;        // [gridDim.x]
-    unsigned *status;
-    unsigned *counter;    // dynamic item counter, zeroed before the launch
+    long long item0;      // first item of this system in the global item list
+};
+
+struct N3Rep {
+    N3Geom g;
     PairConsts c;
 };
 
+struct N3Args {
+    const int4 *xq;
+    long long total;      // items (all systems)
+    long long nstatic;    // items [0, nstatic) split statically
+    int ntot;             // stride of facc
+    double *facc;         // [3][ntot], zeroed before the launch
+    double *upart;        // [gridDim.x] (single system)
+    unsigned *status;
+    unsigned *counter;    // dynamic item counter, zeroed before the launch
+    N3Geom g;             // single system
+    PairConsts c;
+    const N3Rep *reps;    // batch: one entry per replica
+    int nrep;
+    double *ur_rep;       // batch: Ur per replica (zeroed before the launch)
+};
+
 template <int TILE>
-__device__ __forceinline__ void n3_itile(const N3Args &a, int I, int &start, int &end, int &sp, int &first) {
+__device__ __forceinline__ void n3_itile(const N3Geom &a, int I, int &start, int &end, int &sp, int &first) {
     constexpr int SPT = TILE / kN3Sub;
     if (I < a.nIe) {
         sp = 0;
@@ -72,7 +89,7 @@ __device__ __forceinline__ void n3_itile(const N3Args &a, int I, int &start, int
     }
 }
 
-__device__ __forceinline__ void n3_sub(const N3Args &a, int S, int &start, int &cnt, int &sp) {
+__device__ __forceinline__ void n3_sub(const N3Geom &a, int S, int &start, int &cnt, int &sp) {
     if (S < a.nSe) {
         sp = 0;
         start = S * kN3Sub;
@@ -84,9 +101,9 @@ __device__ __forceinline__ void n3_sub(const N3Args &a, int S, int &start, int &
     }
 }
 
-// item index -> (row I, subtile S)
+// local item index of one system -> (row I, subtile S)
 template <int TILE>
-__device__ __forceinline__ void n3_decode(const N3Args &a, long long it, int &I, int &S) {
+__device__ __forceinline__ void n3_decode(const N3Geom &a, long long it, int &I, int &S) {
     long long acc = 0;
     int st, en, sp, first;
     for (I = 0; I < a.nI; ++I) {
@@ -101,16 +118,31 @@ __device__ __forceinline__ void n3_decode(const N3Args &a, long long it, int &I,
     S = a.nS;
 }
 
-template <int TILE>
-__device__ __forceinline__ void n3_advance(const N3Args &a, int &I, int &S) {
-    if (++S == a.nS) {
-        ++I;
-        int st, en, sp, first;
-        if (I < a.nI) {
-            n3_itile<TILE>(a, I, st, en, sp, first);
-            S = first;
+// global item -> replica (0 for a single system), row and subtile
+template <int TILE, bool BATCH>
+__device__ __forceinline__ void n3_locate(const N3Args &a, long long it, int &rep, int &I, int &S) {
+    rep = 0;
+    if (BATCH) {
+        int lo = 0, hi = a.nrep - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a.reps[mid].g.item0 <= it) lo = mid; else hi = mid - 1;
         }
+        rep = lo;
+        n3_decode<TILE>(a.reps[rep].g, it - a.reps[rep].g.item0, I, S);
+    } else {
+        n3_decode<TILE>(a.g, it, I, S);
     }
+}
+
+template <bool BATCH>
+__device__ __forceinline__ const N3Geom &n3_geom(const N3Args &a, int rep) {
+    return BATCH ? a.reps[rep].g : a.g;
+}
+
+template <bool BATCH>
+__device__ __forceinline__ const PairConsts &n3_consts(const N3Args &a, int rep) {
+    return BATCH ? a.reps[rep].c : a.c;
 }
 
 // One pair in units of u = L/2^32.  Returns the force weight w (force on i is
@@ -206,7 +238,7 @@ __device__ __forceinline__ void n3_item(const PairConsts &c, const int4 *__restr
     }
 }
 
-template <bool ENERGY, int R, int UNROLL, int MINB>
+template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH>
 __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args a) {
     constexpr int TILE = 32 * R * kN3Warps;
     constexpr int SPT = TILE / kN3Sub;
@@ -228,24 +260,22 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
     }
     __syncthreads();
 
-    int I = 0, S = 0;
-    if (nst > 0) n3_decode<TILE>(a, it0, I, S);
-    int pI = I, pS = S;   // producer cursor (thread 0)
-    auto issue = [&](int stage, int si) {
+    // subtile copy of global item `it` into ring stage `stage` (thread 0)
+    auto issue = [&](int stage, long long it) {
+        int rep, I_, S_;
+        n3_locate<TILE, BATCH>(a, it, rep, I_, S_);
+        const N3Geom &g = n3_geom<BATCH>(a, rep);
         int js, jc, jsp;
-        n3_sub(a, si, js, jc, jsp);
+        n3_sub(g, S_, js, jc, jsp);
         const uint32_t bytes = (uint32_t)jc * sizeof(int4);
         mbar_arrive_expect_tx(&bars[stage], bytes);
-        bulk_g2s(tiles[stage], a.xq + js, bytes, &bars[stage]);
+        bulk_g2s(tiles[stage], a.xq + g.off + js, bytes, &bars[stage]);
     };
     if (tid == 0)
-        for (int k = 0; k < min(kN3Stages, nst); ++k) {
-            issue(k, pS);
-            n3_advance<TILE>(a, pI, pS);
-        }
+        for (int k = 0; k < min(kN3Stages, nst); ++k) issue(k, it0 + k);
 
     double etot = 0.0;
-    int curI = -1, istart = 0, iend = 0, isp = 0, ifirst = 0;
+    int curRep = -1, curI = -1, istart = 0, iend = 0, isp = 0, ifirst = 0, ioff = 0;
     int4 xi[R];
     int ii[R];
     bool vi[R];
@@ -259,44 +289,59 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
         hi[r][0] = hi[r][1] = hi[r][2] = lo[r][0] = lo[r][1] = lo[r][2] = 0.f;
     }
 
+    // i-forces of the current row to global memory (all threads, uniform)
     auto flush_i = [&]() {
         if (curI < 0) return;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             if (vi[r])
                 for (int k = 0; k < 3; ++k)
-                    atomicAdd(&a.facc[(size_t)k * a.n + ii[r]], kEps * ((double)hi[r][k] + (double)lo[r][k]));
+                    atomicAdd(&a.facc[(size_t)k * a.ntot + ioff + ii[r]],
+                              kEps * ((double)hi[r][k] + (double)lo[r][k]));
             hi[r][0] = hi[r][1] = hi[r][2] = lo[r][0] = lo[r][1] = lo[r][2] = 0.f;
         }
-        etot += (double)eh + (double)el;
+        if (ENERGY) {
+            if (BATCH) {
+                const double t = block_sum((double)eh + (double)el, red);
+                if (tid == 0) atomicAdd(&a.ur_rep[curRep], t);
+            } else {
+                etot += (double)eh + (double)el;
+            }
+        }
         eh = el = 0.f;
     };
 
-    // process item k (ring stage k % kN3Stages) of row I_, subtile S_; false on timeout
-    auto process = [&](int k, int I_, int S_) -> bool {
-        if (I_ != curI) {
+    // process global item `it` in ring slot k; false on timeout
+    auto process = [&](int k, long long it) -> bool {
+        int rep, I_, S_;
+        n3_locate<TILE, BATCH>(a, it, rep, I_, S_);
+        const N3Geom &g = n3_geom<BATCH>(a, rep);
+        if (I_ != curI || rep != curRep) {
             flush_i();
             curI = I_;
-            n3_itile<TILE>(a, I_, istart, iend, isp, ifirst);
+            curRep = rep;
+            ioff = g.off;
+            n3_itile<TILE>(g, I_, istart, iend, isp, ifirst);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 ii[r] = istart + warp * 32 * R + r * 32 + lane;
                 vi[r] = ii[r] < iend;
-                xi[r] = a.xq[vi[r] ? ii[r] : istart];
+                xi[r] = a.xq[ioff + (vi[r] ? ii[r] : istart)];
             }
         }
         int jstart, cnt, jsp;
-        n3_sub(a, S_, jstart, cnt, jsp);
+        n3_sub(g, S_, jstart, cnt, jsp);
         const int pt = isp + jsp;
         const bool masked = (S_ < ifirst + SPT && jsp == isp) || cnt < kN3Sub || (iend - istart) < TILE;
         const int stage = k % kN3Stages;
         const bool ok = mbar_wait_bounded(&bars[stage], (uint32_t)((k / kN3Stages) & 1), kWaitLimitCycles);
+        const PairConsts &c = n3_consts<BATCH>(a, rep);
         float p[R][3], pe = 0.f;
 #pragma unroll
         for (int r = 0; r < R; ++r) p[r][0] = p[r][1] = p[r][2] = 0.f;
-        const int kind = pt == 1 ? (a.c.ei_model == TCP_EI_DEUTSCH ? 1 : (a.c.ei_model == TCP_EI_KELBG ? 2 : 0)) : 0;
+        const int kind = pt == 1 ? (c.ei_model == TCP_EI_DEUTSCH ? 1 : (c.ei_model == TCP_EI_KELBG ? 2 : 0)) : 0;
 #define TCP_N3_ITEM(KIND, MASKED) \
-    n3_item<KIND, ENERGY, MASKED, UNROLL, R>(a.c, tiles[stage], cnt, jstart, xi, ii, vi, sjacc, p, pe)
+    n3_item<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ii, vi, sjacc, p, pe)
         if (masked) {
             if (kind == 1) TCP_N3_ITEM(1, true);
             else if (kind == 2) TCP_N3_ITEM(2, true);
@@ -307,21 +352,22 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
             else TCP_N3_ITEM(0, false);
         }
 #undef TCP_N3_ITEM
-        const float qf = a.c.u_qq_force[pt];
+        const float qf = c.u_qq_force[pt];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             acc2(hi[r][0], lo[r][0], p[r][0] * qf);
             acc2(hi[r][1], lo[r][1], p[r][1] * qf);
             acc2(hi[r][2], lo[r][2], p[r][2] * qf);
         }
-        if (ENERGY) acc2(eh, el, pe * a.c.u_qq_energy[pt]);
+        if (ENERGY) acc2(eh, el, pe * c.u_qq_energy[pt]);
         // all warps are done with this subtile and its reaction sums
         const bool timeout = __syncthreads_or(!ok);
         if (!timeout && tid < cnt) {
             const double sc = -kEps * (double)qf;
-            atomicAdd(&a.facc[jstart + tid], sc * (double)sjacc[tid][0]);
-            atomicAdd(&a.facc[(size_t)a.n + jstart + tid], sc * (double)sjacc[tid][1]);
-            atomicAdd(&a.facc[2 * (size_t)a.n + jstart + tid], sc * (double)sjacc[tid][2]);
+            const size_t j = (size_t)ioff + jstart + tid;
+            atomicAdd(&a.facc[j], sc * (double)sjacc[tid][0]);
+            atomicAdd(&a.facc[(size_t)a.ntot + j], sc * (double)sjacc[tid][1]);
+            atomicAdd(&a.facc[2 * (size_t)a.ntot + j], sc * (double)sjacc[tid][2]);
         }
         if (tid < kN3Sub) sjacc[tid][0] = sjacc[tid][1] = sjacc[tid][2] = 0.f;
         return !timeout;
@@ -329,41 +375,31 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
 
     bool good = true;
     int k = 0;
-    int issued = min(kN3Stages, nst);   // items whose subtile copy has been issued (thread 0's view)
+    int issued = min(kN3Stages, nst);   // items whose subtile copy has been issued
     // static share: contiguous items, subtiles prefetched kN3Stages ahead
     for (; k < nst; ++k) {
-        if (!process(k, I, S)) {
+        if (!process(k, it0 + k)) {
             good = false;
             break;
         }
         if (k + kN3Stages < nst) {
-            if (tid == 0) {
-                issue(k % kN3Stages, pS);
-                n3_advance<TILE>(a, pI, pS);
-            }
+            if (tid == 0) issue(k % kN3Stages, it0 + k + kN3Stages);
             issued = k + kN3Stages + 1;
         }
         __syncthreads();
-        n3_advance<TILE>(a, I, S);
     }
     // dynamic share: one item at a time from the counter
     while (good) {
         if (tid == 0) {
             const long long it = a.nstatic + (long long)atomicAdd(a.counter, 1u);
             s_next = it;
-            if (it < a.total) {
-                int dI, dS;
-                n3_decode<TILE>(a, it, dI, dS);
-                issue(k % kN3Stages, dS);
-            }
+            if (it < a.total) issue(k % kN3Stages, it);
         }
         __syncthreads();
         const long long it = s_next;
         if (it >= a.total) break;
         issued = k + 1;
-        int dI, dS;
-        n3_decode<TILE>(a, it, dI, dS);
-        if (!process(k, dI, dS)) {
+        if (!process(k, it)) {
             good = false;
             break;
         }
@@ -380,7 +416,7 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
         return;
     }
     flush_i();
-    if (ENERGY) {
+    if (ENERGY && !BATCH) {
         const double tot = block_sum(etot, red);
         if (tid == 0) a.upart[blockIdx.x] = tot;
     }
@@ -402,10 +438,10 @@ struct N3Variant {
     const char *name;
 };
 static const N3Variant kVariants[] = {
-    {pair_n3_kernel<true, 2, 2, 3>, pair_n3_kernel<false, 2, 2, 3>, 2, "n3_r2_u2_b3"},
-    {pair_n3_kernel<true, 2, 1, 3>, pair_n3_kernel<false, 2, 1, 3>, 2, "n3_r2_u1_b3"},
-    {pair_n3_kernel<true, 4, 1, 2>, pair_n3_kernel<false, 4, 1, 2>, 4, "n3_r4_u1_b2"},
-    {pair_n3_kernel<true, 4, 2, 2>, pair_n3_kernel<false, 4, 2, 2>, 4, "n3_r4_u2_b2"},
+    {pair_n3_kernel<true, 2, 2, 3, false>, pair_n3_kernel<false, 2, 2, 3, false>, 2, "n3_r2_u2_b3"},
+    {pair_n3_kernel<true, 2, 1, 3, false>, pair_n3_kernel<false, 2, 1, 3, false>, 2, "n3_r2_u1_b3"},
+    {pair_n3_kernel<true, 4, 1, 2, false>, pair_n3_kernel<false, 4, 1, 2, false>, 4, "n3_r4_u1_b2"},
+    {pair_n3_kernel<true, 4, 2, 2, false>, pair_n3_kernel<false, 4, 2, 2, false>, 4, "n3_r4_u2_b2"},
 };
 constexpr int kN3Variants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -424,25 +460,35 @@ int n3_grid(const tcp_ctx *c) {
     return g;
 }
 
+// Tile geometry of a system of nel + nion particles for i-tiles of `tile`.
+N3Geom n3_geometry(int off, int nel, int nion, int tile, long long item0, long long *items) {
+    N3Geom g;
+    const int spt = tile / kN3Sub;
+    g.off = off;
+    g.nel = nel;
+    g.n = nel + nion;
+    g.nIe = cdiv(nel, tile);
+    g.nI = g.nIe + cdiv(nion, tile);
+    g.nSe = cdiv(nel, kN3Sub);
+    g.nS = g.nSe + cdiv(nion, kN3Sub);
+    g.item0 = item0;
+    long long total = 0;
+    for (int I = 0; I < g.nI; ++I) total += g.nS - (I < g.nIe ? I * spt : g.nSe + (I - g.nIe) * spt);
+    *items = total;
+    return g;
+}
+
 int launch_pair_n3(tcp_ctx *c, bool energy) {
     const int v = std::min(std::max(c->pair_variant, 1), kN3Variants);
     const int tile = 32 * kVariants[v - 1].R * kN3Warps;
-    const int spt = tile / kN3Sub;
     N3Args a;
-    a.xq = c->xq;
-    a.nel = c->nel;
-    a.n = c->n;
-    a.nIe = cdiv(c->nel, tile);
-    a.nI = a.nIe + cdiv(c->nion, tile);
-    a.nSe = cdiv(c->nel, kN3Sub);
-    a.nS = a.nSe + cdiv(c->nion, kN3Sub);
+    std::memset(&a, 0, sizeof a);
     long long total = 0;
-    for (int I = 0; I < a.nI; ++I) {
-        const int first = I < a.nIe ? I * spt : a.nSe + (I - a.nIe) * spt;
-        total += a.nS - first;
-    }
+    a.g = n3_geometry(0, c->nel, c->nion, tile, 0, &total);
+    a.xq = c->xq;
     a.total = total;
     a.nstatic = total - total * kN3DynPercent / 100;
+    a.ntot = c->n;
     a.facc = c->fpart;
     a.upart = c->upart;
     a.status = c->status;
@@ -459,6 +505,61 @@ int launch_pair_n3(tcp_ctx *c, bool energy) {
         kVariants[v - 1].plain<<<grid, kN3Threads, 0, c->stream>>>(a);
     }
     c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+// ---- batch of replicas -------------------------------------------------------
+constexpr int kN3BatchR = 2;   // i-particles per lane of the batched kernel
+constexpr int kN3BatchTile = 32 * kN3BatchR * kN3Warps;
+
+int n3_batch_tile() { return kN3BatchTile; }
+size_t n3_rep_bytes() { return sizeof(N3Rep); }
+
+// Fills reps (host) for replicas with the given offsets/counts/constants.
+long long n3_batch_fill(void *reps_host, int nrep, const int *off, const int *nel, const int *nion,
+                        const PairConsts *pc) {
+    N3Rep *r = static_cast<N3Rep *>(reps_host);
+    long long item0 = 0;
+    for (int k = 0; k < nrep; ++k) {
+        long long items = 0;
+        r[k].g = n3_geometry(off[k], nel[k], nion[k], kN3BatchTile, item0, &items);
+        r[k].c = pc[k];
+        item0 += items;
+    }
+    return item0;
+}
+
+int n3_batch_grid(int num_sms) {
+    int bps = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_n3_kernel<true, kN3BatchR, 2, 2, true>, kN3Threads, 0);
+    return std::max(1, num_sms * std::max(1, bps));
+}
+
+int launch_pair_n3_batch(cudaStream_t st, const int4 *xq, int ntot, double *facc, const void *reps_dev, int nrep,
+                         long long total, double *ur_rep, unsigned *status, unsigned *counter, int num_sms,
+                         bool energy) {
+    N3Args a;
+    std::memset(&a, 0, sizeof a);
+    a.xq = xq;
+    a.total = total;
+    a.nstatic = total - total * kN3DynPercent / 100;
+    a.ntot = ntot;
+    a.facc = facc;
+    a.status = status;
+    a.counter = counter;
+    a.reps = static_cast<const N3Rep *>(reps_dev);
+    a.nrep = nrep;
+    a.ur_rep = ur_rep;
+    const int grid = (int)std::min<long long>(n3_batch_grid(num_sms), total);
+    TCP_CUDA(cudaMemsetAsync(facc, 0, sizeof(double) * 3 * (size_t)ntot, st));
+    TCP_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
+    if (energy) {
+        TCP_CUDA(cudaMemsetAsync(ur_rep, 0, sizeof(double) * (size_t)nrep, st));
+        pair_n3_kernel<true, kN3BatchR, 2, 2, true><<<grid, kN3Threads, 0, st>>>(a);
+    } else {
+        pair_n3_kernel<false, kN3BatchR, 2, 2, true><<<grid, kN3Threads, 0, st>>>(a);
+    }
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;
 }

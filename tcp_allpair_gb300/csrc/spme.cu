@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "device_util.cuh"
+#include "spme_math.cuh"
 #include "tcp_internal.h"
 
 namespace tcp {
@@ -32,56 +33,6 @@ struct SpmeArgs {
     double box0, box1, box2;
     int K1, K2, K3;
 };
-
-// B-spline weights W[j] = M_P(w + P-1-j) and dW[j] = dM_P/du on the grid
-// points INT(u) + j - (P-3).  Order 4 uses the reference's explicit cubics
-// (force.f90:703-738); other orders the Cox-de Boor recursion run upward on
-// the P nonzero values.
-template <int P, typename T>
-__device__ __forceinline__ void spline_w(double u, T *W, T *dW) {
-    if (P == 4) {
-        T z = (T)(trunc(u) - u + 1.0);
-        W[0] = z * z * z / (T)6;
-        dW[0] = (T)-3. * z * z / (T)6;
-        z += (T)1;
-        W[1] = ((T)-3. * z * z * z + (T)12. * z * z - (T)12. * z + (T)4.) / (T)6;
-        dW[1] = ((T)9. * z * z - (T)24. * z + (T)12.) / (T)6;
-        z += (T)1;
-        W[2] = ((T)3. * z * z * z - (T)24. * z * z + (T)60. * z - (T)44.) / (T)6;
-        dW[2] = ((T)-9. * z * z + (T)48. * z - (T)60.) / (T)6;
-        z += (T)1;
-        W[3] = (-z * z * z + (T)12. * z * z - (T)48. * z + (T)64.) / (T)6;
-        dW[3] = ((T)3. * z * z - (T)24. * z + (T)48.) / (T)6;
-        return;
-    }
-    const T w = (T)(u - trunc(u));
-    T a[P];
-    a[0] = (T)1;
-#pragma unroll
-    for (int j = 1; j < P; ++j) a[j] = (T)0;
-    // a_n[j] = ((w+n-1-j) a_{n-1}[j-1] + (1-w+j) a_{n-1}[j]) / (n-1)
-#pragma unroll
-    for (int nn = 2; nn <= P; ++nn) {
-        if (nn == P) {
-#pragma unroll
-            for (int j = 0; j < P; ++j) dW[j] = (j > 0 ? a[j - 1] : (T)0) - (j < P - 1 ? a[j] : (T)0);
-        }
-        const T inv = (T)1 / (T)(nn - 1);
-#pragma unroll
-        for (int j = nn - 1; j >= 0; --j) {
-            const T left = j > 0 ? a[j - 1] : (T)0;
-            const T right = j < nn - 1 ? a[j] : (T)0;
-            a[j] = ((w + (T)(nn - 1 - j)) * left + ((T)1 - w + (T)j) * right) * inv;
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < P; ++j) W[j] = a[j];
-}
-
-__device__ __forceinline__ int wrapi(int i, int K) {
-    i %= K;
-    return i < 0 ? i + K : i;
-}
 
 // charge spreading, force.f90:697-820 (atomic FP64 adds into the mesh)
 template <int P>
@@ -276,7 +227,7 @@ static double bspline_M(int n, double y) {
 
 // |b(m)|^-2 per axis (36/(4+2cos)^2 for order 4, force.f90:834-839); odd
 // orders vanish at the Nyquist index, where the mean of the neighbours is used.
-static std::vector<double> bspline_moduli(int order, int K) {
+std::vector<double> bspline_moduli(int order, int K) {
     std::vector<double> den(K), out(K);
     for (int m = 0; m < K; ++m) {
         if (order == 4) {

@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "tcp_gpu.h"
 
@@ -142,6 +143,7 @@ int cuda_check(cudaError_t e, const char *what);
     } while (0)
 
 // pair.cu
+void make_pair_consts(tcp_ctx *c);                 // c->pc from c->p, c->alpha, c->rc2
 int pair_setup(tcp_ctx *c);                        // constants, jsplit, partial buffers
 int launch_pair(tcp_ctx *c, bool energy, bool rdf);
 int launch_force_finalize(tcp_ctx *c, bool add_rec);
@@ -152,8 +154,16 @@ int n3_variant_count();
 const char *n3_variant_name(int v);
 int autotune_pair(tcp_ctx *c);
 int launch_pair_n3(tcp_ctx *c, bool energy);
+int n3_batch_tile();
+size_t n3_rep_bytes();
+long long n3_batch_fill(void *reps_host, int nrep, const int *off, const int *nel, const int *nion,
+                        const PairConsts *pc);
+int launch_pair_n3_batch(cudaStream_t st, const int4 *xq, int ntot, double *facc, const void *reps_dev, int nrep,
+                         long long total, double *ur_rep, unsigned *status, unsigned *counter, int num_sms,
+                         bool energy);
 // spme.cu
 int spme_setup(tcp_ctx *c);                        // meshes, plans, influence function
+std::vector<double> bspline_moduli(int order, int K);
 int spme_free(tcp_ctx *c);
 int launch_spme(tcp_ctx *c, bool energy);
 int ewald_setup(tcp_ctx *c);

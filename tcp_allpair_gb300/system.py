@@ -170,3 +170,19 @@ def make_config_system(name: str, seed: int = 0, n: int | None = None) -> System
     if "ewald_rel_err" in c:
         kw["ewald_rel_err"] = c["ewald_rel_err"]
     return make_system(n if n is not None else c["n"], **kw)
+
+
+def make_batch_systems(nrep: int = 64, seed: int = 0, nmin: int = 512, nmax: int = 8192):
+    """The batched-replica workload: N log-uniform in [nmin, nmax] (equal electrons
+    and ions), Gamma log-uniform in [0.1, 10], lambda_ei uniform in [0.2a, 0.8a],
+    alpha rc = 3.1 (force.f90:23), SPME order 4 on a 32^3 / 48^3 / 64^3 mesh
+    chosen by N; replica r is seeded with seed + r."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(nrep):
+        n = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)) ) / 2)) * 2
+        gamma = math.exp(rng.uniform(math.log(0.1), math.log(10.0)))
+        lam = rng.uniform(0.2, 0.8)
+        K = 32 if n < 2048 else (48 if n < 4096 else 64)
+        out.append(make_system(n, gamma=gamma, lam=lam, seed=seed + r, alpha_rc=3.1, K=K, order=4))
+    return out

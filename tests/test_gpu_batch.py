@@ -1,0 +1,68 @@
+"""Batched replicas (tcp_batch_*) against one context per replica and the oracle."""
+import numpy as np
+import pytest
+
+import oracle
+import tcp_allpair_gb300 as T
+
+pytestmark = pytest.mark.gpu
+
+
+def systems():
+    spec = [(700, 1.0, 0.5, 16), (1024, 0.3, 0.3, 24), (1538, 5.0, 0.7, 32), (512, 2.0, 0.4, 16), (2050, 1.0, 0.6, 24)]
+    return [T.make_system(n, gamma=g, lam=l, seed=50 + k, alpha_rc=3.1, K=K, order=4)
+            for k, (n, g, l, K) in enumerate(spec)]
+
+
+def test_batch_force_matches_single_contexts_and_oracle():
+    ss = systems()
+    params = [T.params_for(s, precision="fp32c", ei="kelbg", recip="spme") for s in ss]
+    with T.Batch(params, [s.nel for s in ss], [s.nion for s in ss]) as b:
+        uo = b.EWALD_SELF()
+        for r, s in enumerate(ss):
+            b.upload(r, x=s.x, v=s.v)
+        eb = b.force()
+        fb = [b.download(r, x=False, v=False)[2] for r in range(len(ss))]
+    for r, s in enumerate(ss):
+        with T.Context(params[r], s.nel, s.nion) as c:
+            c.EWALD_SELF()
+            c.upload(x=s.x, v=s.v)
+            e = c.force()
+            _, _, f, _ = c.download(x=False, v=False, f=True)
+        assert oracle.rms_rel(fb[r], f) < 1e-6
+        assert eb[r]["Ur"] == pytest.approx(e["Ur"], rel=1e-6)
+        assert eb[r]["Um"] == pytest.approx(e["Um"], rel=1e-6)
+        assert uo[r] == pytest.approx(e["Uo"], rel=1e-14)
+        o = oracle.Oracle.from_system(s, ei="kelbg")
+        fo, uro, umo = o.force_total(s.x)
+        assert oracle.rms_rel(fb[r], fo) < 2e-6
+
+
+def test_batch_md_steps_match_single_contexts():
+    ss = systems()
+    params = [T.params_for(s, precision="fp32c", ei="kelbg", recip="spme", thermo=th)
+              for s, th in zip(ss, ["notemp", "isokin", "berend", "notemp", "isokin"])]
+    with T.Batch(params, [s.nel for s in ss], [s.nion for s in ss]) as b:
+        b.EWALD_SELF()
+        for r, s in enumerate(ss):
+            b.upload(r, x=s.x, v=s.v)
+        b.force()
+        eb = b.md_steps(ss[0].dt, 5)
+        xb = [b.download(r, v=False, f=False)[0] for r in range(len(ss))]
+    for r, s in enumerate(ss):
+        with T.Context(params[r], s.nel, s.nion) as c:
+            c.EWALD_SELF()
+            c.upload(x=s.x, v=s.v)
+            c.force()
+            e = c.md_steps(s.dt, 5)
+            x, _, _, _ = c.download(v=False, f=False)
+        assert np.max(np.abs(xb[r] - x)) < 1e-6 * s.box
+        assert eb[r]["mv2el"] == pytest.approx(e["mv2el"], rel=1e-5)
+        assert eb[r]["Epot"] == pytest.approx(e["Epot"], rel=1e-5)
+
+
+def test_batch_rejects_unsupported():
+    s = systems()[0]
+    p = T.params_for(s, precision="fp64", recip="spme")
+    with pytest.raises(T.TcpError):
+        T.Batch([p], [s.nel], [s.nion])
