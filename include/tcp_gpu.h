@@ -227,6 +227,36 @@ int tcp_batch_md_steps(tcp_batch *b, double dt, int nsteps, tcp_energies *e);
 /* Mean device time of one batched step over nsteps graph replays (CUDA events). */
 int tcp_batch_time_steps(tcp_batch *b, double dt, int nsteps, double *ms_per_step);
 
+/* ---- derivatives ---------------------------------------------------------
+ * No counterpart in the reference (it computes no derivatives): the analytic
+ * derivatives of the energy of force.f90 / EWALD_SELF and of the NOTEMP step
+ * of vverlet.f90, for the context's parameters and precision (the real-space
+ * part in the context's precision; the reciprocal part in FP64).  "lambda" is
+ * lambda_ei for TCP_EI_KELBG and rs for TCP_EI_DEUTSCH; every lambda
+ * derivative is 0 for TCP_EI_COULOMB. */
+
+/* At the current positions: *E = Epot + Um (eV, the potential energy of the
+ * ener files), *dE_dlambda (eV/A) and *dE_dscale = dE/ds for charges s q
+ * (every term is quadratic in s, so 2E/s).  The stored forces are kept (the
+ * energy evaluation writes them to scratch first).  Any pointer may be NULL. */
+int tcp_adjoint_energy(tcp_ctx *ctx, double *E, double *dE_dlambda, double *dE_dscale);
+
+/* Hessian-vector product of the potential energy at the current positions:
+ * hw = (d^2 E / dx dx) w, w and hw host arrays [N][3] in particle order
+ * (electrons, then ions), hw in eV/A^2 times the unit of w.  The mean-force
+ * removal of REMOVE_RIGIDMTN is not applied.  *dF_dlambda_w (may be NULL)
+ * = sum_i dF_i/dlambda . w_i with F = -grad E. */
+int tcp_hvp(tcp_ctx *ctx, const double *w, double *hw, double *dF_dlambda_w);
+
+/* Reverse mode through nsteps NOTEMP steps of tcp_md_steps from the current
+ * x, v (the start forces are recomputed, f_0 = F(x_0; lambda)):
+ *   *J = (1/K) sum_{k=1..K} (mv2el_k + mv2ion_k) / (3N)   (K = nsteps)
+ * and *dJ_dlambda by the discrete adjoint of the step, with checkpoints of
+ * (x, v) every `every` steps and the steps in between recomputed.  On return
+ * the context holds the state after step K, as after tcp_md_steps.
+ * TCP_ERR_BAD_PARAM unless thermo = TCP_THERMO_NOTEMP. */
+int tcp_reverse_md(tcp_ctx *ctx, double dt, int nsteps, int every, double *J, double *dJ_dlambda);
+
 /* ---- measurement hooks ---------------------------------------------------- */
 /* Runs `reps` launches of one component on the context's stream and returns
  * the mean device time per launch from CUDA events recorded on that stream.

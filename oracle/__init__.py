@@ -70,6 +70,10 @@ def lib():
             "orc_md_step": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, D, D, D, D, C.c_double,
                                       C.c_int, C.c_int, D, D, D, C.c_int]),
             "orc_max_threads": (C.c_int, []),
+            "orc_adjoint_energy": (None, [P, C.c_int, C.c_int, D, D, C.c_int]),
+            "orc_hvp": (None, [P, C.c_int, C.c_int, D, D, C.c_int, C.c_int, D, D, D, C.c_int]),
+            "orc_reverse_md": (C.c_int, [P, C.c_int, C.c_int, D, D, D, C.c_int, C.c_int, C.c_double, C.c_int,
+                                         C.c_int, D, D, C.c_int]),
         }
         for k, (r, a) in sig.items():
             fn = getattr(_lib, k)
@@ -200,6 +204,45 @@ class Oracle:
         self.L.orc_md_step(C.byref(self.p), THERMO[thermo], int(apply), self.nel, self.nion, dt, _d(x), _d(v),
                            _d(f), _d(self.psi), self.Uo, r, nmax2, _d(e), None, None, self.nthreads)
         return dict(Ur=e[0], Um=e[1], Epot=e[2], mv2el=e[3], mv2ion=e[4])
+
+    # ---- derivatives ----
+    def dE_dlambda(self, x):
+        """dE/dlambda_ei (Kelbg) or dE/drs (Deutsch) of the potential energy, eV/A."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        d = C.c_double()
+        self.L.orc_adjoint_energy(C.byref(self.p), self.nel, self.nion, _d(x), C.byref(d), self.nthreads)
+        return d.value
+
+    def hvp(self, x, w, recip="spme", nmax2=64):
+        """(H w, sum_i dF_i/dlambda . w_i), H the Hessian of the potential energy."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        hw = np.zeros((self.n, 3))
+        d = C.c_double()
+        r = {"none": 0, "spme": 1, "ewald": 2}[recip]
+        self.L.orc_hvp(C.byref(self.p), self.nel, self.nion, _d(x), _d(self.psi), r, nmax2, _d(w), _d(hw),
+                       C.byref(d), self.nthreads)
+        return hw, d.value
+
+    def reverse_md(self, x0, v0, dt, K, M, recip="spme", nmax2=64):
+        """(J, dJ/dlambda): J = mean over K NOTEMP steps of (mv2el+mv2ion)/(3N)."""
+        x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        v0 = np.ascontiguousarray(v0, dtype=np.float64)
+        j, d = C.c_double(), C.c_double()
+        r = {"none": 0, "spme": 1, "ewald": 2}[recip]
+        self.L.orc_reverse_md(C.byref(self.p), self.nel, self.nion, _d(x0), _d(v0), _d(self.psi), r, nmax2, dt,
+                              K, M, C.byref(j), C.byref(d), self.nthreads)
+        return j.value, d.value
+
+    def mean_temperature(self, x0, v0, dt, K, recip="spme", nmax2=64):
+        """J of reverse_md by plain forward steps (for finite differences)."""
+        x, v = x0.copy(), v0.copy()
+        f, _, _ = self.force_total(x, recip=recip, nmax2=nmax2)
+        acc = 0.0
+        for _ in range(K):
+            e = self.md_step(x, v, f, dt, recip=recip, nmax2=nmax2)
+            acc += e["mv2el"] + e["mv2ion"]
+        return acc / (3.0 * self.n * K)
 
 
 def rms_rel(a, ref):

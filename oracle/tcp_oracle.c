@@ -618,3 +618,333 @@ int orc_md_step(const orc_params *p, int thermo, int apply_thermostat, int nel, 
     energies[4] = mv2ion;
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Derivatives of the path (adjoint).  The reference computes none: these
+ * are the analytic derivatives of the energy and of the discrete MD map
+ * restated above, pinned by central finite differences of those routines. */
+/* ------------------------------------------------------------------ */
+
+/* Radial functions of one pair term phi(r) (without eps and q_i q_j):
+ *   G1 = -phi'(r)/r          (force on i = eps qq G1 u, u = x_i - x_j)
+ *   G2 = -G1'(r)/r           (pair Hessian = eps qq (-G1 I + G2 u u^T))
+ *   dl = d phi / d lambda    (lambda = lambda_ei for Kelbg, rs for Deutsch)
+ *   gl = d G1 / d lambda
+ * kind 0: erfc(ar)/r; 1: Deutsch e-i (force.f90:135-139); 2: Kelbg e-i. */
+static void pair_radial(const orc_params *p, int kind, double r2, double r, double *G1, double *G2,
+                        double *dl, double *gl) {
+    const double a = p->a, c = 2.0 * a / ORC_SQRTPI;
+    const double e = exp(-a * a * r2);
+    const double w0 = (erfc(a * r) / r + c * e) / r2;
+    double g1 = w0, g2 = (3.0 * w0 + 2.0 * a * a * c * e) / r2, d = 0.0, gg = 0.0;
+    if (kind == 1) {
+        const double rs = p->rs, y = exp(-r / rs);
+        g1 -= y * (1.0 / (rs * r2) + 1.0 / (r2 * r));
+        g2 -= y * (3.0 / (rs * r2) + 3.0 / (r2 * r) + 1.0 / (rs * rs * r)) / r2;
+        d = -y / (rs * rs);
+        gg = -y / (rs * rs * rs * r);
+    } else if (kind == 2) {
+        const double l = p->lambda_ei, g = exp(-r2 / (l * l));
+        g1 -= g / (r2 * r);
+        g2 -= g * (3.0 / (r2 * r) + 2.0 / (l * l * r)) / r2;
+        d = -ORC_SQRTPI * erfc(r / l) / (l * l);
+        gg = -2.0 * g / (l * l * l * r);
+    }
+    *G1 = g1;
+    *G2 = g2;
+    *dl = d;
+    *gl = gg;
+}
+
+static int pair_kind(const orc_params *p, int si, int sj) {
+    if (si == sj) return 0;
+    if (p->ei_model == ORC_EI_DEUTSCH) return 1;
+    if (p->ei_model == ORC_EI_KELBG) return 2;
+    return 0;
+}
+
+/* Real-space part: hw += H_real w, *dEdl = dE/dlambda (eV/A), *dFdl_w =
+ * sum_i dF_i/dlambda . w_i (F unprojected).  w or hw may be NULL. */
+static void real_adjoint(const orc_params *p, int nel, int nion, const double *x, const double *w, double *hw,
+                         double *dEdl, double *dFdl_w, int nthreads) {
+    const int n = nel + nion;
+    const int nt = nthreads_or_max(nthreads);
+    const double s = p->charge_scale;
+    const double qs[2] = {s * p->q[0], s * p->q[1]};
+    double *hb = hw ? (double *)calloc((size_t)nt * 3 * n, sizeof(double)) : NULL;
+    double el = 0.0, fl = 0.0;
+#pragma omp parallel num_threads(nt) reduction(+ : el, fl)
+    {
+#ifdef _OPENMP
+        int tid = omp_get_thread_num();
+#else
+        int tid = 0;
+#endif
+        double *hl = hb ? hb + (size_t)tid * 3 * n : NULL;
+#pragma omp for schedule(dynamic, 16)
+        for (int i = 0; i < n - 1; ++i) {
+            int si = i < nel ? 0 : 1;
+            for (int j = i + 1; j < n; ++j) {
+                int sj = j < nel ? 0 : 1;
+                double u[3], r2 = 0.0;
+                for (int k = 0; k < 3; ++k) {
+                    u[k] = min_image(x[3 * i + k] - x[3 * j + k], p->box[k]);
+                    r2 += u[k] * u[k];
+                }
+                if (r2 >= p->rc2) continue;
+                const double r = sqrt(r2), qq = ORC_EPS * qs[si] * qs[sj];
+                double G1, G2, dl, gl;
+                pair_radial(p, pair_kind(p, si, sj), r2, r, &G1, &G2, &dl, &gl);
+                el += qq * dl;
+                if (!w) continue;
+                double dw[3], ud = 0.0;
+                for (int k = 0; k < 3; ++k) {
+                    dw[k] = w[3 * i + k] - w[3 * j + k];
+                    ud += u[k] * dw[k];
+                }
+                fl += qq * gl * ud;
+                if (hl)
+                    for (int k = 0; k < 3; ++k) {
+                        const double t = qq * (-G1 * dw[k] + G2 * ud * u[k]);
+                        hl[3 * i + k] += t;
+                        hl[3 * j + k] -= t;
+                    }
+            }
+        }
+    }
+    if (hw)
+        for (int t = 0; t < nt; ++t)
+            for (long i = 0; i < 3L * n; ++i) hw[i] += hb[(size_t)t * 3 * n + i];
+    free(hb);
+    if (dEdl) *dEdl = el;
+    if (dFdl_w) *dFdl_w = fl;
+}
+
+/* SPME part: hw += H_rec w.  With Q(m) = sum_j q_j W_j(m), phi = A Q and
+ * E = c/2 Q.phi (c = eps/(pi V)):
+ *   grad_i E = c q_i sum_m grad W_i(m) phi(m)
+ *   (H w)_i  = c q_i [sum_m (hess W_i(m) w_i) phi(m) + sum_m grad W_i(m) dphi(m)],
+ *   dphi = A dQ,  dQ(m) = sum_j q_j grad W_j(m) . w_j. */
+static void spme_hvp(const orc_params *p, int nel, int nion, const double *x, const double *psi, const double *w,
+                     double *hw) {
+    const int n = nel + nion, P = p->order;
+    const int K1 = p->K[0], K2 = p->K[1], K3 = p->K[2];
+    const int K[3] = {K1, K2, K3};
+    const long KK = (long)K1 * K2 * K3;
+    const double V = p->box[0] * p->box[1] * p->box[2];
+    const double s = p->charge_scale;
+    double complex *A = (double complex *)calloc(KK, sizeof(double complex));
+    double complex *B = (double complex *)calloc(KK, sizeof(double complex));
+    double *bm[3];
+    for (int d = 0; d < 3; ++d) {
+        bm[d] = (double *)malloc(sizeof(double) * K[d]);
+        orc_bspline_moduli(P, K[d], bm[d]);
+    }
+    double W[3][8], dW[3][8], d2W[3][8];
+    int base[3];
+    /* weights, first and second derivatives w.r.t. x (chain factor K/L) */
+#define ORC_WEIGHTS(m)                                                                          \
+    for (int d = 0; d < 3; ++d) {                                                               \
+        double u = (double)K[d] * (x[3 * (m) + d] + p->box[d] * .5) / p->box[d];                \
+        spline_weights(P, u, W[d], dW[d]);                                                      \
+        double fr = u - trunc(u), kl = (double)K[d] / p->box[d];                                \
+        for (int j = 0; j < P; ++j) {                                                           \
+            double y = fr + (double)(P - 1 - j);                                                \
+            d2W[d][j] = (bspline_M(P - 2, y) - 2.0 * bspline_M(P - 2, y - 1.0) +                 \
+                         bspline_M(P - 2, y - 2.0)) * kl * kl;                                   \
+            dW[d][j] *= kl;                                                                     \
+        }                                                                                       \
+        base[d] = (int)trunc(u) - (P - 3);                                                      \
+    }
+    for (int m = 0; m < n; ++m) {
+        const double q = s * p->q[m < nel ? 0 : 1];
+        ORC_WEIGHTS(m)
+        for (int k = 0; k < P; ++k) {
+            int iz = ((base[2] + k) % K3 + K3) % K3;
+            for (int j = 0; j < P; ++j) {
+                int iy = ((base[1] + j) % K2 + K2) % K2;
+                for (int i = 0; i < P; ++i) {
+                    int ix = ((base[0] + i) % K1 + K1) % K1;
+                    long idx = ix + (long)K1 * (iy + (long)K2 * iz);
+                    A[idx] += q * W[0][i] * W[1][j] * W[2][k];
+                    B[idx] += q * (dW[0][i] * W[1][j] * W[2][k] * w[3 * m] + W[0][i] * dW[1][j] * W[2][k] * w[3 * m + 1] +
+                                   W[0][i] * W[1][j] * dW[2][k] * w[3 * m + 2]);
+                }
+            }
+        }
+    }
+    fft3d(A, K1, K2, K3, -1);
+    fft3d(B, K1, K2, K3, -1);
+    for (int k = 0; k < K3; ++k)
+        for (int j = 0; j < K2; ++j)
+            for (int i = 0; i < K1; ++i) {
+                long idx = i + (long)K1 * (j + (long)K2 * k);
+                double g = psi[idx] * bm[0][i] * bm[1][j] * bm[2][k];
+                A[idx] *= g;
+                B[idx] *= g;
+            }
+    fft3d(A, K1, K2, K3, +1);
+    fft3d(B, K1, K2, K3, +1);
+    const double c = ORC_EPS / (ORC_PI * V);
+    for (int m = 0; m < n; ++m) {
+        const double q = s * p->q[m < nel ? 0 : 1];
+        ORC_WEIGHTS(m)
+        double h[3] = {0.0, 0.0, 0.0};
+        const double *wm = w + 3 * m;
+        for (int k = 0; k < P; ++k) {
+            int iz = ((base[2] + k) % K3 + K3) % K3;
+            for (int j = 0; j < P; ++j) {
+                int iy = ((base[1] + j) % K2 + K2) % K2;
+                for (int i = 0; i < P; ++i) {
+                    int ix = ((base[0] + i) % K1 + K1) % K1;
+                    long idx = ix + (long)K1 * (iy + (long)K2 * iz);
+                    const double ph = creal(A[idx]), dph = creal(B[idx]);
+                    const double gx = dW[0][i] * W[1][j] * W[2][k], gy = W[0][i] * dW[1][j] * W[2][k],
+                                 gz = W[0][i] * W[1][j] * dW[2][k];
+                    const double hxx = d2W[0][i] * W[1][j] * W[2][k], hyy = W[0][i] * d2W[1][j] * W[2][k],
+                                 hzz = W[0][i] * W[1][j] * d2W[2][k];
+                    const double hxy = dW[0][i] * dW[1][j] * W[2][k], hxz = dW[0][i] * W[1][j] * dW[2][k],
+                                 hyz = W[0][i] * dW[1][j] * dW[2][k];
+                    h[0] += (hxx * wm[0] + hxy * wm[1] + hxz * wm[2]) * ph + gx * dph;
+                    h[1] += (hxy * wm[0] + hyy * wm[1] + hyz * wm[2]) * ph + gy * dph;
+                    h[2] += (hxz * wm[0] + hyz * wm[1] + hzz * wm[2]) * ph + gz * dph;
+                }
+            }
+        }
+        for (int d = 0; d < 3; ++d) hw[3 * m + d] += c * q * h[d];
+    }
+#undef ORC_WEIGHTS
+    for (int d = 0; d < 3; ++d) free(bm[d]);
+    free(A);
+    free(B);
+}
+
+/* Plain Ewald part: hw += H_k w.  E = C sum_m theta |S|^2, C = eps/(2 pi V),
+ * S = sum_j q_j e^{i ph_j}, ph_j = 2 pi m.x_j, dS = sum_j q_j (2 pi i m.w_j) e^{i ph_j}:
+ *   (H w)_i = -(2 eps/V) q_i sum_m theta m [Im(conj(dS) e^{i ph_i}) + 2 pi (m.w_i) Re(conj(S) e^{i ph_i})] */
+static void ewald_hvp(const orc_params *p, int nel, int nion, const double *x, int nmax2, const double *w,
+                      double *hw) {
+    const int n = nel + nion;
+    const double V = p->box[0] * p->box[1] * p->box[2];
+    const double s = p->charge_scale;
+    const int nm = (int)floor(sqrt((double)nmax2)), side = 2 * nm + 1;
+    for (int t = 0; t < side * side * side; ++t) {
+        int n1 = t % side - nm, n2 = (t / side) % side - nm, n3 = t / (side * side) - nm;
+        int nn = n1 * n1 + n2 * n2 + n3 * n3;
+        if (nn == 0 || nn > nmax2) continue;
+        double m[3] = {n1 / p->box[0], n2 / p->box[1], n3 / p->box[2]};
+        double m2 = m[0] * m[0] + m[1] * m[1] + m[2] * m[2];
+        double th = exp(-m2 * ORC_PI * ORC_PI / (p->a * p->a)) / m2;
+        double sr = 0.0, si = 0.0, dr = 0.0, di = 0.0;
+        for (int j = 0; j < n; ++j) {
+            double q = s * p->q[j < nel ? 0 : 1];
+            double ph = 2.0 * ORC_PI * (m[0] * x[3 * j] + m[1] * x[3 * j + 1] + m[2] * x[3 * j + 2]);
+            double mw = 2.0 * ORC_PI * (m[0] * w[3 * j] + m[1] * w[3 * j + 1] + m[2] * w[3 * j + 2]);
+            sr += q * cos(ph);
+            si += q * sin(ph);
+            dr += -q * mw * sin(ph);   /* i mw e^{i ph} = mw (-sin + i cos) */
+            di += q * mw * cos(ph);
+        }
+        for (int i = 0; i < n; ++i) {
+            double q = s * p->q[i < nel ? 0 : 1];
+            double ph = 2.0 * ORC_PI * (m[0] * x[3 * i] + m[1] * x[3 * i + 1] + m[2] * x[3 * i + 2]);
+            double mw = 2.0 * ORC_PI * (m[0] * w[3 * i] + m[1] * w[3 * i + 1] + m[2] * w[3 * i + 2]);
+            double cs = cos(ph), sn = sin(ph);
+            double im_d = dr * sn - di * cs;   /* Im(conj(dS) e^{i ph}) */
+            double re_s = sr * cs + si * sn;   /* Re(conj(S) e^{i ph}) */
+            double coef = -2.0 * ORC_EPS / V * q * th * (im_d + mw * re_s);
+            for (int k = 0; k < 3; ++k) hw[3 * i + k] += coef * m[k];
+        }
+    }
+}
+
+void orc_adjoint_energy(const orc_params *p, int nel, int nion, const double *x, double *dEdl, int nthreads) {
+    real_adjoint(p, nel, nion, x, NULL, NULL, dEdl, NULL, nthreads);
+}
+
+void orc_hvp(const orc_params *p, int nel, int nion, const double *x, const double *psi, int reciprocal, int nmax2,
+             const double *w, double *hw, double *dFdl_w, int nthreads) {
+    const int n = nel + nion;
+    memset(hw, 0, sizeof(double) * 3 * (size_t)n);
+    real_adjoint(p, nel, nion, x, w, hw, NULL, dFdl_w, nthreads);
+    if (reciprocal == 1) spme_hvp(p, nel, nion, x, psi, w, hw);
+    else if (reciprocal == 2) ewald_hvp(p, nel, nion, x, nmax2, w, hw);
+}
+
+static void project_mean(int n, double *g) {
+    orc_remove_rigidmtn(n, g);   /* the same projection as the force (force.f90:986-1004) */
+}
+
+/* J = (1/K) sum_{k=1..K} (mv2el_k + mv2ion_k)/(3N) over K NOTEMP steps of
+ * orc_md_step from (x0, v0) with f_0 = F(x_0), and dJ/dlambda by the discrete
+ * adjoint of that map.  Checkpoints (x_k, v_k) every M steps; each segment is
+ * recomputed forward and swept in reverse:
+ *   vb += 2 m v_k/(3NK);  g = fb + a vb;  xb -= H(x_k) P g;  lb += dF/dl(x_k) . P g
+ *   vb += dt xb;  fb = a vb                     (a = dt/(2m), P = mean removal)
+ * and finally lb += dF/dl(x_0) . P fb. */
+int orc_reverse_md(const orc_params *p, int nel, int nion, const double *x0, const double *v0, const double *psi,
+                   int reciprocal, int nmax2, double dt, int K, int M, double *J, double *dJdl, int nthreads) {
+    const int n = nel + nion;
+    const size_t sz = 3 * (size_t)n;
+    if (K <= 0 || M <= 0) return -1;
+    const int nck = (K + M - 1) / M;
+    double *ck = (double *)malloc(sizeof(double) * 2 * sz * nck);
+    double *seg = (double *)malloc(sizeof(double) * 2 * sz * (M + 1));
+    double *x = (double *)malloc(sizeof(double) * sz), *v = (double *)malloc(sizeof(double) * sz),
+           *f = (double *)malloc(sizeof(double) * sz);
+    double *xb = (double *)calloc(sz, sizeof(double)), *vb = (double *)calloc(sz, sizeof(double)),
+           *fb = (double *)calloc(sz, sizeof(double)), *g = (double *)malloc(sizeof(double) * sz),
+           *hw = (double *)malloc(sizeof(double) * sz);
+    double ur, um, e[5], jsum = 0.0, lb = 0.0, d;
+    memcpy(x, x0, sizeof(double) * sz);
+    memcpy(v, v0, sizeof(double) * sz);
+    orc_force_total(p, nel, nion, x, psi, reciprocal, nmax2, f, &ur, &um, NULL, nthreads);
+    for (int k = 0; k < K; ++k) {
+        if (k % M == 0) {
+            memcpy(ck + 2 * sz * (k / M), x, sizeof(double) * sz);
+            memcpy(ck + 2 * sz * (k / M) + sz, v, sizeof(double) * sz);
+        }
+        orc_md_step(p, ORC_NOTEMP, 0, nel, nion, dt, x, v, f, psi, 0.0, reciprocal, nmax2, e, NULL, NULL, nthreads);
+        jsum += e[3] + e[4];
+    }
+    *J = jsum / (3.0 * n * K);
+    for (int s = nck - 1; s >= 0; --s) {
+        const int k0 = s * M, k1 = (k0 + M < K) ? k0 + M : K;
+        memcpy(x, ck + 2 * sz * s, sizeof(double) * sz);
+        memcpy(v, ck + 2 * sz * s + sz, sizeof(double) * sz);
+        orc_force_total(p, nel, nion, x, psi, reciprocal, nmax2, f, &ur, &um, NULL, nthreads);
+        for (int k = k0 + 1; k <= k1; ++k) {
+            orc_md_step(p, ORC_NOTEMP, 0, nel, nion, dt, x, v, f, psi, 0.0, reciprocal, nmax2, e, NULL, NULL, nthreads);
+            memcpy(seg + 2 * sz * (k - k0), x, sizeof(double) * sz);
+            memcpy(seg + 2 * sz * (k - k0) + sz, v, sizeof(double) * sz);
+        }
+        for (int k = k1; k > k0; --k) {
+            const double *xk = seg + 2 * sz * (k - k0), *vk = xk + sz;
+            for (int i = 0; i < n; ++i) {
+                const double m = p->xm[i < nel ? 0 : 1], a = 0.5 * dt / m, cj = 2.0 * m / (3.0 * n * K);
+                for (int c = 0; c < 3; ++c) {
+                    vb[3 * i + c] += cj * vk[3 * i + c];
+                    g[3 * i + c] = fb[3 * i + c] + a * vb[3 * i + c];
+                }
+            }
+            project_mean(n, g);
+            orc_hvp(p, nel, nion, xk, psi, reciprocal, nmax2, g, hw, &d, nthreads);
+            lb += d;
+            for (int i = 0; i < n; ++i) {
+                const double a = 0.5 * dt / p->xm[i < nel ? 0 : 1];
+                for (int c = 0; c < 3; ++c) {
+                    xb[3 * i + c] -= hw[3 * i + c];
+                    vb[3 * i + c] += dt * xb[3 * i + c];
+                    fb[3 * i + c] = a * vb[3 * i + c];
+                }
+            }
+        }
+    }
+    memcpy(g, fb, sizeof(double) * sz);
+    project_mean(n, g);
+    real_adjoint(p, nel, nion, x0, g, NULL, NULL, &d, nthreads);
+    lb += d;
+    *dJdl = lb;
+    free(ck); free(seg); free(x); free(v); free(f); free(xb); free(vb); free(fb); free(g); free(hw);
+    return 0;
+}

@@ -149,6 +149,29 @@ int orc_md_step(const orc_params *p, int thermo, int apply_thermostat,
                 const double *psi, double Uo, int reciprocal, int nmax2,
                 double *energies, double *rdf, double *vdf, int nthreads);
 
+/* ---- derivatives (no reference counterpart: the reference computes none).
+ * Pinned by central finite differences of the routines above. ---- */
+
+/* dE/dlambda (eV/A) of the total potential energy: lambda = lambda_ei
+ * (Kelbg) or rs (Deutsch); only the e-i real-space term depends on it. */
+void orc_adjoint_energy(const orc_params *p, int nel, int nion, const double *x,
+                        double *dEdl, int nthreads);
+
+/* hw = H w, H = d^2 E / dx dx of the total potential energy (real space +
+ * reciprocal as in orc_force_total, without the mean-force removal);
+ * *dFdl_w = sum_i dF_i/dlambda . w_i (F = -grad E).  AoS [3N] arrays. */
+void orc_hvp(const orc_params *p, int nel, int nion, const double *x,
+             const double *psi, int reciprocal, int nmax2, const double *w,
+             double *hw, double *dFdl_w, int nthreads);
+
+/* Reverse mode through K NOTEMP steps of orc_md_step from (x0, v0), f_0 =
+ * F(x_0): J = mean over steps 1..K of (mv2el + mv2ion)/(3N) and dJ/dlambda,
+ * checkpoints every M steps with recomputation in between.  Returns 0. */
+int orc_reverse_md(const orc_params *p, int nel, int nion, const double *x0,
+                   const double *v0, const double *psi, int reciprocal,
+                   int nmax2, double dt, int K, int M, double *J, double *dJdl,
+                   int nthreads);
+
 int orc_max_threads(void);
 
 #ifdef __cplusplus

@@ -223,6 +223,27 @@ class Context:
         self._chk(self.lib.tcp_launch_count(self.h, C.byref(n)), "tcp_launch_count")
         return n.value
 
+    # ---- derivatives (tcp_adjoint_energy / tcp_hvp / tcp_reverse_md) ----
+    def adjoint_energy(self):
+        """(E, dE/dlambda, dE/ds) at the current positions (eV, eV/A, eV)."""
+        e, dl, ds = C.c_double(), C.c_double(), C.c_double()
+        self._chk(self.lib.tcp_adjoint_energy(self.h, C.byref(e), C.byref(dl), C.byref(ds)), "tcp_adjoint_energy")
+        return e.value, dl.value, ds.value
+
+    def hvp(self, w):
+        """(H w, dF/dlambda . w) for w of shape (N, 3)."""
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        hw = np.zeros_like(w)
+        d = C.c_double()
+        self._chk(self.lib.tcp_hvp(self.h, w.ctypes.data, hw.ctypes.data, C.byref(d)), "tcp_hvp")
+        return hw, d.value
+
+    def reverse_md(self, dt, nsteps, every):
+        """(J, dJ/dlambda): J = mean over nsteps NOTEMP steps of (mv2el+mv2ion)/(3N)."""
+        j, d = C.c_double(), C.c_double()
+        self._chk(self.lib.tcp_reverse_md(self.h, dt, nsteps, every, C.byref(j), C.byref(d)), "tcp_reverse_md")
+        return j.value, d.value
+
 
 class Batch:
     """Many independent systems stepped together (tcp_batch_* of the C ABI)."""

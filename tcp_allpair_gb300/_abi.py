@@ -82,6 +82,9 @@ SIGNATURES = {
     "tcp_autotune_report": (C.c_int, [_CTX, C.POINTER(C.c_int), _P, C.c_int]),
     "tcp_launch_count": (C.c_int, [_CTX, C.POINTER(C.c_longlong)]),
     "tcp_fp32_peak": (C.c_int, [C.c_int, _P]),
+    "tcp_adjoint_energy": (C.c_int, [_CTX, _P, _P, _P]),
+    "tcp_hvp": (C.c_int, [_CTX, C.c_void_p, C.c_void_p, _P]),
+    "tcp_reverse_md": (C.c_int, [_CTX, C.c_double, C.c_int, C.c_int, _P, _P]),
     "tcp_batch_create": (C.c_int, [C.POINTER(TcpParams), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int,
                                    C.POINTER(C.c_void_p)]),
     "tcp_batch_destroy": (C.c_int, [C.c_void_p]),

@@ -1,0 +1,620 @@
+// adjoint.cu -- derivatives of the force-and-integrate path: dE/dlambda_ei,
+// dE/d(charge scale), Hessian-vector products of the potential energy, and
+// reverse mode of the mean kinetic temperature through K velocity-Verlet
+// steps with checkpoints every M steps and recomputation in between.
+//
+// The reference computes no derivatives.  These are the analytic derivatives
+// of the energy it defines (force.f90 pair terms :99-175, SPME :652-929,
+// EWALD_SELF :44-45) and of its discrete NOTEMP step (vverlet.f90:132-223 with
+// REMOVE_RIGIDMTN, force.f90:986-1004), for the same parameters.
+//
+// Pair terms.  For a pair term phi(r) (u = x_i - x_j, qq = eps q_i q_j):
+//   G1 = -phi'(r)/r            force on i: qq G1 u
+//   G2 = -G1'(r)/r             pair Hessian: qq (-G1 I + G2 u u^T)
+//   dl = d phi / d lambda,  gl = d G1 / d lambda
+// with lambda = lambda_ei (Kelbg) or rs (Deutsch); only the e-i term depends
+// on it.  For erfc(ar)/r, w0 = (erfc(ar)/r + c e)/r^2, c = 2a/sqrt(pi),
+// e = exp(-a^2 r^2): G1 = w0, G2 = (3 w0 + 2 a^2 c e)/r^2.  Kelbg adds
+// G1 -= g/r^3, G2 -= g (3/r^3 + 2/(l^2 r))/r^2, dl = -sqrt(pi) erfc(r/l)/l^2,
+// gl = -2 g/(l^3 r), g = exp(-r^2/l^2).  Deutsch adds G1 -= y (1/(rs r^2) +
+// 1/r^3), G2 -= y (3/(rs r^2) + 3/r^3 + 1/(rs^2 r))/r^2, dl = -y/rs^2,
+// gl = -y/(rs^3 r), y = exp(-r/rs).
+//
+// The real-space kernel visits every ordered pair (i, j) once: thread i sums
+// (H w)_i = sum_j qq (-G1 dw + G2 (u.dw) u), dw = w_i - w_j, and the scalars
+// dE/dlambda = 1/2 sum qq dl and dF/dlambda . w = sum qq gl (u.w_i).  The
+// j-range is split over gridDim.y; rows are added to hw with FP64 atomics.
+// FP64 precision uses CUDA's erfc/exp; FP32C uses the fixed-point separations
+// and the SFU forms of the force kernel, per-tile FP32 partials and FP64 sums.
+// The reciprocal part (spme.cu) is always FP64.
+#include <algorithm>
+#include <cmath>
+#include <type_traits>
+#include <vector>
+
+#include "device_util.cuh"
+#include "pair_math.cuh"
+#include "tcp_internal.h"
+
+namespace tcp {
+
+constexpr int kAdjThreads = 128;
+enum { kAdjDEdl = 0, kAdjDFdl = 1, kAdjJ = 2, kAdjCount = 8 };
+
+struct AdjArgs {
+    const int4 *xq;
+    const double4_32a *xd;
+    const double *w;      // [3][n] (HVP) or nullptr
+    double *hw;           // [3][n], atomic adds
+    double *scal;         // kAdj*
+    int nel, n, jchunk;
+    PairConsts c;
+    double c2a, k_l2, k_dl, k_gl, inv_rs2, inv_rs3;        // see radial_f64
+    float c2a_f, k_l2_f, k_dl_f, k_gl_f, inv_rs2_f, inv_rs3_f;
+};
+
+template <int KIND>
+__device__ __forceinline__ void radial_f64(const AdjArgs &a, double r2, double &G1, double &G2, double &dl,
+                                           double &gl) {
+    const double r = sqrt(r2), rinv = 1.0 / r, rinv2 = rinv * rinv;
+    const double al = a.c.alpha;
+    const double e = exp(-al * al * r2);
+    const double w0 = (erfc(al * r) * rinv + (2.0 * al / kSqrtPi) * e) * rinv2;
+    G1 = w0;
+    G2 = (3.0 * w0 + a.c2a * e) * rinv2;
+    dl = 0.0;
+    gl = 0.0;
+    if (KIND == 1) {
+        const double irs = 1.0 / a.c.rs, y = exp(-r * irs);
+        G1 -= y * (irs + rinv) * rinv2;
+        G2 -= y * (3.0 * irs * rinv2 + 3.0 * rinv2 * rinv + a.inv_rs2 * rinv) * rinv2;
+        dl = -y * a.inv_rs2;
+        gl = -y * a.inv_rs3 * rinv;
+    } else if (KIND == 2) {
+        const double l = a.c.lambda, g = exp(-r2 / (l * l));
+        G1 -= g * rinv2 * rinv;
+        G2 -= g * (3.0 * rinv2 * rinv + a.k_l2 * rinv) * rinv2;
+        dl = -a.k_dl * erfc(r / l);
+        gl = -a.k_gl * g * rinv;
+    }
+}
+
+template <int KIND>
+__device__ __forceinline__ void radial_f32(const AdjArgs &a, float r2, float &G1, float &G2, float &dl, float &gl) {
+    const PairConsts &c = a.c;
+    const float rinv = rsqrt_approx(r2), r = r2 * rinv, rinv2 = rinv * rinv;
+    const float t = rcp_approx(fmaf(c.p_alpha, r, 1.0f));
+    const float e = ex2_approx(c.c_exp * r2);
+    const float w0 = fmaf(c.c_gauss, e, e * erfc_poly(t) * rinv) * rinv2;
+    G1 = w0;
+    G2 = fmaf(3.0f, w0, a.c2a_f * e) * rinv2;
+    dl = 0.0f;
+    gl = 0.0f;
+    if (KIND == 1) {
+        const float y = ex2_approx(c.c_rs * r);
+        G1 -= y * (c.inv_rs + rinv) * rinv2;
+        G2 -= y * (3.0f * c.inv_rs * rinv2 + 3.0f * rinv2 * rinv + a.inv_rs2_f * rinv) * rinv2;
+        dl = -y * a.inv_rs2_f;
+        gl = -y * a.inv_rs3_f * rinv;
+    } else if (KIND == 2) {
+        const float g = ex2_approx(c.c_lam * r2);
+        G1 -= g * rinv2 * rinv;
+        G2 -= g * (3.0f * rinv2 * rinv + a.k_l2_f * rinv) * rinv2;
+        const float t2 = rcp_approx(fmaf(c.p_lam, r, 1.0f));
+        dl = -a.k_dl_f * (g * erfc_poly(t2));
+        gl = -a.k_gl_f * g * rinv;
+    }
+}
+
+template <bool F32, int EIK, bool HVP>
+__global__ void __launch_bounds__(kAdjThreads) adj_pair_kernel(const AdjArgs a) {
+    using T = typename std::conditional<F32, float, double>::type;
+    __shared__ double sw[3][HVP ? kAdjThreads : 1];
+    __shared__ int4 sxq[F32 ? kAdjThreads : 1];
+    __shared__ double4_32a sxd[F32 ? 1 : kAdjThreads];
+    __shared__ double red[32];
+    const int tid = threadIdx.x;
+    const int i = blockIdx.x * kAdjThreads + tid;
+    const bool vi = i < a.n;
+    const int ii = vi ? i : 0;
+    const int si = ii < a.nel ? 0 : 1;
+    int4 xqi = make_int4(0, 0, 0, 0);
+    double4_32a xdi = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+    if (F32) xqi = a.xq[ii];
+    else xdi = a.xd[ii];
+    double wi0 = 0.0, wi1 = 0.0, wi2 = 0.0;
+    if (HVP) {
+        wi0 = a.w[ii];
+        wi1 = a.w[(size_t)a.n + ii];
+        wi2 = a.w[2 * (size_t)a.n + ii];
+    }
+    const int j0 = blockIdx.y * a.jchunk, j1 = min(a.n, j0 + a.jchunk);
+    double h0 = 0.0, h1 = 0.0, h2 = 0.0, el = 0.0, fl = 0.0;
+    for (int jt = j0; jt < j1; jt += kAdjThreads) {
+        __syncthreads();
+        const int jj = jt + tid;
+        if (jj < j1) {
+            if (F32) sxq[tid] = a.xq[jj];
+            else sxd[tid] = a.xd[jj];
+            if (HVP) {
+                sw[0][tid] = a.w[jj];
+                sw[1][tid] = a.w[(size_t)a.n + jj];
+                sw[2][tid] = a.w[2 * (size_t)a.n + jj];
+            }
+        }
+        __syncthreads();
+        if (!vi) continue;
+        const int cnt = min(kAdjThreads, j1 - jt);
+        T t0 = 0, t1 = 0, t2 = 0, te = 0, tf = 0;
+        for (int k = 0; k < cnt; ++k) {
+            const int j = jt + k;
+            if (j == i) continue;
+            const int type = si + (j < a.nel ? 0 : 1);
+            T u0, u1, u2;
+            if (F32) {
+                const int4 xj = sxq[k];
+                // wrapping int32 difference = minimum image in 2^-32 box units
+                u0 = (T)(float)(int)((unsigned)xqi.x - (unsigned)xj.x) * (T)a.c.sx;
+                u1 = (T)(float)(int)((unsigned)xqi.y - (unsigned)xj.y) * (T)a.c.sy;
+                u2 = (T)(float)(int)((unsigned)xqi.z - (unsigned)xj.z) * (T)a.c.sz;
+            } else {
+                const double4_32a xj = sxd[k];
+                double d0 = xdi.x - xj.x, d1 = xdi.y - xj.y, d2 = xdi.z - xj.z;
+                d0 -= a.c.box[0] * round(d0 / a.c.box[0]);
+                d1 -= a.c.box[1] * round(d1 / a.c.box[1]);
+                d2 -= a.c.box[2] * round(d2 / a.c.box[2]);
+                u0 = (T)d0;
+                u1 = (T)d1;
+                u2 = (T)d2;
+            }
+            const T r2 = u0 * u0 + u1 * u1 + u2 * u2;
+            if (!(r2 < (F32 ? (T)a.c.rc2f : (T)a.c.rc2))) continue;
+            T G1, G2, dl, gl;
+            if (F32) {
+                float g1, g2, d, g;
+                if (type == 1 && EIK == 1) radial_f32<1>(a, (float)r2, g1, g2, d, g);
+                else if (type == 1 && EIK == 2) radial_f32<2>(a, (float)r2, g1, g2, d, g);
+                else radial_f32<0>(a, (float)r2, g1, g2, d, g);
+                G1 = g1; G2 = g2; dl = d; gl = g;
+            } else {
+                double g1, g2, d, g;
+                if (type == 1 && EIK == 1) radial_f64<1>(a, (double)r2, g1, g2, d, g);
+                else if (type == 1 && EIK == 2) radial_f64<2>(a, (double)r2, g1, g2, d, g);
+                else radial_f64<0>(a, (double)r2, g1, g2, d, g);
+                G1 = g1; G2 = g2; dl = d; gl = g;
+            }
+            const T qq = F32 ? (T)(a.c.qqf[type] * (float)kEps) : (T)(a.c.qq[type] * kEps);
+            te += qq * dl;
+            if (HVP) {
+                const T dw0 = (T)(wi0 - sw[0][k]), dw1 = (T)(wi1 - sw[1][k]), dw2 = (T)(wi2 - sw[2][k]);
+                const T ud = u0 * dw0 + u1 * dw1 + u2 * dw2;
+                const T a1 = -qq * G1, a2 = qq * G2 * ud;
+                t0 += a1 * dw0 + a2 * u0;
+                t1 += a1 * dw1 + a2 * u1;
+                t2 += a1 * dw2 + a2 * u2;
+                tf += qq * gl * (u0 * (T)wi0 + u1 * (T)wi1 + u2 * (T)wi2);
+            }
+        }
+        h0 += (double)t0;
+        h1 += (double)t1;
+        h2 += (double)t2;
+        el += (double)te;
+        fl += (double)tf;
+    }
+    if (HVP && vi) {
+        atomicAdd(a.hw + i, h0);
+        atomicAdd(a.hw + (size_t)a.n + i, h1);
+        atomicAdd(a.hw + 2 * (size_t)a.n + i, h2);
+    }
+    el = block_sum(el, red);
+    fl = block_sum(fl, red);
+    if (tid == 0) {
+        atomicAdd(a.scal + kAdjDEdl, 0.5 * el);
+        if (HVP) atomicAdd(a.scal + kAdjDFdl, fl);
+    }
+}
+
+// ---- host-layout transposes ---------------------------------------------------
+__global__ void aos_to_soa_kernel(const double *__restrict__ in, double *__restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int d = 0; d < 3; ++d) out[(size_t)d * n + i] = in[3 * (size_t)i + d];
+}
+
+__global__ void soa_to_aos_kernel(const double *__restrict__ in, double *__restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int d = 0; d < 3; ++d) out[3 * (size_t)i + d] = in[(size_t)d * n + i];
+}
+
+// ---- reverse-mode step kernels ------------------------------------------------
+struct RevArgs {
+    const double *v;      // v_k [3][n]
+    double *xb, *vb, *fb, *g, *part;
+    const double *hw;
+    int nel, n;
+    double a0, a1;        // dt/(2 m) per species
+    double cj0, cj1;      // 2 m/(3 N K) per species
+    double dt;
+};
+
+// step k >= 1: vb += 2 m v_k/(3NK), g = fb + a vb (the two uses of F_k);
+// k = 0 (initial_only): g = fb.  Per-block sums of g for the mean.
+__global__ void rev_seed_kernel(const RevArgs r, bool initial_only) {
+    __shared__ double red[32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double s[3] = {0.0, 0.0, 0.0};
+    if (i < r.n) {
+        const bool el = i < r.nel;
+        const double a = el ? r.a0 : r.a1, cj = el ? r.cj0 : r.cj1;
+        for (int d = 0; d < 3; ++d) {
+            const size_t k = (size_t)d * r.n + i;
+            if (initial_only) {
+                s[d] = r.fb[k];
+            } else {
+                const double vb = r.vb[k] + cj * r.v[k];
+                r.vb[k] = vb;
+                s[d] = r.fb[k] + a * vb;
+            }
+            r.g[k] = s[d];
+        }
+    }
+    for (int d = 0; d < 3; ++d) {
+        const double t = block_sum(s[d], red);
+        if (threadIdx.x == 0) r.part[3 * blockIdx.x + d] = t;
+    }
+}
+
+// g -= mean(g) (REMOVE_RIGIDMTN applied to the adjoint, force.f90:986-1004);
+// every block sums the per-block partials in the same order.
+__global__ void rev_center_kernel(const RevArgs r, int nparts) {
+    __shared__ double mean[3];
+    __shared__ double red[32];
+    for (int d = 0; d < 3; ++d) {
+        double s = 0.0;
+        for (int b = threadIdx.x; b < nparts; b += blockDim.x) s += r.part[3 * b + d];
+        s = block_sum(s, red);
+        if (threadIdx.x == 0) mean[d] = s / (double)r.n;
+    }
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= r.n) return;
+    for (int d = 0; d < 3; ++d) r.g[(size_t)d * r.n + i] -= mean[d];
+}
+
+// xb -= H P g;  vb += dt xb;  fb = a vb
+__global__ void rev_update_kernel(const RevArgs r) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= r.n) return;
+    const double a = i < r.nel ? r.a0 : r.a1;
+    for (int d = 0; d < 3; ++d) {
+        const size_t k = (size_t)d * r.n + i;
+        const double xb = r.xb[k] - r.hw[k];
+        const double vb = r.vb[k] + r.dt * xb;
+        r.xb[k] = xb;
+        r.vb[k] = vb;
+        r.fb[k] = a * vb;
+    }
+}
+
+// J accumulator: scal[kAdjJ] += mv2el + mv2ion of the step just taken
+__global__ void rev_accum_kernel(const double *__restrict__ scal, double *__restrict__ adj) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) adj[kAdjJ] += scal[kScalMv2e] + scal[kScalMv2i];
+}
+
+// ---- host side -------------------------------------------------------------------
+constexpr int kRevThreads = 256;
+static int rev_blocks(int n) { return (n + kRevThreads - 1) / kRevThreads; }
+
+void adjoint_free(tcp_ctx *c) {
+    double **bufs[] = {&c->adj_w, &c->adj_hw, &c->adj_xb, &c->adj_vb, &c->adj_fb, &c->adj_save,
+                       &c->adj_io, &c->adj_scal, &c->adj_part, &c->adj_ck, &c->adj_seg};
+    for (double **b : bufs) {
+        cudaFree(*b);
+        *b = nullptr;
+    }
+    c->adj_ck_cap = 0;
+    c->adj_seg_cap = 0;
+}
+
+static int adj_alloc(tcp_ctx *c) {
+    if (c->adj_w) return TCP_OK;
+    const size_t v3 = sizeof(double) * 3 * (size_t)c->n;
+    if (cudaMalloc(&c->adj_w, v3) != cudaSuccess || cudaMalloc(&c->adj_hw, v3) != cudaSuccess ||
+        cudaMalloc(&c->adj_xb, v3) != cudaSuccess || cudaMalloc(&c->adj_vb, v3) != cudaSuccess ||
+        cudaMalloc(&c->adj_fb, v3) != cudaSuccess || cudaMalloc(&c->adj_save, 3 * v3) != cudaSuccess ||
+        cudaMalloc(&c->adj_io, v3) != cudaSuccess ||
+        cudaMalloc(&c->adj_scal, sizeof(double) * kAdjCount) != cudaSuccess ||
+        cudaMalloc(&c->adj_part, sizeof(double) * 3 * (size_t)rev_blocks(c->n)) != cudaSuccess) {
+        adjoint_free(c);
+        return set_error(TCP_ERR_NOMEM, "derivative buffers: device allocation failed");
+    }
+    return TCP_OK;
+}
+
+static AdjArgs adj_args(tcp_ctx *c, const double *w, double *hw) {
+    AdjArgs a;
+    a.xq = c->xq;
+    a.xd = c->xd;
+    a.w = w;
+    a.hw = hw;
+    a.scal = c->adj_scal;
+    a.nel = c->nel;
+    a.n = c->n;
+    a.c = c->pc;
+    const double al = c->alpha, l = c->pc.lambda, rs = c->pc.rs;
+    a.c2a = 2.0 * al * al * (2.0 * al / kSqrtPi);
+    a.k_l2 = 2.0 / (l * l);
+    a.k_dl = kSqrtPi / (l * l);
+    a.k_gl = 2.0 / (l * l * l);
+    a.inv_rs2 = 1.0 / (rs * rs);
+    a.inv_rs3 = 1.0 / (rs * rs * rs);
+    a.c2a_f = (float)a.c2a;
+    a.k_l2_f = (float)a.k_l2;
+    a.k_dl_f = (float)a.k_dl;
+    a.k_gl_f = (float)a.k_gl;
+    a.inv_rs2_f = (float)a.inv_rs2;
+    a.inv_rs3_f = (float)a.inv_rs3;
+    // j-split so that the grid covers about four CTAs per SM
+    const int bx = (c->n + kAdjThreads - 1) / kAdjThreads;
+    int ny = std::max(1, std::min(bx, (4 * c->num_sms + bx - 1) / bx));
+    const int chunk = ((c->n + ny - 1) / ny + kAdjThreads - 1) / kAdjThreads * kAdjThreads;
+    a.jchunk = chunk;
+    return a;
+}
+
+// Real-space part: hw += H_real w (when w), scalars into adj_scal.
+static int launch_adj_pair(tcp_ctx *c, const double *w, double *hw) {
+    AdjArgs a = adj_args(c, w, hw);
+    const int bx = (c->n + kAdjThreads - 1) / kAdjThreads;
+    const int by = (c->n + a.jchunk - 1) / a.jchunk;
+    const dim3 grid(bx, by);
+    const bool f32 = c->p.precision == TCP_PREC_FP32C;
+    const int eik = c->p.ei_model == TCP_EI_DEUTSCH ? 1 : (c->p.ei_model == TCP_EI_KELBG ? 2 : 0);
+#define ADJ_LAUNCH(F, E, H) adj_pair_kernel<F, E, H><<<grid, kAdjThreads, 0, c->stream>>>(a)
+    if (w) {
+        if (f32) {
+            if (eik == 1) ADJ_LAUNCH(true, 1, true);
+            else if (eik == 2) ADJ_LAUNCH(true, 2, true);
+            else ADJ_LAUNCH(true, 0, true);
+        } else {
+            if (eik == 1) ADJ_LAUNCH(false, 1, true);
+            else if (eik == 2) ADJ_LAUNCH(false, 2, true);
+            else ADJ_LAUNCH(false, 0, true);
+        }
+    } else {
+        if (f32) {
+            if (eik == 1) ADJ_LAUNCH(true, 1, false);
+            else if (eik == 2) ADJ_LAUNCH(true, 2, false);
+            else ADJ_LAUNCH(true, 0, false);
+        } else {
+            if (eik == 1) ADJ_LAUNCH(false, 1, false);
+            else if (eik == 2) ADJ_LAUNCH(false, 2, false);
+            else ADJ_LAUNCH(false, 0, false);
+        }
+    }
+#undef ADJ_LAUNCH
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+// hw = H w at the current positions (device SoA), scal[kAdjDFdl] += dF/dl . w
+static int hvp_device(tcp_ctx *c, const double *w, double *hw) {
+    int rc;
+    TCP_CUDA(cudaMemsetAsync(hw, 0, sizeof(double) * 3 * (size_t)c->n, c->stream));
+    if ((rc = launch_adj_pair(c, w, hw))) return rc;
+    if (c->p.reciprocal == TCP_RECIP_SPME) return launch_spme_hvp(c, w, hw);
+    if (c->p.reciprocal == TCP_RECIP_EWALD) return launch_ewald_hvp(c, w, hw);
+    return TCP_OK;
+}
+
+static int read_adj(tcp_ctx *c, double *out, int count) {
+    TCP_CUDA(cudaMemcpyAsync(out, c->adj_scal, sizeof(double) * count, cudaMemcpyDeviceToHost, c->stream));
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    return TCP_OK;
+}
+
+static RevArgs rev_args(tcp_ctx *c, const double *v, double dt, int K) {
+    RevArgs r;
+    r.v = v;
+    r.xb = c->adj_xb;
+    r.vb = c->adj_vb;
+    r.fb = c->adj_fb;
+    r.g = c->adj_w;
+    r.part = c->adj_part;
+    r.hw = c->adj_hw;
+    r.nel = c->nel;
+    r.n = c->n;
+    r.a0 = 0.5 * dt / c->p.xm[0];
+    r.a1 = 0.5 * dt / c->p.xm[1];
+    r.cj0 = 2.0 * c->p.xm[0] / (3.0 * c->n * (double)K);
+    r.cj1 = 2.0 * c->p.xm[1] / (3.0 * c->n * (double)K);
+    r.dt = dt;
+    return r;
+}
+
+// g (adj_w) = P (fb + a vb) for a step k >= 1, P fb for k = 0
+static int rev_seed(tcp_ctx *c, const RevArgs &r, bool initial_only) {
+    const int nb = rev_blocks(c->n);
+    rev_seed_kernel<<<nb, kRevThreads, 0, c->stream>>>(r, initial_only);
+    rev_center_kernel<<<nb, kRevThreads, 0, c->stream>>>(r, nb);
+    c->launches += 2;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+static int copy_state(tcp_ctx *c, double *dst_x, double *dst_v, const double *src_x, const double *src_v) {
+    const size_t b = sizeof(double) * 3 * (size_t)c->n;
+    if (dst_x) TCP_CUDA(cudaMemcpyAsync(dst_x, src_x, b, cudaMemcpyDeviceToDevice, c->stream));
+    if (dst_v) TCP_CUDA(cudaMemcpyAsync(dst_v, src_v, b, cudaMemcpyDeviceToDevice, c->stream));
+    return TCP_OK;
+}
+
+}  // namespace tcp
+
+using namespace tcp;
+
+#define TCP_ADJ_READY(c)                                                                           \
+    do {                                                                                           \
+        if (!(c)) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");                             \
+        if (!(c)->ewald_ready) return set_error(TCP_ERR_STATE, "tcp_ewald_self must be called first"); \
+        cudaSetDevice((c)->device);                                                                \
+        int _rc = adj_alloc(c);                                                                    \
+        if (_rc) return _rc;                                                                       \
+    } while (0)
+
+extern "C" {
+
+int tcp_adjoint_energy(tcp_ctx *c, double *E, double *dE_dlambda, double *dE_dscale) {
+    TCP_ADJ_READY(c);
+    int rc;
+    const size_t b = sizeof(double) * 3 * (size_t)c->n;
+    // the stored forces are state (Finit's f belongs to x - dt v): keep them
+    TCP_CUDA(cudaMemcpyAsync(c->adj_save, c->f, b, cudaMemcpyDeviceToDevice, c->stream));
+    TCP_CUDA(cudaMemcpyAsync(c->adj_save + 3 * (size_t)c->n, c->frec, b, cudaMemcpyDeviceToDevice, c->stream));
+    const unsigned flags = c->flags;
+    c->flags = (flags | TCP_FLAG_ENERGY) & ~(unsigned)TCP_FLAG_RDF;
+    if ((rc = autotune_pair(c))) {
+        c->flags = flags;
+        return rc;
+    }
+    rc = force_eval(c, true);
+    c->flags = flags;
+    if (rc) return rc;
+    TCP_CUDA(cudaMemcpyAsync(c->f, c->adj_save, b, cudaMemcpyDeviceToDevice, c->stream));
+    TCP_CUDA(cudaMemcpyAsync(c->frec, c->adj_save + 3 * (size_t)c->n, b, cudaMemcpyDeviceToDevice, c->stream));
+    TCP_CUDA(cudaMemsetAsync(c->adj_scal, 0, sizeof(double) * kAdjCount, c->stream));
+    if ((rc = launch_adj_pair(c, nullptr, nullptr))) return rc;
+    if ((rc = md_finish(c))) return rc;
+    double s[kAdjCount];
+    if ((rc = read_adj(c, s, kAdjCount))) return rc;
+    const double e = c->last.Epot + c->last.Um;
+    if (E) *E = e;
+    if (dE_dlambda) *dE_dlambda = c->p.ei_model == TCP_EI_COULOMB ? 0.0 : s[kAdjDEdl];
+    // every term (pair, mesh, self) is quadratic in the charge scale s
+    if (dE_dscale) *dE_dscale = 2.0 * e / c->p.charge_scale;
+    return TCP_OK;
+}
+
+int tcp_hvp(tcp_ctx *c, const double *w, double *hw, double *dF_dlambda_w) {
+    TCP_ADJ_READY(c);
+    if (!w || !hw) return set_error(TCP_ERR_BAD_PARAM, "w and hw must not be NULL");
+    int rc;
+    const size_t b = sizeof(double) * 3 * (size_t)c->n;
+    const int nb = rev_blocks(c->n);
+    TCP_CUDA(cudaMemcpyAsync(c->adj_io, w, b, cudaMemcpyHostToDevice, c->stream));
+    aos_to_soa_kernel<<<nb, kRevThreads, 0, c->stream>>>(c->adj_io, c->adj_w, c->n);
+    TCP_CUDA(cudaMemsetAsync(c->adj_scal, 0, sizeof(double) * kAdjCount, c->stream));
+    if ((rc = hvp_device(c, c->adj_w, c->adj_hw))) return rc;
+    soa_to_aos_kernel<<<nb, kRevThreads, 0, c->stream>>>(c->adj_hw, c->adj_io, c->n);
+    c->launches += 2;
+    TCP_CUDA(cudaGetLastError());
+    TCP_CUDA(cudaMemcpyAsync(hw, c->adj_io, b, cudaMemcpyDeviceToHost, c->stream));
+    double s[kAdjCount];
+    if ((rc = read_adj(c, s, kAdjCount))) return rc;
+    if (dF_dlambda_w) *dF_dlambda_w = c->p.ei_model == TCP_EI_COULOMB ? 0.0 : s[kAdjDFdl];
+    return TCP_OK;
+}
+
+int tcp_reverse_md(tcp_ctx *c, double dt, int nsteps, int every, double *J, double *dJ_dlambda) {
+    TCP_ADJ_READY(c);
+    if (nsteps <= 0 || every <= 0) return set_error(TCP_ERR_BAD_PARAM, "nsteps and every must be positive");
+    if (c->p.thermo != TCP_THERMO_NOTEMP)
+        return set_error(TCP_ERR_BAD_PARAM, "reverse mode covers the NOTEMP step only");
+    int rc;
+    const int K = nsteps, M = std::min(every, nsteps);
+    const int nck = (K + M - 1) / M;
+    const size_t n3 = 3 * (size_t)c->n, b = sizeof(double) * n3;
+    if (c->adj_ck_cap < nck) {
+        cudaFree(c->adj_ck);
+        c->adj_ck = nullptr;
+        c->adj_ck_cap = 0;
+        TCP_CUDA(cudaMalloc(&c->adj_ck, 2 * b * (size_t)nck));
+        c->adj_ck_cap = nck;
+    }
+    if (c->adj_seg_cap < M + 1) {
+        cudaFree(c->adj_seg);
+        c->adj_seg = nullptr;
+        c->adj_seg_cap = 0;
+        TCP_CUDA(cudaMalloc(&c->adj_seg, 2 * b * (size_t)(M + 1)));
+        c->adj_seg_cap = M + 1;
+    }
+    if ((rc = autotune_pair(c))) return rc;
+    const long long step0 = c->step_index;
+    TCP_CUDA(cudaMemsetAsync(c->adj_scal, 0, sizeof(double) * kAdjCount, c->stream));
+    // forward: f_0 = F(x_0; lambda), then K steps with checkpoints
+    if ((rc = force_eval(c, true))) return rc;
+    for (int k = 0; k < K; ++k) {
+        if (k % M == 0 && (rc = copy_state(c, c->adj_ck + 2 * n3 * (k / M), c->adj_ck + 2 * n3 * (k / M) + n3, c->x, c->v)))
+            return rc;
+        if ((rc = md_advance(c, dt, 1))) return rc;
+        rev_accum_kernel<<<1, 32, 0, c->stream>>>(c->scal, c->adj_scal);
+        c->launches++;
+    }
+    if ((rc = md_finish(c))) return rc;           // energies of step K, as tcp_md_steps
+    const tcp_energies last = c->last;
+    // final state, restored after the sweep
+    if ((rc = copy_state(c, c->adj_save, c->adj_save + n3, c->x, c->v))) return rc;
+    TCP_CUDA(cudaMemcpyAsync(c->adj_save + 2 * n3, c->f, b, cudaMemcpyDeviceToDevice, c->stream));
+    // scalars and histograms as after step K (the recomputation steps repeat them)
+    double scal_save[kScalCount];
+    std::vector<unsigned long long> hist(5 * kNbin);
+    TCP_CUDA(cudaMemcpyAsync(scal_save, c->scal, sizeof(scal_save), cudaMemcpyDeviceToHost, c->stream));
+    TCP_CUDA(cudaMemcpyAsync(hist.data(), c->rdf, sizeof(unsigned long long) * 3 * kNbin, cudaMemcpyDeviceToHost, c->stream));
+    TCP_CUDA(cudaMemcpyAsync(hist.data() + 3 * kNbin, c->vdf, sizeof(unsigned long long) * 2 * kNbin,
+                             cudaMemcpyDeviceToHost, c->stream));
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    // reverse sweep
+    TCP_CUDA(cudaMemsetAsync(c->adj_xb, 0, b, c->stream));
+    TCP_CUDA(cudaMemsetAsync(c->adj_vb, 0, b, c->stream));
+    TCP_CUDA(cudaMemsetAsync(c->adj_fb, 0, b, c->stream));
+    for (int s = nck - 1; s >= 0; --s) {
+        const int k0 = s * M, k1 = std::min(k0 + M, K);
+        if ((rc = copy_state(c, c->x, c->v, c->adj_ck + 2 * n3 * s, c->adj_ck + 2 * n3 * s + n3))) return rc;
+        if ((rc = launch_refresh_positions(c))) return rc;
+        if ((rc = force_eval(c, true))) return rc;
+        for (int k = k0 + 1; k <= k1; ++k) {
+            if ((rc = md_advance(c, dt, 1))) return rc;
+            if ((rc = copy_state(c, c->adj_seg + 2 * n3 * (k - k0), c->adj_seg + 2 * n3 * (k - k0) + n3, c->x, c->v)))
+                return rc;
+        }
+        for (int k = k1; k > k0; --k) {
+            const double *xk = c->adj_seg + 2 * n3 * (k - k0), *vk = xk + n3;
+            if ((rc = copy_state(c, c->x, nullptr, xk, nullptr))) return rc;
+            if ((rc = launch_refresh_positions(c))) return rc;
+            const RevArgs r = rev_args(c, vk, dt, K);
+            if ((rc = rev_seed(c, r, false))) return rc;
+            if ((rc = hvp_device(c, c->adj_w, c->adj_hw))) return rc;   // scal[kAdjDFdl] accumulates dJ/dlambda
+            rev_update_kernel<<<rev_blocks(c->n), kRevThreads, 0, c->stream>>>(r);
+            c->launches++;
+            TCP_CUDA(cudaGetLastError());
+        }
+    }
+    // f_0 = F(x_0; lambda): the lambda term only
+    if ((rc = copy_state(c, c->x, nullptr, c->adj_ck, nullptr))) return rc;
+    if ((rc = launch_refresh_positions(c))) return rc;
+    {
+        const RevArgs r = rev_args(c, c->v, dt, K);
+        if ((rc = rev_seed(c, r, true))) return rc;
+        if ((rc = launch_adj_pair(c, c->adj_w, c->adj_hw))) return rc;
+    }
+    double sres[kAdjCount];
+    if ((rc = read_adj(c, sres, kAdjCount))) return rc;
+    // restore the state after step K
+    if ((rc = copy_state(c, c->x, c->v, c->adj_save, c->adj_save + n3))) return rc;
+    TCP_CUDA(cudaMemcpyAsync(c->f, c->adj_save + 2 * n3, b, cudaMemcpyDeviceToDevice, c->stream));
+    TCP_CUDA(cudaMemcpyAsync(c->scal, scal_save, sizeof(scal_save), cudaMemcpyHostToDevice, c->stream));
+    TCP_CUDA(cudaMemcpyAsync(c->rdf, hist.data(), sizeof(unsigned long long) * 3 * kNbin, cudaMemcpyHostToDevice, c->stream));
+    TCP_CUDA(cudaMemcpyAsync(c->vdf, hist.data() + 3 * kNbin, sizeof(unsigned long long) * 2 * kNbin,
+                             cudaMemcpyHostToDevice, c->stream));
+    if ((rc = launch_refresh_positions(c))) return rc;
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    c->step_index = step0 + K;
+    c->last = last;
+    if (J) *J = sres[kAdjJ] / (3.0 * c->n * (double)K);
+    if (dJ_dlambda) *dJ_dlambda = c->p.ei_model == TCP_EI_COULOMB ? 0.0 : sres[kAdjDFdl];
+    return TCP_OK;
+}
+
+}  // extern "C"

@@ -149,6 +149,18 @@ static int step_chain(tcp_ctx *c, double dt, bool apply, int *pass) {
     return TCP_OK;
 }
 
+// ---- composition used by the derivative routines (adjoint.cu) ----------------
+int force_eval(tcp_ctx *c, bool remove_net) { return force_chain(c, remove_net); }
+
+int md_finish(tcp_ctx *c) {
+    int rc;
+    if ((rc = sync_scalars(c))) return rc;
+    fill_energies(c, nullptr);
+    c->last.mv2el = c->h_scal[kScalMv2e];
+    c->last.mv2ion = c->h_scal[kScalMv2i];
+    return TCP_OK;
+}
+
 }  // namespace tcp
 
 using namespace tcp;
@@ -252,6 +264,8 @@ int tcp_destroy(tcp_ctx *c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     invalidate_graph(c);
+    adjoint_free(c);
+    spme_hvp_free(c);
     spme_free(c);
     cudaFree(c->x);
     cudaFree(c->v);
@@ -677,3 +691,13 @@ int tcp_fp32_peak(int device, double *tffma) {
 }
 
 }  // extern "C"
+
+namespace tcp {
+int md_advance(tcp_ctx *c, double dt, int nsteps) {
+    int rc;
+    if ((rc = ::ensure_graph(c, dt))) return rc;
+    for (int s = 0; s < nsteps; ++s)
+        if ((rc = ::launch_step(c, dt))) return rc;
+    return TCP_OK;
+}
+}  // namespace tcp

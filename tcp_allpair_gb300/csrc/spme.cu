@@ -434,8 +434,10 @@ int ewald_setup(tcp_ctx *c) {
         return set_error(TCP_ERR_BAD_PARAM, "ewald_nmax2 too large: more k-vectors than the energy buffer holds");
     cudaFree(c->kvec);
     cudaFree(c->ksum);
+    cudaFree(c->kS4);
     c->kvec = nullptr;
     c->ksum = nullptr;
+    c->kS4 = nullptr;
     if (c->nk == 0) return TCP_OK;
     TCP_CUDA(cudaMalloc(&c->kvec, sizeof(double) * kv.size()));
     TCP_CUDA(cudaMalloc(&c->ksum, sizeof(double) * 2 * (size_t)c->nk));
@@ -460,6 +462,246 @@ int launch_ewald(tcp_ctx *c, bool energy) {
         sum_partials_kernel<<<1, 1024, 0, c->stream>>>(epart, c->nk, kEps / (2.0 * kPi * c->V), c->scal + kScalUm);
         c->launches++;
     }
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+// ---- reciprocal-space Hessian-vector products -------------------------------
+// With Q(k) = sum_j q_j W_j(k), phi = A Q (the convolution of launch_spme) and
+// E = c/2 Q.phi, c = eps/(pi V):
+//   (H w)_i = c q_i [sum_k (hess W_i(k) w_i) phi(k) + sum_k grad W_i(k) dphi(k)],
+//   dphi = A dQ, dQ(k) = sum_j q_j grad W_j(k) . w_j.
+// Always FP64 (meshes hQ / hdQ, own D2Z / Z2D plans), whatever the precision
+// of the force path.
+
+// dQ(k) += q_j grad W_j(k) . w_j
+template <int P>
+__global__ void spme_spread_dipole_kernel(const SpmeArgs a, const double *__restrict__ w, double *__restrict__ dQ) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= a.n) return;
+    const double q = m < a.nel ? a.q0 : a.q1;
+    const double L[3] = {a.box0, a.box1, a.box2};
+    const int K[3] = {a.K1, a.K2, a.K3};
+    double W[3][P], dW[3][P];
+    int base[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];
+        spline_w<P, double>(u, W[d], dW[d]);
+        base[d] = (int)trunc(u) - (P - 3);
+    }
+    const double wx = q * w[m] * ((double)a.K1 / a.box0), wy = q * w[(size_t)a.n + m] * ((double)a.K2 / a.box1),
+                 wz = q * w[2 * (size_t)a.n + m] * ((double)a.K3 / a.box2);
+#pragma unroll 1
+    for (int k = 0; k < P; ++k) {
+        const int iz = wrapi(base[2] + k, a.K3);
+#pragma unroll 1
+        for (int j = 0; j < P; ++j) {
+            const int iy = wrapi(base[1] + j, a.K2);
+            const double cx = wx * W[1][j] * W[2][k];
+            const double cyz = wy * dW[1][j] * W[2][k] + wz * W[1][j] * dW[2][k];
+            double *row = dQ + (size_t)a.K1 * (iy + (size_t)a.K2 * iz);
+#pragma unroll
+            for (int i = 0; i < P; ++i) atomicAdd(row + wrapi(base[0] + i, a.K1), cx * dW[0][i] + cyz * W[0][i]);
+        }
+    }
+}
+
+template <int P>
+__global__ void spme_gather_hvp_kernel(const SpmeArgs a, const double *__restrict__ phi,
+                                       const double *__restrict__ dphi, const double *__restrict__ w, double coef,
+                                       double *__restrict__ hw) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= a.n) return;
+    const double q = m < a.nel ? a.q0 : a.q1;
+    const double L[3] = {a.box0, a.box1, a.box2};
+    const int K[3] = {a.K1, a.K2, a.K3};
+    double W[3][P], dW[3][P], d2W[3][P];
+    int base[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];
+        spline_w2<P>(u, W[d], dW[d], d2W[d]);
+        const double kl = (double)K[d] / L[d];
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+            dW[d][j] *= kl;
+            d2W[d][j] *= kl * kl;
+        }
+        base[d] = (int)trunc(u) - (P - 3);
+    }
+    const double w0 = w[m], w1 = w[(size_t)a.n + m], w2 = w[2 * (size_t)a.n + m];
+    double h0 = 0.0, h1 = 0.0, h2 = 0.0;
+#pragma unroll 1
+    for (int k = 0; k < P; ++k) {
+        const int iz = wrapi(base[2] + k, a.K3);
+#pragma unroll 1
+        for (int j = 0; j < P; ++j) {
+            const int iy = wrapi(base[1] + j, a.K2);
+            const size_t ro = (size_t)a.K1 * (iy + (size_t)a.K2 * iz);
+            // per row: sums over i of W, dW, d2W times phi and dphi
+            double sp = 0, sdp = 0, sd2p = 0, sq = 0, sdq = 0;
+#pragma unroll
+            for (int i = 0; i < P; ++i) {
+                const size_t idx = ro + wrapi(base[0] + i, a.K1);
+                const double ph = phi[idx], dph = dphi[idx];
+                sp += W[0][i] * ph;
+                sdp += dW[0][i] * ph;
+                sd2p += d2W[0][i] * ph;
+                sq += W[0][i] * dph;
+                sdq += dW[0][i] * dph;
+            }
+            const double Wy = W[1][j], dWy = dW[1][j], d2Wy = d2W[1][j];
+            const double Wz = W[2][k], dWz = dW[2][k], d2Wz = d2W[2][k];
+            // Hessian of W x gradient rows, times w, times phi; gradient times dphi
+            const double hxx = sd2p * Wy * Wz, hyy = sp * d2Wy * Wz, hzz = sp * Wy * d2Wz;
+            const double hxy = sdp * dWy * Wz, hxz = sdp * Wy * dWz, hyz = sp * dWy * dWz;
+            h0 += hxx * w0 + hxy * w1 + hxz * w2 + sdq * Wy * Wz;
+            h1 += hxy * w0 + hyy * w1 + hyz * w2 + sq * dWy * Wz;
+            h2 += hxz * w0 + hyz * w1 + hzz * w2 + sq * Wy * dWz;
+        }
+    }
+    hw[m] += coef * q * h0;
+    hw[(size_t)a.n + m] += coef * q * h1;
+    hw[2 * (size_t)a.n + m] += coef * q * h2;
+}
+
+template <int P>
+static void launch_hvp_kernels(tcp_ctx *c, const SpmeArgs &a, const double *w, double *hw, int which) {
+    const int threads = 128, blocks = (c->n + threads - 1) / threads;
+    if (which == 0) spme_spread_kernel<P><<<blocks, threads, 0, c->stream>>>(a, c->hQ);
+    else if (which == 1) spme_spread_dipole_kernel<P><<<blocks, threads, 0, c->stream>>>(a, w, c->hdQ);
+    else spme_gather_hvp_kernel<P><<<blocks, threads, 0, c->stream>>>(a, c->hQ, c->hdQ, w, kEps / (kPi * c->V), hw);
+}
+
+static void hvp_kernels(tcp_ctx *c, const SpmeArgs &a, const double *w, double *hw, int which) {
+    switch (c->p.order) {
+        case 4: launch_hvp_kernels<4>(c, a, w, hw, which); break;
+        case 5: launch_hvp_kernels<5>(c, a, w, hw, which); break;
+        case 6: launch_hvp_kernels<6>(c, a, w, hw, which); break;
+        case 7: launch_hvp_kernels<7>(c, a, w, hw, which); break;
+        default: launch_hvp_kernels<8>(c, a, w, hw, which); break;
+    }
+}
+
+void spme_hvp_free(tcp_ctx *c) {
+    if (c->hplans) {
+        cufftDestroy(c->hplan_f);
+        cufftDestroy(c->hplan_b);
+        c->hplans = false;
+    }
+    cudaFree(c->hQ);
+    cudaFree(c->hdQ);
+    cudaFree(c->hQk);
+    cudaFree(c->kS4);
+    c->hQ = c->hdQ = nullptr;
+    c->hQk = nullptr;
+    c->kS4 = nullptr;
+}
+
+int launch_spme_hvp(tcp_ctx *c, const double *w, double *hw) {
+    const size_t nreal = (size_t)c->K1 * c->K2 * c->K3;
+    const size_t nhalf = (size_t)c->Kh * c->K2 * c->K3;
+    if (!c->hQ) {
+        if (cudaMalloc(&c->hQ, sizeof(double) * nreal) != cudaSuccess ||
+            cudaMalloc(&c->hdQ, sizeof(double) * nreal) != cudaSuccess ||
+            cudaMalloc(&c->hQk, sizeof(cufftDoubleComplex) * nhalf) != cudaSuccess)
+            return set_error(TCP_ERR_NOMEM, "SPME Hessian mesh allocation failed");
+    }
+    if (!c->hplans) {
+        if (cufftPlan3d(&c->hplan_f, c->K3, c->K2, c->K1, CUFFT_D2Z) != CUFFT_SUCCESS)
+            return set_error(TCP_ERR_CUFFT, "cufftPlan3d D2Z failed");
+        if (cufftPlan3d(&c->hplan_b, c->K3, c->K2, c->K1, CUFFT_Z2D) != CUFFT_SUCCESS) {
+            cufftDestroy(c->hplan_f);
+            return set_error(TCP_ERR_CUFFT, "cufftPlan3d Z2D failed");
+        }
+        cufftSetStream(c->hplan_f, c->stream);
+        cufftSetStream(c->hplan_b, c->stream);
+        c->hplans = true;
+    }
+    const SpmeArgs a = spme_args(c);
+    const long total = (long)nhalf;
+    const int eb = spme_energy_blocks(c);
+    double *mesh[2] = {c->hQ, c->hdQ};
+    for (int pass = 0; pass < 2; ++pass) {    // phi = A Q, then dphi = A dQ
+        TCP_CUDA(cudaMemsetAsync(mesh[pass], 0, sizeof(double) * nreal, c->stream));
+        hvp_kernels(c, a, w, hw, pass);
+        if (cufftExecD2Z(c->hplan_f, mesh[pass], c->hQk) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecD2Z failed");
+        spme_influence_kernel<<<eb, 256, 0, c->stream>>>(c->hQk, c->infl, total, c->Kh, c->K1, nullptr, false);
+        if (cufftExecZ2D(c->hplan_b, c->hQk, mesh[pass]) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecZ2D failed");
+        c->launches += 2;
+    }
+    hvp_kernels(c, a, w, hw, 2);
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+// plain Ewald: S(m) and dS(m) = sum_j q_j (2 pi i m.w_j) e^{i ph_j} per k-vector
+__global__ void ewald_dsfac_kernel(const double *__restrict__ x, const double *__restrict__ w, int nel, int n,
+                                   double q0, double q1, const double *__restrict__ kvec, double *__restrict__ kS4) {
+    __shared__ double red[32];
+    const double mx = kvec[4 * blockIdx.x], my = kvec[4 * blockIdx.x + 1], mz = kvec[4 * blockIdx.x + 2];
+    double sr = 0.0, si = 0.0, dr = 0.0, di = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double q = j < nel ? q0 : q1;
+        const double ph = 2.0 * kPi * (mx * x[j] + my * x[(size_t)n + j] + mz * x[2 * (size_t)n + j]);
+        const double mw = 2.0 * kPi * (mx * w[j] + my * w[(size_t)n + j] + mz * w[2 * (size_t)n + j]);
+        double s, c;
+        sincos(ph, &s, &c);
+        sr += q * c;
+        si += q * s;
+        dr -= q * mw * s;
+        di += q * mw * c;
+    }
+    sr = block_sum(sr, red);
+    si = block_sum(si, red);
+    dr = block_sum(dr, red);
+    di = block_sum(di, red);
+    if (threadIdx.x == 0) {
+        kS4[4 * blockIdx.x] = sr;
+        kS4[4 * blockIdx.x + 1] = si;
+        kS4[4 * blockIdx.x + 2] = dr;
+        kS4[4 * blockIdx.x + 3] = di;
+    }
+}
+
+// (H w)_i = -(2 eps/V) q_i sum_m theta m [Im(conj(dS) e^{i ph_i}) + 2 pi (m.w_i) Re(conj(S) e^{i ph_i})]
+__global__ void ewald_hvp_kernel(const double *__restrict__ x, const double *__restrict__ w, int nel, int n,
+                                 double q0, double q1, const double *__restrict__ kvec,
+                                 const double *__restrict__ kS4, int nk, double coef, double *__restrict__ hw) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double q = i < nel ? q0 : q1;
+    const double xi = x[i], yi = x[(size_t)n + i], zi = x[2 * (size_t)n + i];
+    const double wx = w[i], wy = w[(size_t)n + i], wz = w[2 * (size_t)n + i];
+    double h0 = 0.0, h1 = 0.0, h2 = 0.0;
+    for (int k = 0; k < nk; ++k) {
+        const double mx = kvec[4 * k], my = kvec[4 * k + 1], mz = kvec[4 * k + 2], th = kvec[4 * k + 3];
+        double s, c;
+        sincos(2.0 * kPi * (mx * xi + my * yi + mz * zi), &s, &c);
+        const double mw = 2.0 * kPi * (mx * wx + my * wy + mz * wz);
+        const double im_d = kS4[4 * k + 2] * s - kS4[4 * k + 3] * c;
+        const double re_s = kS4[4 * k] * c + kS4[4 * k + 1] * s;
+        const double t = th * (im_d + mw * re_s);
+        h0 += t * mx;
+        h1 += t * my;
+        h2 += t * mz;
+    }
+    hw[i] += coef * q * h0;
+    hw[(size_t)n + i] += coef * q * h1;
+    hw[2 * (size_t)n + i] += coef * q * h2;
+}
+
+int launch_ewald_hvp(tcp_ctx *c, const double *w, double *hw) {
+    if (c->nk == 0) return TCP_OK;
+    if (!c->kS4 && cudaMalloc(&c->kS4, sizeof(double) * 4 * (size_t)c->nk) != cudaSuccess)
+        return set_error(TCP_ERR_NOMEM, "Ewald Hessian buffer allocation failed");
+    const double q0 = c->p.charge_scale * c->p.q[0], q1 = c->p.charge_scale * c->p.q[1];
+    ewald_dsfac_kernel<<<c->nk, 256, 0, c->stream>>>(c->x, w, c->nel, c->n, q0, q1, c->kvec, c->kS4);
+    ewald_hvp_kernel<<<(c->n + 127) / 128, 128, 0, c->stream>>>(c->x, w, c->nel, c->n, q0, q1, c->kvec, c->kS4,
+                                                                c->nk, -2.0 * kEps / c->V, hw);
+    c->launches += 2;
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;
 }

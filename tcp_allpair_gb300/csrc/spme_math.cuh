@@ -51,6 +51,41 @@ __device__ __forceinline__ void spline_w(double u, T *W, T *dW) {
     for (int j = 0; j < P; ++j) W[j] = a[j];
 }
 
+// Weights with first and second derivatives (d/du, d^2/du^2) for every order
+// P >= 4 by the same recursion: the order P-2 values give
+// M_P''(y) = M_{P-2}(y) - 2 M_{P-2}(y-1) + M_{P-2}(y-2), the order P-1 values
+// M_P'(y) = M_{P-1}(y) - M_{P-1}(y-1).
+template <int P>
+__device__ __forceinline__ void spline_w2(double u, double *W, double *dW, double *d2W) {
+    const double w = u - trunc(u);
+    double a[P];
+    a[0] = 1.0;
+#pragma unroll
+    for (int j = 1; j < P; ++j) a[j] = 0.0;
+#pragma unroll
+    for (int nn = 2; nn <= P; ++nn) {
+        if (nn == P - 1) {
+#pragma unroll
+            for (int j = 0; j < P; ++j)
+                d2W[j] = (j >= 2 ? a[j - 2] : 0.0) - 2.0 * (j >= 1 && j - 1 < P - 2 ? a[j - 1] : 0.0) +
+                         (j < P - 2 ? a[j] : 0.0);
+        }
+        if (nn == P) {
+#pragma unroll
+            for (int j = 0; j < P; ++j) dW[j] = (j > 0 ? a[j - 1] : 0.0) - (j < P - 1 ? a[j] : 0.0);
+        }
+        const double inv = 1.0 / (double)(nn - 1);
+#pragma unroll
+        for (int j = nn - 1; j >= 0; --j) {
+            const double left = j > 0 ? a[j - 1] : 0.0;
+            const double right = j < nn - 1 ? a[j] : 0.0;
+            a[j] = ((w + (double)(nn - 1 - j)) * left + (1.0 - w + (double)j) * right) * inv;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < P; ++j) W[j] = a[j];
+}
+
 __device__ __forceinline__ int wrapi(int i, int K) {
     i %= K;
     return i < 0 ? i + K : i;

@@ -123,6 +123,22 @@ struct tcp_ctx {
     size_t l2_flush_bytes = 0;
     long long step_index = 0;
     tcp_energies last{};
+    // derivatives (allocated on first use): vectors SoA [3][n]
+    double *adj_w = nullptr, *adj_hw = nullptr;       // Hessian-vector product input / output
+    double *adj_xb = nullptr, *adj_vb = nullptr, *adj_fb = nullptr;   // reverse-mode adjoints
+    double *adj_save = nullptr;        // [3][3][n] x, v, f after the forward pass
+    double *adj_io = nullptr;          // [3][n] host-layout staging
+    double *adj_scal = nullptr;        // kAdj* scalars
+    double *adj_part = nullptr;        // per-block partial sums
+    double *adj_ck = nullptr;          // checkpoints [nck][2][3][n]
+    int adj_ck_cap = 0;
+    double *adj_seg = nullptr;         // recomputed segment [M+1][2][3][n]
+    int adj_seg_cap = 0;
+    double *hQ = nullptr, *hdQ = nullptr;   // FP64 meshes phi and dphi of the reciprocal HVP
+    cufftDoubleComplex *hQk = nullptr;
+    cufftHandle hplan_f = 0, hplan_b = 0;
+    bool hplans = false;
+    double *kS4 = nullptr;             // plain Ewald HVP: [nk][4] S re, S im, dS re, dS im
 };
 
 namespace tcp {
@@ -185,6 +201,17 @@ int launch_reduce(tcp_ctx *c, int mask, int pass);
 int launch_extract(tcp_ctx *c, int first, int count, long stride, long off_x, long off_v, long off_f);
 int launch_pack(tcp_ctx *c, int first, int count, bool x, bool v, bool f, bool frec, int *nf);
 int launch_fp32_peak(int device, double *tffma);
+
+// ctx.cu: step and force composition for the derivative routines
+int force_eval(tcp_ctx *c, bool remove_net);        // main.f90:100-141 on the stream
+int md_advance(tcp_ctx *c, double dt, int nsteps);  // nsteps MD steps (graph), no host sync
+int md_finish(tcp_ctx *c);                          // sync scalars, fill c->last
+// spme.cu: reciprocal Hessian-vector products, hw += H_rec w (w, hw SoA [3][n])
+int launch_spme_hvp(tcp_ctx *c, const double *w, double *hw);
+int launch_ewald_hvp(tcp_ctx *c, const double *w, double *hw);
+void spme_hvp_free(tcp_ctx *c);
+// adjoint.cu
+void adjoint_free(tcp_ctx *c);
 
 // reduce targets for launch_reduce
 enum { kRedUr = 1, kRedMv2 = 4 };
