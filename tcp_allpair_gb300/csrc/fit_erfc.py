@@ -2,26 +2,29 @@
 
     erfc(x) = exp(-x^2) * t * Q(t),   t = 1 / (1 + P x),   x >= 0
 
-Q is a degree-8 polynomial in t fitted to erfcx(x)/t = erfc(x) exp(x^2)/t by
+Q is a degree-7 polynomial in t fitted to erfcx(x)/t = erfc(x) exp(x^2)/t by
 Lawson's iteratively reweighted least squares, which converges to the minimax
-fit in relative error, on x in [0, XMAX].  The exp(-x^2) factor is shared with
+fit in relative error, on x in [0, XMAX].  P = 0.4 and XMAX = 6 minimise the
+FP32 error on the arguments the kernels see: alpha r <= alpha rc (3.1 by
+default, 3.46 for a 1e-6 Ewald error) and r/lambda < 6 (the Kelbg terms are
+skipped beyond 6 lambda).  The exp(-x^2) factor is shared with
 the Gaussian term of the Ewald pair force, so a Coulomb pair costs one ex2 and
 one reciprocal on the SFU for both erfc and the Gaussian.
 
-Fit error (FP64 evaluation): 3.8e-8 relative.  Evaluated in FP32 Horner form
-on x in [0, 6]: 3.6e-7 max, 7.8e-8 rms relative (the FP32 rounding of t
-dominates).  Run `python fit_erfc.py` to reproduce the coefficients in
-pair_fp32c.cu (printed highest power first).
+Fit error (FP64 evaluation): 1.0e-7 relative.  Evaluated in FP32 Horner form
+on x in [0, 6]: 4.4e-7 max, 1.15e-7 rms relative (the FP32 rounding of t
+dominates; degree 8 gives 3.3e-7 / 7.6e-8 for one more FFMA per erfc).  Run `python fit_erfc.py` to reproduce the coefficients in
+pair_math.cuh (printed highest power first).
 """
 import numpy as np
 from scipy.special import erfc, erfcx
 
-P = 0.5
-DEG = 8
-XMAX = 8.0
+P = 0.4
+DEG = 7
+XMAX = 6.0
 
 
-def fit(p=P, deg=DEG, xmax=XMAX, iters=200):
+def fit(p=P, deg=DEG, xmax=XMAX, iters=400):
     t = np.linspace(1.0 / (1.0 + p * xmax), 1.0, 20000)
     x = (1.0 / t - 1.0) / p
     target = erfcx(x) / t

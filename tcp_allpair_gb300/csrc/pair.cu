@@ -111,22 +111,26 @@ __device__ __forceinline__ void tile_f32(const int4 *__restrict__ tj, int cnt, i
         bool ok = r2 < rc2;
         if (DIAG) ok = ok && (r2 > 0.0f);
         if (!FULL) ok = ok && (jj < cnt);
-        const float rinv = rsqrt_approx(r2);
-        const float r = r2 * rinv;
+        // the mask is applied once, to 1/r (er, energy and weight carry it);
+        // DIAG / partial tiles may hold the i-particle or padding (r2 = 0)
+        const float r2s = (DIAG || !FULL) ? (ok ? r2 : 1.0f) : r2;
+        const float rinv = rsqrt_approx(r2s);
+        const float rinv_m = ok ? rinv : 0.0f;
+        const float r = r2s * rinv;
         const float t = rcp_approx(fmaf(p_alpha, r, 1.0f));
-        const float e = ex2_approx(c_exp * r2);
-        const float er = (e * erfc_poly(t)) * rinv;     // erfc(ar)/r, shared by energy and force
+        const float e = ex2_approx(c_exp * r2s);
+        const float er = (e * erfc_poly(t)) * rinv_m;   // erfc(ar)/r, shared by energy and force
         float s = fmaf(c_gauss, e, er);                  // (erfc(ar) + 2ar/sqrt(pi) exp(-a^2r^2)) / r
         float u = er;
         if (KIND == 1) {                                 // Deutsch, force.f90:136-139
             const float y = ex2_approx(c_rs * r);        // exp(-r/rs)
             s = fmaf(-y, rinv + inv_rs, s);
-            if (ENERGY) u = fmaf(-y, rinv, u);
+            if (ENERGY) u = fmaf(-y, rinv_m, u);
         }
         if (KIND == 2) {                                 // Kelbg
-            const bool near = ok && (r2 < rshort2);
+            const bool near = ok && (r2s < rshort2);
             if (__any_sync(0xffffffffu, near)) {
-                const float g = near ? ex2_approx(c_lam * r2) : 0.0f;   // exp(-r^2/lambda^2)
+                const float g = near ? ex2_approx(c_lam * r2s) : 0.0f;   // exp(-r^2/lambda^2)
                 s = fmaf(-g, rinv, s);
                 if (ENERGY) {
                     const float t2 = rcp_approx(fmaf(p_lam, r, 1.0f));
@@ -135,12 +139,11 @@ __device__ __forceinline__ void tile_f32(const int4 *__restrict__ tj, int cnt, i
                 }
             }
         }
-        float w = s * (rinv * rinv);
-        w = ok ? w : 0.0f;
+        const float w = s * (rinv_m * rinv_m);
         px = fmaf(w, dx, px);
         py = fmaf(w, dy, py);
         pz = fmaf(w, dz, pz);
-        if (ENERGY) pe += ok ? u : 0.0f;                 // select: r = 0 gives inf/NaN
+        if (ENERGY) pe += u;
         if (RDF) {
             if (ok) {
                 const int bin = (int)(r * inv_dx);
@@ -478,14 +481,14 @@ void make_pair_consts(tcp_ctx *c) {
     k.rc2f = (float)c->rc2;
     const double log2e = 1.4426950408889634;
     k.c_exp = (float)(-c->alpha * c->alpha * log2e);
-    k.p_alpha = (float)(0.5 * c->alpha);
+    k.p_alpha = (float)(kErfcP * c->alpha);
     k.c_gauss = (float)(2.0 * c->alpha / kSqrtPi);
     const double rs = p.rs > 0 ? p.rs : 1.0;
     k.c_rs = (float)(-log2e / rs);
     k.inv_rs = (float)(1.0 / rs);
     const double lam = p.lambda_ei > 0 ? p.lambda_ei : 1.0;
     k.c_lam = (float)(-log2e / (lam * lam));
-    k.p_lam = (float)(0.5 / lam);
+    k.p_lam = (float)(kErfcP / lam);
     k.sqrtpi_lam = (float)(kSqrtPi / lam);
     k.rshort2 = (float)(36.0 * lam * lam);
     const double dxs[3] = {p.dx_ee, p.dx_ei, p.dx_ii};
@@ -501,13 +504,13 @@ void make_pair_consts(tcp_ctx *c) {
     k.cubic = (p.box[0] == p.box[1] && p.box[1] == p.box[2]) ? 1 : 0;
     const double u = p.box[0] / two32;
     k.u_rc2 = (float)(c->rc2 / (u * u));
-    k.u_p_alpha = (float)(0.5 * c->alpha * u);
+    k.u_p_alpha = (float)(kErfcP * c->alpha * u);
     k.u_c_exp = (float)(-c->alpha * c->alpha * log2e * u * u);
     k.u_c_gauss = (float)(2.0 * c->alpha / kSqrtPi * u);
     k.u_c_rs = (float)(-log2e / rs * u);
     k.u_inv_rs = (float)(u / rs);
     k.u_c_lam = (float)(-log2e / (lam * lam) * u * u);
-    k.u_p_lam = (float)(0.5 / lam * u);
+    k.u_p_lam = (float)(kErfcP / lam * u);
     k.u_sqrtpi_lam = (float)(kSqrtPi / lam * u);
     k.u_rshort2 = (float)(36.0 * lam * lam / (u * u));
     for (int t = 0; t < 3; ++t) {

@@ -151,23 +151,29 @@ __device__ __forceinline__ const PairConsts &n3_consts(const N3Args &a, int rep)
 //   w  = [erfc(ar)/r + 2a/sqrt(pi) exp(-a^2r^2) (- e-i terms)] / r^2.
 // KIND 2 (Kelbg) adds its Gaussian terms only when `near_any` (a warp vote
 // taken by the caller for all i-particles of the lane) is set.
-template <int KIND, bool ENERGY>
+template <int KIND, bool ENERGY, bool MASKED>
 __device__ __forceinline__ float n3_pair(const PairConsts &c, float r2, bool ok, bool near_any, float &pe) {
-    const float rinv = rsqrt_approx(r2);
-    const float r = r2 * rinv;
+    // The cut-off / index mask is applied once, to 1/r: er, the energy and
+    // the weight all carry a factor rinv_m, so a masked pair adds exact zeros.
+    // Unmasked items only hold distinct particles (r2 > 0); masked items may
+    // pair a particle with itself or with padding, so r2 is replaced first.
+    const float r2s = MASKED ? (ok ? r2 : 1.0f) : r2;
+    const float rinv = rsqrt_approx(r2s);
+    const float rinv_m = ok ? rinv : 0.0f;
+    const float r = r2s * rinv;
     const float t = rcp_approx(fmaf(c.u_p_alpha, r, 1.0f));
-    const float e = ex2_approx(c.u_c_exp * r2);
-    const float er = (e * erfc_poly(t)) * rinv;          // erfc(ar)/r
+    const float e = ex2_approx(c.u_c_exp * r2s);
+    const float er = (e * erfc_poly(t)) * rinv_m;        // erfc(ar)/r
     float s = fmaf(c.u_c_gauss, e, er);                   // (erfc(ar) + 2ar/sqrt(pi) e^{-a^2r^2}) / r
     float u = er;
     if (KIND == 1) {                                      // Deutsch, force.f90:136-139
         const float y = ex2_approx(c.u_c_rs * r);         // exp(-r/rs)
         s = fmaf(-y, rinv + c.u_inv_rs, s);
-        if (ENERGY) u = fmaf(-y, rinv, u);
+        if (ENERGY) u = fmaf(-y, rinv_m, u);
     }
     if (KIND == 2 && near_any) {                          // Kelbg
-        const bool near = ok && (r2 < c.u_rshort2);
-        const float g = near ? ex2_approx(c.u_c_lam * r2) : 0.0f;   // exp(-r^2/lambda^2)
+        const bool near = ok && (r2s < c.u_rshort2);
+        const float g = near ? ex2_approx(c.u_c_lam * r2s) : 0.0f;   // exp(-r^2/lambda^2)
         s = fmaf(-g, rinv, s);
         if (ENERGY) {
             const float t2 = rcp_approx(fmaf(c.u_p_lam, r, 1.0f));
@@ -175,9 +181,8 @@ __device__ __forceinline__ float n3_pair(const PairConsts &c, float r2, bool ok,
             u += fmaf(c.u_sqrtpi_lam, erfc_rl, -g * rinv);
         }
     }
-    if (ENERGY) pe += ok ? u : 0.0f;
-    const float w = s * (rinv * rinv);
-    return ok ? w : 0.0f;
+    if (ENERGY) pe += u;
+    return s * (rinv_m * rinv_m);
 }
 
 // One item: the R i-particles of this lane against a j-subtile in shared
@@ -214,7 +219,7 @@ __device__ __forceinline__ void n3_item(const PairConsts &c, const int4 *__restr
             if (KIND == 2) near_any = __any_sync(0xffffffffu, r2min < c.u_rshort2);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const float w = n3_pair<KIND, ENERGY>(c, r2[r], ok[r], near_any, pe);
+                const float w = n3_pair<KIND, ENERGY, MASKED>(c, r2[r], ok[r], near_any, pe);
                 p[r][0] = fmaf(w, d[r][0], p[r][0]);
                 p[r][1] = fmaf(w, d[r][1], p[r][1]);
                 p[r][2] = fmaf(w, d[r][2], p[r][2]);

@@ -30,12 +30,12 @@ struct PairConsts {
     float sx, sy, sz;          // box / 2^32
     float rc2f;                // cut-off^2
     float c_exp;               // -alpha^2 log2(e): exp(-a^2 r^2) = ex2(c_exp r^2)
-    float p_alpha;             // 0.5 alpha: t = 1/(1 + 0.5 alpha r)
+    float p_alpha;             // P alpha: t = 1/(1 + P alpha r), P = kErfcP (pair_math.cuh)
     float c_gauss;             // 2 alpha / sqrt(pi)
     float c_rs;                // Deutsch: -log2(e)/rs
     float inv_rs;              // 1/rs
     float c_lam;               // Kelbg: -log2(e)/lambda^2
-    float p_lam;               // 0.5/lambda
+    float p_lam;               // P/lambda
     float sqrtpi_lam;          // sqrt(pi)/lambda
     float rshort2;             // (6 lambda)^2: Kelbg Gaussian terms below FP64 resolution beyond
     float inv_dx[3];           // RDF 1/dx per pair type ee|ei|ii

@@ -3,7 +3,8 @@ reverse mode through NOTEMP steps) against central finite differences of the
 oracle's own energy, forces and MD steps.  The reference computes no
 derivatives, so these pin the derivative oracle that the CUDA library's
 adjoint is checked against.  Step h = 1e-4 relative (lambda, charge scale) and
-1e-5 a along a unit Gaussian direction (positions)."""
+1e-5 a along a unit Gaussian direction (positions; no pair of this
+system crosses the cut-off within that step)."""
 import numpy as np
 import pytest
 
