@@ -216,6 +216,12 @@ int tcp_create(const tcp_params *p_in, int nel, int nion, int device, tcp_ctx **
     c->n = nel + nion;
     c->device = device;
     c->num_sms = prop.multiProcessorCount;
+    {
+        int pageable = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
+        const char *env = getenv("TCP_HOST_DIRECT");
+        c->host_direct = pageable == 1 && !(env && env[0] == '0');
+    }
     const size_t n = c->n;
     auto fail = [&](int code) {
         tcp_destroy(c);
@@ -368,9 +374,13 @@ int tcp_upload(tcp_ctx *c, int species, const double *xx, const double *xv, cons
     }
     const size_t span = (size_t)(count - 1) * stride + (size_t)(top - base) + 24;
     int rc;
-    if ((rc = ensure_stage(c, span))) return rc;
-    TCP_CUDA(cudaMemcpyAsync(c->d_stage, base, span, cudaMemcpyHostToDevice, c->stream));
-    if ((rc = launch_extract(c, first, count, stride, off[0], off[1], off[2]))) return rc;
+    const unsigned char *src = reinterpret_cast<const unsigned char *>(base);
+    if (!c->host_direct) {      // staged: one copy of the record span, then the same gather
+        if ((rc = ensure_stage(c, span))) return rc;
+        TCP_CUDA(cudaMemcpyAsync(c->d_stage, base, span, cudaMemcpyHostToDevice, c->stream));
+        src = c->d_stage;
+    }
+    if ((rc = launch_extract(c, src, first, count, stride, off[0], off[1], off[2]))) return rc;
     if (xx && (rc = launch_refresh_positions(c))) return rc;
     invalidate_graph(c);   // no-op for correctness; graphs read device memory
     TCP_CUDA(cudaStreamSynchronize(c->stream));
@@ -384,6 +394,22 @@ int tcp_download(tcp_ctx *c, int species, double *xx, double *xv, double *ff, lo
     if (count == 0 || (!xx && !xv && !ff)) return TCP_OK;
     if (stride < 24 || stride % 8) return set_error(TCP_ERR_BAD_PARAM, "bad stride");
     int nf = 0, rc;
+    if (c->host_direct) {       // the device writes the caller's records in place
+        const double *ptrs[3] = {xx, xv, ff};
+        const char *base = nullptr;
+        for (const double *q : ptrs)
+            if (q && (!base || reinterpret_cast<const char *>(q) < base)) base = reinterpret_cast<const char *>(q);
+        long off[3];
+        for (int k = 0; k < 3; ++k) {
+            off[k] = ptrs[k] ? (long)(reinterpret_cast<const char *>(ptrs[k]) - base) : -1;
+            if (off[k] >= 0 && off[k] % 8) return set_error(TCP_ERR_BAD_PARAM, "fields must be 8-byte aligned");
+        }
+        if ((rc = launch_scatter(c, reinterpret_cast<unsigned char *>(const_cast<char *>(base)), first, count, stride,
+                                 off[0], off[1], off[2], c->f)))
+            return rc;
+        TCP_CUDA(cudaStreamSynchronize(c->stream));
+        return TCP_OK;
+    }
     if ((rc = ensure_stage(c, (size_t)count * 4 * 3 * sizeof(double)))) return rc;
     if ((rc = launch_pack(c, first, count, xx != nullptr, xv != nullptr, ff != nullptr, false, &nf))) return rc;
     TCP_CUDA(cudaMemcpyAsync(c->h_stage, c->d_stage, (size_t)count * nf * 3 * sizeof(double), cudaMemcpyDeviceToHost,
@@ -409,8 +435,14 @@ int tcp_upload_soa(tcp_ctx *c, const double *x, const double *v, const double *f
     const double *src[3] = {x, v, f};
     for (int q = 0; q < 3; ++q) {
         if (!src[q]) continue;
-        TCP_CUDA(cudaMemcpyAsync(c->d_stage, src[q], (size_t)c->n * 3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-        if ((rc = launch_extract(c, 0, c->n, 24, q == 0 ? 0 : -1, q == 1 ? 0 : -1, q == 2 ? 0 : -1))) return rc;
+        const unsigned char *from = reinterpret_cast<const unsigned char *>(src[q]);
+        if (!c->host_direct) {
+            // the stream is in order: the previous extract has read d_stage before this copy lands
+            TCP_CUDA(cudaMemcpyAsync(c->d_stage, src[q], (size_t)c->n * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                                     c->stream));
+            from = c->d_stage;
+        }
+        if ((rc = launch_extract(c, from, 0, c->n, 24, q == 0 ? 0 : -1, q == 1 ? 0 : -1, q == 2 ? 0 : -1))) return rc;
     }
     if (x && (rc = launch_refresh_positions(c))) return rc;
     TCP_CUDA(cudaStreamSynchronize(c->stream));
@@ -421,6 +453,16 @@ int tcp_download_soa(tcp_ctx *c, double *x, double *v, double *f, double *frec) 
     if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
     cudaSetDevice(c->device);
     int nf = 0, rc;
+    if (c->host_direct) {
+        // (n, 3) row-major host arrays are records of stride 24 with one field
+        if (x && (rc = launch_scatter(c, reinterpret_cast<unsigned char *>(x), 0, c->n, 24, 0, -1, -1, c->f))) return rc;
+        if (v && (rc = launch_scatter(c, reinterpret_cast<unsigned char *>(v), 0, c->n, 24, -1, 0, -1, c->f))) return rc;
+        if (f && (rc = launch_scatter(c, reinterpret_cast<unsigned char *>(f), 0, c->n, 24, -1, -1, 0, c->f))) return rc;
+        if (frec && (rc = launch_scatter(c, reinterpret_cast<unsigned char *>(frec), 0, c->n, 24, -1, -1, 0, c->frec)))
+            return rc;
+        TCP_CUDA(cudaStreamSynchronize(c->stream));
+        return TCP_OK;
+    }
     if ((rc = ensure_stage(c, (size_t)c->n * 4 * 3 * sizeof(double)))) return rc;
     if ((rc = launch_pack(c, 0, c->n, x != nullptr, v != nullptr, f != nullptr, frec != nullptr, &nf))) return rc;
     if (nf == 0) return TCP_OK;

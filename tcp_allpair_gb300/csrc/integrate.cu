@@ -291,6 +291,21 @@ __global__ void extract_kernel(const unsigned char *__restrict__ stage, long str
     }
 }
 
+// SoA -> host records: the inverse of extract_kernel, writing the fields of
+// record r at dst + r*stride + off (dst in host memory the device can address)
+__global__ void scatter_kernel(unsigned char *__restrict__ dst, long stride, long off_x, long off_v, long off_f,
+                               int count, int first, int n, const double *x, const double *v, const double *f) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= count) return;
+    unsigned char *rec = dst + (size_t)r * stride;
+    const int i = first + r;
+    for (int d = 0; d < 3; ++d) {
+        if (off_x >= 0) reinterpret_cast<double *>(rec + off_x)[d] = x[(size_t)d * n + i];
+        if (off_v >= 0) reinterpret_cast<double *>(rec + off_v)[d] = v[(size_t)d * n + i];
+        if (off_f >= 0) reinterpret_cast<double *>(rec + off_f)[d] = f[(size_t)d * n + i];
+    }
+}
+
 // SoA -> [count][fields][3] packed doubles
 __global__ void pack_kernel(double *__restrict__ out, int count, int first, int n, const double *x,
                             const double *v, const double *f, const double *f2, int nf) {
@@ -448,9 +463,19 @@ int launch_reduce(tcp_ctx *c, int mask, int pass) {
     return TCP_OK;
 }
 
-int launch_extract(tcp_ctx *c, int first, int count, long stride, long off_x, long off_v, long off_f) {
-    extract_kernel<<<nblocks(count), kIntThreads, 0, c->stream>>>(c->d_stage, stride, off_x, off_v, off_f, count,
+int launch_extract(tcp_ctx *c, const unsigned char *src, int first, int count, long stride, long off_x, long off_v,
+                   long off_f) {
+    extract_kernel<<<nblocks(count), kIntThreads, 0, c->stream>>>(src, stride, off_x, off_v, off_f, count,
                                                                   first, c->n, c->x, c->v, c->f);
+    c->launches++;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+int launch_scatter(tcp_ctx *c, unsigned char *dst, int first, int count, long stride, long off_x, long off_v,
+                   long off_f, const double *fsrc) {
+    scatter_kernel<<<nblocks(count), kIntThreads, 0, c->stream>>>(dst, stride, off_x, off_v, off_f, count, first,
+                                                                  c->n, c->x, c->v, fsrc);
     c->launches++;
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;

@@ -97,6 +97,9 @@ struct tcp_ctx {
     size_t d_stage_bytes = 0;
     double *h_stage = nullptr;          // pinned
     size_t h_stage_bytes = 0;
+    // the device reads and writes the caller's (pageable) host arrays directly:
+    // cudaDevAttrPageableMemoryAccess (coherent NVLink-C2C on Grace hosts)
+    bool host_direct = false;
     // SPME
     int K1 = 0, K2 = 0, K3 = 0, Kh = 0; // Kh = K1/2+1
     double *Q = nullptr;                // real mesh [K3][K2][K1]
@@ -198,7 +201,10 @@ int launch_fsum(tcp_ctx *c);
 int launch_remove_rigid(tcp_ctx *c);
 int launch_kick2(tcp_ctx *c, double dt, bool remove_net, bool apply_thermo, bool vdf, int *final_pass);
 int launch_reduce(tcp_ctx *c, int mask, int pass);
-int launch_extract(tcp_ctx *c, int first, int count, long stride, long off_x, long off_v, long off_f);
+int launch_extract(tcp_ctx *c, const unsigned char *src, int first, int count, long stride, long off_x, long off_v,
+                   long off_f);
+int launch_scatter(tcp_ctx *c, unsigned char *dst, int first, int count, long stride, long off_x, long off_v,
+                   long off_f, const double *fsrc);
 int launch_pack(tcp_ctx *c, int first, int count, bool x, bool v, bool f, bool frec, int *nf);
 int launch_fp32_peak(int device, double *tffma);
 

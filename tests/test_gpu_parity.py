@@ -211,6 +211,32 @@ def test_pt_roundtrip_and_stride():
     assert np.all(a["id"] == 7) and np.all(b["id"] == 9)     # other fields untouched
 
 
+@pytest.mark.parametrize("direct", ["1", "0"])
+def test_transfer_paths(direct, monkeypatch):
+    """PT records and (N, 3) arrays through both transfer paths: the device
+    reading / writing the caller's host arrays in place (where the device can
+    address pageable memory) and the staged copies (TCP_HOST_DIRECT=0)."""
+    monkeypatch.setenv("TCP_HOST_DIRECT", direct)
+    s = make(300, seed=15, K=16)
+    qel, qion = s.to_pt()
+    qel["ff"] = np.random.default_rng(3).normal(size=(s.nel, 3))
+    qion["ff"] = np.random.default_rng(4).normal(size=(s.nion, 3))
+    p = T.params_for(s, precision="fp64", recip="spme")
+    with T.Context(p, s.nel, s.nion) as c:
+        c.upload_pt(qel, qion)
+        a, b = np.zeros_like(qel), np.zeros_like(qion)
+        a["id"], b["id"] = 5, 6
+        c.download_pt(a, b)
+        x, v, f, _ = c.download(x=True, v=True, f=True)
+        c.upload(x=x[::-1].copy(), v=None, f=f * 2)
+        x2, v2, f2, _ = c.download(x=True, v=True, f=True)
+    for k in ("xx", "xv", "ff"):
+        assert np.array_equal(a[k], qel[k]) and np.array_equal(b[k], qion[k])
+    assert np.all(a["id"] == 5) and np.all(b["id"] == 6)
+    assert np.array_equal(x, s.x) and np.array_equal(v, s.v)
+    assert np.array_equal(x2, s.x[::-1]) and np.array_equal(v2, s.v) and np.array_equal(f2, 2 * f)
+
+
 def test_errors():
     s = make(64, seed=14, K=16)
     p = T.params_for(s, precision="fp64", recip="spme")
