@@ -243,7 +243,142 @@ __device__ __forceinline__ void n3_item(const PairConsts &c, const int4 *__restr
     }
 }
 
-template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH>
+// ---- paired FP32 (f32x2) form -------------------------------------------------
+// The same pair arithmetic on two pairs per instruction with Blackwell's
+// packed FP32 operations (__ffma2_rn / __fmul2_rn / __fadd2_rn, one issue slot
+// for two lanes of work): the R i-particles of a lane form R/2 pairs (i_2g,
+// i_2g+1) that share every FP32 step; the SFU operations, the int -> float
+// conversions, compares and selects stay scalar.  Results equal the scalar
+// form up to FMA contraction order (both are IEEE round-to-nearest per op).
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+
+// The coefficients as (c, c) pairs in constant memory, so the packed FMAs can
+// take them as 64-bit constant operands instead of register pairs.
+__constant__ float2 kErfcQ2[8] = {{6.807732388e-02f, 6.807732388e-02f},   {-3.663086635e-01f, -3.663086635e-01f},
+                                  {6.308091155e-01f, 6.308091155e-01f},   {-3.190751584e-01f, -3.190751584e-01f},
+                                  {3.760577549e-01f, 3.760577549e-01f},   {1.510029235e-01f, 1.510029235e-01f},
+                                  {2.343213173e-01f, 2.343213173e-01f},   {2.251152860e-01f, 2.251152860e-01f}};
+
+__device__ __forceinline__ float2 erfc_poly2(float2 t) {
+    float2 q = kErfcQ2[0];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) q = __ffma2_rn(q, t, kErfcQ2[k]);
+    return __fmul2_rn(q, t);
+}
+
+template <int KIND, bool ENERGY, bool MASKED>
+__device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, bool ok0, bool ok1, bool near_any,
+                                             float2 &pe) {
+    const float2 r2s = MASKED ? make_float2(ok0 ? r2.x : 1.0f, ok1 ? r2.y : 1.0f) : r2;
+    const float2 rinv = make_float2(rsqrt_approx(r2s.x), rsqrt_approx(r2s.y));
+    const float2 rinv_m = make_float2(ok0 ? rinv.x : 0.0f, ok1 ? rinv.y : 0.0f);
+    const float2 r = __fmul2_rn(r2s, rinv);
+    const float2 ta = __ffma2_rn(f2(c.u_p_alpha), r, f2(1.0f));
+    const float2 t = make_float2(rcp_approx(ta.x), rcp_approx(ta.y));
+    const float2 ea = __fmul2_rn(f2(c.u_c_exp), r2s);
+    const float2 e = make_float2(ex2_approx(ea.x), ex2_approx(ea.y));
+    const float2 er = __fmul2_rn(__fmul2_rn(e, erfc_poly2(t)), rinv_m);   // erfc(ar)/r
+    float2 s = __ffma2_rn(f2(c.u_c_gauss), e, er);
+    float2 u = er;
+    if (KIND == 1) {                                      // Deutsch, force.f90:136-139
+        const float2 ya = __fmul2_rn(f2(c.u_c_rs), r);
+        const float2 y = make_float2(ex2_approx(ya.x), ex2_approx(ya.y));   // exp(-r/rs)
+        s = __ffma2_rn(y, __ffma2_rn(rinv, f2(-1.0f), f2(-c.u_inv_rs)), s);
+        if (ENERGY) u = __ffma2_rn(y, __fmul2_rn(rinv_m, f2(-1.0f)), u);
+    }
+    if (KIND == 2 && near_any) {                          // Kelbg
+        const bool n0 = ok0 && (r2s.x < c.u_rshort2), n1 = ok1 && (r2s.y < c.u_rshort2);
+        const float2 ga = __fmul2_rn(f2(c.u_c_lam), r2s);
+        const float2 g = make_float2(n0 ? ex2_approx(ga.x) : 0.0f, n1 ? ex2_approx(ga.y) : 0.0f);
+        const float2 nrinv = __fmul2_rn(rinv, f2(-1.0f));
+        s = __ffma2_rn(g, nrinv, s);
+        if (ENERGY) {
+            const float2 t2a = __ffma2_rn(f2(c.u_p_lam), r, f2(1.0f));
+            const float2 t2 = make_float2(rcp_approx(t2a.x), rcp_approx(t2a.y));
+            const float2 erfc_rl = __fmul2_rn(g, erfc_poly2(t2));                 // erfc(r/lambda)
+            u = __fadd2_rn(u, __ffma2_rn(f2(c.u_sqrtpi_lam), erfc_rl, __fmul2_rn(g, nrinv)));
+        }
+    }
+    if (ENERGY) pe = __fadd2_rn(pe, u);
+    return __fmul2_rn(s, __fmul2_rn(rinv_m, rinv_m));
+}
+
+__device__ __forceinline__ float idiff(int a, int b) { return (float)(int)((unsigned)a - (unsigned)b); }
+
+template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R>
+__device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__restrict__ tj, int cnt, int jstart,
+                                           const int4 (&xi)[R], const int (&ii)[R], const bool (&vi)[R],
+                                           float (*sjacc)[3], float (&p)[R][3], float &pe) {
+    static_assert(R % 2 == 0, "paired form needs an even number of i-particles per lane");
+    constexpr int G = R / 2;
+    const int lane = threadIdx.x & 31;
+    const int src = (lane + 1) & 31;
+    float2 pg[G][3];
+    float2 pe2 = f2(0.0f);
+#pragma unroll
+    for (int g = 0; g < G; ++g) pg[g][0] = pg[g][1] = pg[g][2] = f2(0.0f);
+    for (int ch = 0; ch * 32 < cnt; ++ch) {
+        int4 xj = tj[ch * 32 + lane];
+        float2 jx = f2(0.0f), jy = f2(0.0f), jz = f2(0.0f);
+#pragma unroll UNROLL
+        for (int s = 0; s < 32; ++s) {
+            float2 d[G][3], r2[G];
+            bool ok[R];
+            float r2min = 3.0e38f;
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                d[g][0] = make_float2(idiff(xi[2 * g].x, xj.x), idiff(xi[2 * g + 1].x, xj.x));
+                d[g][1] = make_float2(idiff(xi[2 * g].y, xj.y), idiff(xi[2 * g + 1].y, xj.y));
+                d[g][2] = make_float2(idiff(xi[2 * g].z, xj.z), idiff(xi[2 * g + 1].z, xj.z));
+                r2[g] = __ffma2_rn(d[g][0], d[g][0], __ffma2_rn(d[g][1], d[g][1], __fmul2_rn(d[g][2], d[g][2])));
+                ok[2 * g] = r2[g].x < c.u_rc2;
+                ok[2 * g + 1] = r2[g].y < c.u_rc2;
+                if (MASKED) {
+                    const int jo = ch * 32 + ((lane + s) & 31);
+                    ok[2 * g] = ok[2 * g] && vi[2 * g] && (jo < cnt) && (ii[2 * g] < jstart + jo);
+                    ok[2 * g + 1] = ok[2 * g + 1] && vi[2 * g + 1] && (jo < cnt) && (ii[2 * g + 1] < jstart + jo);
+                }
+                if (KIND == 2) r2min = fminf(r2min, fminf(r2[g].x, r2[g].y));
+            }
+            bool near_any = false;
+            if (KIND == 2) near_any = __any_sync(0xffffffffu, r2min < c.u_rshort2);
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                const float2 w = n3_pair_x2<KIND, ENERGY, MASKED>(c, r2[g], ok[2 * g], ok[2 * g + 1], near_any, pe2);
+                pg[g][0] = __ffma2_rn(w, d[g][0], pg[g][0]);
+                pg[g][1] = __ffma2_rn(w, d[g][1], pg[g][1]);
+                pg[g][2] = __ffma2_rn(w, d[g][2], pg[g][2]);
+                jx = __ffma2_rn(w, d[g][0], jx);
+                jy = __ffma2_rn(w, d[g][1], jy);
+                jz = __ffma2_rn(w, d[g][2], jz);
+            }
+            // rotate j (position and both halves of the reaction) to the next lane
+            xj.x = __shfl_sync(0xffffffffu, xj.x, src);
+            xj.y = __shfl_sync(0xffffffffu, xj.y, src);
+            xj.z = __shfl_sync(0xffffffffu, xj.z, src);
+            jx.x = __shfl_sync(0xffffffffu, jx.x, src);
+            jx.y = __shfl_sync(0xffffffffu, jx.y, src);
+            jy.x = __shfl_sync(0xffffffffu, jy.x, src);
+            jy.y = __shfl_sync(0xffffffffu, jy.y, src);
+            jz.x = __shfl_sync(0xffffffffu, jz.x, src);
+            jz.y = __shfl_sync(0xffffffffu, jz.y, src);
+        }
+        float *q = sjacc[ch * 32 + lane];
+        atomicAdd(q + 0, jx.x + jx.y);
+        atomicAdd(q + 1, jy.x + jy.y);
+        atomicAdd(q + 2, jz.x + jz.y);
+    }
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {     // p is zero on entry
+            p[2 * g][k] = pg[g][k].x;
+            p[2 * g + 1][k] = pg[g][k].y;
+        }
+    pe = pe2.x + pe2.y;
+}
+
+template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH, bool X2 = false>
 __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args a) {
     constexpr int TILE = 32 * R * kN3Warps;
     constexpr int SPT = TILE / kN3Sub;
@@ -252,6 +387,9 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
     __shared__ float sjacc[kN3Sub][3];
     __shared__ double red[32];
     __shared__ long long s_next;
+    // per-thread TwoSum (hi, lo) i-force accumulators, touched once per item:
+    // kept in shared memory ([slot][thread], conflict-free) to free registers
+    __shared__ float sacc[2 * 3 * R][kN3Threads];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     const long long it0 = a.nstatic * (long long)blockIdx.x / gridDim.x;
@@ -284,26 +422,28 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
     int4 xi[R];
     int ii[R];
     bool vi[R];
-    float hi[R][3], lo[R][3];
     float eh = 0.f, el = 0.f;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         xi[r] = make_int4(0, 0, 0, 0);
         ii[r] = 0;
         vi[r] = false;
-        hi[r][0] = hi[r][1] = hi[r][2] = lo[r][0] = lo[r][1] = lo[r][2] = 0.f;
     }
+#pragma unroll
+    for (int q = 0; q < 6 * R; ++q) sacc[q][tid] = 0.f;   // slot 6r+2k: hi, 6r+2k+1: lo
 
     // i-forces of the current row to global memory (all threads, uniform)
     auto flush_i = [&]() {
         if (curI < 0) return;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            if (vi[r])
-                for (int k = 0; k < 3; ++k)
-                    atomicAdd(&a.facc[(size_t)k * a.ntot + ioff + ii[r]],
-                              kEps * ((double)hi[r][k] + (double)lo[r][k]));
-            hi[r][0] = hi[r][1] = hi[r][2] = lo[r][0] = lo[r][1] = lo[r][2] = 0.f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float &h = sacc[6 * r + 2 * k][tid], &l = sacc[6 * r + 2 * k + 1][tid];
+                if (vi[r]) atomicAdd(&a.facc[(size_t)k * a.ntot + ioff + ii[r]], kEps * ((double)h + (double)l));
+                h = 0.f;
+                l = 0.f;
+            }
         }
         if (ENERGY) {
             if (BATCH) {
@@ -345,8 +485,13 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
 #pragma unroll
         for (int r = 0; r < R; ++r) p[r][0] = p[r][1] = p[r][2] = 0.f;
         const int kind = pt == 1 ? (c.ei_model == TCP_EI_DEUTSCH ? 1 : (c.ei_model == TCP_EI_KELBG ? 2 : 0)) : 0;
-#define TCP_N3_ITEM(KIND, MASKED) \
-    n3_item<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ii, vi, sjacc, p, pe)
+#define TCP_N3_ITEM(KIND, MASKED)                                                                      \
+    do {                                                                                                \
+        if (X2)                                                                                         \
+            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ii, vi, sjacc, p, pe); \
+        else                                                                                            \
+            n3_item<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ii, vi, sjacc, p, pe);    \
+    } while (0)
         if (masked) {
             if (kind == 1) TCP_N3_ITEM(1, true);
             else if (kind == 2) TCP_N3_ITEM(2, true);
@@ -359,11 +504,14 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
 #undef TCP_N3_ITEM
         const float qf = c.u_qq_force[pt];
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            acc2(hi[r][0], lo[r][0], p[r][0] * qf);
-            acc2(hi[r][1], lo[r][1], p[r][1] * qf);
-            acc2(hi[r][2], lo[r][2], p[r][2] * qf);
-        }
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float h = sacc[6 * r + 2 * k][tid], l = sacc[6 * r + 2 * k + 1][tid];
+                acc2(h, l, p[r][k] * qf);
+                sacc[6 * r + 2 * k][tid] = h;
+                sacc[6 * r + 2 * k + 1][tid] = l;
+            }
         if (ENERGY) acc2(eh, el, pe * c.u_qq_energy[pt]);
         // all warps are done with this subtile and its reaction sums
         const bool timeout = __syncthreads_or(!ok);
@@ -447,6 +595,9 @@ static const N3Variant kVariants[] = {
     {pair_n3_kernel<true, 2, 1, 3, false>, pair_n3_kernel<false, 2, 1, 3, false>, 2, "n3_r2_u1_b3"},
     {pair_n3_kernel<true, 4, 1, 2, false>, pair_n3_kernel<false, 4, 1, 2, false>, 4, "n3_r4_u1_b2"},
     {pair_n3_kernel<true, 4, 2, 2, false>, pair_n3_kernel<false, 4, 2, 2, false>, 4, "n3_r4_u2_b2"},
+    {pair_n3_kernel<true, 4, 2, 2, false, true>, pair_n3_kernel<false, 4, 2, 2, false, true>, 4, "n3_r4_u2_b2_x2"},
+    {pair_n3_kernel<true, 4, 1, 2, false, true>, pair_n3_kernel<false, 4, 1, 2, false, true>, 4, "n3_r4_u1_b2_x2"},
+    {pair_n3_kernel<true, 2, 2, 3, false, true>, pair_n3_kernel<false, 2, 2, 3, false, true>, 2, "n3_r2_u2_b3_x2"},
 };
 constexpr int kN3Variants = sizeof(kVariants) / sizeof(kVariants[0]);
 
