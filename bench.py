@@ -308,7 +308,7 @@ def run_gpu(args, world, rank, local, dist):
     traffic = profile_traffic()
     roof = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "Top/s",
             "frac": achieved / peak, "traffic": traffic,
-            "kernel": kname, "autotune_ms": [round(x, 4) for x in variant_ms[:5].tolist()],
+            "kernel": kname, "autotune_ms": [round(x, 4) for x in variant_ms.tolist() if x > 0],
             "recipe": f"{recipe} FP32/ALU-pipe ops + {RECIPE_SFU_OPS} SFU ops per {runit}",
             "peak_source": "measured FFMA issue rate (tcp_fp32_peak) on this GPU, not MEASURED_PEAKS.json "
                            "(which has HBM and bf16 only)",

@@ -40,7 +40,8 @@ static int validate(const tcp_params *p, int nel, int nion) {
     if (p->reciprocal == TCP_RECIP_SPME) {
         if (p->order < 4 || p->order > kMaxOrder) return set_error(TCP_ERR_BAD_PARAM, "SPME order must be in 4..8");
         for (int d = 0; d < 3; ++d)
-            if (p->K[d] < p->order) return set_error(TCP_ERR_BAD_PARAM, "SPME mesh must be >= order in every dimension");
+            if (p->K[d] < p->order || p->K[d] > 1024)
+                return set_error(TCP_ERR_BAD_PARAM, "SPME mesh must be in [order, 1024] in every dimension");
     }
     if (p->reciprocal == TCP_RECIP_EWALD && p->ewald_nmax2 < 0) return set_error(TCP_ERR_BAD_PARAM, "ewald_nmax2 < 0");
     if (p->thermo < TCP_THERMO_NOTEMP || p->thermo > TCP_THERMO_STOCH) return set_error(TCP_ERR_BAD_PARAM, "unknown thermo");

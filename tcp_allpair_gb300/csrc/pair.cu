@@ -877,7 +877,7 @@ static int cache_lookup(const char *path, const std::string &key) {
 int autotune_pair(tcp_ctx *c) {
     if (c->p.precision != TCP_PREC_FP32C || c->tuned) return TCP_OK;
     c->tuned = true;
-    const int nv = c->pc.cubic ? n3_variant_count() : 0;
+    const int nv = c->pc.cubic ? std::min(n3_variant_count(), 15) : 0;
     c->pair_variant = c->pc.cubic ? 1 : 0;
     if (const char *forced = getenv("TCP_PAIR_VARIANT")) {
         c->pair_variant = std::min(std::max(atoi(forced), 0), nv);
@@ -937,6 +937,6 @@ extern "C" int tcp_autotune_report(tcp_ctx *c, int *variant, double *ms, int nma
     using namespace tcp;
     if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
     if (variant) *variant = c->pair_variant;
-    for (int k = 0; ms && k < nmax && k < 8; ++k) ms[k] = c->pair_variant_ms[k];
+    for (int k = 0; ms && k < nmax && k < 16; ++k) ms[k] = c->pair_variant_ms[k];
     return TCP_OK;
 }

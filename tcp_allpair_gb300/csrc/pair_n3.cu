@@ -266,7 +266,21 @@ __device__ __forceinline__ float2 erfc_poly2(float2 t) {
     return __fmul2_rn(q, t);
 }
 
-template <int KIND, bool ENERGY, bool MASKED>
+// Estrin's scheme for the same polynomial: 2 more operations, dependency
+// depth 4 instead of 8 (kErfcQ2[k] holds the coefficient of t^(7-k)).
+__device__ __forceinline__ float2 erfc_poly2_estrin(float2 t) {
+    const float2 t2 = __fmul2_rn(t, t);
+    const float2 t4 = __fmul2_rn(t2, t2);
+    const float2 a0 = __ffma2_rn(kErfcQ2[6], t, kErfcQ2[7]);
+    const float2 a1 = __ffma2_rn(kErfcQ2[4], t, kErfcQ2[5]);
+    const float2 a2 = __ffma2_rn(kErfcQ2[2], t, kErfcQ2[3]);
+    const float2 a3 = __ffma2_rn(kErfcQ2[0], t, kErfcQ2[1]);
+    const float2 b0 = __ffma2_rn(a1, t2, a0);
+    const float2 b1 = __ffma2_rn(a3, t2, a2);
+    return __fmul2_rn(__ffma2_rn(b1, t4, b0), t);
+}
+
+template <int KIND, bool ENERGY, bool MASKED, bool EST>
 __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, bool ok0, bool ok1, bool near_any,
                                              float2 &pe) {
     const float2 r2s = MASKED ? make_float2(ok0 ? r2.x : 1.0f, ok1 ? r2.y : 1.0f) : r2;
@@ -277,7 +291,7 @@ __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, boo
     const float2 t = make_float2(rcp_approx(ta.x), rcp_approx(ta.y));
     const float2 ea = __fmul2_rn(f2(c.u_c_exp), r2s);
     const float2 e = make_float2(ex2_approx(ea.x), ex2_approx(ea.y));
-    const float2 er = __fmul2_rn(__fmul2_rn(e, erfc_poly2(t)), rinv_m);   // erfc(ar)/r
+    const float2 er = __fmul2_rn(__fmul2_rn(e, EST ? erfc_poly2_estrin(t) : erfc_poly2(t)), rinv_m);   // erfc(ar)/r
     float2 s = __ffma2_rn(f2(c.u_c_gauss), e, er);
     float2 u = er;
     if (KIND == 1) {                                      // Deutsch, force.f90:136-139
@@ -295,7 +309,7 @@ __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, boo
         if (ENERGY) {
             const float2 t2a = __ffma2_rn(f2(c.u_p_lam), r, f2(1.0f));
             const float2 t2 = make_float2(rcp_approx(t2a.x), rcp_approx(t2a.y));
-            const float2 erfc_rl = __fmul2_rn(g, erfc_poly2(t2));                 // erfc(r/lambda)
+            const float2 erfc_rl = __fmul2_rn(g, EST ? erfc_poly2_estrin(t2) : erfc_poly2(t2));   // erfc(r/lambda)
             u = __fadd2_rn(u, __ffma2_rn(f2(c.u_sqrtpi_lam), erfc_rl, __fmul2_rn(g, nrinv)));
         }
     }
@@ -305,7 +319,7 @@ __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, boo
 
 __device__ __forceinline__ float idiff(int a, int b) { return (float)(int)((unsigned)a - (unsigned)b); }
 
-template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R>
+template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R, bool EST>
 __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__restrict__ tj, int cnt, int jstart,
                                            const int4 (&xi)[R], const int (&ii)[R], const bool (&vi)[R],
                                            float (*sjacc)[3], float (&p)[R][3], float &pe) {
@@ -344,7 +358,7 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
             if (KIND == 2) near_any = __any_sync(0xffffffffu, r2min < c.u_rshort2);
 #pragma unroll
             for (int g = 0; g < G; ++g) {
-                const float2 w = n3_pair_x2<KIND, ENERGY, MASKED>(c, r2[g], ok[2 * g], ok[2 * g + 1], near_any, pe2);
+                const float2 w = n3_pair_x2<KIND, ENERGY, MASKED, EST>(c, r2[g], ok[2 * g], ok[2 * g + 1], near_any, pe2);
                 pg[g][0] = __ffma2_rn(w, d[g][0], pg[g][0]);
                 pg[g][1] = __ffma2_rn(w, d[g][1], pg[g][1]);
                 pg[g][2] = __ffma2_rn(w, d[g][2], pg[g][2]);
@@ -378,8 +392,12 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
     pe = pe2.x + pe2.y;
 }
 
-template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH, bool X2 = false>
+// MODE 0: scalar FP32, i-force accumulators in registers; 1: packed FP32x2
+// (Horner erfc), accumulators in shared memory; 2: as 1 with Estrin's erfc.
+template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH, int MODE = 0>
 __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args a) {
+    constexpr bool X2 = MODE >= 1;
+    constexpr bool SACC = MODE >= 1;
     constexpr int TILE = 32 * R * kN3Warps;
     constexpr int SPT = TILE / kN3Sub;
     __shared__ __align__(128) int4 tiles[kN3Stages][kN3Sub];
@@ -388,8 +406,10 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
     __shared__ double red[32];
     __shared__ long long s_next;
     // per-thread TwoSum (hi, lo) i-force accumulators, touched once per item:
-    // kept in shared memory ([slot][thread], conflict-free) to free registers
-    __shared__ float sacc[2 * 3 * R][kN3Threads];
+    // in shared memory ([slot][thread], conflict-free) for the packed forms,
+    // whose constant pairs need the registers
+    __shared__ float sacc[SACC ? 2 * 3 * R : 1][SACC ? kN3Threads : 1];
+    float hi[SACC ? 1 : R][3], lo[SACC ? 1 : R][3];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     const long long it0 = a.nstatic * (long long)blockIdx.x / gridDim.x;
@@ -429,8 +449,13 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
         ii[r] = 0;
         vi[r] = false;
     }
+    if constexpr (SACC) {
 #pragma unroll
-    for (int q = 0; q < 6 * R; ++q) sacc[q][tid] = 0.f;   // slot 6r+2k: hi, 6r+2k+1: lo
+        for (int q = 0; q < 6 * R; ++q) sacc[q][tid] = 0.f;   // slot 6r+2k: hi, 6r+2k+1: lo
+    } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) hi[r][0] = hi[r][1] = hi[r][2] = lo[r][0] = lo[r][1] = lo[r][2] = 0.f;
+    }
 
     // i-forces of the current row to global memory (all threads, uniform)
     auto flush_i = [&]() {
@@ -439,7 +464,8 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
         for (int r = 0; r < R; ++r) {
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                float &h = sacc[6 * r + 2 * k][tid], &l = sacc[6 * r + 2 * k + 1][tid];
+                float &h = SACC ? sacc[6 * r + 2 * k][tid] : hi[SACC ? 0 : r][k];
+                float &l = SACC ? sacc[6 * r + 2 * k + 1][tid] : lo[SACC ? 0 : r][k];
                 if (vi[r]) atomicAdd(&a.facc[(size_t)k * a.ntot + ioff + ii[r]], kEps * ((double)h + (double)l));
                 h = 0.f;
                 l = 0.f;
@@ -488,7 +514,7 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
 #define TCP_N3_ITEM(KIND, MASKED)                                                                      \
     do {                                                                                                \
         if (X2)                                                                                         \
-            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ii, vi, sjacc, p, pe); \
+            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R, MODE == 2>(c, tiles[stage], cnt, jstart, xi, ii, vi, sjacc, p, pe); \
         else                                                                                            \
             n3_item<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ii, vi, sjacc, p, pe);    \
     } while (0)
@@ -507,10 +533,14 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
         for (int r = 0; r < R; ++r)
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                float h = sacc[6 * r + 2 * k][tid], l = sacc[6 * r + 2 * k + 1][tid];
-                acc2(h, l, p[r][k] * qf);
-                sacc[6 * r + 2 * k][tid] = h;
-                sacc[6 * r + 2 * k + 1][tid] = l;
+                if constexpr (SACC) {
+                    float h = sacc[6 * r + 2 * k][tid], l = sacc[6 * r + 2 * k + 1][tid];
+                    acc2(h, l, p[r][k] * qf);
+                    sacc[6 * r + 2 * k][tid] = h;
+                    sacc[6 * r + 2 * k + 1][tid] = l;
+                } else {
+                    acc2(hi[r][k], lo[r][k], p[r][k] * qf);
+                }
             }
         if (ENERGY) acc2(eh, el, pe * c.u_qq_energy[pt]);
         // all warps are done with this subtile and its reaction sums
@@ -595,9 +625,11 @@ static const N3Variant kVariants[] = {
     {pair_n3_kernel<true, 2, 1, 3, false>, pair_n3_kernel<false, 2, 1, 3, false>, 2, "n3_r2_u1_b3"},
     {pair_n3_kernel<true, 4, 1, 2, false>, pair_n3_kernel<false, 4, 1, 2, false>, 4, "n3_r4_u1_b2"},
     {pair_n3_kernel<true, 4, 2, 2, false>, pair_n3_kernel<false, 4, 2, 2, false>, 4, "n3_r4_u2_b2"},
-    {pair_n3_kernel<true, 4, 2, 2, false, true>, pair_n3_kernel<false, 4, 2, 2, false, true>, 4, "n3_r4_u2_b2_x2"},
-    {pair_n3_kernel<true, 4, 1, 2, false, true>, pair_n3_kernel<false, 4, 1, 2, false, true>, 4, "n3_r4_u1_b2_x2"},
-    {pair_n3_kernel<true, 2, 2, 3, false, true>, pair_n3_kernel<false, 2, 2, 3, false, true>, 2, "n3_r2_u2_b3_x2"},
+    {pair_n3_kernel<true, 4, 2, 2, false, 1>, pair_n3_kernel<false, 4, 2, 2, false, 1>, 4, "n3_r4_u2_b2_x2"},
+    {pair_n3_kernel<true, 4, 1, 2, false, 1>, pair_n3_kernel<false, 4, 1, 2, false, 1>, 4, "n3_r4_u1_b2_x2"},
+    {pair_n3_kernel<true, 2, 2, 3, false, 1>, pair_n3_kernel<false, 2, 2, 3, false, 1>, 2, "n3_r2_u2_b3_x2"},
+    {pair_n3_kernel<true, 4, 1, 2, false, 2>, pair_n3_kernel<false, 4, 1, 2, false, 2>, 4, "n3_r4_u1_b2_x2e"},
+    {pair_n3_kernel<true, 4, 1, 3, false, 1>, pair_n3_kernel<false, 4, 1, 3, false, 1>, 4, "n3_r4_u1_b3_x2"},
 };
 constexpr int kN3Variants = sizeof(kVariants) / sizeof(kVariants[0]);
 

@@ -3,13 +3,14 @@
 //
 // Mesh layout: Q[iz][iy][ix] (ix fastest, the Fortran order of Q(ix,iy,iz)),
 // FP64.  The 3-D FFT is cuFFT D2Z / Z2D on that layout (the only library
-// call of the path); spreading, the influence-function multiply fused with
-// the energy reduction, and the force gather are kernels of this file.
+// call of the path); spreading (atomic-free, one CTA per mesh brick), the
+// influence-function multiply fused with the energy reduction, and the force
+// gather are kernels of this file.
 // In the compensated-FP32 mode the charges are still accumulated in FP64
-// (the structure-factor accumulation) and the mesh is then rounded to FP32
-// for R2C / C2R transforms, the influence multiply (energy summed in FP64)
-// and the force gather: on GB300 FP64 runs at 1/64 of the FP32 rate, which
-// makes a 128^3 FP64 transform compute-bound.
+// (the structure-factor accumulation) and each mesh point is rounded to FP32
+// when its brick is written, for R2C / C2R transforms, the influence multiply
+// (energy summed in FP64) and the force gather: on GB300 FP64 runs at 1/64 of
+// the FP32 rate, which makes a 128^3 FP64 transform compute-bound.
 //
 // Normalisation: both transforms are unnormalised, so the real mesh after the
 // inverse transform is phi = K^3 Qfin of the reference; its 1/K^3 (FFTE
@@ -34,33 +35,146 @@ struct SpmeArgs {
     int K1, K2, K3;
 };
 
-// charge spreading, force.f90:697-820 (atomic FP64 adds into the mesh)
+// ---- atomic-free charge spreading ---------------------------------------------
+// The mesh is cut into bricks of kBrick^3 points, one CTA per brick.  A
+// particle's support is the P^3 points from its base index b = INT(u)-(P-3)
+// (force.f90:742-744), so it reaches a brick [o, o + kBrick) in a dimension
+// iff (b - (o - P + 1)) mod K < kBrick + P - 1.  spme_cells_kernel packs the
+// wrapped base of every particle (10 bits per dimension); each brick CTA scans
+// the packed bases, keeps the particles that reach it in per-warp lists
+// (ballot order), stages their weights in shared memory and sums them per
+// (y, z) row in registers: thread (ty, tz) owns the kBrick points of one row.
+// No atomics; every mesh point is summed in the same order on every run.
+constexpr int kBrick = 16;
+constexpr int kBrickThreads = kBrick * kBrick;
+constexpr int kBrickWarps = kBrickThreads / 32;
+constexpr int kCandPerWarp = 256;
+constexpr int kScanIters = 4;        // scan iterations per warp between flush checks
+constexpr int kStageW = 64;          // candidates whose weights are staged at a time
+
 template <int P>
-__global__ void spme_spread_kernel(const SpmeArgs a, double *__restrict__ Q) {
+__global__ void spme_cells_kernel(const SpmeArgs a, unsigned *__restrict__ cell) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= a.n) return;
-    const double q = m < a.nel ? a.q0 : a.q1;
     const double L[3] = {a.box0, a.box1, a.box2};
     const int K[3] = {a.K1, a.K2, a.K3};
-    double W[3][P], dW[3][P];
-    int base[3];
+    unsigned packed = 0;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];   // :700-702
-        spline_w<P, double>(u, W[d], dW[d]);
-        base[d] = (int)trunc(u) - (P - 3);
+        packed |= (unsigned)wrapi((int)trunc(u) - (P - 3), K[d]) << (10 * d);
     }
-#pragma unroll 1
-    for (int k = 0; k < P; ++k) {
-        const int iz = wrapi(base[2] + k, a.K3);
-#pragma unroll 1
-        for (int j = 0; j < P; ++j) {
-            const int iy = wrapi(base[1] + j, a.K2);
-            const double qyz = q * W[1][j] * W[2][k];
-            double *row = Q + (size_t)a.K1 * (iy + (size_t)a.K2 * iz);
+    cell[m] = packed;
+}
+
+__device__ __forceinline__ bool reaches(int b, int lo, int span, int K) {
+    int t = b - lo;
+    t += t < 0 ? K : 0;
+    return t < span;
+}
+
+template <int P, bool F32OUT>
+__global__ void __launch_bounds__(kBrickThreads) spme_brick_spread_kernel(const SpmeArgs a,
+                                                                          const unsigned *__restrict__ cell,
+                                                                          double *__restrict__ Q,
+                                                                          float *__restrict__ Qf) {
+    __shared__ int cand[kBrickWarps][kCandPerWarp];
+    __shared__ int woff[kBrickWarps + 1];
+    __shared__ int wcnt[kBrickWarps];
+    __shared__ double sw[kStageW][3][P];
+    __shared__ double sq[kStageW];
+    __shared__ int sb[kStageW][3];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int x0 = blockIdx.x * kBrick, y0 = blockIdx.y * kBrick, z0 = blockIdx.z * kBrick;
+    const int y = y0 + tid % kBrick, z = z0 + tid / kBrick;
+    const bool row = y < a.K2 && z < a.K3;
+    const int lox = wrapi(x0 - P + 1, a.K1), loy = wrapi(y0 - P + 1, a.K2), loz = wrapi(z0 - P + 1, a.K3);
+    const int spx = min(kBrick + P - 1, a.K1), spy = min(kBrick + P - 1, a.K2), spz = min(kBrick + P - 1, a.K3);
+    double acc[kBrick];
 #pragma unroll
-            for (int i = 0; i < P; ++i) atomicAdd(row + wrapi(base[0] + i, a.K1), qyz * W[0][i]);
+    for (int k = 0; k < kBrick; ++k) acc[k] = 0.0;
+    int cnt = 0;                                   // this warp's list length (warp-uniform)
+
+    auto flush = [&]() {
+        if (lane == 0) wcnt[warp] = cnt;
+        __syncthreads();
+        if (tid == 0) {
+            woff[0] = 0;
+            for (int w = 0; w < kBrickWarps; ++w) woff[w + 1] = woff[w] + wcnt[w];
         }
+        __syncthreads();
+        const int total = woff[kBrickWarps];
+        for (int c0 = 0; c0 < total; c0 += kStageW) {
+            if (tid < kStageW && c0 + tid < total) {
+                const int c = c0 + tid;
+                int w = 0;
+                while (c >= woff[w + 1]) ++w;
+                const int m = cand[w][c - woff[w]];
+                const double L[3] = {a.box0, a.box1, a.box2};
+                const int K[3] = {a.K1, a.K2, a.K3};
+                double W[P], dW[P];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];
+                    spline_w<P, double>(u, W, dW);
+#pragma unroll
+                    for (int j = 0; j < P; ++j) sw[tid][d][j] = W[j];
+                    sb[tid][d] = wrapi((int)trunc(u) - (P - 3), K[d]);
+                }
+                sq[tid] = m < a.nel ? a.q0 : a.q1;
+            }
+            __syncthreads();
+            const int nb = min(kStageW, total - c0);
+            if (row) {
+                for (int c = 0; c < nb; ++c) {
+                    int ry = y - sb[c][1];
+                    ry += ry < 0 ? a.K2 : 0;
+                    int rz = z - sb[c][2];
+                    rz += rz < 0 ? a.K3 : 0;
+                    if (ry < P && rz < P) {
+                        const double wyz = sq[c] * sw[c][1][ry] * sw[c][2][rz];
+                        const int rx0 = x0 - sb[c][0];
+#pragma unroll
+                        for (int k = 0; k < kBrick; ++k) {
+                            int rx = rx0 + k;
+                            rx += rx < 0 ? a.K1 : 0;
+                            rx -= rx >= a.K1 ? a.K1 : 0;
+                            if (rx < P) acc[k] = fma(wyz, sw[c][0][rx], acc[k]);
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        cnt = 0;
+    };
+
+    for (int i0 = 0; i0 < a.n; i0 += kBrickThreads * kScanIters) {
+#pragma unroll
+        for (int it = 0; it < kScanIters; ++it) {
+            const int i = i0 + it * kBrickThreads + tid;
+            bool hit = false;
+            if (i < a.n) {
+                const unsigned cq = cell[i];
+                hit = reaches((int)(cq & 1023u), lox, spx, a.K1) && reaches((int)((cq >> 10) & 1023u), loy, spy, a.K2) &&
+                      reaches((int)(cq >> 20), loz, spz, a.K3);
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, hit);
+            if (hit) cand[warp][cnt + __popc(bal & ((1u << lane) - 1u))] = i;
+            cnt += __popc(bal);
+        }
+        // a warp adds at most 32 * kScanIters candidates per round
+        if (__syncthreads_or(cnt > kCandPerWarp - 32 * kScanIters)) flush();
+    }
+    flush();
+    if (row) {
+        const size_t ro = (size_t)a.K1 * (y + (size_t)a.K2 * z);
+#pragma unroll
+        for (int k = 0; k < kBrick; ++k)
+            if (x0 + k < a.K1) {
+                if (F32OUT) Qf[ro + x0 + k] = (float)acc[k];
+                else Q[ro + x0 + k] = acc[k];
+            }
     }
 }
 
@@ -130,12 +244,6 @@ __global__ void spme_gather_kernel(const SpmeArgs a, const T *__restrict__ phi, 
     frec[m] = -coef * q * (double)gx * ((double)a.K1 / a.box0);
     frec[(size_t)a.n + m] = -coef * q * (double)gy * ((double)a.K2 / a.box1);
     frec[2 * (size_t)a.n + m] = -coef * q * (double)gz * ((double)a.K3 / a.box2);
-}
-
-// FP32C mode: the FP64 charge mesh rounded to FP32 for the transforms
-__global__ void mesh_to_float_kernel(const double *__restrict__ q, float *__restrict__ qf, long n) {
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        qf[i] = (float)q[i];
 }
 
 // FP32C influence multiply; the energy sum is kept in FP64
@@ -255,6 +363,8 @@ int spme_free(tcp_ctx *c) {
         cufftDestroy(c->plan_b);
         c->plans = false;
     }
+    cudaFree(c->spme_cell);
+    c->spme_cell = nullptr;
     cudaFree(c->Q);
     cudaFree(c->Qk);
     cudaFree(c->infl);
@@ -285,7 +395,8 @@ int spme_setup(tcp_ctx *c) {
     const size_t nhalf = (size_t)c->Kh * c->K2 * c->K3;
     c->spme_fp32 = c->p.precision == TCP_PREC_FP32C;
     if (!c->Q) {
-        if (cudaMalloc(&c->Q, sizeof(double) * nreal) != cudaSuccess ||
+        if (cudaMalloc(&c->spme_cell, sizeof(unsigned) * (size_t)c->n) != cudaSuccess ||
+            cudaMalloc(&c->Q, sizeof(double) * nreal) != cudaSuccess ||
             cudaMalloc(&c->Qk, sizeof(cufftDoubleComplex) * nhalf) != cudaSuccess ||
             cudaMalloc(&c->infl, sizeof(double) * nhalf) != cudaSuccess)
             return set_error(TCP_ERR_NOMEM, "SPME mesh allocation failed");
@@ -356,24 +467,44 @@ static SpmeArgs spme_args(const tcp_ctx *c) {
     return a;
 }
 
+// atomic-free spread into Q (FP64) or straight into Qf (FP32C mode: the FP64
+// sums are rounded once, when the brick is written)
 template <int P>
-static void launch_spread_gather(tcp_ctx *c, const SpmeArgs &a, bool gather, double coef) {
+static void launch_brick_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Qf) {
     const int threads = 128, blocks = (c->n + threads - 1) / threads;
-    if (!gather)
-        spme_spread_kernel<P><<<blocks, threads, 0, c->stream>>>(a, c->Q);
-    else if (c->spme_fp32)
+    spme_cells_kernel<P><<<blocks, threads, 0, c->stream>>>(a, c->spme_cell);
+    const dim3 grid((c->K1 + kBrick - 1) / kBrick, (c->K2 + kBrick - 1) / kBrick, (c->K3 + kBrick - 1) / kBrick);
+    if (Qf) spme_brick_spread_kernel<P, true><<<grid, kBrickThreads, 0, c->stream>>>(a, c->spme_cell, nullptr, Qf);
+    else spme_brick_spread_kernel<P, false><<<grid, kBrickThreads, 0, c->stream>>>(a, c->spme_cell, Q, nullptr);
+    c->launches += 2;
+}
+
+static void brick_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Qf) {
+    switch (c->p.order) {
+        case 4: launch_brick_spread<4>(c, a, Q, Qf); break;
+        case 5: launch_brick_spread<5>(c, a, Q, Qf); break;
+        case 6: launch_brick_spread<6>(c, a, Q, Qf); break;
+        case 7: launch_brick_spread<7>(c, a, Q, Qf); break;
+        default: launch_brick_spread<8>(c, a, Q, Qf); break;
+    }
+}
+
+template <int P>
+static void launch_gather(tcp_ctx *c, const SpmeArgs &a, double coef) {
+    const int threads = 128, blocks = (c->n + threads - 1) / threads;
+    if (c->spme_fp32)
         spme_gather_kernel<P, float><<<blocks, threads, 0, c->stream>>>(a, c->Qf, coef, c->frec);
     else
         spme_gather_kernel<P, double><<<blocks, threads, 0, c->stream>>>(a, c->Q, coef, c->frec);
 }
 
-static void spread_gather(tcp_ctx *c, const SpmeArgs &a, bool gather, double coef) {
+static void gather(tcp_ctx *c, const SpmeArgs &a, double coef) {
     switch (c->p.order) {
-        case 4: launch_spread_gather<4>(c, a, gather, coef); break;
-        case 5: launch_spread_gather<5>(c, a, gather, coef); break;
-        case 6: launch_spread_gather<6>(c, a, gather, coef); break;
-        case 7: launch_spread_gather<7>(c, a, gather, coef); break;
-        default: launch_spread_gather<8>(c, a, gather, coef); break;
+        case 4: launch_gather<4>(c, a, coef); break;
+        case 5: launch_gather<5>(c, a, coef); break;
+        case 6: launch_gather<6>(c, a, coef); break;
+        case 7: launch_gather<7>(c, a, coef); break;
+        default: launch_gather<8>(c, a, coef); break;
     }
 }
 
@@ -382,16 +513,12 @@ double *recip_epart(tcp_ctx *c);
 
 int launch_spme(tcp_ctx *c, bool energy) {
     const SpmeArgs a = spme_args(c);
-    const size_t nreal = (size_t)c->K1 * c->K2 * c->K3;
-    TCP_CUDA(cudaMemsetAsync(c->Q, 0, sizeof(double) * nreal, c->stream));
-    spread_gather(c, a, false, 0.0);                       // FP64 charge accumulation
-    c->launches++;
+    // FP64 charge accumulation, atomic-free (every mesh point is written)
+    brick_spread(c, a, c->spme_fp32 ? nullptr : c->Q, c->spme_fp32 ? c->Qf : nullptr);
     const long total = (long)c->K3 * c->K2 * c->Kh;
     const int eb = spme_energy_blocks(c);
     double *epart = recip_epart(c);
     if (c->spme_fp32) {
-        mesh_to_float_kernel<<<std::min<long>((nreal + 255) / 256, 4096), 256, 0, c->stream>>>(c->Q, c->Qf, (long)nreal);
-        c->launches++;
         if (cufftExecR2C(c->plan_f, c->Qf, c->Qkf) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecR2C failed");
         spme_influence_f_kernel<<<eb, 256, 0, c->stream>>>(c->Qkf, c->infl_f, total, c->Kh, c->K1, epart, energy);
         c->launches++;
@@ -402,7 +529,7 @@ int launch_spme(tcp_ctx *c, bool energy) {
         c->launches++;
         if (cufftExecZ2D(c->plan_b, c->Qk, c->Q) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecZ2D failed");
     }
-    spread_gather(c, a, true, kEps / (kPi * c->V));
+    gather(c, a, kEps / (kPi * c->V));
     c->launches++;
     if (energy) {
         sum_partials_kernel<<<1, 1024, 0, c->stream>>>(epart, eb, kEps / (2.0 * kPi * c->V), c->scal + kScalUm);
@@ -569,7 +696,7 @@ __global__ void spme_gather_hvp_kernel(const SpmeArgs a, const double *__restric
 template <int P>
 static void launch_hvp_kernels(tcp_ctx *c, const SpmeArgs &a, const double *w, double *hw, int which) {
     const int threads = 128, blocks = (c->n + threads - 1) / threads;
-    if (which == 0) spme_spread_kernel<P><<<blocks, threads, 0, c->stream>>>(a, c->hQ);
+    if (which == 0) launch_brick_spread<P>(c, a, c->hQ, nullptr);
     else if (which == 1) spme_spread_dipole_kernel<P><<<blocks, threads, 0, c->stream>>>(a, w, c->hdQ);
     else spme_gather_hvp_kernel<P><<<blocks, threads, 0, c->stream>>>(a, c->hQ, c->hdQ, w, kEps / (kPi * c->V), hw);
 }
@@ -624,7 +751,7 @@ int launch_spme_hvp(tcp_ctx *c, const double *w, double *hw) {
     const int eb = spme_energy_blocks(c);
     double *mesh[2] = {c->hQ, c->hdQ};
     for (int pass = 0; pass < 2; ++pass) {    // phi = A Q, then dphi = A dQ
-        TCP_CUDA(cudaMemsetAsync(mesh[pass], 0, sizeof(double) * nreal, c->stream));
+        if (pass == 1) TCP_CUDA(cudaMemsetAsync(mesh[pass], 0, sizeof(double) * nreal, c->stream));
         hvp_kernels(c, a, w, hw, pass);
         if (cufftExecD2Z(c->hplan_f, mesh[pass], c->hQk) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecD2Z failed");
         spme_influence_kernel<<<eb, 256, 0, c->stream>>>(c->hQk, c->infl, total, c->Kh, c->K1, nullptr, false);

@@ -79,7 +79,7 @@ struct tcp_ctx {
     int fpart_splits = 1;      // splits written by the last pair launch
     int pair_variant = 1;      // FP32C real-space kernel: 0 ordered pairs, >= 1 Newton-3 variant
     bool tuned = false;        // autotuner ran for the current parameters
-    double pair_variant_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // autotuner timings
+    double pair_variant_ms[16] = {};   // autotuner timings per variant
     double *fpart = nullptr;   // [jsplit][3][n]
     double *upart = nullptr;   // energy partial per pair block
     int n_upart = 0;
@@ -102,6 +102,7 @@ struct tcp_ctx {
     bool host_direct = false;
     // SPME
     int K1 = 0, K2 = 0, K3 = 0, Kh = 0; // Kh = K1/2+1
+    unsigned *spme_cell = nullptr;      // packed spline base index per particle (atomic-free spread)
     double *Q = nullptr;                // real mesh [K3][K2][K1]
     cufftDoubleComplex *Qk = nullptr;   // [K3][K2][Kh]
     double *infl = nullptr;             // theta * |b|^-2 on the half mesh
