@@ -372,6 +372,23 @@ def run_pair_only(args):
     return 0
 
 
+def run_recip_only(args):
+    """Launch the SPME chain alone on the headline system with N particles
+    (profiling target: `ncu -k regex:spme ... python bench.py --recip-only N`)."""
+    import tcp_allpair_gb300 as T
+    from tcp_allpair_gb300.system import make_config_system
+    s = make_config_system(WORKLOAD, n=args.recip_only)
+    p = T.params_for(s, precision=args.precision, ei="kelbg", recip="spme")
+    with T.Context(p, s.nel, s.nion) as c:
+        c.EWALD_SELF()
+        c.upload(x=s.x, v=s.v)
+        for _ in range(3):
+            c.Force_SPME4()
+        ms = c.time_component(1, 5)
+    print(json.dumps({"recip_only": args.recip_only, "precision": args.precision, "spme_ms": ms}))
+    return 0
+
+
 def run_batch(args):
     """The batched-replica workload: 64 independent systems (N log-uniform in
     [512, 8192], Gamma log-uniform in [0.1, 10], lambda uniform in [0.2a, 0.8a],
@@ -426,6 +443,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--ref-rows", type=int, default=4096)
     ap.add_argument("--pair-only", type=int, default=0, help="profile target: pair kernel alone at this N")
+    ap.add_argument("--recip-only", type=int, default=0, help="profile target: SPME chain alone at this N")
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--batch", action="store_true", help="batched-replica workload instead of the headline")
     ap.add_argument("--batch-reps", type=int, default=64)
@@ -434,6 +452,8 @@ def main():
         return run_batch(args)
     if args.pair_only:
         return run_pair_only(args)
+    if args.recip_only:
+        return run_recip_only(args)
     args.warmup = max(args.warmup, 3)
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":

@@ -38,19 +38,29 @@ struct SpmeArgs {
 // ---- atomic-free charge spreading ---------------------------------------------
 // The mesh is cut into bricks of kBrick^3 points, one CTA per brick.  A
 // particle's support is the P^3 points from its base index b = INT(u)-(P-3)
-// (force.f90:742-744), so it reaches a brick [o, o + kBrick) in a dimension
-// iff (b - (o - P + 1)) mod K < kBrick + P - 1.  spme_cells_kernel packs the
-// wrapped base of every particle (10 bits per dimension); each brick CTA scans
-// the packed bases, keeps the particles that reach it in per-warp lists
-// (ballot order), stages their weights in shared memory and sums them per
-// (y, z) row in registers: thread (ty, tz) owns the kBrick points of one row.
-// No atomics; every mesh point is summed in the same order on every run.
+// (force.f90:742-744), so it reaches a brick [o, o + w) in a dimension iff
+// (b - (o - P + 1)) mod K < w + P - 1.  spme_cells_kernel packs the wrapped
+// base of every particle (10 bits per dimension); each brick CTA scans the
+// packed bases and keeps the particles that reach it in per-warp lists
+// (ballot order: deterministic), stages their weights in shared memory and
+// adds them into a shared-memory copy of the brick.  Warp w owns the planes
+// z = w and w + 8 of the brick; for a particle, its lanes cover the P x P
+// support points of each owned plane, so no two lanes (and no two warps)
+// touch the same point: no atomics, and every mesh point is summed in the
+// same order on every run.  FP64 mode sums FP64 products in FP64; FP32C mode
+// sums FP32 products in compensated two-float FP32 (TwoSum hi/lo) and writes
+// the FP32 mesh the FP32 transforms read (GB300's FP64 rate is 1/64 of FP32).
 constexpr int kBrick = 16;
-constexpr int kBrickThreads = kBrick * kBrick;
+constexpr int kBrickThreads = 256;
 constexpr int kBrickWarps = kBrickThreads / 32;
-constexpr int kCandPerWarp = 256;
-constexpr int kScanIters = 4;        // scan iterations per warp between flush checks
-constexpr int kStageW = 64;          // candidates whose weights are staged at a time
+constexpr int kBrickRow = kBrick + 1;        // padded row (shared-memory banks)
+constexpr int kCandPerWarp = 128;
+constexpr int kScanIters = 2;                // scan iterations per warp between flush checks
+// candidates whose weights are staged at a time (static shared memory <= 48 KB)
+template <int P, typename T>
+struct StageWidth {
+    static constexpr int value = (sizeof(T) == 8 && P >= 6) ? 32 : 64;
+};
 
 template <int P>
 __global__ void spme_cells_kernel(const SpmeArgs a, unsigned *__restrict__ cell) {
@@ -73,26 +83,31 @@ __device__ __forceinline__ bool reaches(int b, int lo, int span, int K) {
     return t < span;
 }
 
-template <int P, bool F32OUT>
+// T = double: FP64 accumulation (hi only); T = float: TwoSum (hi, lo)
+template <int P, typename T>
 __global__ void __launch_bounds__(kBrickThreads) spme_brick_spread_kernel(const SpmeArgs a,
                                                                           const unsigned *__restrict__ cell,
                                                                           double *__restrict__ Q,
                                                                           float *__restrict__ Qf) {
+    constexpr bool F32 = sizeof(T) == 4;
+    constexpr int kStageW = StageWidth<P, T>::value;
+    __shared__ T bhi[kBrick][kBrick][kBrickRow];
+    __shared__ T blo[F32 ? kBrick : 1][F32 ? kBrick : 1][F32 ? kBrickRow : 1];
     __shared__ int cand[kBrickWarps][kCandPerWarp];
     __shared__ int woff[kBrickWarps + 1];
     __shared__ int wcnt[kBrickWarps];
-    __shared__ double sw[kStageW][3][P];
-    __shared__ double sq[kStageW];
+    __shared__ T sw[kStageW][3][P];
+    __shared__ T sq[kStageW];
     __shared__ int sb[kStageW][3];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int x0 = blockIdx.x * kBrick, y0 = blockIdx.y * kBrick, z0 = blockIdx.z * kBrick;
-    const int y = y0 + tid % kBrick, z = z0 + tid / kBrick;
-    const bool row = y < a.K2 && z < a.K3;
+    const int wx = min(kBrick, a.K1 - x0), wy = min(kBrick, a.K2 - y0), wz = min(kBrick, a.K3 - z0);
     const int lox = wrapi(x0 - P + 1, a.K1), loy = wrapi(y0 - P + 1, a.K2), loz = wrapi(z0 - P + 1, a.K3);
-    const int spx = min(kBrick + P - 1, a.K1), spy = min(kBrick + P - 1, a.K2), spz = min(kBrick + P - 1, a.K3);
-    double acc[kBrick];
-#pragma unroll
-    for (int k = 0; k < kBrick; ++k) acc[k] = 0.0;
+    const int spx = min(wx + P - 1, a.K1), spy = min(wy + P - 1, a.K2), spz = min(wz + P - 1, a.K3);
+    for (int k = tid; k < kBrick * kBrick * kBrickRow; k += kBrickThreads) {
+        (&bhi[0][0][0])[k] = (T)0;
+        if (F32) (&blo[0][0][0])[k] = (T)0;
+    }
     int cnt = 0;                                   // this warp's list length (warp-uniform)
 
     auto flush = [&]() {
@@ -112,34 +127,45 @@ __global__ void __launch_bounds__(kBrickThreads) spme_brick_spread_kernel(const 
                 const int m = cand[w][c - woff[w]];
                 const double L[3] = {a.box0, a.box1, a.box2};
                 const int K[3] = {a.K1, a.K2, a.K3};
-                double W[P], dW[P];
+                T W[P], dW[P];
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];
-                    spline_w<P, double>(u, W, dW);
+                    spline_w<P, T>(u, W, dW);
 #pragma unroll
                     for (int j = 0; j < P; ++j) sw[tid][d][j] = W[j];
                     sb[tid][d] = wrapi((int)trunc(u) - (P - 3), K[d]);
                 }
-                sq[tid] = m < a.nel ? a.q0 : a.q1;
+                sq[tid] = (T)(m < a.nel ? a.q0 : a.q1);
             }
             __syncthreads();
             const int nb = min(kStageW, total - c0);
-            if (row) {
-                for (int c = 0; c < nb; ++c) {
-                    int ry = y - sb[c][1];
-                    ry += ry < 0 ? a.K2 : 0;
-                    int rz = z - sb[c][2];
-                    rz += rz < 0 ? a.K3 : 0;
-                    if (ry < P && rz < P) {
-                        const double wyz = sq[c] * sw[c][1][ry] * sw[c][2][rz];
-                        const int rx0 = x0 - sb[c][0];
+            for (int c = 0; c < nb; ++c) {
 #pragma unroll
-                        for (int k = 0; k < kBrick; ++k) {
-                            int rx = rx0 + k;
-                            rx += rx < 0 ? a.K1 : 0;
-                            rx -= rx >= a.K1 ? a.K1 : 0;
-                            if (rx < P) acc[k] = fma(wyz, sw[c][0][rx], acc[k]);
+                for (int h = 0; h < 2; ++h) {
+                    const int zl = warp + kBrickWarps * h;
+                    if (zl >= wz) continue;
+                    int rz = z0 + zl - sb[c][2];
+                    rz += rz < 0 ? a.K3 : 0;
+                    if (rz >= P) continue;                        // warp-uniform
+                    const T wq = sq[c] * sw[c][2][rz];
+                    for (int l = lane; l < P * P; l += 32) {
+                        const int jy = l / P, jx = l - jy * P;
+                        int y = sb[c][1] + jy;
+                        y -= y >= a.K2 ? a.K2 : 0;
+                        int x = sb[c][0] + jx;
+                        x -= x >= a.K1 ? a.K1 : 0;
+                        const int yl = y - y0, xl = x - x0;
+                        if ((unsigned)yl < (unsigned)wy && (unsigned)xl < (unsigned)wx) {
+                            const T v = wq * sw[c][1][jy] * sw[c][0][jx];
+                            T &hi = bhi[zl][yl][xl];
+                            if (F32) {
+                                const T s = hi + v, bp = s - hi;
+                                blo[F32 ? zl : 0][F32 ? yl : 0][F32 ? xl : 0] += (hi - (s - bp)) + (v - bp);
+                                hi = s;
+                            } else {
+                                hi += v;
+                            }
                         }
                     }
                 }
@@ -156,8 +182,8 @@ __global__ void __launch_bounds__(kBrickThreads) spme_brick_spread_kernel(const 
             bool hit = false;
             if (i < a.n) {
                 const unsigned cq = cell[i];
-                hit = reaches((int)(cq & 1023u), lox, spx, a.K1) && reaches((int)((cq >> 10) & 1023u), loy, spy, a.K2) &&
-                      reaches((int)(cq >> 20), loz, spz, a.K3);
+                hit = reaches((int)((cq >> 20) & 1023u), loz, spz, a.K3) &&
+                      reaches((int)((cq >> 10) & 1023u), loy, spy, a.K2) && reaches((int)(cq & 1023u), lox, spx, a.K1);
             }
             const unsigned bal = __ballot_sync(0xffffffffu, hit);
             if (hit) cand[warp][cnt + __popc(bal & ((1u << lane) - 1u))] = i;
@@ -167,14 +193,14 @@ __global__ void __launch_bounds__(kBrickThreads) spme_brick_spread_kernel(const 
         if (__syncthreads_or(cnt > kCandPerWarp - 32 * kScanIters)) flush();
     }
     flush();
-    if (row) {
-        const size_t ro = (size_t)a.K1 * (y + (size_t)a.K2 * z);
-#pragma unroll
-        for (int k = 0; k < kBrick; ++k)
-            if (x0 + k < a.K1) {
-                if (F32OUT) Qf[ro + x0 + k] = (float)acc[k];
-                else Q[ro + x0 + k] = acc[k];
-            }
+    // thread t writes the x-row (zl, yl) = (t / 16, t % 16)
+    const int zl = tid / kBrick, yl = tid % kBrick;
+    if (zl < wz && yl < wy) {
+        const size_t ro = (size_t)a.K1 * ((y0 + yl) + (size_t)a.K2 * (z0 + zl)) + x0;
+        for (int k = 0; k < wx; ++k) {
+            if (F32) Qf[ro + k] = (float)(bhi[zl][yl][k] + blo[F32 ? zl : 0][F32 ? yl : 0][F32 ? k : 0]);
+            else Q[ro + k] = (double)bhi[zl][yl][k];
+        }
     }
 }
 
@@ -467,15 +493,14 @@ static SpmeArgs spme_args(const tcp_ctx *c) {
     return a;
 }
 
-// atomic-free spread into Q (FP64) or straight into Qf (FP32C mode: the FP64
-// sums are rounded once, when the brick is written)
+// atomic-free spread into Q (FP64) or straight into Qf (FP32C mode)
 template <int P>
 static void launch_brick_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Qf) {
     const int threads = 128, blocks = (c->n + threads - 1) / threads;
     spme_cells_kernel<P><<<blocks, threads, 0, c->stream>>>(a, c->spme_cell);
     const dim3 grid((c->K1 + kBrick - 1) / kBrick, (c->K2 + kBrick - 1) / kBrick, (c->K3 + kBrick - 1) / kBrick);
-    if (Qf) spme_brick_spread_kernel<P, true><<<grid, kBrickThreads, 0, c->stream>>>(a, c->spme_cell, nullptr, Qf);
-    else spme_brick_spread_kernel<P, false><<<grid, kBrickThreads, 0, c->stream>>>(a, c->spme_cell, Q, nullptr);
+    if (Qf) spme_brick_spread_kernel<P, float><<<grid, kBrickThreads, 0, c->stream>>>(a, c->spme_cell, nullptr, Qf);
+    else spme_brick_spread_kernel<P, double><<<grid, kBrickThreads, 0, c->stream>>>(a, c->spme_cell, Q, nullptr);
     c->launches += 2;
 }
 
