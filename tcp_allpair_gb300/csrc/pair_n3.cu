@@ -189,7 +189,7 @@ __device__ __forceinline__ float n3_pair(const PairConsts &c, float r2, bool ok,
 // memory.  MASKED: apply validity and i < j index masks.
 template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R>
 __device__ __forceinline__ void n3_item(const PairConsts &c, const int4 *__restrict__ tj, int cnt, int jstart,
-                                        const int4 (&xi)[R], const int (&ii)[R], const bool (&vi)[R],
+                                        const int4 (&xi)[R], int ibase, int iend,
                                         float (*sjacc)[3], float (&p)[R][3], float &pe) {
     const int lane = threadIdx.x & 31;
     const int src = (lane + 1) & 31;
@@ -210,7 +210,8 @@ __device__ __forceinline__ void n3_item(const PairConsts &c, const int4 *__restr
                 ok[r] = r2[r] < c.u_rc2;
                 if (MASKED) {
                     const int jo = ch * 32 + ((lane + s) & 31);
-                    ok[r] = ok[r] && vi[r] && (jo < cnt) && (ii[r] < jstart + jo);
+                    const int ir = ibase + 32 * r;     // i-particle r of this lane
+                    ok[r] = ok[r] && (ir < iend) && (jo < cnt) && (ir < jstart + jo);
                 }
                 if (KIND == 2) r2min = fminf(r2min, r2[r]);
             }
@@ -321,7 +322,7 @@ __device__ __forceinline__ float idiff(int a, int b) { return (float)(int)((unsi
 
 template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R, bool EST>
 __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__restrict__ tj, int cnt, int jstart,
-                                           const int4 (&xi)[R], const int (&ii)[R], const bool (&vi)[R],
+                                           const int4 (&xi)[R], int ibase, int iend,
                                            float (*sjacc)[3], float (&p)[R][3], float &pe) {
     static_assert(R % 2 == 0, "paired form needs an even number of i-particles per lane");
     constexpr int G = R / 2;
@@ -349,8 +350,9 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
                 ok[2 * g + 1] = r2[g].y < c.u_rc2;
                 if (MASKED) {
                     const int jo = ch * 32 + ((lane + s) & 31);
-                    ok[2 * g] = ok[2 * g] && vi[2 * g] && (jo < cnt) && (ii[2 * g] < jstart + jo);
-                    ok[2 * g + 1] = ok[2 * g + 1] && vi[2 * g + 1] && (jo < cnt) && (ii[2 * g + 1] < jstart + jo);
+                    const int i0 = ibase + 64 * g, i1 = i0 + 32;   // i-particles 2g, 2g+1 of this lane
+                    ok[2 * g] = ok[2 * g] && (i0 < iend) && (jo < cnt) && (i0 < jstart + jo);
+                    ok[2 * g + 1] = ok[2 * g + 1] && (i1 < iend) && (jo < cnt) && (i1 < jstart + jo);
                 }
                 if (KIND == 2) r2min = fminf(r2min, fminf(r2[g].x, r2[g].y));
             }
@@ -440,14 +442,11 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
     double etot = 0.0;
     int curRep = -1, curI = -1, istart = 0, iend = 0, isp = 0, ifirst = 0, ioff = 0;
     int4 xi[R];
-    int ii[R];
-    bool vi[R];
+    int ibase = 0;           // i-particle 0 of this lane; particle r is ibase + 32 r
     float eh = 0.f, el = 0.f;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         xi[r] = make_int4(0, 0, 0, 0);
-        ii[r] = 0;
-        vi[r] = false;
     }
     if constexpr (SACC) {
 #pragma unroll
@@ -466,7 +465,8 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
             for (int k = 0; k < 3; ++k) {
                 float &h = SACC ? sacc[6 * r + 2 * k][tid] : hi[SACC ? 0 : r][k];
                 float &l = SACC ? sacc[6 * r + 2 * k + 1][tid] : lo[SACC ? 0 : r][k];
-                if (vi[r]) atomicAdd(&a.facc[(size_t)k * a.ntot + ioff + ii[r]], kEps * ((double)h + (double)l));
+                if (ibase + 32 * r < iend)
+                    atomicAdd(&a.facc[(size_t)k * a.ntot + ioff + ibase + 32 * r], kEps * ((double)h + (double)l));
                 h = 0.f;
                 l = 0.f;
             }
@@ -493,11 +493,11 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
             curRep = rep;
             ioff = g.off;
             n3_itile<TILE>(g, I_, istart, iend, isp, ifirst);
+            ibase = istart + warp * 32 * R + lane;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                ii[r] = istart + warp * 32 * R + r * 32 + lane;
-                vi[r] = ii[r] < iend;
-                xi[r] = a.xq[ioff + (vi[r] ? ii[r] : istart)];
+                const int ir = istart + warp * 32 * R + r * 32 + lane;
+                xi[r] = a.xq[ioff + (ir < iend ? ir : istart)];
             }
         }
         int jstart, cnt, jsp;
@@ -514,9 +514,9 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
 #define TCP_N3_ITEM(KIND, MASKED)                                                                      \
     do {                                                                                                \
         if (X2)                                                                                         \
-            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R, MODE == 2>(c, tiles[stage], cnt, jstart, xi, ii, vi, sjacc, p, pe); \
+            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R, MODE == 2>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe); \
         else                                                                                            \
-            n3_item<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ii, vi, sjacc, p, pe);    \
+            n3_item<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe);    \
     } while (0)
         if (masked) {
             if (kind == 1) TCP_N3_ITEM(1, true);

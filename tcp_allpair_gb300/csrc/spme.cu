@@ -3,12 +3,11 @@
 //
 // Mesh layout: Q[iz][iy][ix] (ix fastest, the Fortran order of Q(ix,iy,iz)),
 // FP64.  The 3-D FFT is cuFFT D2Z / Z2D on that layout (the only library
-// call of the path); spreading (atomic-free, one CTA per mesh brick), the
+// call of the path); spreading (cell-sorted and atomic-free), the
 // influence-function multiply fused with the energy reduction, and the force
 // gather are kernels of this file.
-// In the compensated-FP32 mode the charges are still accumulated in FP64
-// (the structure-factor accumulation) and each mesh point is rounded to FP32
-// when its brick is written, for R2C / C2R transforms, the influence multiply
+// In the compensated-FP32 mode the charge mesh is summed in two-float FP32
+// and written as FP32 for R2C / C2R transforms, the influence multiply
 // (energy summed in FP64) and the force gather: on GB300 FP64 runs at 1/64 of
 // the FP32 rate, which makes a 128^3 FP64 transform compute-bound.
 //
@@ -35,173 +34,201 @@ struct SpmeArgs {
     int K1, K2, K3;
 };
 
-// ---- atomic-free charge spreading ---------------------------------------------
-// The mesh is cut into bricks of kBrick^3 points, one CTA per brick.  A
-// particle's support is the P^3 points from its base index b = INT(u)-(P-3)
-// (force.f90:742-744), so it reaches a brick [o, o + w) in a dimension iff
-// (b - (o - P + 1)) mod K < w + P - 1.  spme_cells_kernel packs the wrapped
-// base of every particle (10 bits per dimension); each brick CTA scans the
-// packed bases and keeps the particles that reach it in per-warp lists
-// (ballot order: deterministic), stages their weights in shared memory and
-// adds them into a shared-memory copy of the brick.  Warp w owns the planes
-// z = w and w + 8 of the brick; for a particle, its lanes cover the P x P
-// support points of each owned plane, so no two lanes (and no two warps)
-// touch the same point: no atomics, and every mesh point is summed in the
-// same order on every run.  FP64 mode sums FP64 products in FP64; FP32C mode
-// sums FP32 products in compensated two-float FP32 (TwoSum hi/lo) and writes
-// the FP32 mesh the FP32 transforms read (GB300's FP64 rate is 1/64 of FP32).
-constexpr int kBrick = 16;
-constexpr int kBrickThreads = 256;
-constexpr int kBrickWarps = kBrickThreads / 32;
-constexpr int kBrickRow = kBrick + 1;        // padded row (shared-memory banks)
-constexpr int kCandPerWarp = 128;
-constexpr int kScanIters = 2;                // scan iterations per warp between flush checks
-// candidates whose weights are staged at a time (static shared memory <= 48 KB)
-template <int P, typename T>
-struct StageWidth {
-    static constexpr int value = (sizeof(T) == 8 && P >= 6) ? 32 : 64;
+// ---- atomic-free charge spreading (cell-sorted) --------------------------------
+// A particle's support is the P^3 mesh points from its base index
+// b = INT(u)-(P-3) (force.f90:742-744).  Particles are counting-sorted by the
+// (y, z) mesh column of their base (bin = by + K2 bz); each bin is then put in
+// particle-index order and the B-spline weights of every particle are stored
+// once in sorted order.  The spread itself is a gather: thread (s, y, z) owns
+// the x-segment [16 s, 16 s + 16) of mesh row (y, z), visits the P^2 bins
+// (y - jy, z - jz) whose particles can reach the row (jy, jz < P), and adds
+// the contributions that fall in its segment to registers.  Every mesh point
+// has one owner thread, so the accumulation needs no atomics, and it runs in
+// the same order (bins, then particle index) on every call.  The bin counts
+// and slots come from integer atomics; the sum does not depend on them.
+// FP64 mode adds FP64 products in FP64; FP32C mode adds FP32 products in
+// compensated two-float FP32 (TwoSum hi/lo) and writes the FP32 mesh read by
+// the FP32 transforms (GB300's FP64 rate is 1/64 of FP32).
+constexpr int kSeg = 16;                 // x-points per spreading thread
+constexpr int kScanBlock = 1024;         // bins per block of the prefix sum
+
+struct SpreadBins {
+    int *count, *start, *bsum, *rank, *list, *ebx;
+    void *ew, *eq;                       // [n][3][P] weights, [n] charges (T = float or double)
 };
 
 template <int P>
-__global__ void spme_cells_kernel(const SpmeArgs a, unsigned *__restrict__ cell) {
+__global__ void spme_bin_count_kernel(const SpmeArgs a, SpreadBins b) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= a.n) return;
     const double L[3] = {a.box0, a.box1, a.box2};
     const int K[3] = {a.K1, a.K2, a.K3};
-    unsigned packed = 0;
+    int base[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];   // :700-702
-        packed |= (unsigned)wrapi((int)trunc(u) - (P - 3), K[d]) << (10 * d);
+        base[d] = wrapi((int)trunc(u) - (P - 3), K[d]);
     }
-    cell[m] = packed;
+    b.rank[m] = atomicAdd(&b.count[base[1] + a.K2 * base[2]], 1);
 }
 
-__device__ __forceinline__ bool reaches(int b, int lo, int span, int K) {
-    int t = b - lo;
-    t += t < 0 ? K : 0;
-    return t < span;
-}
-
-// T = double: FP64 accumulation (hi only); T = float: TwoSum (hi, lo)
-template <int P, typename T>
-__global__ void __launch_bounds__(kBrickThreads) spme_brick_spread_kernel(const SpmeArgs a,
-                                                                          const unsigned *__restrict__ cell,
-                                                                          double *__restrict__ Q,
-                                                                          float *__restrict__ Qf) {
-    constexpr bool F32 = sizeof(T) == 4;
-    constexpr int kStageW = StageWidth<P, T>::value;
-    __shared__ T bhi[kBrick][kBrick][kBrickRow];
-    __shared__ T blo[F32 ? kBrick : 1][F32 ? kBrick : 1][F32 ? kBrickRow : 1];
-    __shared__ int cand[kBrickWarps][kCandPerWarp];
-    __shared__ int woff[kBrickWarps + 1];
-    __shared__ int wcnt[kBrickWarps];
-    __shared__ T sw[kStageW][3][P];
-    __shared__ T sq[kStageW];
-    __shared__ int sb[kStageW][3];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int x0 = blockIdx.x * kBrick, y0 = blockIdx.y * kBrick, z0 = blockIdx.z * kBrick;
-    const int wx = min(kBrick, a.K1 - x0), wy = min(kBrick, a.K2 - y0), wz = min(kBrick, a.K3 - z0);
-    const int lox = wrapi(x0 - P + 1, a.K1), loy = wrapi(y0 - P + 1, a.K2), loz = wrapi(z0 - P + 1, a.K3);
-    const int spx = min(wx + P - 1, a.K1), spy = min(wy + P - 1, a.K2), spz = min(wz + P - 1, a.K3);
-    for (int k = tid; k < kBrick * kBrick * kBrickRow; k += kBrickThreads) {
-        (&bhi[0][0][0])[k] = (T)0;
-        if (F32) (&blo[0][0][0])[k] = (T)0;
+// exclusive prefix sum of count[0..nbins) into start[0..nbins], in three steps
+__global__ void scan_block_kernel(const int *__restrict__ count, int nbins, int *__restrict__ start,
+                                  int *__restrict__ bsum) {
+    __shared__ int ws[32];
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    const int v = i < nbins ? count[i] : 0;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
-    int cnt = 0;                                   // this warp's list length (warp-uniform)
-
-    auto flush = [&]() {
-        if (lane == 0) wcnt[warp] = cnt;
-        __syncthreads();
-        if (tid == 0) {
-            woff[0] = 0;
-            for (int w = 0; w < kBrickWarps; ++w) woff[w + 1] = woff[w] + wcnt[w];
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int t = ws[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
         }
-        __syncthreads();
-        const int total = woff[kBrickWarps];
-        for (int c0 = 0; c0 < total; c0 += kStageW) {
-            if (tid < kStageW && c0 + tid < total) {
-                const int c = c0 + tid;
-                int w = 0;
-                while (c >= woff[w + 1]) ++w;
-                const int m = cand[w][c - woff[w]];
-                const double L[3] = {a.box0, a.box1, a.box2};
-                const int K[3] = {a.K1, a.K2, a.K3};
-                T W[P], dW[P];
+        ws[lane] = t;
+    }
+    __syncthreads();
+    const int incl = x + (w > 0 ? ws[w - 1] : 0);
+    if (i < nbins) start[i] = incl - v;
+    if (threadIdx.x == kScanBlock - 1) bsum[blockIdx.x] = incl;
+}
+
+__global__ void scan_sums_kernel(int *__restrict__ bsum, int nblocks) {
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int k = 0; k < nblocks; ++k) {
+            const int t = bsum[k];
+            bsum[k] = acc;
+            acc += t;
+        }
+    }
+}
+
+__global__ void scan_add_kernel(int *__restrict__ start, int nbins, const int *__restrict__ bsum, int total) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nbins) start[i] += bsum[i / kScanBlock];
+    if (i == 0) start[nbins] = total;
+}
+
+__global__ void spme_bin_scatter_kernel(const SpmeArgs a, SpreadBins b, int P) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= a.n) return;
+    const double L1 = a.box1, L2 = a.box2;
+    const double uy = (double)a.K2 * (a.x[(size_t)a.n + m] + L1 * .5) / L1;
+    const double uz = (double)a.K3 * (a.x[2 * (size_t)a.n + m] + L2 * .5) / L2;
+    const int by = wrapi((int)trunc(uy) - (P - 3), a.K2), bz = wrapi((int)trunc(uz) - (P - 3), a.K3);
+    b.list[b.start[by + a.K2 * bz] + b.rank[m]] = m;
+}
+
+// each bin in particle-index order (bins hold a few particles: insertion sort)
+__global__ void spme_bin_sort_kernel(SpreadBins b, int nbins) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nbins) return;
+    const int s = b.start[k], e = b.start[k + 1];
+    for (int i = s + 1; i < e; ++i) {
+        const int v = b.list[i];
+        int j = i - 1;
+        while (j >= s && b.list[j] > v) {
+            b.list[j + 1] = b.list[j];
+            --j;
+        }
+        b.list[j + 1] = v;
+    }
+}
+
+template <int P, typename T>
+__global__ void spme_bin_weights_kernel(const SpmeArgs a, SpreadBins b) {
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= a.n) return;
+    const int m = b.list[pos];
+    const double L[3] = {a.box0, a.box1, a.box2};
+    const int K[3] = {a.K1, a.K2, a.K3};
+    T *w = static_cast<T *>(b.ew) + (size_t)pos * 3 * P;
+    T W[P], dW[P];
 #pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];
-                    spline_w<P, T>(u, W, dW);
+    for (int d = 0; d < 3; ++d) {
+        const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];
+        spline_w<P, T>(u, W, dW);
 #pragma unroll
-                    for (int j = 0; j < P; ++j) sw[tid][d][j] = W[j];
-                    sb[tid][d] = wrapi((int)trunc(u) - (P - 3), K[d]);
-                }
-                sq[tid] = (T)(m < a.nel ? a.q0 : a.q1);
-            }
-            __syncthreads();
-            const int nb = min(kStageW, total - c0);
-            for (int c = 0; c < nb; ++c) {
+        for (int j = 0; j < P; ++j) w[d * P + j] = W[j];
+        if (d == 0) b.ebx[pos] = wrapi((int)trunc(u) - (P - 3), K[0]);
+    }
+    static_cast<T *>(b.eq)[pos] = (T)(m < a.nel ? a.q0 : a.q1);
+}
+
+// thread (s, y, z): x-segment s of row (y, z); T = double: FP64 sums;
+// T = float: TwoSum (hi, lo) sums written as one FP32 value
+template <int P, typename T>
+__global__ void __launch_bounds__(256) spme_row_spread_kernel(const SpmeArgs a, const SpreadBins b, int nseg,
+                                                              double *__restrict__ Q, float *__restrict__ Qf) {
+    constexpr bool F32 = sizeof(T) == 4;
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (t >= (long)nseg * a.K2 * a.K3) return;
+    const int s = (int)(t % nseg);
+    const int y = (int)((t / nseg) % a.K2);
+    const int z = (int)(t / ((long)nseg * a.K2));
+    const int x0 = s * kSeg;
+    const int lox = wrapi(x0 - P + 1, a.K1), spx = min(kSeg + P - 1, a.K1);
+    const T *__restrict__ ew = static_cast<const T *>(b.ew);
+    const T *__restrict__ eq = static_cast<const T *>(b.eq);
+    T hi[kSeg], lo[F32 ? kSeg : 1];
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int zl = warp + kBrickWarps * h;
-                    if (zl >= wz) continue;
-                    int rz = z0 + zl - sb[c][2];
-                    rz += rz < 0 ? a.K3 : 0;
-                    if (rz >= P) continue;                        // warp-uniform
-                    const T wq = sq[c] * sw[c][2][rz];
-                    for (int l = lane; l < P * P; l += 32) {
-                        const int jy = l / P, jx = l - jy * P;
-                        int y = sb[c][1] + jy;
-                        y -= y >= a.K2 ? a.K2 : 0;
-                        int x = sb[c][0] + jx;
-                        x -= x >= a.K1 ? a.K1 : 0;
-                        const int yl = y - y0, xl = x - x0;
-                        if ((unsigned)yl < (unsigned)wy && (unsigned)xl < (unsigned)wx) {
-                            const T v = wq * sw[c][1][jy] * sw[c][0][jx];
-                            T &hi = bhi[zl][yl][xl];
-                            if (F32) {
-                                const T s = hi + v, bp = s - hi;
-                                blo[F32 ? zl : 0][F32 ? yl : 0][F32 ? xl : 0] += (hi - (s - bp)) + (v - bp);
-                                hi = s;
-                            } else {
-                                hi += v;
-                            }
+    for (int k = 0; k < kSeg; ++k) {
+        hi[k] = (T)0;
+        if (F32) lo[F32 ? k : 0] = (T)0;
+    }
+    for (int jz = 0; jz < P; ++jz) {
+        int bz = z - jz;
+        bz += bz < 0 ? a.K3 : 0;
+        for (int jy = 0; jy < P; ++jy) {
+            int by = y - jy;
+            by += by < 0 ? a.K2 : 0;
+            const int bin = by + a.K2 * bz;
+            const int e = b.start[bin + 1];
+            for (int pos = b.start[bin]; pos < e; ++pos) {
+                const int bx = b.ebx[pos];
+                int tt = bx - lox;
+                tt += tt < 0 ? a.K1 : 0;
+                if (tt >= spx) continue;                  // support misses this segment
+                const T *w = ew + (size_t)pos * 3 * P;
+                const T wyz = eq[pos] * w[P + jy] * w[2 * P + jz];
+                const int rx0 = x0 - bx;
+#pragma unroll
+                for (int k = 0; k < kSeg; ++k) {
+                    int rx = rx0 + k;
+                    rx += rx < 0 ? a.K1 : 0;
+                    rx -= rx >= a.K1 ? a.K1 : 0;
+                    if (rx < P) {
+                        const T v = wyz * w[rx];
+                        if (F32) {
+                            const T sum = hi[k] + v, bp = sum - hi[k];
+                            lo[F32 ? k : 0] += (hi[k] - (sum - bp)) + (v - bp);
+                            hi[k] = sum;
+                        } else {
+                            hi[k] += v;
                         }
                     }
                 }
             }
-            __syncthreads();
         }
-        cnt = 0;
-    };
-
-    for (int i0 = 0; i0 < a.n; i0 += kBrickThreads * kScanIters) {
+    }
+    const size_t ro = (size_t)a.K1 * (y + (size_t)a.K2 * z) + x0;
+    const int wx = min(kSeg, a.K1 - x0);
 #pragma unroll
-        for (int it = 0; it < kScanIters; ++it) {
-            const int i = i0 + it * kBrickThreads + tid;
-            bool hit = false;
-            if (i < a.n) {
-                const unsigned cq = cell[i];
-                hit = reaches((int)((cq >> 20) & 1023u), loz, spz, a.K3) &&
-                      reaches((int)((cq >> 10) & 1023u), loy, spy, a.K2) && reaches((int)(cq & 1023u), lox, spx, a.K1);
-            }
-            const unsigned bal = __ballot_sync(0xffffffffu, hit);
-            if (hit) cand[warp][cnt + __popc(bal & ((1u << lane) - 1u))] = i;
-            cnt += __popc(bal);
+    for (int k = 0; k < kSeg; ++k)
+        if (k < wx) {
+            if (F32) Qf[ro + k] = (float)(hi[k] + lo[F32 ? k : 0]);
+            else Q[ro + k] = (double)hi[k];
         }
-        // a warp adds at most 32 * kScanIters candidates per round
-        if (__syncthreads_or(cnt > kCandPerWarp - 32 * kScanIters)) flush();
-    }
-    flush();
-    // thread t writes the x-row (zl, yl) = (t / 16, t % 16)
-    const int zl = tid / kBrick, yl = tid % kBrick;
-    if (zl < wz && yl < wy) {
-        const size_t ro = (size_t)a.K1 * ((y0 + yl) + (size_t)a.K2 * (z0 + zl)) + x0;
-        for (int k = 0; k < wx; ++k) {
-            if (F32) Qf[ro + k] = (float)(bhi[zl][yl][k] + blo[F32 ? zl : 0][F32 ? yl : 0][F32 ? k : 0]);
-            else Q[ro + k] = (double)bhi[zl][yl][k];
-        }
-    }
 }
 
 // Qk *= theta B; energy partial sum_m w_m theta B |Qk|^2 (w = 2 for the
@@ -389,8 +416,14 @@ int spme_free(tcp_ctx *c) {
         cufftDestroy(c->plan_b);
         c->plans = false;
     }
-    cudaFree(c->spme_cell);
-    c->spme_cell = nullptr;
+    int **ib[] = {&c->bin_count, &c->bin_start, &c->bin_bsum, &c->bin_rank, &c->bin_list, &c->bin_ebx};
+    for (int **q : ib) {
+        cudaFree(*q);
+        *q = nullptr;
+    }
+    cudaFree(c->bin_ew);
+    cudaFree(c->bin_eq);
+    c->bin_ew = c->bin_eq = nullptr;
     cudaFree(c->Q);
     cudaFree(c->Qk);
     cudaFree(c->infl);
@@ -421,7 +454,15 @@ int spme_setup(tcp_ctx *c) {
     const size_t nhalf = (size_t)c->Kh * c->K2 * c->K3;
     c->spme_fp32 = c->p.precision == TCP_PREC_FP32C;
     if (!c->Q) {
-        if (cudaMalloc(&c->spme_cell, sizeof(unsigned) * (size_t)c->n) != cudaSuccess ||
+        const size_t nbins = (size_t)c->K2 * c->K3;
+        if (cudaMalloc(&c->bin_count, sizeof(int) * (nbins + 1)) != cudaSuccess ||
+            cudaMalloc(&c->bin_start, sizeof(int) * (nbins + 1)) != cudaSuccess ||
+            cudaMalloc(&c->bin_bsum, sizeof(int) * ((nbins + kScanBlock - 1) / kScanBlock)) != cudaSuccess ||
+            cudaMalloc(&c->bin_rank, sizeof(int) * (size_t)c->n) != cudaSuccess ||
+            cudaMalloc(&c->bin_list, sizeof(int) * (size_t)c->n) != cudaSuccess ||
+            cudaMalloc(&c->bin_ebx, sizeof(int) * (size_t)c->n) != cudaSuccess ||
+            cudaMalloc(&c->bin_ew, sizeof(double) * 3 * kMaxOrder * (size_t)c->n) != cudaSuccess ||
+            cudaMalloc(&c->bin_eq, sizeof(double) * (size_t)c->n) != cudaSuccess ||
             cudaMalloc(&c->Q, sizeof(double) * nreal) != cudaSuccess ||
             cudaMalloc(&c->Qk, sizeof(cufftDoubleComplex) * nhalf) != cudaSuccess ||
             cudaMalloc(&c->infl, sizeof(double) * nhalf) != cudaSuccess)
@@ -494,23 +535,54 @@ static SpmeArgs spme_args(const tcp_ctx *c) {
 }
 
 // atomic-free spread into Q (FP64) or straight into Qf (FP32C mode)
-template <int P>
-static void launch_brick_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Qf) {
-    const int threads = 128, blocks = (c->n + threads - 1) / threads;
-    spme_cells_kernel<P><<<blocks, threads, 0, c->stream>>>(a, c->spme_cell);
-    const dim3 grid((c->K1 + kBrick - 1) / kBrick, (c->K2 + kBrick - 1) / kBrick, (c->K3 + kBrick - 1) / kBrick);
-    if (Qf) spme_brick_spread_kernel<P, float><<<grid, kBrickThreads, 0, c->stream>>>(a, c->spme_cell, nullptr, Qf);
-    else spme_brick_spread_kernel<P, double><<<grid, kBrickThreads, 0, c->stream>>>(a, c->spme_cell, Q, nullptr);
-    c->launches += 2;
+static SpreadBins spread_bins(tcp_ctx *c) {
+    SpreadBins b;
+    b.count = c->bin_count;
+    b.start = c->bin_start;
+    b.bsum = c->bin_bsum;
+    b.rank = c->bin_rank;
+    b.list = c->bin_list;
+    b.ebx = c->bin_ebx;
+    b.ew = c->bin_ew;
+    b.eq = c->bin_eq;
+    return b;
 }
 
-static void brick_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Qf) {
+template <int P>
+static int launch_cell_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Qf) {
+    const SpreadBins b = spread_bins(c);
+    const int threads = 256, pblocks = (c->n + threads - 1) / threads;
+    const int nbins = c->K2 * c->K3;
+    const int sblocks = (nbins + kScanBlock - 1) / kScanBlock;
+    TCP_CUDA(cudaMemsetAsync(c->bin_count, 0, sizeof(int) * (size_t)nbins, c->stream));
+    spme_bin_count_kernel<P><<<pblocks, threads, 0, c->stream>>>(a, b);
+    scan_block_kernel<<<sblocks, kScanBlock, 0, c->stream>>>(c->bin_count, nbins, c->bin_start, c->bin_bsum);
+    scan_sums_kernel<<<1, 32, 0, c->stream>>>(c->bin_bsum, sblocks);
+    scan_add_kernel<<<(nbins + threads - 1) / threads, threads, 0, c->stream>>>(c->bin_start, nbins, c->bin_bsum, c->n);
+    spme_bin_scatter_kernel<<<pblocks, threads, 0, c->stream>>>(a, b, P);
+    spme_bin_sort_kernel<<<(nbins + threads - 1) / threads, threads, 0, c->stream>>>(b, nbins);
+    const int nseg = (c->K1 + kSeg - 1) / kSeg;
+    const long rows = (long)nseg * c->K2 * c->K3;
+    const int rblocks = (int)((rows + 255) / 256);
+    if (Qf) {
+        spme_bin_weights_kernel<P, float><<<pblocks, threads, 0, c->stream>>>(a, b);
+        spme_row_spread_kernel<P, float><<<rblocks, 256, 0, c->stream>>>(a, b, nseg, nullptr, Qf);
+    } else {
+        spme_bin_weights_kernel<P, double><<<pblocks, threads, 0, c->stream>>>(a, b);
+        spme_row_spread_kernel<P, double><<<rblocks, 256, 0, c->stream>>>(a, b, nseg, Q, nullptr);
+    }
+    c->launches += 8;
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
+static int cell_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Qf) {
     switch (c->p.order) {
-        case 4: launch_brick_spread<4>(c, a, Q, Qf); break;
-        case 5: launch_brick_spread<5>(c, a, Q, Qf); break;
-        case 6: launch_brick_spread<6>(c, a, Q, Qf); break;
-        case 7: launch_brick_spread<7>(c, a, Q, Qf); break;
-        default: launch_brick_spread<8>(c, a, Q, Qf); break;
+        case 4: return launch_cell_spread<4>(c, a, Q, Qf);
+        case 5: return launch_cell_spread<5>(c, a, Q, Qf);
+        case 6: return launch_cell_spread<6>(c, a, Q, Qf);
+        case 7: return launch_cell_spread<7>(c, a, Q, Qf);
+        default: return launch_cell_spread<8>(c, a, Q, Qf);
     }
 }
 
@@ -538,8 +610,9 @@ double *recip_epart(tcp_ctx *c);
 
 int launch_spme(tcp_ctx *c, bool energy) {
     const SpmeArgs a = spme_args(c);
-    // FP64 charge accumulation, atomic-free (every mesh point is written)
-    brick_spread(c, a, c->spme_fp32 ? nullptr : c->Q, c->spme_fp32 ? c->Qf : nullptr);
+    // charge accumulation, atomic-free (every mesh point is written)
+    int rcs = cell_spread(c, a, c->spme_fp32 ? nullptr : c->Q, c->spme_fp32 ? c->Qf : nullptr);
+    if (rcs) return rcs;
     const long total = (long)c->K3 * c->K2 * c->Kh;
     const int eb = spme_energy_blocks(c);
     double *epart = recip_epart(c);
@@ -721,7 +794,7 @@ __global__ void spme_gather_hvp_kernel(const SpmeArgs a, const double *__restric
 template <int P>
 static void launch_hvp_kernels(tcp_ctx *c, const SpmeArgs &a, const double *w, double *hw, int which) {
     const int threads = 128, blocks = (c->n + threads - 1) / threads;
-    if (which == 0) launch_brick_spread<P>(c, a, c->hQ, nullptr);
+    if (which == 0) (void)launch_cell_spread<P>(c, a, c->hQ, nullptr);
     else if (which == 1) spme_spread_dipole_kernel<P><<<blocks, threads, 0, c->stream>>>(a, w, c->hdQ);
     else spme_gather_hvp_kernel<P><<<blocks, threads, 0, c->stream>>>(a, c->hQ, c->hdQ, w, kEps / (kPi * c->V), hw);
 }

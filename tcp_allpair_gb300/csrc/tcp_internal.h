@@ -102,7 +102,10 @@ struct tcp_ctx {
     bool host_direct = false;
     // SPME
     int K1 = 0, K2 = 0, K3 = 0, Kh = 0; // Kh = K1/2+1
-    unsigned *spme_cell = nullptr;      // packed spline base index per particle (atomic-free spread)
+    // cell-sorted spreading: counting sort by the (y, z) mesh column of the spline base
+    int *bin_count = nullptr, *bin_start = nullptr, *bin_bsum = nullptr;   // [K2 K3 (+1)], block sums
+    int *bin_rank = nullptr, *bin_list = nullptr, *bin_ebx = nullptr;      // [n]
+    void *bin_ew = nullptr, *bin_eq = nullptr;                               // weights [n][3][P], charges [n]
     double *Q = nullptr;                // real mesh [K3][K2][K1]
     cufftDoubleComplex *Qk = nullptr;   // [K3][K2][Kh]
     double *infl = nullptr;             // theta * |b|^-2 on the half mesh
