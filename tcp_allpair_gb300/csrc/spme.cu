@@ -37,23 +37,27 @@ struct SpmeArgs {
 // ---- atomic-free charge spreading (cell-sorted) --------------------------------
 // A particle's support is the P^3 mesh points from its base index
 // b = INT(u)-(P-3) (force.f90:742-744).  Particles are counting-sorted by the
-// (y, z) mesh column of their base (bin = by + K2 bz); each bin is then put in
+// (y, z) mesh column of their base (bin = by + K2 bz); each bin is put in
 // particle-index order and the B-spline weights of every particle are stored
-// once in sorted order.  The spread itself is a gather: thread (s, y, z) owns
-// the x-segment [16 s, 16 s + 16) of mesh row (y, z), visits the P^2 bins
-// (y - jy, z - jz) whose particles can reach the row (jy, jz < P), and adds
-// the contributions that fall in its segment to registers.  Every mesh point
-// has one owner thread, so the accumulation needs no atomics, and it runs in
-// the same order (bins, then particle index) on every call.  The bin counts
-// and slots come from integer atomics; the sum does not depend on them.
-// FP64 mode adds FP64 products in FP64; FP32C mode adds FP32 products in
-// compensated two-float FP32 (TwoSum hi/lo) and writes the FP32 mesh read by
-// the FP32 transforms (GB300's FP64 rate is 1/64 of FP32).
-constexpr int kSeg = 16;                 // x-points per spreading thread
+// once, in sorted order.  The spread is then a gather by mesh rows: a warp
+// owns kRows consecutive rows (y0 .. y0 + kRows - 1, z) in shared memory and
+// visits, for jz < P, the bins (y0 - P + 1 .. y0 + kRows - 1, z - jz) -- a
+// contiguous (or wrapped) range of the sorted list, staged 32 particles at a
+// time.  For one particle its lanes cover the P x P points (jy, jx) of plane
+// z, so no two lanes and no two warps touch the same point: no atomics, and
+// every mesh point is summed in the same order (jz, bins, particle index) on
+// every call.  The bin counts and slots come from integer atomics; the sum
+// does not depend on them.  FP64 mode adds FP64 products in FP64; FP32C mode
+// adds FP32 products in compensated two-float FP32 (TwoSum hi/lo) and writes
+// the FP32 mesh read by the FP32 transforms (GB300's FP64 rate is 1/64 of
+// FP32).
+constexpr int kRows = 8;                 // mesh rows per warp
+constexpr int kRowWarps = 4;             // warps per CTA (fewer when the rows of a large mesh need the space)
 constexpr int kScanBlock = 1024;         // bins per block of the prefix sum
+constexpr int kSortReg = 8;              // bins up to this size are sorted in registers
 
 struct SpreadBins {
-    int *count, *start, *bsum, *rank, *list, *ebx;
+    int *count, *start, *bsum, *rank, *list, *ebx, *eby;
     void *ew, *eq;                       // [n][3][P] weights, [n] charges (T = float or double)
 };
 
@@ -65,11 +69,13 @@ __global__ void spme_bin_count_kernel(const SpmeArgs a, SpreadBins b) {
     const int K[3] = {a.K1, a.K2, a.K3};
     int base[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
+    for (int d = 1; d < 3; ++d) {
         const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];   // :700-702
         base[d] = wrapi((int)trunc(u) - (P - 3), K[d]);
     }
-    b.rank[m] = atomicAdd(&b.count[base[1] + a.K2 * base[2]], 1);
+    const int bin = base[1] + a.K2 * base[2];
+    b.rank[m] = atomicAdd(&b.count[bin], 1);
+    b.ebx[m] = bin;                      // the bin of particle m (read back by the scatter)
 }
 
 // exclusive prefix sum of count[0..nbins) into start[0..nbins], in three steps
@@ -119,21 +125,37 @@ __global__ void scan_add_kernel(int *__restrict__ start, int nbins, const int *_
     if (i == 0) start[nbins] = total;
 }
 
-__global__ void spme_bin_scatter_kernel(const SpmeArgs a, SpreadBins b, int P) {
+__global__ void spme_bin_scatter_kernel(int n, SpreadBins b) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= a.n) return;
-    const double L1 = a.box1, L2 = a.box2;
-    const double uy = (double)a.K2 * (a.x[(size_t)a.n + m] + L1 * .5) / L1;
-    const double uz = (double)a.K3 * (a.x[2 * (size_t)a.n + m] + L2 * .5) / L2;
-    const int by = wrapi((int)trunc(uy) - (P - 3), a.K2), bz = wrapi((int)trunc(uz) - (P - 3), a.K3);
-    b.list[b.start[by + a.K2 * bz] + b.rank[m]] = m;
+    if (m >= n) return;
+    b.list[b.start[b.ebx[m]] + b.rank[m]] = m;
 }
 
-// each bin in particle-index order (bins hold a few particles: insertion sort)
+// each bin in particle-index order: small bins by a register sorting pass,
+// larger ones by insertion sort in place
 __global__ void spme_bin_sort_kernel(SpreadBins b, int nbins) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nbins) return;
-    const int s = b.start[k], e = b.start[k + 1];
+    const int s = b.start[k], e = b.start[k + 1], cnt = e - s;
+    if (cnt <= 1) return;
+    if (cnt <= kSortReg) {
+        int v[kSortReg];
+#pragma unroll
+        for (int i = 0; i < kSortReg; ++i) v[i] = i < cnt ? b.list[s + i] : 0x7fffffff;
+#pragma unroll
+        for (int i = 0; i < kSortReg; ++i)            // odd-even transposition sort
+#pragma unroll
+            for (int j = i & 1; j + 1 < kSortReg; j += 2)
+                if (v[j] > v[j + 1]) {
+                    const int t = v[j];
+                    v[j] = v[j + 1];
+                    v[j + 1] = t;
+                }
+#pragma unroll
+        for (int i = 0; i < kSortReg; ++i)
+            if (i < cnt) b.list[s + i] = v[i];
+        return;
+    }
     for (int i = s + 1; i < e; ++i) {
         const int v = b.list[i];
         int j = i - 1;
@@ -154,81 +176,117 @@ __global__ void spme_bin_weights_kernel(const SpmeArgs a, SpreadBins b) {
     const int K[3] = {a.K1, a.K2, a.K3};
     T *w = static_cast<T *>(b.ew) + (size_t)pos * 3 * P;
     T W[P], dW[P];
+    int base[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];
         spline_w<P, T>(u, W, dW);
 #pragma unroll
         for (int j = 0; j < P; ++j) w[d * P + j] = W[j];
-        if (d == 0) b.ebx[pos] = wrapi((int)trunc(u) - (P - 3), K[0]);
+        base[d] = wrapi((int)trunc(u) - (P - 3), K[d]);
     }
+    b.ebx[pos] = base[0];
+    b.eby[pos] = base[1];
     static_cast<T *>(b.eq)[pos] = (T)(m < a.nel ? a.q0 : a.q1);
 }
 
-// thread (s, y, z): x-segment s of row (y, z); T = double: FP64 sums;
-// T = float: TwoSum (hi, lo) sums written as one FP32 value
+// Shared memory of one warp: kRows rows of hi (T) [and lo (float)] of K1
+// points, then 32 staged particles (bx, by, q, weights).
 template <int P, typename T>
-__global__ void __launch_bounds__(256) spme_row_spread_kernel(const SpmeArgs a, const SpreadBins b, int nseg,
-                                                              double *__restrict__ Q, float *__restrict__ Qf) {
+__host__ __device__ constexpr size_t row_warp_bytes(int K1) {
+    return (size_t)kRows * K1 * (sizeof(T) + (sizeof(T) == 4 ? 4 : 0)) + 32 * (2 * sizeof(int) + (1 + 3 * P) * sizeof(T));
+}
+
+template <int P, typename T>
+__global__ void __launch_bounds__(32 * kRowWarps) spme_row_spread_kernel(const SpmeArgs a, const SpreadBins b,
+                                                                         double *__restrict__ Q,
+                                                                         float *__restrict__ Qf) {
     constexpr bool F32 = sizeof(T) == 4;
-    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= (long)nseg * a.K2 * a.K3) return;
-    const int s = (int)(t % nseg);
-    const int y = (int)((t / nseg) % a.K2);
-    const int z = (int)(t / ((long)nseg * a.K2));
-    const int x0 = s * kSeg;
-    const int lox = wrapi(x0 - P + 1, a.K1), spx = min(kSeg + P - 1, a.K1);
-    const T *__restrict__ ew = static_cast<const T *>(b.ew);
-    const T *__restrict__ eq = static_cast<const T *>(b.eq);
-    T hi[kSeg], lo[F32 ? kSeg : 1];
-#pragma unroll
-    for (int k = 0; k < kSeg; ++k) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ngy = (a.K2 + kRows - 1) / kRows;
+    const long grp = (long)blockIdx.x * (blockDim.x >> 5) + warp;  // (row group, z)
+    if (grp >= (long)ngy * a.K3) return;                          // warp-uniform
+    const int y0 = (int)(grp % ngy) * kRows, z = (int)(grp / ngy);
+    const int nrow = min(kRows, a.K2 - y0);
+    unsigned char *base = smem + (size_t)warp * row_warp_bytes<P, T>(a.K1);
+    T *hi = reinterpret_cast<T *>(base);                            // [kRows][K1]
+    float *lo = reinterpret_cast<float *>(base + (size_t)kRows * a.K1 * sizeof(T));
+    unsigned char *st = base + (size_t)kRows * a.K1 * (sizeof(T) + (F32 ? 4 : 0));
+    T *sw = reinterpret_cast<T *>(st);                              // [32][3P]
+    T *sq = sw + 32 * 3 * P;                                        // [32]
+    int *sbx = reinterpret_cast<int *>(sq + 32), *sby = sbx + 32;   // [32], [32]
+    for (int k = lane; k < kRows * a.K1; k += 32) {
         hi[k] = (T)0;
-        if (F32) lo[F32 ? k : 0] = (T)0;
+        if (F32) lo[k] = 0.f;
     }
+    __syncwarp();
+    const int nb = nrow + P - 1;                                    // bins by = y0-P+1 .. y0+nrow-1
     for (int jz = 0; jz < P; ++jz) {
         int bz = z - jz;
         bz += bz < 0 ? a.K3 : 0;
-        for (int jy = 0; jy < P; ++jy) {
-            int by = y - jy;
-            by += by < 0 ? a.K2 : 0;
-            const int bin = by + a.K2 * bz;
-            const int e = b.start[bin + 1];
-            for (int pos = b.start[bin]; pos < e; ++pos) {
-                const int bx = b.ebx[pos];
-                int tt = bx - lox;
-                tt += tt < 0 ? a.K1 : 0;
-                if (tt >= spx) continue;                  // support misses this segment
-                const T *w = ew + (size_t)pos * 3 * P;
-                const T wyz = eq[pos] * w[P + jy] * w[2 * P + jz];
-                const int rx0 = x0 - bx;
+        // the by range as at most two contiguous pieces of the sorted list
+        int by0 = y0 - P + 1, len0 = nb, len1 = 0;
+        if (by0 < 0) {
+            by0 += a.K2;
+            len0 = min(nb, a.K2 - by0);
+            len1 = nb - len0;
+        }
+        if (nb >= a.K2) {                                           // the range covers every bin
+            by0 = 0;
+            len0 = a.K2;
+            len1 = 0;
+        }
+        for (int piece = 0; piece < 2; ++piece) {
+            const int blo = (piece == 0 ? by0 : 0) + a.K2 * bz, len = piece == 0 ? len0 : len1;
+            if (len <= 0) continue;
+            const int p0 = b.start[blo], p1 = b.start[blo + len];
+            for (int c0 = p0; c0 < p1; c0 += 32) {
+                const int ne = min(32, p1 - c0);
+                if (lane < ne) {
+                    const int pos = c0 + lane;
+                    const T *w = static_cast<const T *>(b.ew) + (size_t)pos * 3 * P;
 #pragma unroll
-                for (int k = 0; k < kSeg; ++k) {
-                    int rx = rx0 + k;
-                    rx += rx < 0 ? a.K1 : 0;
-                    rx -= rx >= a.K1 ? a.K1 : 0;
-                    if (rx < P) {
-                        const T v = wyz * w[rx];
-                        if (F32) {
-                            const T sum = hi[k] + v, bp = sum - hi[k];
-                            lo[F32 ? k : 0] += (hi[k] - (sum - bp)) + (v - bp);
-                            hi[k] = sum;
-                        } else {
-                            hi[k] += v;
+                    for (int j = 0; j < 3 * P; ++j) sw[lane * 3 * P + j] = w[j];
+                    sq[lane] = static_cast<const T *>(b.eq)[pos];
+                    sbx[lane] = b.ebx[pos];
+                    sby[lane] = b.eby[pos];
+                }
+                __syncwarp();
+                for (int e = 0; e < ne; ++e) {
+                    const T *w = sw + e * 3 * P;
+                    const T qz = sq[e] * w[2 * P + jz];
+                    const int bx = sbx[e], by = sby[e];
+                    for (int l = lane; l < P * P; l += 32) {
+                        const int jy = l / P, jx = l - jy * P;
+                        int rl = by + jy - y0;                      // owned row of point (jy, jx)
+                        rl += rl < 0 ? a.K2 : 0;
+                        rl -= rl >= a.K2 ? a.K2 : 0;
+                        if (rl < nrow) {
+                            int x = bx + jx;
+                            x -= x >= a.K1 ? a.K1 : 0;
+                            const T v = qz * w[P + jy] * w[jx];
+                            const int k = rl * a.K1 + x;
+                            if (F32) {
+                                const T s = hi[k] + v, bp = s - hi[k];
+                                lo[k] += (hi[k] - (s - bp)) + (v - bp);
+                                hi[k] = s;
+                            } else {
+                                hi[k] += v;
+                            }
                         }
                     }
+                    __syncwarp();
                 }
             }
         }
     }
-    const size_t ro = (size_t)a.K1 * (y + (size_t)a.K2 * z) + x0;
-    const int wx = min(kSeg, a.K1 - x0);
-#pragma unroll
-    for (int k = 0; k < kSeg; ++k)
-        if (k < wx) {
-            if (F32) Qf[ro + k] = (float)(hi[k] + lo[F32 ? k : 0]);
-            else Q[ro + k] = (double)hi[k];
-        }
+    for (int k = lane; k < nrow * a.K1; k += 32) {
+        const int rl = k / a.K1, x = k - rl * a.K1;
+        const size_t g = (size_t)a.K1 * ((y0 + rl) + (size_t)a.K2 * z) + x;
+        if (F32) Qf[g] = (float)(hi[k] + lo[k]);
+        else Q[g] = (double)hi[k];
+    }
 }
 
 // Qk *= theta B; energy partial sum_m w_m theta B |Qk|^2 (w = 2 for the
@@ -416,7 +474,7 @@ int spme_free(tcp_ctx *c) {
         cufftDestroy(c->plan_b);
         c->plans = false;
     }
-    int **ib[] = {&c->bin_count, &c->bin_start, &c->bin_bsum, &c->bin_rank, &c->bin_list, &c->bin_ebx};
+    int **ib[] = {&c->bin_count, &c->bin_start, &c->bin_bsum, &c->bin_rank, &c->bin_list, &c->bin_ebx, &c->bin_eby};
     for (int **q : ib) {
         cudaFree(*q);
         *q = nullptr;
@@ -461,6 +519,7 @@ int spme_setup(tcp_ctx *c) {
             cudaMalloc(&c->bin_rank, sizeof(int) * (size_t)c->n) != cudaSuccess ||
             cudaMalloc(&c->bin_list, sizeof(int) * (size_t)c->n) != cudaSuccess ||
             cudaMalloc(&c->bin_ebx, sizeof(int) * (size_t)c->n) != cudaSuccess ||
+            cudaMalloc(&c->bin_eby, sizeof(int) * (size_t)c->n) != cudaSuccess ||
             cudaMalloc(&c->bin_ew, sizeof(double) * 3 * kMaxOrder * (size_t)c->n) != cudaSuccess ||
             cudaMalloc(&c->bin_eq, sizeof(double) * (size_t)c->n) != cudaSuccess ||
             cudaMalloc(&c->Q, sizeof(double) * nreal) != cudaSuccess ||
@@ -543,6 +602,7 @@ static SpreadBins spread_bins(tcp_ctx *c) {
     b.rank = c->bin_rank;
     b.list = c->bin_list;
     b.ebx = c->bin_ebx;
+    b.eby = c->bin_eby;
     b.ew = c->bin_ew;
     b.eq = c->bin_eq;
     return b;
@@ -559,17 +619,21 @@ static int launch_cell_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Q
     scan_block_kernel<<<sblocks, kScanBlock, 0, c->stream>>>(c->bin_count, nbins, c->bin_start, c->bin_bsum);
     scan_sums_kernel<<<1, 32, 0, c->stream>>>(c->bin_bsum, sblocks);
     scan_add_kernel<<<(nbins + threads - 1) / threads, threads, 0, c->stream>>>(c->bin_start, nbins, c->bin_bsum, c->n);
-    spme_bin_scatter_kernel<<<pblocks, threads, 0, c->stream>>>(a, b, P);
+    spme_bin_scatter_kernel<<<pblocks, threads, 0, c->stream>>>(c->n, b);
     spme_bin_sort_kernel<<<(nbins + threads - 1) / threads, threads, 0, c->stream>>>(b, nbins);
-    const int nseg = (c->K1 + kSeg - 1) / kSeg;
-    const long rows = (long)nseg * c->K2 * c->K3;
-    const int rblocks = (int)((rows + 255) / 256);
+    const long groups = (long)((c->K2 + kRows - 1) / kRows) * c->K3;
+    const size_t per_warp = Qf ? row_warp_bytes<P, float>(c->K1) : row_warp_bytes<P, double>(c->K1);
+    const int warps = (int)std::max<size_t>(1, std::min<size_t>(kRowWarps, (200u << 10) / per_warp));
+    const size_t sm = warps * per_warp;
+    const int rblocks = (int)((groups + warps - 1) / warps);
     if (Qf) {
+        TCP_CUDA(cudaFuncSetAttribute(spme_row_spread_kernel<P, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         spme_bin_weights_kernel<P, float><<<pblocks, threads, 0, c->stream>>>(a, b);
-        spme_row_spread_kernel<P, float><<<rblocks, 256, 0, c->stream>>>(a, b, nseg, nullptr, Qf);
+        spme_row_spread_kernel<P, float><<<rblocks, 32 * warps, sm, c->stream>>>(a, b, nullptr, Qf);
     } else {
+        TCP_CUDA(cudaFuncSetAttribute(spme_row_spread_kernel<P, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         spme_bin_weights_kernel<P, double><<<pblocks, threads, 0, c->stream>>>(a, b);
-        spme_row_spread_kernel<P, double><<<rblocks, 256, 0, c->stream>>>(a, b, nseg, Q, nullptr);
+        spme_row_spread_kernel<P, double><<<rblocks, 32 * warps, sm, c->stream>>>(a, b, Q, nullptr);
     }
     c->launches += 8;
     TCP_CUDA(cudaGetLastError());

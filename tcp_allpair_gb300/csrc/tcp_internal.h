@@ -104,7 +104,7 @@ struct tcp_ctx {
     int K1 = 0, K2 = 0, K3 = 0, Kh = 0; // Kh = K1/2+1
     // cell-sorted spreading: counting sort by the (y, z) mesh column of the spline base
     int *bin_count = nullptr, *bin_start = nullptr, *bin_bsum = nullptr;   // [K2 K3 (+1)], block sums
-    int *bin_rank = nullptr, *bin_list = nullptr, *bin_ebx = nullptr;      // [n]
+    int *bin_rank = nullptr, *bin_list = nullptr, *bin_ebx = nullptr, *bin_eby = nullptr;   // [n]
     void *bin_ew = nullptr, *bin_eq = nullptr;                               // weights [n][3][P], charges [n]
     double *Q = nullptr;                // real mesh [K3][K2][K1]
     cufftDoubleComplex *Qk = nullptr;   // [K3][K2][Kh]
