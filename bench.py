@@ -146,7 +146,7 @@ def reduce_sum(dist, x: float) -> float:
 
 def profile_traffic():
     """DRAM bytes per launch of the pair kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "pair_fp32c_kelbg_n32768.md"
+    p = ROOT / "profiles" / "pair_n3_x2_kelbg_n32768.md"
     if not p.exists():
         return None
     m = re.search(r"dram_bytes_per_launch_full_size:\s*([0-9.eE+]+)", p.read_text())
