@@ -15,10 +15,15 @@ namespace tcp {
 
 constexpr int kIntThreads = 256;
 
+// GB300's FP64 pipe runs at 1/64 of the FP32 rate and an FP64 division is a
+// chain of about ten FP64 operations, so the per-particle kernels divide by
+// the box length through its reciprocal (iL = 1/L, set on the host) and by
+// the mass through dt/(2m) computed once per thread.
+
 // 2^32 units per box length; the int32 difference of two coordinates is the
 // minimum-image separation.
-__device__ __forceinline__ int fixed_coord(double x, double L) {
-    double t = x / L + 0.5;
+__device__ __forceinline__ int fixed_coord(double x, double iL) {
+    double t = fma(x, iL, 0.5);
     t -= floor(t);
     const unsigned long long u = (unsigned long long)llrint(t * 4294967296.0);
     return (int)(unsigned)(u & 0xffffffffull);
@@ -31,18 +36,24 @@ struct IntArgs {
     int nel, n;
     double xm0, xm1;
     double L0, L1, L2;
+    double iL0, iL1, iL2;    // 1/L
 };
 
 __device__ __forceinline__ void store_pos(const IntArgs &a, int i, double x0, double x1, double x2) {
     a.x[i] = x0;
     a.x[(size_t)a.n + i] = x1;
     a.x[2 * (size_t)a.n + i] = x2;
-    a.xq[i] = make_int4(fixed_coord(x0, a.L0), fixed_coord(x1, a.L1), fixed_coord(x2, a.L2), 0);
+    a.xq[i] = make_int4(fixed_coord(x0, a.iL0), fixed_coord(x1, a.iL1), fixed_coord(x2, a.iL2), 0);
     a.xd[i] = make_double4_32a(x0, x1, x2, 0.0);
 }
 
-// x - L DNINT(x/L) (vverlet.f90:153)
-__device__ __forceinline__ double wrap(double x, double L) { return x - L * round(x / L); }
+// x - L DNINT(x/L) (vverlet.f90:153); x/L from the reciprocal with one FMA
+// correction (the quotient to within rounding of the divided value)
+__device__ __forceinline__ double wrap(double x, double L, double iL) {
+    double q = x * iL;
+    q = fma(fma(-q, L, x), iL, q);
+    return x - L * round(q);
+}
 
 __global__ void refresh_kernel(const IntArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -55,8 +66,8 @@ __global__ void shift_kernel(const IntArgs a, double sdt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     double y[3];
-    const double L[3] = {a.L0, a.L1, a.L2};
-    for (int k = 0; k < 3; ++k) y[k] = wrap(a.x[(size_t)k * a.n + i] + sdt * a.v[(size_t)k * a.n + i], L[k]);
+    const double L[3] = {a.L0, a.L1, a.L2}, iL[3] = {a.iL0, a.iL1, a.iL2};
+    for (int k = 0; k < 3; ++k) y[k] = wrap(a.x[(size_t)k * a.n + i] + sdt * a.v[(size_t)k * a.n + i], L[k], iL[k]);
     store_pos(a, i, y[0], y[1], y[2]);
 }
 
@@ -65,17 +76,19 @@ __global__ void vverlet1_kernel(const IntArgs a, double dt, double alpha_lgv, in
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const double xm = i < a.nel ? a.xm0 : a.xm1;
-    const double L[3] = {a.L0, a.L1, a.L2};
+    const double hdm = 0.5 * dt / xm;                  // dt/(2m)
+    const double damp = 1.0 - alpha_lgv * hdm;
+    const double L[3] = {a.L0, a.L1, a.L2}, iL[3] = {a.iL0, a.iL1, a.iL2};
     double y[3];
     for (int k = 0; k < 3; ++k) {
         const size_t o = (size_t)k * a.n + i;
         double vk = a.v[o];
         if (stoch)
-            vk = vk * (1.0 - 0.5 * alpha_lgv * dt / xm) + 0.5 * dt * a.f[o] / xm;
+            vk = vk * damp + hdm * a.f[o];             // vverlet.f90:37-38
         else
-            vk = vk + 0.5 * dt * a.f[o] / xm;
+            vk = vk + hdm * a.f[o];                    // vverlet.f90:151
         a.v[o] = vk;
-        y[k] = wrap(a.x[o] + dt * vk, L[k]);
+        y[k] = wrap(a.x[o] + dt * vk, L[k], iL[k]);    // vverlet.f90:152-153
     }
     store_pos(a, i, y[0], y[1], y[2]);
 }
@@ -154,6 +167,8 @@ __global__ void kick2_kernel(const KickArgs k) {
     if (i < a.n) {
         const int s = i < a.nel ? 0 : 1;
         const double xm = s == 0 ? a.xm0 : a.xm1;
+        const double hdm = 0.5 * k.dt / xm;               // dt/(2m)
+        const double idamp = k.thermo == TCP_THERMO_STOCH ? 1.0 / (1.0 + k.alpha_lgv * hdm) : 1.0;
         double vv[3];
         double eta[3] = {0.0, 0.0, 0.0};
         if (k.thermo == TCP_THERMO_STOCH) gauss3(k.seed, (long long)*k.step, i, eta);
@@ -164,9 +179,9 @@ __global__ void kick2_kernel(const KickArgs k) {
             if (k.remove_net) fd -= fbar[d];                                 // force.f90:999-1004
             if (k.thermo == TCP_THERMO_STOCH) {
                 fd = fd + eta[d] * beta;                                     // vverlet.f90:95
-                vv[d] = (a.v[o] + 0.5 * k.dt * fd / xm) / (1.0 + 0.5 * k.alpha_lgv * k.dt / xm);
+                vv[d] = (a.v[o] + hdm * fd) * idamp;                          // vverlet.f90:96-97
             } else {
-                vv[d] = a.v[o] + 0.5 * k.dt * fd / xm;                       // vverlet.f90:197
+                vv[d] = a.v[o] + hdm * fd;                                   // vverlet.f90:197
             }
             if (k.remove_net || k.thermo == TCP_THERMO_STOCH) a.f[o] = fd;
             a.v[o] = vv[d];
@@ -357,6 +372,9 @@ static IntArgs int_args(tcp_ctx *c) {
     a.L0 = c->p.box[0];
     a.L1 = c->p.box[1];
     a.L2 = c->p.box[2];
+    a.iL0 = 1.0 / a.L0;
+    a.iL1 = 1.0 / a.L1;
+    a.iL2 = 1.0 / a.L2;
     return a;
 }
 

@@ -396,11 +396,14 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
 
 // MODE 0: scalar FP32, i-force accumulators in registers; 1: packed FP32x2
 // (Horner erfc), accumulators in shared memory; 2: as 1 with Estrin's erfc.
-template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH, int MODE = 0>
-__global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args a) {
+// W: warps per CTA (i-tile = 32 R W particles).
+template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH, int MODE = 0, int W = kN3Warps>
+__global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
+    static_assert(W >= 4, "the reaction flush needs at least kN3Sub threads");
+    constexpr int NT = 32 * W;
     constexpr bool X2 = MODE >= 1;
     constexpr bool SACC = MODE >= 1;
-    constexpr int TILE = 32 * R * kN3Warps;
+    constexpr int TILE = 32 * R * W;
     constexpr int SPT = TILE / kN3Sub;
     __shared__ __align__(128) int4 tiles[kN3Stages][kN3Sub];
     __shared__ __align__(8) uint64_t bars[kN3Stages];
@@ -410,7 +413,7 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
     // per-thread TwoSum (hi, lo) i-force accumulators, touched once per item:
     // in shared memory ([slot][thread], conflict-free) for the packed forms,
     // whose constant pairs need the registers
-    __shared__ float sacc[SACC ? 2 * 3 * R : 1][SACC ? kN3Threads : 1];
+    __shared__ float sacc[SACC ? 2 * 3 * R : 1][SACC ? NT : 1];
     float hi[SACC ? 1 : R][3], lo[SACC ? 1 : R][3];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -418,7 +421,7 @@ __global__ void __launch_bounds__(kN3Threads, MINB) pair_n3_kernel(const N3Args 
     const long long it1 = a.nstatic * (long long)(blockIdx.x + 1) / gridDim.x;
     const int nst = (int)(it1 - it0);
 
-    for (int k = tid; k < kN3Sub * 3; k += kN3Threads) (&sjacc[0][0])[k] = 0.f;
+    for (int k = tid; k < kN3Sub * 3; k += NT) (&sjacc[0][0])[k] = 0.f;
     if (tid == 0) {
         for (int s = 0; s < kN3Stages; ++s) mbar_init(&bars[s], 1);
         fence_mbar_init();
@@ -617,19 +620,19 @@ bool n3_applicable(const tcp_ctx *c) {
 typedef void (*N3Kernel)(const N3Args);
 struct N3Variant {
     N3Kernel energy, plain;
-    int R;
+    int R, W;
     const char *name;
 };
 static const N3Variant kVariants[] = {
-    {pair_n3_kernel<true, 2, 2, 3, false>, pair_n3_kernel<false, 2, 2, 3, false>, 2, "n3_r2_u2_b3"},
-    {pair_n3_kernel<true, 2, 1, 3, false>, pair_n3_kernel<false, 2, 1, 3, false>, 2, "n3_r2_u1_b3"},
-    {pair_n3_kernel<true, 4, 1, 2, false>, pair_n3_kernel<false, 4, 1, 2, false>, 4, "n3_r4_u1_b2"},
-    {pair_n3_kernel<true, 4, 2, 2, false>, pair_n3_kernel<false, 4, 2, 2, false>, 4, "n3_r4_u2_b2"},
-    {pair_n3_kernel<true, 4, 2, 2, false, 1>, pair_n3_kernel<false, 4, 2, 2, false, 1>, 4, "n3_r4_u2_b2_x2"},
-    {pair_n3_kernel<true, 4, 1, 2, false, 1>, pair_n3_kernel<false, 4, 1, 2, false, 1>, 4, "n3_r4_u1_b2_x2"},
-    {pair_n3_kernel<true, 2, 2, 3, false, 1>, pair_n3_kernel<false, 2, 2, 3, false, 1>, 2, "n3_r2_u2_b3_x2"},
-    {pair_n3_kernel<true, 4, 1, 2, false, 2>, pair_n3_kernel<false, 4, 1, 2, false, 2>, 4, "n3_r4_u1_b2_x2e"},
-    {pair_n3_kernel<true, 4, 1, 3, false, 1>, pair_n3_kernel<false, 4, 1, 3, false, 1>, 4, "n3_r4_u1_b3_x2"},
+    {pair_n3_kernel<true, 2, 2, 3, false>, pair_n3_kernel<false, 2, 2, 3, false>, 2, 8, "n3_r2_u2_b3"},
+    {pair_n3_kernel<true, 2, 1, 3, false>, pair_n3_kernel<false, 2, 1, 3, false>, 2, 8, "n3_r2_u1_b3"},
+    {pair_n3_kernel<true, 4, 1, 2, false>, pair_n3_kernel<false, 4, 1, 2, false>, 4, 8, "n3_r4_u1_b2"},
+    {pair_n3_kernel<true, 4, 2, 2, false>, pair_n3_kernel<false, 4, 2, 2, false>, 4, 8, "n3_r4_u2_b2"},
+    {pair_n3_kernel<true, 4, 2, 2, false, 1>, pair_n3_kernel<false, 4, 2, 2, false, 1>, 4, 8, "n3_r4_u2_b2_x2"},
+    {pair_n3_kernel<true, 4, 1, 2, false, 1>, pair_n3_kernel<false, 4, 1, 2, false, 1>, 4, 8, "n3_r4_u1_b2_x2"},
+    {pair_n3_kernel<true, 2, 2, 3, false, 1>, pair_n3_kernel<false, 2, 2, 3, false, 1>, 2, 8, "n3_r2_u2_b3_x2"},
+    {pair_n3_kernel<true, 4, 1, 5, false, 1, 4>, pair_n3_kernel<false, 4, 1, 5, false, 1, 4>, 4, 4, "n3_r4_u1_w4b5_x2"},
+    {pair_n3_kernel<true, 4, 1, 3, false, 1>, pair_n3_kernel<false, 4, 1, 3, false, 1>, 4, 8, "n3_r4_u1_b3_x2"},
 };
 constexpr int kN3Variants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -638,7 +641,7 @@ const char *n3_variant_name(int v) { return v >= 1 && v <= kN3Variants ? kVarian
 
 int n3_grid_for(const tcp_ctx *c, int v) {
     int bps = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kVariants[v - 1].energy, kN3Threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kVariants[v - 1].energy, 32 * kVariants[v - 1].W, 0);
     return std::max(1, c->num_sms * std::max(1, bps));
 }
 
@@ -668,7 +671,8 @@ N3Geom n3_geometry(int off, int nel, int nion, int tile, long long item0, long l
 
 int launch_pair_n3(tcp_ctx *c, bool energy) {
     const int v = std::min(std::max(c->pair_variant, 1), kN3Variants);
-    const int tile = 32 * kVariants[v - 1].R * kN3Warps;
+    const int tile = 32 * kVariants[v - 1].R * kVariants[v - 1].W;
+    const int nt = 32 * kVariants[v - 1].W;
     N3Args a;
     std::memset(&a, 0, sizeof a);
     long long total = 0;
@@ -688,9 +692,9 @@ int launch_pair_n3(tcp_ctx *c, bool energy) {
     TCP_CUDA(cudaMemsetAsync(c->counter, 0, sizeof(unsigned), c->stream));
     if (energy) {
         TCP_CUDA(cudaMemsetAsync(c->upart, 0, sizeof(double) * (size_t)c->n_upart, c->stream));
-        kVariants[v - 1].energy<<<grid, kN3Threads, 0, c->stream>>>(a);
+        kVariants[v - 1].energy<<<grid, nt, 0, c->stream>>>(a);
     } else {
-        kVariants[v - 1].plain<<<grid, kN3Threads, 0, c->stream>>>(a);
+        kVariants[v - 1].plain<<<grid, nt, 0, c->stream>>>(a);
     }
     c->launches++;
     TCP_CUDA(cudaGetLastError());
