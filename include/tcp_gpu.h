@@ -224,6 +224,9 @@ int tcp_batch_download(tcp_batch *b, int rep, double *x, double *v, double *f);
 int tcp_batch_force(tcp_batch *b, tcp_energies *e);
 /* nsteps MD steps of every replica with time step dt; e[nrep] may be NULL. */
 int tcp_batch_md_steps(tcp_batch *b, double dt, int nsteps, tcp_energies *e);
+/* The batched real-space kernel the batch autotuner picked (variant index) and
+ * the per-candidate times in ms (0 when not timed), up to nmax entries. */
+int tcp_batch_autotune_report(tcp_batch *b, int *variant, double *ms, int nmax);
 /* Mean device time of one batched step over nsteps graph replays (CUDA events). */
 int tcp_batch_time_steps(tcp_batch *b, double dt, int nsteps, double *ms_per_step);
 

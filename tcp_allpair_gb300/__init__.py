@@ -309,6 +309,14 @@ class Batch:
         self._chk(self.lib.tcp_batch_time_steps(self.h, dt, nsteps, C.byref(ms)), "tcp_batch_time_steps")
         return ms.value
 
+    def autotune_report(self):
+        """(chosen batched pair-kernel variant, per-variant ms measured by the batch autotuner)."""
+        v = C.c_int()
+        ms = np.zeros(8)
+        self._chk(self.lib.tcp_batch_autotune_report(self.h, C.byref(v), ms.ctypes.data_as(C.POINTER(C.c_double)), 8),
+                  "tcp_batch_autotune_report")
+        return v.value, ms
+
 
 def fp32_peak(device: int = 0) -> float:
     """Measured FP32 FFMA rate of the device in 1e12 FFMA/s."""

@@ -34,6 +34,7 @@ struct BRep {
     double xm[2], q[2];      // masses, scaled charges
     int K[3], Kh;
     long long mesh_off, half_off;
+    int bin_off, grp_off;    // first spreading bin (K2 K3 per replica) and first 8-row group
     double V;
     double Te, Ti, tau;
     int thermo;
@@ -100,37 +101,147 @@ __global__ void b_refresh_kernel(const BParticles a) {
                         fixed_coord_b(a.x[2 * (size_t)a.ntot + i], R.L[2]), 0);
 }
 
+// ---- atomic-free spreading, cell-sorted per replica ------------------------------
+// The single-system scheme of spme.cu over all replicas: particles are binned by
+// the (y, z) mesh column of their spline base (replica r owns bins
+// [bin_off, bin_off + K2 K3)), the bins are index-ordered, and a warp gathers 8
+// mesh rows of one replica from the bins that reach them, summing in
+// compensated two-float FP32 (no atomics; the same order on every call).
+constexpr int kBRows = 8;
+constexpr int kBRowWarps = 4;
+
 template <int P>
-__global__ void b_spread_kernel(const BParticles a, double *__restrict__ Q) {
+__global__ void b_bin_count_kernel(const BParticles a, SpreadBins bins) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.ntot) return;
     const BRep &R = a.reps[a.rep_of[i]];
-    const double q = (i - R.off) < R.nel ? R.q[0] : R.q[1];
-    double W[3][P], dW[3][P];
     int base[3];
-    for (int d = 0; d < 3; ++d) {
-        const double u = (double)R.K[d] * (a.x[(size_t)d * a.ntot + i] + R.L[d] * .5) / R.L[d];
-        spline_w<P, double>(u, W[d], dW[d]);
-        base[d] = (int)trunc(u) - (P - 3);
-    }
-    double *mesh = Q + R.mesh_off;
-#pragma unroll 1
-    for (int k = 0; k < P; ++k) {
-        const int iz = wrapi(base[2] + k, R.K[2]);
-#pragma unroll 1
-        for (int j = 0; j < P; ++j) {
-            const int iy = wrapi(base[1] + j, R.K[1]);
-            const double qyz = q * W[1][j] * W[2][k];
-            double *row = mesh + (size_t)R.K[0] * (iy + (size_t)R.K[1] * iz);
 #pragma unroll
-            for (int ii = 0; ii < P; ++ii) atomicAdd(row + wrapi(base[0] + ii, R.K[0]), qyz * W[0][ii]);
-        }
+    for (int d = 1; d < 3; ++d) {
+        const double u = (double)R.K[d] * (a.x[(size_t)d * a.ntot + i] + R.L[d] * .5) / R.L[d];
+        base[d] = wrapi((int)trunc(u) - (P - 3), R.K[d]);
     }
+    const int bin = R.bin_off + base[1] + R.K[1] * base[2];
+    bins.rank[i] = atomicAdd(&bins.count[bin], 1);
+    bins.ebx[i] = bin;
 }
 
-__global__ void b_to_float_kernel(const double *__restrict__ q, float *__restrict__ qf, long n) {
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        qf[i] = (float)q[i];
+template <int P>
+__global__ void b_bin_weights_kernel(const BParticles a, SpreadBins bins) {
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= a.ntot) return;
+    const int i = bins.list[pos];
+    const BRep &R = a.reps[a.rep_of[i]];
+    float *w = static_cast<float *>(bins.ew) + (size_t)pos * 3 * P;
+    float W[P], dW[P];
+    int base[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double u = (double)R.K[d] * (a.x[(size_t)d * a.ntot + i] + R.L[d] * .5) / R.L[d];
+        spline_w<P, float>(u, W, dW);
+#pragma unroll
+        for (int j = 0; j < P; ++j) w[d * P + j] = W[j];
+        base[d] = wrapi((int)trunc(u) - (P - 3), R.K[d]);
+    }
+    bins.ebx[pos] = base[0];
+    bins.eby[pos] = base[1];
+    static_cast<float *>(bins.eq)[pos] = (float)((i - R.off) < R.nel ? R.q[0] : R.q[1]);
+}
+
+__host__ __device__ constexpr size_t b_row_warp_bytes(int P, int k1max) {
+    return (size_t)kBRows * k1max * 8 + 32 * (8 + (1 + 3 * P) * 4);
+}
+
+template <int P>
+__global__ void __launch_bounds__(32 * kBRowWarps) b_row_spread_kernel(const BParticles a, const SpreadBins bins,
+                                                                       int nrep, int ngroups, int k1max,
+                                                                       float *__restrict__ Qf) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = blockIdx.x * (blockDim.x >> 5) + warp;
+    if (g >= ngroups) return;                                     // warp-uniform
+    int lo = 0, hi_ = nrep - 1;
+    while (lo < hi_) {
+        const int mid = (lo + hi_ + 1) >> 1;
+        if (a.reps[mid].grp_off <= g) lo = mid; else hi_ = mid - 1;
+    }
+    const BRep &R = a.reps[lo];
+    const int K1 = R.K[0], K2 = R.K[1], K3 = R.K[2];
+    const int ngy = (K2 + kBRows - 1) / kBRows, lg = g - R.grp_off;
+    const int y0 = (lg % ngy) * kBRows, z = lg / ngy;
+    const int nrow = min(kBRows, K2 - y0);
+    unsigned char *base = smem + (size_t)warp * b_row_warp_bytes(P, k1max);
+    float *hi = reinterpret_cast<float *>(base);                    // [kBRows][K1]
+    float *lo_ = hi + (size_t)kBRows * k1max;
+    float *sw = lo_ + (size_t)kBRows * k1max;                       // [32][3P]
+    float *sq = sw + 32 * 3 * P;
+    int *sbx = reinterpret_cast<int *>(sq + 32), *sby = sbx + 32;
+    for (int k = lane; k < kBRows * K1; k += 32) {
+        hi[k] = 0.f;
+        lo_[k] = 0.f;
+    }
+    __syncwarp();
+    const float *ew = static_cast<const float *>(bins.ew);
+    const float *eq = static_cast<const float *>(bins.eq);
+    const int nb = nrow + P - 1;
+    for (int jz = 0; jz < P; ++jz) {
+        int bz = z - jz;
+        bz += bz < 0 ? K3 : 0;
+        int by0 = y0 - P + 1, len0 = nb, len1 = 0;
+        if (by0 < 0) {
+            by0 += K2;
+            len0 = min(nb, K2 - by0);
+            len1 = nb - len0;
+        }
+        if (nb >= K2) {
+            by0 = 0;
+            len0 = K2;
+            len1 = 0;
+        }
+        for (int piece = 0; piece < 2; ++piece) {
+            const int blo = R.bin_off + (piece == 0 ? by0 : 0) + K2 * bz, len = piece == 0 ? len0 : len1;
+            if (len <= 0) continue;
+            const int p0 = bins.start[blo], p1 = bins.start[blo + len];
+            for (int c0 = p0; c0 < p1; c0 += 32) {
+                const int ne = min(32, p1 - c0);
+                if (lane < ne) {
+                    const int pos = c0 + lane;
+#pragma unroll
+                    for (int j = 0; j < 3 * P; ++j) sw[lane * 3 * P + j] = ew[(size_t)pos * 3 * P + j];
+                    sq[lane] = eq[pos];
+                    sbx[lane] = bins.ebx[pos];
+                    sby[lane] = bins.eby[pos];
+                }
+                __syncwarp();
+                for (int e = 0; e < ne; ++e) {
+                    const float *w = sw + e * 3 * P;
+                    const float qz = sq[e] * w[2 * P + jz];
+                    const int bx = sbx[e], by = sby[e];
+                    for (int l = lane; l < P * P; l += 32) {
+                        const int jy = l / P, jx = l - jy * P;
+                        int rl = by + jy - y0;
+                        rl += rl < 0 ? K2 : 0;
+                        rl -= rl >= K2 ? K2 : 0;
+                        if (rl < nrow) {
+                            int x = bx + jx;
+                            x -= x >= K1 ? K1 : 0;
+                            const float v = qz * w[P + jy] * w[jx];
+                            const int k = rl * K1 + x;
+                            const float sum = hi[k] + v, bp = sum - hi[k];
+                            lo_[k] += (hi[k] - (sum - bp)) + (v - bp);
+                            hi[k] = sum;
+                        }
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+    }
+    float *mesh = Qf + R.mesh_off;
+    for (int k = lane; k < nrow * K1; k += 32) {
+        const int rl = k / K1, x = k - rl * K1;
+        mesh[(size_t)K1 * ((y0 + rl) + (size_t)K2 * z) + x] = hi[k] + lo_[k];
+    }
 }
 
 // influence multiply; blocks [blk0[r], blk0[r+1]) belong to replica r
@@ -288,12 +399,20 @@ struct tcp_batch {
     std::vector<tcp::BRep> h_reps;
     void *n3reps = nullptr;             // device Newton-3 table
     long long n3_items = 0;
+    std::vector<tcp::PairConsts> pcs;   // per-replica pair constants (the table is refilled per variant)
+    int pair_variant = 0;               // batched Newton-3 variant (batch autotuner)
+    bool tuned = false;
+    double variant_ms[8] = {};
     double *acc = nullptr;              // accumulator block
     double *h_acc = nullptr;            // pinned copy
     unsigned *status = nullptr, *counter = nullptr;
     // SPME
-    double *Q = nullptr;
     float *Qf = nullptr, *infl = nullptr;
+    // cell-sorted spreading
+    int *bin_count = nullptr, *bin_start = nullptr, *bin_bsum = nullptr, *bin_rank = nullptr;
+    int *bin_list = nullptr, *bin_ebx = nullptr, *bin_eby = nullptr;
+    float *bin_ew = nullptr, *bin_eq = nullptr;
+    int nbins = 0, ngroups = 0, k1max = 0;
     cufftComplex *Qk = nullptr;
     long long mesh_total = 0, half_total = 0;
     int *blk0 = nullptr;
@@ -338,13 +457,52 @@ static BParticles parts(tcp_batch *b) {
     return a;
 }
 
+static SpreadBins b_bins(tcp_batch *b) {
+    SpreadBins s;
+    s.count = b->bin_count;
+    s.start = b->bin_start;
+    s.bsum = b->bin_bsum;
+    s.rank = b->bin_rank;
+    s.list = b->bin_list;
+    s.ebx = b->bin_ebx;
+    s.eby = b->bin_eby;
+    s.ew = b->bin_ew;
+    s.eq = b->bin_eq;
+    return s;
+}
+
 template <int P>
 static void b_spme_launch(tcp_batch *b, bool gather) {
     const int blocks = (b->ntot + 127) / 128;
-    if (!gather)
-        b_spread_kernel<P><<<blocks, 128, 0, b->stream>>>(parts(b), b->Q);
-    else
+    if (gather) {
         b_gather_kernel<P><<<blocks, 128, 0, b->stream>>>(parts(b), b->Qf);
+        return;
+    }
+    const SpreadBins bins = b_bins(b);
+    cudaMemsetAsync(b->bin_count, 0, sizeof(int) * (size_t)b->nbins, b->stream);
+    b_bin_count_kernel<P><<<blocks, 128, 0, b->stream>>>(parts(b), bins);
+    launch_bin_sort(b->stream, b->ntot, b->nbins, bins);
+    b_bin_weights_kernel<P><<<blocks, 128, 0, b->stream>>>(parts(b), bins);
+    const size_t sm = kBRowWarps * b_row_warp_bytes(P, b->k1max);   // attribute set at tcp_batch_create
+    b_row_spread_kernel<P><<<(b->ngroups + kBRowWarps - 1) / kBRowWarps, 32 * kBRowWarps, sm, b->stream>>>(
+        parts(b), bins, b->nrep, b->ngroups, b->k1max, b->Qf);
+}
+
+template <int P>
+static int b_prepare_spread_p(tcp_batch *b) {
+    TCP_CUDA(cudaFuncSetAttribute(b_row_spread_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(kBRowWarps * b_row_warp_bytes(P, b->k1max))));
+    return TCP_OK;
+}
+
+static int b_prepare_spread(tcp_batch *b) {
+    switch (b->order) {
+        case 4: return b_prepare_spread_p<4>(b);
+        case 5: return b_prepare_spread_p<5>(b);
+        case 6: return b_prepare_spread_p<6>(b);
+        case 7: return b_prepare_spread_p<7>(b);
+        default: return b_prepare_spread_p<8>(b);
+    }
 }
 
 static void b_spme(tcp_batch *b, bool gather) {
@@ -365,10 +523,7 @@ static int b_step(tcp_batch *b, double dt) {
     (void)launches_before;
     TCP_CUDA(cudaMemsetAsync(A.um, 0, sizeof(double) * 8 * (size_t)b->nrep, b->stream));   // um, mv0, mv1, fsum
     b_vverlet1_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), dt);
-    TCP_CUDA(cudaMemsetAsync(b->Q, 0, sizeof(double) * (size_t)b->mesh_total, b->stream));
-    b_spme(b, false);
-    b_to_float_kernel<<<(int)std::min<long long>((b->mesh_total + 255) / 256, 8192), 256, 0, b->stream>>>(
-        b->Q, b->Qf, (long)b->mesh_total);
+    b_spme(b, false);                                   // atomic-free, every mesh point written
     for (auto &g : b->groups)
         if (cufftExecR2C(g.fwd, b->Qf + g.mesh_off, b->Qk + g.half_off) != CUFFT_SUCCESS)
             return set_error(TCP_ERR_CUFFT, "batched cufftExecR2C failed");
@@ -378,14 +533,65 @@ static int b_step(tcp_batch *b, double dt) {
             return set_error(TCP_ERR_CUFFT, "batched cufftExecC2R failed");
     b_spme(b, true);
     int rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
-                                  b->status, b->counter, b->num_sms, true);
+                                  b->status, b->counter, b->num_sms, true, b->pair_variant);
     if (rc) return rc;
     b_finalize_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), A.fsum);
     b_kick2_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), dt, A.fsum, A.mv0);
     b_rescale_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), dt, A.mv0, A.mv1);
-    b->launches += 9;
+    b->launches += 15;
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;
+}
+
+// Newton-3 item table for variant v (its i-tile), uploaded on the stream
+static int b_fill_n3(tcp_batch *b, int v) {
+    std::vector<unsigned char> n3h(n3_rep_bytes() * b->nrep);
+    b->n3_items = n3_batch_fill(n3h.data(), b->nrep, b->off.data(), b->nel.data(), b->nion.data(), b->pcs.data(),
+                                n3_batch_tile(v));
+    TCP_CUDA(cudaMemcpyAsync(b->n3reps, n3h.data(), n3h.size(), cudaMemcpyHostToDevice, b->stream));
+    TCP_CUDA(cudaStreamSynchronize(b->stream));
+    b->pair_variant = v;
+    return TCP_OK;
+}
+
+// Batch autotuner: times every batched Newton-3 variant on this batch's items
+// (one warm-up and two timed launches each, CUDA events) and keeps the
+// fastest; TCP_BATCH_VARIANT forces one.  Runs before the step graph is captured.
+static int b_autotune(tcp_batch *b) {
+    if (b->tuned) return TCP_OK;
+    b->tuned = true;
+    const int nv = n3_batch_variant_count();
+    if (const char *forced = getenv("TCP_BATCH_VARIANT")) return b_fill_n3(b, std::min(std::max(atoi(forced), 0), nv - 1));
+    const BAcc A = acc_of(b);
+    const int nb = (b->ntot + kBThreads - 1) / kBThreads;
+    b_refresh_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b));
+    cudaEvent_t e0, e1;
+    TCP_CUDA(cudaEventCreate(&e0));
+    TCP_CUDA(cudaEventCreate(&e1));
+    double best = 1e300;
+    int best_v = 0, rc = TCP_OK;
+    for (int v = 0; v < nv && v < 8 && !rc; ++v) {
+        if ((rc = b_fill_n3(b, v))) break;
+        rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
+                                  b->status, b->counter, b->num_sms, true, v);
+        cudaEventRecord(e0, b->stream);
+        for (int r = 0; r < 2 && !rc; ++r)
+            rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
+                                      b->status, b->counter, b->num_sms, true, v);
+        cudaEventRecord(e1, b->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        b->variant_ms[v] = ms / 2;
+        if (ms / 2 < best) {
+            best = ms / 2;
+            best_v = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    return b_fill_n3(b, best_v);
 }
 
 static int b_sync(tcp_batch *b) {
@@ -430,8 +636,10 @@ int tcp_batch_destroy(tcp_batch *b) {
     }
     for (void *ptr : {(void *)b->x, (void *)b->v, (void *)b->f, (void *)b->frec, (void *)b->facc, (void *)b->xq,
                       (void *)b->rep_of, (void *)b->reps, b->n3reps, (void *)b->acc, (void *)b->status,
-                      (void *)b->counter, (void *)b->Q, (void *)b->Qf, (void *)b->infl, (void *)b->Qk,
-                      (void *)b->blk0})
+                      (void *)b->counter, (void *)b->Qf, (void *)b->infl, (void *)b->Qk, (void *)b->blk0,
+                      (void *)b->bin_count, (void *)b->bin_start, (void *)b->bin_bsum, (void *)b->bin_rank,
+                      (void *)b->bin_list, (void *)b->bin_ebx, (void *)b->bin_eby, (void *)b->bin_ew,
+                      (void *)b->bin_eq})
         cudaFree(ptr);
     if (b->h_acc) cudaFreeHost(b->h_acc);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -544,8 +752,26 @@ int tcp_batch_create(const tcp_params *params, const int *nel, const int *nion, 
         cufftSetStream(g.inv, b->stream);
         b->groups.push_back(g);
     }
-    TCP_BALLOC(b->Q, sizeof(double) * (size_t)b->mesh_total);
     TCP_BALLOC(b->Qf, sizeof(float) * (size_t)b->mesh_total);
+    // spreading bins (K2 K3 per replica) and 8-row groups (ceil(K2/8) K3 per replica)
+    for (int r = 0; r < nrep; ++r) {
+        BRep &R = b->h_reps[r];
+        R.bin_off = b->nbins;
+        R.grp_off = b->ngroups;
+        b->nbins += b->p[r].K[1] * b->p[r].K[2];
+        b->ngroups += ((b->p[r].K[1] + kBRows - 1) / kBRows) * b->p[r].K[2];
+        b->k1max = std::max(b->k1max, b->p[r].K[0]);
+    }
+    TCP_BALLOC(b->bin_count, sizeof(int) * ((size_t)b->nbins + 1));
+    TCP_BALLOC(b->bin_start, sizeof(int) * ((size_t)b->nbins + 1));
+    TCP_BALLOC(b->bin_bsum, sizeof(int) * (size_t)((b->nbins + bin_scan_block() - 1) / bin_scan_block()));
+    TCP_BALLOC(b->bin_rank, sizeof(int) * (size_t)b->ntot);
+    TCP_BALLOC(b->bin_list, sizeof(int) * (size_t)b->ntot);
+    TCP_BALLOC(b->bin_ebx, sizeof(int) * (size_t)b->ntot);
+    TCP_BALLOC(b->bin_eby, sizeof(int) * (size_t)b->ntot);
+    TCP_BALLOC(b->bin_ew, sizeof(float) * 3 * kMaxOrder * (size_t)b->ntot);
+    TCP_BALLOC(b->bin_eq, sizeof(float) * (size_t)b->ntot);
+    if (b_prepare_spread(b)) return fail(TCP_ERR_CUDA);
     TCP_BALLOC(b->infl, sizeof(float) * (size_t)b->half_total);
     TCP_BALLOC(b->Qk, sizeof(cufftComplex) * (size_t)b->half_total);
     TCP_BALLOC(b->blk0, sizeof(int) * (nrep + 1));
@@ -623,10 +849,11 @@ int tcp_batch_ewald_self(tcp_batch *b, double *Uo) {
         blk0[r + 1] = blk0[r] + (int)std::max<long long>(1, std::min<long long>((half + 255) / 256, 512));
     }
     b->infl_blocks = blk0[nrep];
-    std::vector<unsigned char> n3h(n3_rep_bytes() * nrep);
-    b->n3_items = n3_batch_fill(n3h.data(), nrep, b->off.data(), b->nel.data(), b->nion.data(), pcs.data());
+    b->pcs = pcs;
+    b->tuned = false;
+    int frc = b_fill_n3(b, b->pair_variant);
+    if (frc) return frc;
     TCP_CUDA(cudaMemcpyAsync(b->reps, b->h_reps.data(), sizeof(BRep) * nrep, cudaMemcpyHostToDevice, b->stream));
-    TCP_CUDA(cudaMemcpyAsync(b->n3reps, n3h.data(), n3h.size(), cudaMemcpyHostToDevice, b->stream));
     TCP_CUDA(cudaMemcpyAsync(b->blk0, blk0.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice, b->stream));
     TCP_CUDA(cudaMemcpyAsync(b->infl, infl.data(), sizeof(float) * infl.size(), cudaMemcpyHostToDevice, b->stream));
     TCP_CUDA(cudaStreamSynchronize(b->stream));
@@ -686,14 +913,12 @@ int tcp_batch_download(tcp_batch *b, int rep, double *x, double *v, double *f) {
 int tcp_batch_force(tcp_batch *b, tcp_energies *e) {
     if (!b || !b->ready) return set_error(TCP_ERR_STATE, "tcp_batch_ewald_self must be called first");
     cudaSetDevice(b->device);
+    if (int arc = b_autotune(b)) return arc;
     const BAcc A = acc_of(b);
     const int nb = (b->ntot + kBThreads - 1) / kBThreads;
     b_refresh_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b));
     TCP_CUDA(cudaMemsetAsync(A.um, 0, sizeof(double) * 8 * (size_t)b->nrep, b->stream));
-    TCP_CUDA(cudaMemsetAsync(b->Q, 0, sizeof(double) * (size_t)b->mesh_total, b->stream));
-    b_spme(b, false);
-    b_to_float_kernel<<<(int)std::min<long long>((b->mesh_total + 255) / 256, 8192), 256, 0, b->stream>>>(
-        b->Q, b->Qf, (long)b->mesh_total);
+    b_spme(b, false);                                   // atomic-free, every mesh point written
     for (auto &g : b->groups)
         if (cufftExecR2C(g.fwd, b->Qf + g.mesh_off, b->Qk + g.half_off) != CUFFT_SUCCESS)
             return set_error(TCP_ERR_CUFFT, "batched cufftExecR2C failed");
@@ -703,7 +928,7 @@ int tcp_batch_force(tcp_batch *b, tcp_energies *e) {
             return set_error(TCP_ERR_CUFFT, "batched cufftExecC2R failed");
     b_spme(b, true);
     int rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
-                                  b->status, b->counter, b->num_sms, true);
+                                  b->status, b->counter, b->num_sms, true, b->pair_variant);
     if (rc) return rc;
     b_finalize_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), A.fsum);
     // the net-force removal of the step is fused into the kick; here apply it alone
@@ -720,6 +945,7 @@ int tcp_batch_md_steps(tcp_batch *b, double dt, int nsteps, tcp_energies *e) {
     if (nsteps < 0) return set_error(TCP_ERR_BAD_PARAM, "nsteps < 0");
     cudaSetDevice(b->device);
     int rc;
+    if ((rc = b_autotune(b))) return rc;                // timing launches cannot run inside a capture
     if (!b->graph || b->graph_dt != dt) {
         if (b->graph) cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
@@ -743,6 +969,13 @@ int tcp_batch_md_steps(tcp_batch *b, double dt, int nsteps, tcp_energies *e) {
     }
     if ((rc = b_sync(b))) return rc;
     b_energies(b, e);
+    return TCP_OK;
+}
+
+int tcp_batch_autotune_report(tcp_batch *b, int *variant, double *ms, int nmax) {
+    if (!b) return set_error(TCP_ERR_BAD_PARAM, "batch is NULL");
+    if (variant) *variant = b->pair_variant;
+    for (int k = 0; ms && k < nmax && k < 8; ++k) ms[k] = b->variant_ms[k];
     return TCP_OK;
 }
 

@@ -702,35 +702,54 @@ int launch_pair_n3(tcp_ctx *c, bool energy) {
 }
 
 // ---- batch of replicas -------------------------------------------------------
-constexpr int kN3BatchR = 2;   // i-particles per lane of the batched kernel
-constexpr int kN3BatchTile = 32 * kN3BatchR * kN3Warps;
+// Variants of the batched launch (the batch autotuner picks one per batch):
+// i-particles per lane x packed FP32 x CTAs per SM.
+struct N3BatchVariant {
+    N3Kernel energy, plain;
+    int R, W;
+    const char *name;
+};
+static const N3BatchVariant kBatchVariants[] = {
+    {pair_n3_kernel<true, 2, 2, 2, true>, pair_n3_kernel<false, 2, 2, 2, true>, 2, 8, "b_r2_u2_b2"},
+    {pair_n3_kernel<true, 4, 1, 2, true, 1>, pair_n3_kernel<false, 4, 1, 2, true, 1>, 4, 8, "b_r4_u1_b2_x2"},
+    {pair_n3_kernel<true, 2, 2, 3, true, 1>, pair_n3_kernel<false, 2, 2, 3, true, 1>, 2, 8, "b_r2_u2_b3_x2"},
+    {pair_n3_kernel<true, 4, 1, 3, true, 1>, pair_n3_kernel<false, 4, 1, 3, true, 1>, 4, 8, "b_r4_u1_b3_x2"},
+};
+constexpr int kN3BatchVariants = sizeof(kBatchVariants) / sizeof(kBatchVariants[0]);
 
-int n3_batch_tile() { return kN3BatchTile; }
+int n3_batch_variant_count() { return kN3BatchVariants; }
+const char *n3_batch_variant_name(int v) { return kBatchVariants[std::min(std::max(v, 0), kN3BatchVariants - 1)].name; }
+int n3_batch_tile(int v) {
+    const N3BatchVariant &k = kBatchVariants[std::min(std::max(v, 0), kN3BatchVariants - 1)];
+    return 32 * k.R * k.W;
+}
 size_t n3_rep_bytes() { return sizeof(N3Rep); }
 
-// Fills reps (host) for replicas with the given offsets/counts/constants.
+// Fills reps (host) for replicas with the given offsets/counts/constants and
+// the i-tile of the variant.
 long long n3_batch_fill(void *reps_host, int nrep, const int *off, const int *nel, const int *nion,
-                        const PairConsts *pc) {
+                        const PairConsts *pc, int tile) {
     N3Rep *r = static_cast<N3Rep *>(reps_host);
     long long item0 = 0;
     for (int k = 0; k < nrep; ++k) {
         long long items = 0;
-        r[k].g = n3_geometry(off[k], nel[k], nion[k], kN3BatchTile, item0, &items);
+        r[k].g = n3_geometry(off[k], nel[k], nion[k], tile, item0, &items);
         r[k].c = pc[k];
         item0 += items;
     }
     return item0;
 }
 
-int n3_batch_grid(int num_sms) {
+static int n3_batch_grid(int num_sms, int v) {
     int bps = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_n3_kernel<true, kN3BatchR, 2, 2, true>, kN3Threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kBatchVariants[v].energy, 32 * kBatchVariants[v].W, 0);
     return std::max(1, num_sms * std::max(1, bps));
 }
 
 int launch_pair_n3_batch(cudaStream_t st, const int4 *xq, int ntot, double *facc, const void *reps_dev, int nrep,
                          long long total, double *ur_rep, unsigned *status, unsigned *counter, int num_sms,
-                         bool energy) {
+                         bool energy, int variant) {
+    const int v = std::min(std::max(variant, 0), kN3BatchVariants - 1);
     N3Args a;
     std::memset(&a, 0, sizeof a);
     a.xq = xq;
@@ -743,14 +762,15 @@ int launch_pair_n3_batch(cudaStream_t st, const int4 *xq, int ntot, double *facc
     a.reps = static_cast<const N3Rep *>(reps_dev);
     a.nrep = nrep;
     a.ur_rep = ur_rep;
-    const int grid = (int)std::min<long long>(n3_batch_grid(num_sms), total);
+    const int grid = (int)std::min<long long>(n3_batch_grid(num_sms, v), total);
+    const int nt = 32 * kBatchVariants[v].W;
     TCP_CUDA(cudaMemsetAsync(facc, 0, sizeof(double) * 3 * (size_t)ntot, st));
     TCP_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
     if (energy) {
         TCP_CUDA(cudaMemsetAsync(ur_rep, 0, sizeof(double) * (size_t)nrep, st));
-        pair_n3_kernel<true, kN3BatchR, 2, 2, true><<<grid, kN3Threads, 0, st>>>(a);
+        kBatchVariants[v].energy<<<grid, nt, 0, st>>>(a);
     } else {
-        pair_n3_kernel<false, kN3BatchR, 2, 2, true><<<grid, kN3Threads, 0, st>>>(a);
+        kBatchVariants[v].plain<<<grid, nt, 0, st>>>(a);
     }
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;

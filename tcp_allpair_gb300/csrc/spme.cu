@@ -56,10 +56,6 @@ constexpr int kRowWarps = 4;             // warps per CTA (fewer when the rows o
 constexpr int kScanBlock = 1024;         // bins per block of the prefix sum
 constexpr int kSortReg = 8;              // bins up to this size are sorted in registers
 
-struct SpreadBins {
-    int *count, *start, *bsum, *rank, *list, *ebx, *eby;
-    void *ew, *eq;                       // [n][3][P] weights, [n] charges (T = float or double)
-};
 
 template <int P>
 __global__ void spme_bin_count_kernel(const SpmeArgs a, SpreadBins b) {
@@ -502,6 +498,8 @@ static int spme_energy_blocks(const tcp_ctx *c) {
     return (int)std::min<long>((total + 255) / 256, 4096);
 }
 
+static int prepare_cell_spread(tcp_ctx *c);
+
 int spme_setup(tcp_ctx *c) {
     const tcp_params &p = c->p;
     c->K1 = p.K[0];
@@ -544,6 +542,7 @@ int spme_setup(tcp_ctx *c) {
         cufftSetStream(c->plan_b, c->stream);
         c->plans = true;
     }
+    if (int rc = prepare_cell_spread(c)) return rc;
     // theta(m) = exp(-pi^2 m^2/a^2)/m^2 (EWALD_SELF, force.f90:27-42) times
     // the B-spline moduli, on the half spectrum; theta(0) = 0.
     std::vector<double> bx = bspline_moduli(p.order, c->K1), by = bspline_moduli(p.order, c->K2),
@@ -593,6 +592,20 @@ static SpmeArgs spme_args(const tcp_ctx *c) {
     return a;
 }
 
+// prefix sum of the bin counts, placement by the counting-sort slots, and
+// each bin in particle-index order (shared by the single-system and batched paths)
+void launch_bin_sort(cudaStream_t st, int n, int nbins, const SpreadBins &b) {
+    const int threads = 256;
+    const int sblocks = (nbins + kScanBlock - 1) / kScanBlock;
+    scan_block_kernel<<<sblocks, kScanBlock, 0, st>>>(b.count, nbins, b.start, b.bsum);
+    scan_sums_kernel<<<1, 32, 0, st>>>(b.bsum, sblocks);
+    scan_add_kernel<<<(nbins + threads - 1) / threads, threads, 0, st>>>(b.start, nbins, b.bsum, n);
+    spme_bin_scatter_kernel<<<(n + threads - 1) / threads, threads, 0, st>>>(n, b);
+    spme_bin_sort_kernel<<<(nbins + threads - 1) / threads, threads, 0, st>>>(b, nbins);
+}
+
+int bin_scan_block() { return kScanBlock; }
+
 // atomic-free spread into Q (FP64) or straight into Qf (FP32C mode)
 static SpreadBins spread_bins(tcp_ctx *c) {
     SpreadBins b;
@@ -613,31 +626,47 @@ static int launch_cell_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Q
     const SpreadBins b = spread_bins(c);
     const int threads = 256, pblocks = (c->n + threads - 1) / threads;
     const int nbins = c->K2 * c->K3;
-    const int sblocks = (nbins + kScanBlock - 1) / kScanBlock;
     TCP_CUDA(cudaMemsetAsync(c->bin_count, 0, sizeof(int) * (size_t)nbins, c->stream));
     spme_bin_count_kernel<P><<<pblocks, threads, 0, c->stream>>>(a, b);
-    scan_block_kernel<<<sblocks, kScanBlock, 0, c->stream>>>(c->bin_count, nbins, c->bin_start, c->bin_bsum);
-    scan_sums_kernel<<<1, 32, 0, c->stream>>>(c->bin_bsum, sblocks);
-    scan_add_kernel<<<(nbins + threads - 1) / threads, threads, 0, c->stream>>>(c->bin_start, nbins, c->bin_bsum, c->n);
-    spme_bin_scatter_kernel<<<pblocks, threads, 0, c->stream>>>(c->n, b);
-    spme_bin_sort_kernel<<<(nbins + threads - 1) / threads, threads, 0, c->stream>>>(b, nbins);
+    launch_bin_sort(c->stream, c->n, nbins, b);
     const long groups = (long)((c->K2 + kRows - 1) / kRows) * c->K3;
     const size_t per_warp = Qf ? row_warp_bytes<P, float>(c->K1) : row_warp_bytes<P, double>(c->K1);
     const int warps = (int)std::max<size_t>(1, std::min<size_t>(kRowWarps, (200u << 10) / per_warp));
     const size_t sm = warps * per_warp;
     const int rblocks = (int)((groups + warps - 1) / warps);
     if (Qf) {
-        TCP_CUDA(cudaFuncSetAttribute(spme_row_spread_kernel<P, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         spme_bin_weights_kernel<P, float><<<pblocks, threads, 0, c->stream>>>(a, b);
         spme_row_spread_kernel<P, float><<<rblocks, 32 * warps, sm, c->stream>>>(a, b, nullptr, Qf);
     } else {
-        TCP_CUDA(cudaFuncSetAttribute(spme_row_spread_kernel<P, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         spme_bin_weights_kernel<P, double><<<pblocks, threads, 0, c->stream>>>(a, b);
         spme_row_spread_kernel<P, double><<<rblocks, 32 * warps, sm, c->stream>>>(a, b, Q, nullptr);
     }
     c->launches += 8;
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;
+}
+
+// shared-memory limits of the spread kernels for this mesh (set once, outside
+// any stream capture; a launch uses at most kRowWarps warps' worth)
+template <int P>
+static int prepare_cell_spread_p(tcp_ctx *c) {
+    const size_t sf = std::min<size_t>(kRowWarps * row_warp_bytes<P, float>(c->K1), 200u << 10);
+    const size_t sd = std::min<size_t>(kRowWarps * row_warp_bytes<P, double>(c->K1), 200u << 10);
+    TCP_CUDA(cudaFuncSetAttribute(spme_row_spread_kernel<P, float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)std::max(sf, row_warp_bytes<P, float>(c->K1))));
+    TCP_CUDA(cudaFuncSetAttribute(spme_row_spread_kernel<P, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)std::max(sd, row_warp_bytes<P, double>(c->K1))));
+    return TCP_OK;
+}
+
+static int prepare_cell_spread(tcp_ctx *c) {
+    switch (c->p.order) {
+        case 4: return prepare_cell_spread_p<4>(c);
+        case 5: return prepare_cell_spread_p<5>(c);
+        case 6: return prepare_cell_spread_p<6>(c);
+        case 7: return prepare_cell_spread_p<7>(c);
+        default: return prepare_cell_spread_p<8>(c);
+    }
 }
 
 static int cell_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Qf) {

@@ -177,13 +177,15 @@ int n3_variant_count();
 const char *n3_variant_name(int v);
 int autotune_pair(tcp_ctx *c);
 int launch_pair_n3(tcp_ctx *c, bool energy);
-int n3_batch_tile();
+int n3_batch_variant_count();
+const char *n3_batch_variant_name(int v);
+int n3_batch_tile(int variant);
 size_t n3_rep_bytes();
 long long n3_batch_fill(void *reps_host, int nrep, const int *off, const int *nel, const int *nion,
-                        const PairConsts *pc);
+                        const PairConsts *pc, int tile);
 int launch_pair_n3_batch(cudaStream_t st, const int4 *xq, int ntot, double *facc, const void *reps_dev, int nrep,
                          long long total, double *ur_rep, unsigned *status, unsigned *counter, int num_sms,
-                         bool energy);
+                         bool energy, int variant);
 // spme.cu
 int spme_setup(tcp_ctx *c);                        // meshes, plans, influence function
 std::vector<double> bspline_moduli(int order, int K);
@@ -211,6 +213,16 @@ int launch_scatter(tcp_ctx *c, unsigned char *dst, int first, int count, long st
                    long off_f, const double *fsrc);
 int launch_pack(tcp_ctx *c, int first, int count, bool x, bool v, bool f, bool frec, int *nf);
 int launch_fp32_peak(int device, double *tffma);
+
+// spme.cu: cell sort of the atomic-free spread (single system and batch)
+struct SpreadBins {
+    int *count, *start, *bsum, *rank, *list, *ebx, *eby;
+    void *ew, *eq;                       // [n][3][P] weights, [n] charges (float or double)
+};
+// start = exclusive prefix of count (plus start[nbins] = n), list = particles
+// by bin (ebx[m] holds the bin of particle m on entry), each bin index-ordered
+void launch_bin_sort(cudaStream_t st, int n, int nbins, const SpreadBins &b);
+int bin_scan_block();
 
 // ctx.cu: step and force composition for the derivative routines
 int force_eval(tcp_ctx *c, bool remove_net);        // main.f90:100-141 on the stream
