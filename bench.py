@@ -272,6 +272,31 @@ def run_gpu(args, world, rank, local, dist):
     step64_ms = t64["step"] / t64["nsteps"]
     ctx64.close()
 
+    # NVE energy drift of the FP32C step over the headline run length (500 steps),
+    # total energy Etot = (mv2el + mv2ion)/2 + Epot + Um as in the ener files
+    drift = None
+    if args.nve_steps > 0 and rank == 0:
+        ctx_d = T.Context(p32, s.nel, s.nion, device=local)
+        ctx_d.EWALD_SELF()
+        ctx_d.upload(x=s.x, v=s.v)
+        ctx_d.force()
+
+        def etot(e):
+            return 0.5 * (e["mv2el"] + e["mv2ion"]) + e["Epot"] + e["Um"]
+
+        e = ctx_d.md_steps(s.dt, 1)
+        E0 = etot(e)
+        worst, done = 0.0, 1
+        every = max(1, args.nve_steps // 10)
+        while done < args.nve_steps:
+            k = min(every, args.nve_steps - done)
+            e = ctx_d.md_steps(s.dt, k)
+            done += k
+            worst = max(worst, abs(etot(e) - E0) / abs(E0))
+        drift = {"steps": args.nve_steps, "E_step1_eV": E0, "rel_drift_end": abs(etot(e) - E0) / abs(E0),
+                 "rel_drift_max_sampled": worst, "sampled_every": every, "precision": "fp32c"}
+        ctx_d.close()
+
     # e2e through the C ABI with host PT records
     qel, qion = s.to_pt()
     ctx_e = T.Context(p32, s.nel, s.nion, device=local)
@@ -341,6 +366,7 @@ def run_gpu(args, world, rank, local, dist):
         "force_error": {"rms_rel_fp32c_vs_fp64_gpu": err_vs_fp64, "rms_rel_fp32c_vs_fp64_oracle_rows": err_vs_oracle,
                         "bound": 2e-6},
         "energies_initial": {"Ur": e0["Ur"], "Um": e0["Um"], "Uo": e0["Uo"]},
+        "nve_drift": drift,
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "pair-int/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
@@ -442,6 +468,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--ref-rows", type=int, default=4096)
+    ap.add_argument("--nve-steps", type=int, default=500, help="FP32C NVE energy-drift run (0: skip)")
     ap.add_argument("--pair-only", type=int, default=0, help="profile target: pair kernel alone at this N")
     ap.add_argument("--recip-only", type=int, default=0, help="profile target: SPME chain alone at this N")
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
