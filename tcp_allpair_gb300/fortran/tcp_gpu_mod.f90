@@ -87,6 +87,33 @@ MODULE TCP_GPU
        REAL(C_DOUBLE), INTENT(OUT) :: rdf(*), vdf(*)
        INTEGER(C_INT), VALUE :: reset
      END FUNCTION
+     INTEGER(C_INT) FUNCTION tcp_md_steps(c, dt, nsteps, e) BIND(C, NAME='tcp_md_steps')
+       IMPORT :: C_INT, C_PTR, C_DOUBLE, tcp_energies
+       TYPE(C_PTR), VALUE :: c
+       REAL(C_DOUBLE), VALUE :: dt
+       INTEGER(C_INT), VALUE :: nsteps
+       TYPE(tcp_energies), INTENT(OUT) :: e
+     END FUNCTION
+     ! derivatives (no counterpart in the reference)
+     INTEGER(C_INT) FUNCTION tcp_adjoint_energy(c, e, dedl, deds) BIND(C, NAME='tcp_adjoint_energy')
+       IMPORT :: C_INT, C_PTR, C_DOUBLE
+       TYPE(C_PTR), VALUE :: c
+       REAL(C_DOUBLE), INTENT(OUT) :: e, dedl, deds
+     END FUNCTION
+     INTEGER(C_INT) FUNCTION tcp_hvp(c, w, hw, dfdl_w) BIND(C, NAME='tcp_hvp')
+       IMPORT :: C_INT, C_PTR, C_DOUBLE
+       TYPE(C_PTR), VALUE :: c
+       REAL(C_DOUBLE), INTENT(IN) :: w(3, *)
+       REAL(C_DOUBLE), INTENT(OUT) :: hw(3, *)
+       REAL(C_DOUBLE), INTENT(OUT) :: dfdl_w
+     END FUNCTION
+     INTEGER(C_INT) FUNCTION tcp_reverse_md(c, dt, nsteps, every, j, djdl) BIND(C, NAME='tcp_reverse_md')
+       IMPORT :: C_INT, C_PTR, C_DOUBLE
+       TYPE(C_PTR), VALUE :: c
+       REAL(C_DOUBLE), VALUE :: dt
+       INTEGER(C_INT), VALUE :: nsteps, every
+       REAL(C_DOUBLE), INTENT(OUT) :: j, djdl
+     END FUNCTION
      FUNCTION tcp_last_error() BIND(C, NAME='tcp_last_error')
        IMPORT :: C_PTR
        TYPE(C_PTR) :: tcp_last_error

@@ -145,23 +145,34 @@ def test_hvp_models_vs_oracle(ei, recip):
         assert dl == pytest.approx(o.dE_dlambda(s.x), rel=1e-10)
 
 
-def test_reverse_md_vs_oracle():
-    """Small case (6 checkpointed segments, the last one partial) against the
-    oracle's reverse mode."""
+@pytest.mark.parametrize("ei,recip", [("kelbg", "spme"), ("deutsch", "ewald"), ("kelbg", "none")])
+def test_reverse_md_vs_oracle(ei, recip):
+    """Small case (5 checkpointed segments, the last one partial) against the
+    oracle's reverse mode, and the state after the sweep against plain steps."""
     s = T.make_system(256, gamma=1.0, lam=0.5, seed=21, alpha_rc=3.1, K=16, order=4)
-    o = oracle.Oracle.from_system(s, ei="kelbg")
-    Jo, dJo = o.reverse_md(s.x, s.v, s.dt, 20, 4)
-    with ctx_for(s, precision="fp64", ei="kelbg", recip="spme") as c:
-        J, dJ = c.reverse_md(s.dt, 20, 4)
+    o = oracle.Oracle.from_system(s, ei=ei)
+    Jo, dJo = o.reverse_md(s.x, s.v, s.dt, 18, 4, recip=recip, nmax2=27)
+    with ctx_for(s, precision="fp64", ei=ei, recip=recip, nmax2=27) as c:
+        J, dJ = c.reverse_md(s.dt, 18, 4)
         x, v, _, _ = c.download(x=True, v=True, f=False)
     assert J == pytest.approx(Jo, rel=1e-11)
     assert dJ == pytest.approx(dJo, rel=1e-8)
     xo, vo = s.x.copy(), s.v.copy()
-    f, _, _ = o.force_total(xo)
-    for _ in range(20):
-        o.md_step(xo, vo, f, s.dt)
+    f, _, _ = o.force_total(xo, recip=recip, nmax2=27)
+    for _ in range(18):
+        o.md_step(xo, vo, f, s.dt, recip=recip, nmax2=27)
     assert np.max(np.abs(x - xo)) < 1e-9 * s.box
     assert oracle.rms_rel(v, vo) < 1e-9
+
+
+def test_reverse_md_fp32c_small_vs_oracle():
+    s = T.make_system(512, gamma=1.0, lam=0.5, seed=22, alpha_rc=3.1, K=16, order=4)
+    o = oracle.Oracle.from_system(s, ei="kelbg")
+    Jo, dJo = o.reverse_md(s.x, s.v, s.dt, 20, 5)
+    with ctx_for(s, precision="fp32c", ei="kelbg", recip="spme") as c:
+        J, dJ = c.reverse_md(s.dt, 20, 5)
+    assert J == pytest.approx(Jo, rel=1e-6)
+    assert dJ == pytest.approx(dJo, rel=1e-4)
 
 
 def mean_temperature(c, s, dt, K):

@@ -100,3 +100,27 @@ def test_nve_energy_drift(precision):
     es = np.array(es)
     assert np.all(np.isfinite(es))
     assert np.max(np.abs(es - es[0])) < 5e-3 * ke
+
+
+def test_nve_drift_fp32c_tracks_fp64():
+    """500 NVE steps at N = 4096 (the headline run length): the total-energy
+    drift of the compensated-FP32 step stays at the level of the FP64 step's
+    (the drift is the integrator's, not the pair arithmetic's)."""
+    s = make(4096, seed=7, K=32, order=5)
+    drift = {}
+    for prec in ("fp64", "fp32c"):
+        p = T.params_for(s, precision=prec, ei="kelbg", recip="spme")
+        with T.Context(p, s.nel, s.nion) as c:
+            c.EWALD_SELF()
+            c.upload(x=s.x, v=s.v)
+            c.force()
+            e = c.md_steps(s.dt, 1)
+            E0 = e["Epot"] + e["Um"] + 0.5 * (e["mv2el"] + e["mv2ion"])
+            worst = 0.0
+            for _ in range(10):
+                e = c.md_steps(s.dt, 50)
+                E = e["Epot"] + e["Um"] + 0.5 * (e["mv2el"] + e["mv2ion"])
+                worst = max(worst, abs(E - E0) / abs(E0))
+        drift[prec] = worst
+    assert drift["fp64"] < 1e-3
+    assert drift["fp32c"] < 2.0 * drift["fp64"] + 1e-6, drift
