@@ -467,6 +467,7 @@ using namespace tcp;
 extern "C" {
 
 int tcp_adjoint_energy(tcp_ctx *c, double *E, double *dE_dlambda, double *dE_dscale) {
+    TCP_TRACE("tcp_adjoint_energy");
     TCP_ADJ_READY(c);
     int rc;
     const size_t b = sizeof(double) * 3 * (size_t)c->n;
@@ -498,6 +499,7 @@ int tcp_adjoint_energy(tcp_ctx *c, double *E, double *dE_dlambda, double *dE_dsc
 }
 
 int tcp_hvp(tcp_ctx *c, const double *w, double *hw, double *dF_dlambda_w) {
+    TCP_TRACE("tcp_hvp");
     TCP_ADJ_READY(c);
     if (!w || !hw) return set_error(TCP_ERR_BAD_PARAM, "w and hw must not be NULL");
     int rc;
@@ -518,6 +520,7 @@ int tcp_hvp(tcp_ctx *c, const double *w, double *hw, double *dF_dlambda_w) {
 }
 
 int tcp_reverse_md(tcp_ctx *c, double dt, int nsteps, int every, double *J, double *dJ_dlambda) {
+    TCP_TRACE("tcp_reverse_md");
     TCP_ADJ_READY(c);
     if (nsteps <= 0 || every <= 0) return set_error(TCP_ERR_BAD_PARAM, "nsteps and every must be positive");
     if (c->p.thermo != TCP_THERMO_NOTEMP)

@@ -649,6 +649,7 @@ int tcp_batch_destroy(tcp_batch *b) {
 
 int tcp_batch_create(const tcp_params *params, const int *nel, const int *nion, int nrep, int device,
                      tcp_batch **out) {
+    TCP_TRACE("tcp_batch_create");
     if (!out || !params || !nel || !nion || nrep <= 0) return set_error(TCP_ERR_BAD_PARAM, "bad arguments");
     *out = nullptr;
     for (int r = 0; r < nrep; ++r) {
@@ -911,6 +912,7 @@ int tcp_batch_download(tcp_batch *b, int rep, double *x, double *v, double *f) {
 // Forces of all replicas at the current positions (main.f90:100-141 per
 // replica): SPME, real-space sum, SPME_SUM and REMOVE_RIGIDMTN.
 int tcp_batch_force(tcp_batch *b, tcp_energies *e) {
+    TCP_TRACE("tcp_batch_force");
     if (!b || !b->ready) return set_error(TCP_ERR_STATE, "tcp_batch_ewald_self must be called first");
     cudaSetDevice(b->device);
     if (int arc = b_autotune(b)) return arc;
@@ -941,6 +943,7 @@ int tcp_batch_force(tcp_batch *b, tcp_energies *e) {
 
 // nsteps MD steps of every replica, one CUDA graph per step.
 int tcp_batch_md_steps(tcp_batch *b, double dt, int nsteps, tcp_energies *e) {
+    TCP_TRACE("tcp_batch_md_steps");
     if (!b || !b->ready) return set_error(TCP_ERR_STATE, "tcp_batch_ewald_self must be called first");
     if (nsteps < 0) return set_error(TCP_ERR_BAD_PARAM, "nsteps < 0");
     cudaSetDevice(b->device);

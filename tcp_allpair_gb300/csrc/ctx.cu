@@ -8,11 +8,21 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "tcp_internal.h"
 
 namespace tcp {
 
 static thread_local std::string g_err;
+
+TraceRange::TraceRange(const char *name) { nvtxRangePushA(name); }
+TraceRange::~TraceRange() { nvtxRangePop(); }
+
+bool inject_fault(const char *site) {
+    const char *e = getenv("TCP_INJECT_FAULT");
+    return e && std::strcmp(e, site) == 0;
+}
 
 int set_error(int code, const std::string &msg) {
     g_err = msg;
@@ -193,6 +203,7 @@ int tcp_version(int *major, int *minor, int *arch) {
 }
 
 int tcp_create(const tcp_params *p_in, int nel, int nion, int device, tcp_ctx **out) {
+    TCP_TRACE("tcp_create");
     if (!out) return set_error(TCP_ERR_BAD_PARAM, "out is NULL");
     *out = nullptr;
     int rc = validate(p_in, nel, nion);
@@ -209,6 +220,7 @@ int tcp_create(const tcp_params *p_in, int nel, int nion, int device, tcp_ctx **
         return set_error(TCP_ERR_NO_DEVICE, "libtcpgpu is built for sm_103a (GB300); device is sm_" +
                                                 std::to_string(prop.major) + std::to_string(prop.minor));
     TCP_CUDA(cudaSetDevice(device));
+    if (inject_fault("alloc")) return set_error(TCP_ERR_NOMEM, "injected: device allocation failed");
     tcp_ctx *c = new tcp_ctx();
     c->p = *p_in;
     normalise(&c->p);
@@ -267,6 +279,7 @@ int tcp_create(const tcp_params *p_in, int nel, int nion, int device, tcp_ctx **
 }
 
 int tcp_destroy(tcp_ctx *c) {
+    TCP_TRACE("tcp_destroy");
     if (!c) return TCP_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
@@ -302,6 +315,7 @@ int tcp_destroy(tcp_ctx *c) {
 }
 
 int tcp_ewald_self(tcp_ctx *c, double *alpha_out, double *Uo_out) {
+    TCP_TRACE("tcp_ewald_self");
     if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
     cudaSetDevice(c->device);
     const tcp_params &p = c->p;
@@ -327,6 +341,7 @@ int tcp_ewald_self(tcp_ctx *c, double *alpha_out, double *Uo_out) {
 }
 
 int tcp_set_params(tcp_ctx *c, const tcp_params *p) {
+    TCP_TRACE("tcp_set_params");
     if (!c || !p) return set_error(TCP_ERR_BAD_PARAM, "NULL argument");
     int rc = validate(p, c->nel, c->nion);
     if (rc) return rc;
@@ -354,6 +369,7 @@ int tcp_set_flags(tcp_ctx *c, unsigned flags) {
 
 // ---- transfers ---------------------------------------------------------------
 int tcp_upload(tcp_ctx *c, int species, const double *xx, const double *xv, const double *ff, long stride) {
+    TCP_TRACE("tcp_upload");
     if (!c || (species != 0 && species != 1)) return set_error(TCP_ERR_BAD_PARAM, "bad ctx or species");
     cudaSetDevice(c->device);
     const int count = species == 0 ? c->nel : c->nion, first = species == 0 ? 0 : c->nel;
@@ -389,6 +405,7 @@ int tcp_upload(tcp_ctx *c, int species, const double *xx, const double *xv, cons
 }
 
 int tcp_download(tcp_ctx *c, int species, double *xx, double *xv, double *ff, long stride) {
+    TCP_TRACE("tcp_download");
     if (!c || (species != 0 && species != 1)) return set_error(TCP_ERR_BAD_PARAM, "bad ctx or species");
     cudaSetDevice(c->device);
     const int count = species == 0 ? c->nel : c->nion, first = species == 0 ? 0 : c->nel;
@@ -429,6 +446,7 @@ int tcp_download(tcp_ctx *c, int species, double *xx, double *xv, double *ff, lo
 }
 
 int tcp_upload_soa(tcp_ctx *c, const double *x, const double *v, const double *f) {
+    TCP_TRACE("tcp_upload_soa");
     if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
     cudaSetDevice(c->device);
     int rc;
@@ -451,6 +469,7 @@ int tcp_upload_soa(tcp_ctx *c, const double *x, const double *v, const double *f
 }
 
 int tcp_download_soa(tcp_ctx *c, double *x, double *v, double *f, double *frec) {
+    TCP_TRACE("tcp_download_soa");
     if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
     cudaSetDevice(c->device);
     int nf = 0, rc;
@@ -490,6 +509,7 @@ int tcp_download_soa(tcp_ctx *c, double *x, double *v, double *f, double *frec) 
     } while (0)
 
 int tcp_force_direct(tcp_ctx *c, double *Ur) {
+    TCP_TRACE("tcp_force_direct");
     TCP_REQUIRE_READY(c);
     int rc;
     if ((rc = autotune_pair(c))) return rc;
@@ -502,6 +522,7 @@ int tcp_force_direct(tcp_ctx *c, double *Ur) {
 }
 
 int tcp_force_spme(tcp_ctx *c, double *Um) {
+    TCP_TRACE("tcp_force_spme");
     TCP_REQUIRE_READY(c);
     int rc;
     if (c->p.reciprocal == TCP_RECIP_NONE) {
@@ -516,6 +537,7 @@ int tcp_force_spme(tcp_ctx *c, double *Um) {
 }
 
 int tcp_spme_sum(tcp_ctx *c) {
+    TCP_TRACE("tcp_spme_sum");
     TCP_REQUIRE_READY(c);
     int rc;
     if ((rc = launch_spme_sum(c))) return rc;
@@ -524,6 +546,7 @@ int tcp_spme_sum(tcp_ctx *c) {
 }
 
 int tcp_remove_rigidmtn(tcp_ctx *c) {
+    TCP_TRACE("tcp_remove_rigidmtn");
     TCP_REQUIRE_READY(c);
     int rc;
     if ((rc = launch_fsum(c))) return rc;
@@ -533,6 +556,7 @@ int tcp_remove_rigidmtn(tcp_ctx *c) {
 }
 
 int tcp_force(tcp_ctx *c, tcp_energies *e) {
+    TCP_TRACE("tcp_force");
     TCP_REQUIRE_READY(c);
     int rc;
     if ((rc = autotune_pair(c))) return rc;
@@ -543,6 +567,7 @@ int tcp_force(tcp_ctx *c, tcp_energies *e) {
 }
 
 int tcp_vverlet1(tcp_ctx *c, double dt) {
+    TCP_TRACE("tcp_vverlet1");
     TCP_REQUIRE_READY(c);
     int rc;
     if ((rc = launch_vverlet1(c, dt, 0.0))) return rc;
@@ -551,6 +576,7 @@ int tcp_vverlet1(tcp_ctx *c, double dt) {
 }
 
 int tcp_vverlet2(tcp_ctx *c, double dt, double *mv2el, double *mv2ion) {
+    TCP_TRACE("tcp_vverlet2");
     TCP_REQUIRE_READY(c);
     int rc, pass = 0;
     if ((rc = launch_kick2(c, dt, false, thermostat_due(c), (c->flags & TCP_FLAG_VDF) != 0, &pass))) return rc;
@@ -565,6 +591,7 @@ int tcp_vverlet2(tcp_ctx *c, double dt, double *mv2el, double *mv2ion) {
 }
 
 int tcp_finit(tcp_ctx *c, double dt, tcp_energies *e) {
+    TCP_TRACE("tcp_finit");
     TCP_REQUIRE_READY(c);
     int rc;
     if ((rc = autotune_pair(c))) return rc;
@@ -624,6 +651,7 @@ static int launch_step(tcp_ctx *c, double dt) {
 }
 
 int tcp_md_steps(tcp_ctx *c, double dt, int nsteps, tcp_energies *e) {
+    TCP_TRACE("tcp_md_steps");
     TCP_REQUIRE_READY(c);
     if (nsteps < 0) return set_error(TCP_ERR_BAD_PARAM, "nsteps < 0");
     int rc;
@@ -693,6 +721,7 @@ int tcp_time_component(tcp_ctx *c, int which, int reps, double dt, double *ms) {
 }
 
 int tcp_time_steps(tcp_ctx *c, double dt, int nsteps, int flush_l2, double *out) {
+    TCP_TRACE("tcp_time_steps");
     TCP_REQUIRE_READY(c);
     if (nsteps <= 0 || !out) return set_error(TCP_ERR_BAD_PARAM, "nsteps must be positive");
     int rc;

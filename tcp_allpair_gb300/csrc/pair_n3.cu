@@ -71,6 +71,7 @@ struct N3Args {
     const N3Rep *reps;    // batch: one entry per replica
     int nrep;
     double *ur_rep;       // batch: Ur per replica (zeroed before the launch)
+    int inject_skip;      // test hook: CTA 0 never issues its first subtile copy (its bounded wait runs out)
 };
 
 template <int TILE>
@@ -440,7 +441,8 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
         bulk_g2s(tiles[stage], a.xq + g.off + js, bytes, &bars[stage]);
     };
     if (tid == 0)
-        for (int k = 0; k < min(kN3Stages, nst); ++k) issue(k, it0 + k);
+        for (int k = 0; k < min(kN3Stages, nst); ++k)
+            if (!(a.inject_skip && blockIdx.x == 0 && k == 0)) issue(k, it0 + k);
 
     double etot = 0.0;
     int curRep = -1, curI = -1, istart = 0, iend = 0, isp = 0, ifirst = 0, ioff = 0;
@@ -686,6 +688,7 @@ int launch_pair_n3(tcp_ctx *c, bool energy) {
     a.status = c->status;
     a.counter = c->counter;
     a.c = c->pc;
+    a.inject_skip = inject_fault("tile_wait") ? 1 : 0;
     const int grid = (int)std::min<long long>(n3_grid_for(c, v), total);
     if (grid > c->n_upart) return set_error(TCP_ERR_STATE, "energy partial buffer smaller than the Newton-3 grid");
     TCP_CUDA(cudaMemsetAsync(c->fpart, 0, sizeof(double) * 3 * (size_t)c->n, c->stream));

@@ -530,6 +530,7 @@ int spme_setup(tcp_ctx *c) {
             return set_error(TCP_ERR_NOMEM, "SPME FP32 mesh allocation failed");
     }
     if (!c->plans) {
+        if (inject_fault("cufft_plan")) return set_error(TCP_ERR_CUFFT, "injected: cufftPlan3d failed");
         const cufftType tf = c->spme_fp32 ? CUFFT_R2C : CUFFT_D2Z;
         const cufftType tb = c->spme_fp32 ? CUFFT_C2R : CUFFT_Z2D;
         if (cufftPlan3d(&c->plan_f, c->K3, c->K2, c->K1, tf) != CUFFT_SUCCESS)

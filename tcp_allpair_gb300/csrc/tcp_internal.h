@@ -158,6 +158,21 @@ enum {
 };
 
 int set_error(int code, const std::string &msg);
+
+// Tracing: an NVTX range per C-ABI call (visible in nsys / ncu timelines;
+// a no-op when no tool is attached).
+struct TraceRange {
+    explicit TraceRange(const char *name);
+    ~TraceRange();
+};
+#define TCP_TRACE(name) tcp::TraceRange tcp_trace_range_(name)
+
+// Fault injection for tests: TCP_INJECT_FAULT=<site>.  Host sites make the
+// named call report failure ("alloc" in tcp_create, "cufft_plan" in the SPME
+// setup); "tile_wait" makes CTA 0 of the Newton-3 kernel skip its first
+// subtile copy, so its bounded mbarrier wait runs out (about 2 s), the kernel
+// sets the timeout status and returns, and the call reports TCP_ERR_TIMEOUT.
+bool inject_fault(const char *site);
 int cuda_check(cudaError_t e, const char *what);
 #define TCP_CUDA(call)                                        \
     do {                                                      \
