@@ -71,7 +71,7 @@ struct N3Args {
     const N3Rep *reps;    // batch: one entry per replica
     int nrep;
     double *ur_rep;       // batch: Ur per replica (zeroed before the launch)
-    int inject_skip;      // test hook: CTA 0 never issues its first subtile copy (its bounded wait runs out)
+    int inject_skip;      // test hook: CTA 0 never issues the copy of its first item (its bounded wait runs out)
 };
 
 template <int TILE>
@@ -581,7 +581,7 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
         if (tid == 0) {
             const long long it = a.nstatic + (long long)atomicAdd(a.counter, 1u);
             s_next = it;
-            if (it < a.total) issue(k % kN3Stages, it);
+            if (it < a.total && !(a.inject_skip && blockIdx.x == 0 && k == 0)) issue(k % kN3Stages, it);
         }
         __syncthreads();
         const long long it = s_next;
