@@ -291,3 +291,39 @@ def test_autotuner_picks_a_timed_variant(monkeypatch):
         v, ms = c.autotune_report()
     assert 0 <= v <= 9
     assert ms[v] > 0 and ms[v] == min(m for m in ms if m > 0)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_noncubic_box_and_mesh_uneven_species(precision):
+    """Box (L, 1.1 L, 0.9 L), mesh (20, 16, 24), order 5, 600 electrons and 424
+    ions: the ordered-pair FP32C kernel's general-box path and the spread's
+    unequal mesh dimensions against the oracle."""
+    rng = np.random.default_rng(77)
+    nel, nion = 600, 424
+    L = T.make_system(nel + nion, seed=1).box
+    box = (L, 1.1 * L, 0.9 * L)
+    x = (rng.random((nel + nion, 3)) - 0.5) * np.array(box)
+    v = rng.normal(0.0, 0.1, size=(nel + nion, 3))
+    rc = 0.45 * min(box)
+    alpha = 3.1 / rc
+    o = oracle.Oracle(nel, nion, box, rc, alpha=alpha, lambda_ei=0.5 * T.EPS, rs=0.5 * T.EPS, ei="kelbg",
+                      K=(20, 16, 24), order=5)
+    fo, uro, umo = o.force_total(x, recip="spme")
+    s = T.make_system(nel + nion, seed=1)
+    p = T.params_for(s, precision=precision, ei="kelbg", recip="spme")
+    for d in range(3):
+        p.box[d] = box[d]
+    p.K[0], p.K[1], p.K[2] = 20, 16, 24
+    p.order = 5
+    p.rc = rc
+    p.a = alpha
+    p.lambda_ei = p.rs = 0.5 * T.EPS
+    with T.Context(p, nel, nion) as c:
+        c.EWALD_SELF()
+        c.upload(x=x, v=v)
+        e = c.force()
+        _, _, f, _ = c.download(x=False, v=False, f=True)
+    tol = 1e-10 if precision == "fp64" else FP32_FORCE_RMS
+    assert oracle.rms_rel(f, fo) < tol
+    assert e["Um"] == pytest.approx(umo, rel=1e-10 if precision == "fp64" else 1e-6)
+    assert e["Ur"] == pytest.approx(uro, rel=1e-10 if precision == "fp64" else 2e-5)
