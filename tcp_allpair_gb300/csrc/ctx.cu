@@ -399,7 +399,7 @@ int tcp_upload(tcp_ctx *c, int species, const double *xx, const double *xv, cons
     }
     if ((rc = launch_extract(c, src, first, count, stride, off[0], off[1], off[2]))) return rc;
     if (xx && (rc = launch_refresh_positions(c))) return rc;
-    invalidate_graph(c);   // no-op for correctness; graphs read device memory
+    // the step graph reads the device arrays in place: new data needs no new graph
     TCP_CUDA(cudaStreamSynchronize(c->stream));
     return TCP_OK;
 }
