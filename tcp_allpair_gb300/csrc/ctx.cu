@@ -397,8 +397,7 @@ int tcp_upload(tcp_ctx *c, int species, const double *xx, const double *xv, cons
         TCP_CUDA(cudaMemcpyAsync(c->d_stage, base, span, cudaMemcpyHostToDevice, c->stream));
         src = c->d_stage;
     }
-    if ((rc = launch_extract(c, src, first, count, stride, off[0], off[1], off[2]))) return rc;
-    if (xx && (rc = launch_refresh_positions(c))) return rc;
+    if ((rc = launch_extract(c, src, first, count, stride, off[0], off[1], off[2]))) return rc;   // refreshes xq, xd
     // the step graph reads the device arrays in place: new data needs no new graph
     TCP_CUDA(cudaStreamSynchronize(c->stream));
     return TCP_OK;
@@ -463,7 +462,6 @@ int tcp_upload_soa(tcp_ctx *c, const double *x, const double *v, const double *f
         }
         if ((rc = launch_extract(c, from, 0, c->n, 24, q == 0 ? 0 : -1, q == 1 ? 0 : -1, q == 2 ? 0 : -1))) return rc;
     }
-    if (x && (rc = launch_refresh_positions(c))) return rc;
     TCP_CUDA(cudaStreamSynchronize(c->stream));
     return TCP_OK;
 }

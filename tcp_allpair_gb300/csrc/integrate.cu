@@ -293,16 +293,20 @@ __global__ void reduce_scalars_kernel(const double *__restrict__ upart, int nu, 
 // ---- host records <-> SoA ------------------------------------------------
 // stage holds `count` records of `stride` bytes; fields at byte offsets
 // off_x/off_v/off_f (or < 0 to skip), 3 doubles each.
+// records -> SoA; new positions also refresh the two pair-kernel copies
 __global__ void extract_kernel(const unsigned char *__restrict__ stage, long stride, long off_x, long off_v,
-                               long off_f, int count, int first, int n, double *x, double *v, double *f) {
+                               long off_f, int count, int first, const IntArgs a) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= count) return;
     const unsigned char *rec = stage + (size_t)r * stride;
-    const int i = first + r;
+    const int i = first + r, n = a.n;
     for (int d = 0; d < 3; ++d) {
-        if (off_x >= 0) x[(size_t)d * n + i] = reinterpret_cast<const double *>(rec + off_x)[d];
-        if (off_v >= 0) v[(size_t)d * n + i] = reinterpret_cast<const double *>(rec + off_v)[d];
-        if (off_f >= 0) f[(size_t)d * n + i] = reinterpret_cast<const double *>(rec + off_f)[d];
+        if (off_v >= 0) a.v[(size_t)d * n + i] = reinterpret_cast<const double *>(rec + off_v)[d];
+        if (off_f >= 0) a.f[(size_t)d * n + i] = reinterpret_cast<const double *>(rec + off_f)[d];
+    }
+    if (off_x >= 0) {
+        const double *px = reinterpret_cast<const double *>(rec + off_x);
+        store_pos(a, i, px[0], px[1], px[2]);
     }
 }
 
@@ -484,7 +488,7 @@ int launch_reduce(tcp_ctx *c, int mask, int pass) {
 int launch_extract(tcp_ctx *c, const unsigned char *src, int first, int count, long stride, long off_x, long off_v,
                    long off_f) {
     extract_kernel<<<nblocks(count), kIntThreads, 0, c->stream>>>(src, stride, off_x, off_v, off_f, count,
-                                                                  first, c->n, c->x, c->v, c->f);
+                                                                  first, int_args(c));
     c->launches++;
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;
