@@ -269,8 +269,10 @@ int tcp_time_component(tcp_ctx *ctx, int which, int reps, double dt, double *ms_
  * context's stream (also inside the captured step graph), optionally writing
  * a buffer of twice the L2 size between steps (outside the timed spans).
  * out[6] receives the summed milliseconds of: whole steps, first half kick,
- * reciprocal sum, real-space pair kernel, force epilogue + second half kick,
- * and the number of steps timed. */
+ * reciprocal sum (its span on the second stream, where it runs concurrently
+ * with the pair kernel), real-space pair kernel, force epilogue + second half
+ * kick (from the later of the two to the step end), and the number of steps
+ * timed. */
 int tcp_time_steps(tcp_ctx *ctx, double dt, int nsteps, int flush_l2, double *out);
 /* The FP32C real-space kernel the autotuner picked for this context (0 =
  * ordered pairs, >= 1 = Newton-3 variants) and the per-candidate times in ms

@@ -627,20 +627,20 @@ static int launch_cell_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Q
     const SpreadBins b = spread_bins(c);
     const int threads = 256, pblocks = (c->n + threads - 1) / threads;
     const int nbins = c->K2 * c->K3;
-    TCP_CUDA(cudaMemsetAsync(c->bin_count, 0, sizeof(int) * (size_t)nbins, c->stream));
-    spme_bin_count_kernel<P><<<pblocks, threads, 0, c->stream>>>(a, b);
-    launch_bin_sort(c->stream, c->n, nbins, b);
+    TCP_CUDA(cudaMemsetAsync(c->bin_count, 0, sizeof(int) * (size_t)nbins, c->rstream));
+    spme_bin_count_kernel<P><<<pblocks, threads, 0, c->rstream>>>(a, b);
+    launch_bin_sort(c->rstream, c->n, nbins, b);
     const long groups = (long)((c->K2 + kRows - 1) / kRows) * c->K3;
     const size_t per_warp = Qf ? row_warp_bytes<P, float>(c->K1) : row_warp_bytes<P, double>(c->K1);
     const int warps = (int)std::max<size_t>(1, std::min<size_t>(kRowWarps, (200u << 10) / per_warp));
     const size_t sm = warps * per_warp;
     const int rblocks = (int)((groups + warps - 1) / warps);
     if (Qf) {
-        spme_bin_weights_kernel<P, float><<<pblocks, threads, 0, c->stream>>>(a, b);
-        spme_row_spread_kernel<P, float><<<rblocks, 32 * warps, sm, c->stream>>>(a, b, nullptr, Qf);
+        spme_bin_weights_kernel<P, float><<<pblocks, threads, 0, c->rstream>>>(a, b);
+        spme_row_spread_kernel<P, float><<<rblocks, 32 * warps, sm, c->rstream>>>(a, b, nullptr, Qf);
     } else {
-        spme_bin_weights_kernel<P, double><<<pblocks, threads, 0, c->stream>>>(a, b);
-        spme_row_spread_kernel<P, double><<<rblocks, 32 * warps, sm, c->stream>>>(a, b, Q, nullptr);
+        spme_bin_weights_kernel<P, double><<<pblocks, threads, 0, c->rstream>>>(a, b);
+        spme_row_spread_kernel<P, double><<<rblocks, 32 * warps, sm, c->rstream>>>(a, b, Q, nullptr);
     }
     c->launches += 8;
     TCP_CUDA(cudaGetLastError());
@@ -684,9 +684,9 @@ template <int P>
 static void launch_gather(tcp_ctx *c, const SpmeArgs &a, double coef) {
     const int threads = 128, blocks = (c->n + threads - 1) / threads;
     if (c->spme_fp32)
-        spme_gather_kernel<P, float><<<blocks, threads, 0, c->stream>>>(a, c->Qf, coef, c->frec);
+        spme_gather_kernel<P, float><<<blocks, threads, 0, c->rstream>>>(a, c->Qf, coef, c->frec);
     else
-        spme_gather_kernel<P, double><<<blocks, threads, 0, c->stream>>>(a, c->Q, coef, c->frec);
+        spme_gather_kernel<P, double><<<blocks, threads, 0, c->rstream>>>(a, c->Q, coef, c->frec);
 }
 
 static void gather(tcp_ctx *c, const SpmeArgs &a, double coef) {
@@ -710,21 +710,23 @@ int launch_spme(tcp_ctx *c, bool energy) {
     const long total = (long)c->K3 * c->K2 * c->Kh;
     const int eb = spme_energy_blocks(c);
     double *epart = recip_epart(c);
+    cufftSetStream(c->plan_f, c->rstream);
+    cufftSetStream(c->plan_b, c->rstream);
     if (c->spme_fp32) {
         if (cufftExecR2C(c->plan_f, c->Qf, c->Qkf) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecR2C failed");
-        spme_influence_f_kernel<<<eb, 256, 0, c->stream>>>(c->Qkf, c->infl_f, total, c->Kh, c->K1, epart, energy);
+        spme_influence_f_kernel<<<eb, 256, 0, c->rstream>>>(c->Qkf, c->infl_f, total, c->Kh, c->K1, epart, energy);
         c->launches++;
         if (cufftExecC2R(c->plan_b, c->Qkf, c->Qf) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecC2R failed");
     } else {
         if (cufftExecD2Z(c->plan_f, c->Q, c->Qk) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecD2Z failed");
-        spme_influence_kernel<<<eb, 256, 0, c->stream>>>(c->Qk, c->infl, total, c->Kh, c->K1, epart, energy);
+        spme_influence_kernel<<<eb, 256, 0, c->rstream>>>(c->Qk, c->infl, total, c->Kh, c->K1, epart, energy);
         c->launches++;
         if (cufftExecZ2D(c->plan_b, c->Qk, c->Q) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecZ2D failed");
     }
     gather(c, a, kEps / (kPi * c->V));
     c->launches++;
     if (energy) {
-        sum_partials_kernel<<<1, 1024, 0, c->stream>>>(epart, eb, kEps / (2.0 * kPi * c->V), c->scal + kScalUm);
+        sum_partials_kernel<<<1, 1024, 0, c->rstream>>>(epart, eb, kEps / (2.0 * kPi * c->V), c->scal + kScalUm);
         c->launches++;
     }
     TCP_CUDA(cudaGetLastError());
@@ -767,18 +769,18 @@ int ewald_setup(tcp_ctx *c) {
 
 int launch_ewald(tcp_ctx *c, bool energy) {
     if (c->nk == 0) {
-        TCP_CUDA(cudaMemsetAsync(c->frec, 0, sizeof(double) * 3 * (size_t)c->n, c->stream));
-        TCP_CUDA(cudaMemsetAsync(c->scal + kScalUm, 0, sizeof(double), c->stream));
+        TCP_CUDA(cudaMemsetAsync(c->frec, 0, sizeof(double) * 3 * (size_t)c->n, c->rstream));
+        TCP_CUDA(cudaMemsetAsync(c->scal + kScalUm, 0, sizeof(double), c->rstream));
         return TCP_OK;
     }
     const double q0 = c->p.charge_scale * c->p.q[0], q1 = c->p.charge_scale * c->p.q[1];
     double *epart = recip_epart(c);
-    ewald_sfac_kernel<<<c->nk, 256, 0, c->stream>>>(c->x, c->nel, c->n, q0, q1, c->kvec, c->ksum, epart);
-    ewald_force_kernel<<<(c->n + 127) / 128, 128, 0, c->stream>>>(c->x, c->nel, c->n, q0, q1, c->kvec, c->ksum,
+    ewald_sfac_kernel<<<c->nk, 256, 0, c->rstream>>>(c->x, c->nel, c->n, q0, q1, c->kvec, c->ksum, epart);
+    ewald_force_kernel<<<(c->n + 127) / 128, 128, 0, c->rstream>>>(c->x, c->nel, c->n, q0, q1, c->kvec, c->ksum,
                                                                   c->nk, 2.0 * kEps / c->V, c->frec);
     c->launches += 2;
     if (energy) {
-        sum_partials_kernel<<<1, 1024, 0, c->stream>>>(epart, c->nk, kEps / (2.0 * kPi * c->V), c->scal + kScalUm);
+        sum_partials_kernel<<<1, 1024, 0, c->rstream>>>(epart, c->nk, kEps / (2.0 * kPi * c->V), c->scal + kScalUm);
         c->launches++;
     }
     TCP_CUDA(cudaGetLastError());

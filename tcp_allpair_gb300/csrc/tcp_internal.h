@@ -65,6 +65,10 @@ struct tcp_ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    // the reciprocal chain's stream: `stream`, or `stream2` while a step runs the
+    // reciprocal sum concurrently with the real-space kernel (fork/join events)
+    cudaStream_t rstream = nullptr, stream2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     unsigned flags = TCP_FLAG_ENERGY;
     bool ewald_ready = false;
     double alpha = 0, rc2 = 0, Uo = 0, V = 0;
