@@ -309,11 +309,19 @@ def run_gpu(args, world, rank, local, dist):
     ctx_e.download_pt(qel, qion)
     ctx_e.md_steps(s.dt, 1)
     barrier(dist)
+    ph = [0.0, 0.0, 0.0]                       # host wall time of upload, step, download
     te0 = time.perf_counter()
     for _ in range(args.steps):
+        t0 = time.perf_counter()
         ctx_e.upload_pt(qel, qion)
+        t1 = time.perf_counter()
         ctx_e.md_steps(s.dt, 1)
+        t2 = time.perf_counter()
         ctx_e.download_pt(qel, qion)
+        t3 = time.perf_counter()
+        ph[0] += t1 - t0
+        ph[1] += t2 - t1
+        ph[2] += t3 - t2
     te = time.perf_counter() - te0
     te = reduce_max(dist, te)
     ctx_e.close()
@@ -379,6 +387,8 @@ def run_gpu(args, world, rank, local, dist):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "pair-int/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": te / args.steps * 1e3,
+                "host_ms_per_step": {"upload": ph[0] / args.steps * 1e3, "md_steps": ph[1] / args.steps * 1e3,
+                                     "download": ph[2] / args.steps * 1e3},
                 "path": "tcp_upload (PT records x,v,f) + tcp_md_steps(1) + tcp_download (x,v,f), pageable host memory"},
         "gpu_launches": int(launches),
         "clocks": clocks,

@@ -392,6 +392,8 @@ struct tcp_batch {
     std::vector<int> nel, nion, off;
     std::vector<double> alpha, Uo;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;     // the SPME chain of a step, beside the pair launch
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double *x = nullptr, *v = nullptr, *f = nullptr, *frec = nullptr, *facc = nullptr;
     int4 *xq = nullptr;
     int *rep_of = nullptr;
@@ -472,19 +474,19 @@ static SpreadBins b_bins(tcp_batch *b) {
 }
 
 template <int P>
-static void b_spme_launch(tcp_batch *b, bool gather) {
+static void b_spme_launch(tcp_batch *b, bool gather, cudaStream_t st) {
     const int blocks = (b->ntot + 127) / 128;
     if (gather) {
-        b_gather_kernel<P><<<blocks, 128, 0, b->stream>>>(parts(b), b->Qf);
+        b_gather_kernel<P><<<blocks, 128, 0, st>>>(parts(b), b->Qf);
         return;
     }
     const SpreadBins bins = b_bins(b);
-    cudaMemsetAsync(b->bin_count, 0, sizeof(int) * (size_t)b->nbins, b->stream);
-    b_bin_count_kernel<P><<<blocks, 128, 0, b->stream>>>(parts(b), bins);
-    launch_bin_sort(b->stream, b->ntot, b->nbins, bins);
-    b_bin_weights_kernel<P><<<blocks, 128, 0, b->stream>>>(parts(b), bins);
+    cudaMemsetAsync(b->bin_count, 0, sizeof(int) * (size_t)b->nbins, st);
+    b_bin_count_kernel<P><<<blocks, 128, 0, st>>>(parts(b), bins);
+    launch_bin_sort(st, b->ntot, b->nbins, bins);
+    b_bin_weights_kernel<P><<<blocks, 128, 0, st>>>(parts(b), bins);
     const size_t sm = kBRowWarps * b_row_warp_bytes(P, b->k1max);   // attribute set at tcp_batch_create
-    b_row_spread_kernel<P><<<(b->ngroups + kBRowWarps - 1) / kBRowWarps, 32 * kBRowWarps, sm, b->stream>>>(
+    b_row_spread_kernel<P><<<(b->ngroups + kBRowWarps - 1) / kBRowWarps, 32 * kBRowWarps, sm, st>>>(
         parts(b), bins, b->nrep, b->ngroups, b->k1max, b->Qf);
 }
 
@@ -505,35 +507,56 @@ static int b_prepare_spread(tcp_batch *b) {
     }
 }
 
-static void b_spme(tcp_batch *b, bool gather) {
+static void b_spme(tcp_batch *b, bool gather, cudaStream_t st) {
     switch (b->order) {
-        case 4: b_spme_launch<4>(b, gather); break;
-        case 5: b_spme_launch<5>(b, gather); break;
-        case 6: b_spme_launch<6>(b, gather); break;
-        case 7: b_spme_launch<7>(b, gather); break;
-        default: b_spme_launch<8>(b, gather); break;
+        case 4: b_spme_launch<4>(b, gather, st); break;
+        case 5: b_spme_launch<5>(b, gather, st); break;
+        case 6: b_spme_launch<6>(b, gather, st); break;
+        case 7: b_spme_launch<7>(b, gather, st); break;
+        default: b_spme_launch<8>(b, gather, st); break;
     }
+}
+
+// The SPME chain of every replica (spread, batched R2C per mesh size,
+// influence multiply + energy, C2R, gather into frec), forked onto stream2
+// after the work queued on the main stream, so that it runs beside the
+// real-space launch; b_recip_join makes the main stream wait for it.
+static int b_recip_fork(tcp_batch *b, const BAcc &A) {
+    TCP_CUDA(cudaEventRecord(b->ev_fork, b->stream));
+    TCP_CUDA(cudaStreamWaitEvent(b->stream2, b->ev_fork, 0));
+    b_spme(b, false, b->stream2);                       // atomic-free, every mesh point written
+    for (auto &g : b->groups) {
+        cufftSetStream(g.fwd, b->stream2);
+        if (cufftExecR2C(g.fwd, b->Qf + g.mesh_off, b->Qk + g.half_off) != CUFFT_SUCCESS)
+            return set_error(TCP_ERR_CUFFT, "batched cufftExecR2C failed");
+    }
+    b_influence_kernel<<<b->infl_blocks, 256, 0, b->stream2>>>(b->Qk, b->infl, b->reps, b->blk0, b->nrep, A.um);
+    for (auto &g : b->groups) {
+        cufftSetStream(g.inv, b->stream2);
+        if (cufftExecC2R(g.inv, b->Qk + g.half_off, b->Qf + g.mesh_off) != CUFFT_SUCCESS)
+            return set_error(TCP_ERR_CUFFT, "batched cufftExecC2R failed");
+    }
+    b_spme(b, true, b->stream2);
+    return TCP_OK;
+}
+
+static int b_recip_join(tcp_batch *b) {
+    TCP_CUDA(cudaEventRecord(b->ev_join, b->stream2));
+    TCP_CUDA(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
+    return TCP_OK;
 }
 
 // One batched MD step (main.f90:81-153 for every replica) on b->stream.
 static int b_step(tcp_batch *b, double dt) {
     const BAcc A = acc_of(b);
     const int nb = (b->ntot + kBThreads - 1) / kBThreads;
-    const int launches_before = 0;
-    (void)launches_before;
     TCP_CUDA(cudaMemsetAsync(A.um, 0, sizeof(double) * 8 * (size_t)b->nrep, b->stream));   // um, mv0, mv1, fsum
     b_vverlet1_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), dt);
-    b_spme(b, false);                                   // atomic-free, every mesh point written
-    for (auto &g : b->groups)
-        if (cufftExecR2C(g.fwd, b->Qf + g.mesh_off, b->Qk + g.half_off) != CUFFT_SUCCESS)
-            return set_error(TCP_ERR_CUFFT, "batched cufftExecR2C failed");
-    b_influence_kernel<<<b->infl_blocks, 256, 0, b->stream>>>(b->Qk, b->infl, b->reps, b->blk0, b->nrep, A.um);
-    for (auto &g : b->groups)
-        if (cufftExecC2R(g.inv, b->Qk + g.half_off, b->Qf + g.mesh_off) != CUFFT_SUCCESS)
-            return set_error(TCP_ERR_CUFFT, "batched cufftExecC2R failed");
-    b_spme(b, true);
-    int rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
+    int rc = b_recip_fork(b, A);
+    if (!rc)
+        rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
                                   b->status, b->counter, b->num_sms, true, b->pair_variant);
+    if (int jrc = b_recip_join(b)) return jrc;
     if (rc) return rc;
     b_finalize_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), A.fsum);
     b_kick2_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), dt, A.fsum, A.mv0);
@@ -642,6 +665,12 @@ int tcp_batch_destroy(tcp_batch *b) {
                       (void *)b->bin_eq})
         cudaFree(ptr);
     if (b->h_acc) cudaFreeHost(b->h_acc);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
+    if (b->stream2) {
+        cudaStreamSynchronize(b->stream2);
+        cudaStreamDestroy(b->stream2);
+    }
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return TCP_OK;
@@ -697,7 +726,10 @@ int tcp_batch_create(const tcp_params *params, const int *nel, const int *nion, 
         cudaError_t _e = cudaMalloc(&(ptr), (bytes));                               \
         if (_e != cudaSuccess) return fail(cuda_check(_e, "cudaMalloc " #ptr));     \
     } while (0)
-    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess)
         return fail(cuda_check(cudaGetLastError(), "cudaStreamCreate"));
     TCP_BALLOC(b->x, sizeof(double) * 3 * n);
     TCP_BALLOC(b->v, sizeof(double) * 3 * n);
@@ -920,17 +952,11 @@ int tcp_batch_force(tcp_batch *b, tcp_energies *e) {
     const int nb = (b->ntot + kBThreads - 1) / kBThreads;
     b_refresh_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b));
     TCP_CUDA(cudaMemsetAsync(A.um, 0, sizeof(double) * 8 * (size_t)b->nrep, b->stream));
-    b_spme(b, false);                                   // atomic-free, every mesh point written
-    for (auto &g : b->groups)
-        if (cufftExecR2C(g.fwd, b->Qf + g.mesh_off, b->Qk + g.half_off) != CUFFT_SUCCESS)
-            return set_error(TCP_ERR_CUFFT, "batched cufftExecR2C failed");
-    b_influence_kernel<<<b->infl_blocks, 256, 0, b->stream>>>(b->Qk, b->infl, b->reps, b->blk0, b->nrep, A.um);
-    for (auto &g : b->groups)
-        if (cufftExecC2R(g.inv, b->Qk + g.half_off, b->Qf + g.mesh_off) != CUFFT_SUCCESS)
-            return set_error(TCP_ERR_CUFFT, "batched cufftExecC2R failed");
-    b_spme(b, true);
-    int rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
+    int rc = b_recip_fork(b, A);
+    if (!rc)
+        rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
                                   b->status, b->counter, b->num_sms, true, b->pair_variant);
+    if (int jrc = b_recip_join(b)) return jrc;
     if (rc) return rc;
     b_finalize_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), A.fsum);
     // the net-force removal of the step is fused into the kick; here apply it alone
