@@ -67,6 +67,10 @@ extern "C" {
 #define TCP_FLAG_RDF 1u         /* accumulate RDF histograms in the pair sum   */
 #define TCP_FLAG_VDF 2u         /* accumulate VDF histograms in the 2nd kick   */
 #define TCP_FLAG_ENERGY 4u      /* compute Ur/Um (default on)                  */
+#define TCP_FLAG_DETERMINISTIC 8u /* ordered-pair real-space kernels with a fixed
+                                   * summation order: bitwise reproducible forces
+                                   * and energies (the Newton-3 kernels add with
+                                   * atomics in a varying order)               */
 
 /* Parameters: the fields of TYPE PM (data.f90:68-74), the histogram
  * spacings of TYPE NM (data.f90:99) and the GPU build's own knobs. */

@@ -15,7 +15,7 @@ import ctypes as C
 import numpy as np
 
 from . import _abi
-from ._abi import (EI_COULOMB, EI_DEUTSCH, EI_KELBG, FLAG_ENERGY, FLAG_RDF, FLAG_VDF, PREC_FP32C,
+from ._abi import (EI_COULOMB, EI_DEUTSCH, EI_KELBG, FLAG_DETERMINISTIC, FLAG_ENERGY, FLAG_RDF, FLAG_VDF, PREC_FP32C,
                    PREC_FP64, RECIP_EWALD, RECIP_NONE, RECIP_SPME, THERMO_BEREND, THERMO_ISOKIN,
                    THERMO_NOTEMP, THERMO_STOCH, TcpEnergies, TcpError, TcpParams)
 from .system import EPS, NDIST, PT_DTYPE, System, make_config_system, make_system

@@ -24,7 +24,7 @@ PREC_FP64, PREC_FP32C = 0, 1
 EI_DEUTSCH, EI_KELBG, EI_COULOMB = 0, 1, 2
 THERMO_NOTEMP, THERMO_ISOKIN, THERMO_BEREND, THERMO_STOCH = 0, 1, 2, 3
 RECIP_NONE, RECIP_SPME, RECIP_EWALD = 0, 1, 2
-FLAG_RDF, FLAG_VDF, FLAG_ENERGY = 1, 2, 4
+FLAG_RDF, FLAG_VDF, FLAG_ENERGY, FLAG_DETERMINISTIC = 1, 2, 4, 8
 
 
 class TcpParams(C.Structure):

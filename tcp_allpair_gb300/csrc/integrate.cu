@@ -291,38 +291,87 @@ __global__ void reduce_scalars_kernel(const double *__restrict__ upart, int nu, 
 }
 
 // ---- host records <-> SoA ------------------------------------------------
-// stage holds `count` records of `stride` bytes; fields at byte offsets
-// off_x/off_v/off_f (or < 0 to skip), 3 doubles each.
-// records -> SoA; new positions also refresh the two pair-kernel copies
-__global__ void extract_kernel(const unsigned char *__restrict__ stage, long stride, long off_x, long off_v,
-                               long off_f, int count, int first, const IntArgs a) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= count) return;
-    const unsigned char *rec = stage + (size_t)r * stride;
-    const int i = first + r, n = a.n;
-    for (int d = 0; d < 3; ++d) {
-        if (off_v >= 0) a.v[(size_t)d * n + i] = reinterpret_cast<const double *>(rec + off_v)[d];
-        if (off_f >= 0) a.f[(size_t)d * n + i] = reinterpret_cast<const double *>(rec + off_f)[d];
+// The fields a transfer moves: up to three 3-double fields of a record (x, v,
+// f), listed by increasing byte offset so that consecutive words of a record
+// are consecutive in memory.
+struct RecFields {
+    long off[3];   // byte offset of each field in the record
+    int id[3];     // 0 = x, 1 = v, 2 = f
+    int nf;
+};
+
+static RecFields rec_fields(long off_x, long off_v, long off_f) {
+    RecFields fl;
+    fl.nf = 0;
+    const long offs[3] = {off_x, off_v, off_f};
+    for (int k = 0; k < 3; ++k)
+        if (offs[k] >= 0) {
+            int at = fl.nf++;
+            while (at > 0 && fl.off[at - 1] > offs[k]) {
+                fl.off[at] = fl.off[at - 1];
+                fl.id[at] = fl.id[at - 1];
+                --at;
+            }
+            fl.off[at] = offs[k];
+            fl.id[at] = k;
+        }
+    for (int k = fl.nf; k < 3; ++k) {
+        fl.off[k] = 0;
+        fl.id[k] = -1;
     }
-    if (off_x >= 0) {
-        const double *px = reinterpret_cast<const double *>(rec + off_x);
-        store_pos(a, i, px[0], px[1], px[2]);
+    return fl;
+}
+
+// stage holds `count` records of `stride` bytes (device memory, or host
+// memory the device can address).  Records -> SoA; new positions also refresh
+// the two pair-kernel copies.  A CTA takes kIntThreads records: its threads
+// first read the records' words in order (consecutive threads, consecutive
+// words: a warp's loads fall on a few contiguous runs instead of 32 records)
+// into shared memory, then one thread per record stores its fields.
+__global__ void __launch_bounds__(kIntThreads) extract_kernel(const unsigned char *__restrict__ stage, long stride,
+                                                              const RecFields fl, int count, int first,
+                                                              const IntArgs a) {
+    __shared__ double buf[kIntThreads * 9];
+    const int r0 = blockIdx.x * kIntThreads;
+    const int nr = min(kIntThreads, count - r0);
+    const int nw = 3 * fl.nf;
+    for (int w = threadIdx.x; w < nr * nw; w += kIntThreads) {
+        const int r = w / nw, q = w - r * nw, k = q / 3;
+        const long off = k == 0 ? fl.off[0] : (k == 1 ? fl.off[1] : fl.off[2]);
+        buf[w] = reinterpret_cast<const double *>(stage + (size_t)(r0 + r) * stride + off)[q - 3 * k];
+    }
+    __syncthreads();
+    const int r = threadIdx.x;
+    if (r >= nr) return;
+    const int i = first + r0 + r, n = a.n;
+    const double *rec = buf + r * nw;
+    for (int k = 0; k < fl.nf; ++k) {
+        const int id = k == 0 ? fl.id[0] : (k == 1 ? fl.id[1] : fl.id[2]);
+        const double *w = rec + 3 * k;
+        if (id == 0) {
+            store_pos(a, i, w[0], w[1], w[2]);
+        } else {
+            double *dst = id == 1 ? a.v : a.f;
+            for (int d = 0; d < 3; ++d) dst[(size_t)d * n + i] = w[d];
+        }
     }
 }
 
 // SoA -> host records: the inverse of extract_kernel, writing the fields of
-// record r at dst + r*stride + off (dst in host memory the device can address)
-__global__ void scatter_kernel(unsigned char *__restrict__ dst, long stride, long off_x, long off_v, long off_f,
-                               int count, int first, int n, const double *x, const double *v, const double *f) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= count) return;
-    unsigned char *rec = dst + (size_t)r * stride;
-    const int i = first + r;
-    for (int d = 0; d < 3; ++d) {
-        if (off_x >= 0) reinterpret_cast<double *>(rec + off_x)[d] = x[(size_t)d * n + i];
-        if (off_v >= 0) reinterpret_cast<double *>(rec + off_v)[d] = v[(size_t)d * n + i];
-        if (off_f >= 0) reinterpret_cast<double *>(rec + off_f)[d] = f[(size_t)d * n + i];
-    }
+// record r at dst + r*stride + off (dst in host memory the device can
+// address).  One thread per 8-byte word, consecutive threads on consecutive
+// words of the record span, so that a warp's stores fall on a few contiguous
+// runs of host memory.
+__global__ void scatter_kernel(unsigned char *__restrict__ dst, long stride, const RecFields fl, int count,
+                               int first, int n, const double *x, const double *v, const double *f) {
+    const int nw = 3 * fl.nf;
+    const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= (long long)count * nw) return;
+    const int r = (int)(w / nw), q = (int)(w - (long long)r * nw), k = q / 3, d = q - 3 * k;
+    const long off = k == 0 ? fl.off[0] : (k == 1 ? fl.off[1] : fl.off[2]);
+    const int id = k == 0 ? fl.id[0] : (k == 1 ? fl.id[1] : fl.id[2]);
+    const double *src = id == 0 ? x : (id == 1 ? v : f);
+    reinterpret_cast<double *>(dst + (size_t)r * stride + off)[d] = src[(size_t)d * n + first + r];
 }
 
 // SoA -> [count][fields][3] packed doubles
@@ -487,8 +536,9 @@ int launch_reduce(tcp_ctx *c, int mask, int pass) {
 
 int launch_extract(tcp_ctx *c, const unsigned char *src, int first, int count, long stride, long off_x, long off_v,
                    long off_f) {
-    extract_kernel<<<nblocks(count), kIntThreads, 0, c->stream>>>(src, stride, off_x, off_v, off_f, count,
-                                                                  first, int_args(c));
+    const RecFields fl = rec_fields(off_x, off_v, off_f);
+    if (fl.nf == 0 || count <= 0) return TCP_OK;
+    extract_kernel<<<nblocks(count), kIntThreads, 0, c->stream>>>(src, stride, fl, count, first, int_args(c));
     c->launches++;
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;
@@ -496,8 +546,11 @@ int launch_extract(tcp_ctx *c, const unsigned char *src, int first, int count, l
 
 int launch_scatter(tcp_ctx *c, unsigned char *dst, int first, int count, long stride, long off_x, long off_v,
                    long off_f, const double *fsrc) {
-    scatter_kernel<<<nblocks(count), kIntThreads, 0, c->stream>>>(dst, stride, off_x, off_v, off_f, count, first,
-                                                                  c->n, c->x, c->v, fsrc);
+    const RecFields fl = rec_fields(off_x, off_v, off_f);
+    if (fl.nf == 0 || count <= 0) return TCP_OK;
+    const long long words = (long long)count * 3 * fl.nf;
+    scatter_kernel<<<(unsigned)((words + kIntThreads - 1) / kIntThreads), kIntThreads, 0, c->stream>>>(
+        dst, stride, fl, count, first, c->n, c->x, c->v, fsrc);
     c->launches++;
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;

@@ -518,11 +518,20 @@ void make_pair_consts(tcp_ctx *c) {
         k.u_qq_force[t] = (float)(qq[t] / (u * u));
         k.u_qq_energy[t] = (float)(qq[t] / u);
     }
-    for (int d = 0; d < 3; ++d) k.box[d] = p.box[d];
+    for (int d = 0; d < 3; ++d) {
+        k.box[d] = p.box[d];
+        k.inv_box[d] = 1.0 / p.box[d];
+    }
     k.rc2 = c->rc2;
     k.alpha = c->alpha;
     k.rs = rs;
     k.lambda = lam;
+    k.alpha2 = c->alpha * c->alpha;
+    k.c_gauss_d = 2.0 * c->alpha / kSqrtPi;
+    k.inv_rs_d = 1.0 / rs;
+    k.inv_lam2 = 1.0 / (lam * lam);
+    k.inv_lam = 1.0 / lam;
+    k.sqrtpi_lam_d = kSqrtPi / lam;
     k.ei_model = p.ei_model;
 }
 
@@ -581,7 +590,7 @@ int pair_setup(tcp_ctx *c) {
     c->fpart = nullptr;
     c->upart = nullptr;
     c->jsplit = js;
-    c->n_upart = std::max(g.nblk * js, fp64 ? 1 : n3_grid(c));
+    c->n_upart = std::max(g.nblk * js, fp64 ? n3_f64_grid(c) : n3_grid(c));
     TCP_CUDA(cudaMalloc(&c->fpart, sizeof(double) * 3 * (size_t)c->n * js));
     TCP_CUDA(cudaMalloc(&c->upart, sizeof(double) * (size_t)c->n_upart));
     TCP_CUDA(cudaMemsetAsync(c->upart, 0, sizeof(double) * (size_t)c->n_upart, c->stream));
@@ -593,6 +602,10 @@ int launch_pair(tcp_ctx *c, bool energy, bool rdf) {
     if (!rdf && n3_applicable(c)) {
         c->fpart_splits = 1;
         return launch_pair_n3(c, energy);
+    }
+    if (!rdf && n3_f64_applicable(c)) {
+        c->fpart_splits = 1;
+        return launch_pair_n3_f64(c, energy);
     }
     c->fpart_splits = c->jsplit;
     Geometry g = geometry(c, fp64);

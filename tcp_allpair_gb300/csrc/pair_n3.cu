@@ -32,119 +32,9 @@
 #include <cstring>
 
 #include "device_util.cuh"
-#include "pair_math.cuh"
-#include "tcp_internal.h"
+#include "pair_n3.cuh"
 
 namespace tcp {
-
-constexpr int kN3Warps = 8;
-constexpr int kN3Threads = 32 * kN3Warps;
-constexpr int kN3Sub = 128;                // j-subtile
-constexpr int kN3Stages = 3;
-constexpr int kN3DynPercent = 10;          // share of the items handed out dynamically
-
-// Tile geometry of one system (a replica of a batch, or the only system).
-struct N3Geom {
-    int off;              // first particle in the global arrays
-    int nel, n;           // electrons, particles
-    int nIe, nI;          // i-tiles, electron tiles first
-    int nSe, nS;          // j-subtiles, electron subtiles first
-    long long item0;      // first item of this system in the global item list
-};
-
-struct N3Rep {
-    N3Geom g;
-    PairConsts c;
-};
-
-struct N3Args {
-    const int4 *xq;
-    long long total;      // items (all systems)
-    long long nstatic;    // items [0, nstatic) split statically
-    int ntot;             // stride of facc
-    double *facc;         // [3][ntot], zeroed before the launch
-    double *upart;        // [gridDim.x] (single system)
-    unsigned *status;
-    unsigned *counter;    // dynamic item counter, zeroed before the launch
-    N3Geom g;             // single system
-    PairConsts c;
-    const N3Rep *reps;    // batch: one entry per replica
-    int nrep;
-    double *ur_rep;       // batch: Ur per replica (zeroed before the launch)
-    int inject_skip;      // test hook: CTA 0 never issues the copy of its first item (its bounded wait runs out)
-};
-
-template <int TILE>
-__device__ __forceinline__ void n3_itile(const N3Geom &a, int I, int &start, int &end, int &sp, int &first) {
-    constexpr int SPT = TILE / kN3Sub;
-    if (I < a.nIe) {
-        sp = 0;
-        start = I * TILE;
-        end = min(start + TILE, a.nel);
-        first = I * SPT;
-    } else {
-        sp = 1;
-        start = a.nel + (I - a.nIe) * TILE;
-        end = min(start + TILE, a.n);
-        first = a.nSe + (I - a.nIe) * SPT;
-    }
-}
-
-__device__ __forceinline__ void n3_sub(const N3Geom &a, int S, int &start, int &cnt, int &sp) {
-    if (S < a.nSe) {
-        sp = 0;
-        start = S * kN3Sub;
-        cnt = min(kN3Sub, a.nel - start);
-    } else {
-        sp = 1;
-        start = a.nel + (S - a.nSe) * kN3Sub;
-        cnt = min(kN3Sub, a.n - start);
-    }
-}
-
-// local item index of one system -> (row I, subtile S)
-template <int TILE>
-__device__ __forceinline__ void n3_decode(const N3Geom &a, long long it, int &I, int &S) {
-    long long acc = 0;
-    int st, en, sp, first;
-    for (I = 0; I < a.nI; ++I) {
-        n3_itile<TILE>(a, I, st, en, sp, first);
-        const long long len = a.nS - first;
-        if (it < acc + len) {
-            S = first + (int)(it - acc);
-            return;
-        }
-        acc += len;
-    }
-    S = a.nS;
-}
-
-// global item -> replica (0 for a single system), row and subtile
-template <int TILE, bool BATCH>
-__device__ __forceinline__ void n3_locate(const N3Args &a, long long it, int &rep, int &I, int &S) {
-    rep = 0;
-    if (BATCH) {
-        int lo = 0, hi = a.nrep - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (a.reps[mid].g.item0 <= it) lo = mid; else hi = mid - 1;
-        }
-        rep = lo;
-        n3_decode<TILE>(a.reps[rep].g, it - a.reps[rep].g.item0, I, S);
-    } else {
-        n3_decode<TILE>(a.g, it, I, S);
-    }
-}
-
-template <bool BATCH>
-__device__ __forceinline__ const N3Geom &n3_geom(const N3Args &a, int rep) {
-    return BATCH ? a.reps[rep].g : a.g;
-}
-
-template <bool BATCH>
-__device__ __forceinline__ const PairConsts &n3_consts(const N3Args &a, int rep) {
-    return BATCH ? a.reps[rep].c : a.c;
-}
 
 // One pair in units of u = L/2^32.  Returns the force weight w (force on i is
 // eps qq/u^2 * w * d) and, with ENERGY, adds the energy term / r to pe.
@@ -614,7 +504,8 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
 static int cdiv(int x, int y) { return (x + y - 1) / y; }
 
 bool n3_applicable(const tcp_ctx *c) {
-    return c->p.precision == TCP_PREC_FP32C && c->pc.cubic && c->n >= 2 && c->pair_variant > 0;
+    return c->p.precision == TCP_PREC_FP32C && c->pc.cubic && c->n >= 2 && c->pair_variant > 0 &&
+           !(c->flags & TCP_FLAG_DETERMINISTIC);
 }
 
 // Variants 1..V (0 = the ordered-pair kernel): i-particles per lane x unroll

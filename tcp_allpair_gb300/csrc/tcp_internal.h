@@ -49,6 +49,13 @@ struct PairConsts {
     // FP64 path
     double box[3];
     double rc2, alpha, rs, lambda;
+    double inv_box[3];         // 1/box (minimum image by multiplication)
+    double alpha2;             // alpha^2
+    double c_gauss_d;          // 2 alpha / sqrt(pi)
+    double inv_rs_d;           // 1/rs
+    double inv_lam2;           // 1/lambda^2
+    double inv_lam;            // 1/lambda
+    double sqrtpi_lam_d;       // sqrt(pi)/lambda
     double inv_dxd[3];
     double qq[3];
     int ei_model;
@@ -191,6 +198,9 @@ int launch_pair(tcp_ctx *c, bool energy, bool rdf);
 int launch_force_finalize(tcp_ctx *c, bool add_rec);
 // pair_n3.cu
 bool n3_applicable(const tcp_ctx *c);
+bool n3_f64_applicable(const tcp_ctx *c);
+int n3_f64_grid(const tcp_ctx *c);
+int launch_pair_n3_f64(tcp_ctx *c, bool energy);
 int n3_grid(const tcp_ctx *c);
 int n3_variant_count();
 const char *n3_variant_name(int v);

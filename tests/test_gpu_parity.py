@@ -327,3 +327,43 @@ def test_noncubic_box_and_mesh_uneven_species(precision):
     assert oracle.rms_rel(f, fo) < tol
     assert e["Um"] == pytest.approx(umo, rel=1e-10 if precision == "fp64" else 1e-6)
     assert e["Ur"] == pytest.approx(uro, rel=1e-10 if precision == "fp64" else 2e-5)
+
+
+@pytest.mark.parametrize("ei", ["deutsch", "kelbg", "coulomb"])
+@pytest.mark.parametrize("nel,nion", [(1024, 1024), (700, 333), (1, 300), (257, 0)])
+def test_fp64_newton3_vs_ordered(ei, nel, nion):
+    """The FP64 Newton-3 kernel (default) against the ordered-pair FP64
+    kernel (TCP_FLAG_DETERMINISTIC) and the oracle: partial i-tiles and
+    j-subtiles, a single electron, one species only."""
+    s = T.make_system(nel + nion, gamma=1.0, lam=0.5, seed=8, alpha_rc=3.1, K=16, order=4)
+    s.nel, s.nion = nel, nion
+    o = oracle.Oracle.from_system(s, ei=ei)
+    fo, uo = o.force_direct(s.x)
+    out = {}
+    for det in (False, True):
+        with ctx_for(s, precision="fp64", ei=ei, recip="none") as c:
+            if det:
+                c.set_flags(T.FLAG_ENERGY | T.FLAG_DETERMINISTIC)
+            ur = c.Force_direct_self()
+            _, _, f, _ = c.download(x=False, v=False, f=True)
+        out[det] = (ur, f)
+        assert ur == pytest.approx(uo, rel=FP64_REL, abs=1e-12)
+        assert oracle.rms_rel(f, fo) < FP64_REL
+    assert oracle.rms_rel(out[False][1], out[True][1]) < 1e-13
+    assert out[False][0] == pytest.approx(out[True][0], rel=1e-13, abs=1e-13)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_deterministic_flag_is_bitwise_reproducible(precision):
+    """With TCP_FLAG_DETERMINISTIC two force evaluations of the same state give
+    identical bits (ordered-pair kernels, fixed-order reductions, atomic-free
+    SPME spread)."""
+    s = make(3000, seed=9, K=24, order=5)
+    with ctx_for(s, precision=precision, ei="kelbg", recip="spme") as c:
+        c.set_flags(T.FLAG_ENERGY | T.FLAG_DETERMINISTIC)
+        e1 = c.force()
+        _, _, f1, _ = c.download(x=False, v=False, f=True)
+        e2 = c.force()
+        _, _, f2, _ = c.download(x=False, v=False, f=True)
+    assert np.array_equal(f1, f2)
+    assert e1["Ur"] == e2["Ur"] and e1["Um"] == e2["Um"]
