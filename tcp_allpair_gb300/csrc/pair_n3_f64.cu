@@ -3,9 +3,9 @@
 // particles (Force_direct_self / _ext / _sum of force.f90:52-372, whose
 // triangular loops also evaluate each pair once).
 //
-// The item schedule is that of the compensated-FP32 Newton-3 kernel
-// (pair_n3.cuh: i-tiles of 32 R W particles x j-subtiles of kN3Sub, a static
-// share plus an atomic counter, bulk copies into a kN3Stages-deep ring); the
+// The items are those of the compensated-FP32 Newton-3 kernel (pair_n3.cuh:
+// i-tiles of 32 R W particles x j-subtiles of kN3Sub, bulk copies into a
+// kN3Stages-deep ring), all taken one at a time from an atomic counter; the
 // warp-rotation of j (position and reaction) runs on doubles.  Forces and
 // energies are summed in FP64: per item in registers, then i-forces into
 // registers along the row and j-reactions through shared-memory FP64 atomics,
@@ -305,7 +305,9 @@ int launch_pair_n3_f64(tcp_ctx *c, bool energy) {
     a.g = n3_geometry(0, c->nel, c->nion, tile, 0, &total);
     a.xd = c->xd;
     a.total = total;
-    a.nstatic = total - total * kN3DynPercent / 100;
+    // all items from the counter: an FP64 item takes milliseconds, so the
+    // per-item copy latency is negligible and the tail is at most one item
+    a.nstatic = 0;
     a.ntot = c->n;
     a.facc = c->fpart;
     a.upart = c->upart;
