@@ -47,12 +47,12 @@ WORKLOAD = "n65536_spme128"
 # pair_n3.cu n3_pair/n3_item), Coulomb pair with energy, cubic box: 3 integer
 # subtractions + 3 int->float conversions (minimum image), r^2 (3), cut-off
 # test (1), r (1), rcp argument (1), exp argument (1), erfc polynomial
-# (degree 7) and products (10), force numerator (1), 1/r mask select and r^-2
-# weight (3), force accumulation (3), energy add (1) = 31 per ordered pair; the
-# Newton-3 kernel adds the reaction accumulation (3) = 34 per unique pair.
+# (degree 6) and products (9), force numerator (1), 1/r mask select and r^-2
+# weight (3), force accumulation (3), energy add (1) = 30 per ordered pair; the
+# Newton-3 kernel adds the reaction accumulation (3) = 33 per unique pair.
 # SFU: rsqrt, rcp, ex2 (3) per pair in both.
-RECIPE_ORDERED = 31
-RECIPE_N3 = 34
+RECIPE_ORDERED = 30
+RECIPE_N3 = 33
 RECIPE_SFU_OPS = 3
 SFU_RATE = 16.0 / 128.0       # SFU lanes per SM relative to FP32 lanes
 

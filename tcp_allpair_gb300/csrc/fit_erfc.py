@@ -1,27 +1,31 @@
-"""Derive the FP32 erfc approximation used by the FP32 pair kernel.
+"""Derive the FP32 erfc approximation used by the FP32 pair kernels.
 
     erfc(x) = exp(-x^2) * t * Q(t),   t = 1 / (1 + P x),   x >= 0
 
-Q is a degree-7 polynomial in t fitted to erfcx(x)/t = erfc(x) exp(x^2)/t by
+Q is a degree-6 polynomial in t fitted to erfcx(x)/t = erfc(x) exp(x^2)/t by
 Lawson's iteratively reweighted least squares, which converges to the minimax
-fit in relative error, on x in [0, XMAX].  P = 0.4 and XMAX = 6 minimise the
-FP32 error on the arguments the kernels see: alpha r <= alpha rc (3.1 by
-default, 3.46 for a 1e-6 Ewald error) and r/lambda < 6 (the Kelbg terms are
-skipped beyond 6 lambda).  The exp(-x^2) factor is shared with
-the Gaussian term of the Ewald pair force, so a Coulomb pair costs one ex2 and
-one reciprocal on the SFU for both erfc and the Gaussian.
+fit in relative error, on x in [0, XMAX].  The arguments the kernels see are
+alpha r <= alpha rc (3.1 by default, 3.46 for a 1e-6 Ewald error) and
+r/lambda < 6 (the Kelbg terms are skipped beyond 6 lambda).  The exp(-x^2)
+factor is shared with the Gaussian term of the Ewald pair force, so a Coulomb
+pair costs one ex2 and one reciprocal on the SFU for both erfc and the
+Gaussian.
 
-Fit error (FP64 evaluation): 1.0e-7 relative.  Evaluated in FP32 Horner form
-on x in [0, 6]: 4.4e-7 max, 1.15e-7 rms relative (the FP32 rounding of t
-dominates; degree 8 gives 3.3e-7 / 7.6e-8 for one more FFMA per erfc).  Run `python fit_erfc.py` to reproduce the coefficients in
-pair_math.cuh (printed highest power first).
+The fit error depends sharply on P: at degree 6, P = 0.36 on [0, 4.5] reaches
+a fit error of 1.0e-7 relative, and in FP32 Horner form 4.6e-7 max / 1.2e-7
+rms on [0, 4.5] (the FP32 rounding of t dominates), the accuracy the degree-7
+fit with P = 0.4 had on [0, 6] (4.4e-7 / 1.15e-7) for one FFMA less per
+erfc.  Beyond 4.5 the relative error grows to 6.4e-6 at x = 6, where erfc is
+below 2e-10 and the term no longer counts at FP32 precision.  Run
+`python fit_erfc.py` to reproduce the coefficients in pair_math.cuh (printed
+highest power first).
 """
 import numpy as np
 from scipy.special import erfc, erfcx
 
-P = 0.4
-DEG = 7
-XMAX = 6.0
+P = 0.36
+DEG = 6
+XMAX = 4.5
 
 
 def fit(p=P, deg=DEG, xmax=XMAX, iters=400):
@@ -53,6 +57,6 @@ def fp32_error(c, p=P, xmax=6.0):
 
 if __name__ == "__main__":
     c, e = fit()
-    mx, rms = fp32_error(c)
+    mx, rms = fp32_error(c, xmax=XMAX)
     print(f"P={P} DEG={DEG} fit max rel {e:.3e}; fp32 max rel {mx:.3e}, rms {rms:.3e}")
     print(", ".join(f"{v:.9e}f" for v in c))

@@ -96,6 +96,9 @@ __device__ __forceinline__ void tile_f32(const int4 *__restrict__ tj, int cnt, i
     const float p_lam = CUBIC ? c.u_p_lam : c.p_lam;
     const float sqrtpi_lam = CUBIC ? c.u_sqrtpi_lam : c.sqrtpi_lam;
     const float rshort2 = CUBIC ? c.u_rshort2 : c.rshort2;
+    const float close2 = CUBIC ? c.u_close2 : c.close2;
+    const float inv_lam2 = CUBIC ? c.u_inv_lam2 : c.inv_lam2f;
+    const float alpha_ = CUBIC ? c.u_alpha : c.alphaf;
 #pragma unroll 8
     for (int jj = sub; jj < cnt_up; jj += TPP) {
         const int4 xj = tj[jj];
@@ -132,10 +135,18 @@ __device__ __forceinline__ void tile_f32(const int4 *__restrict__ tj, int cnt, i
             if (__any_sync(0xffffffffu, near)) {
                 const float g = near ? ex2_approx(c_lam * r2s) : 0.0f;   // exp(-r^2/lambda^2)
                 s = fmaf(-g, rinv, s);
+                float erfc_rl = 0.0f;
                 if (ENERGY) {
                     const float t2 = rcp_approx(fmaf(p_lam, r, 1.0f));
-                    const float erfc_rl = g * erfc_poly(t2);   // erfc(r/lambda)
+                    erfc_rl = g * erfc_poly(t2);                 // erfc(r/lambda)
                     u += fmaf(sqrtpi_lam, erfc_rl, -g * rinv);
+                }
+                const bool close = near && (r2s < close2);
+                if (__any_sync(0xffffffffu, close) && close) {
+                    float nf, ne;
+                    kelbg_close(r2s * inv_lam2, r * alpha_, nf, ne);
+                    s = nf * rinv;
+                    if (ENERGY) u = fmaf(sqrtpi_lam, erfc_rl, ne * rinv);
                 }
             }
         }
@@ -491,6 +502,10 @@ void make_pair_consts(tcp_ctx *c) {
     k.p_lam = (float)(kErfcP / lam);
     k.sqrtpi_lam = (float)(kSqrtPi / lam);
     k.rshort2 = (float)(36.0 * lam * lam);
+    const double close2 = std::min(0.25 * lam * lam, 0.25 / (c->alpha * c->alpha));
+    k.close2 = (float)close2;
+    k.inv_lam2f = (float)(1.0 / (lam * lam));
+    k.alphaf = (float)c->alpha;
     const double dxs[3] = {p.dx_ee, p.dx_ei, p.dx_ii};
     const double s = p.charge_scale;
     const double qq[3] = {s * p.q[0] * s * p.q[0], s * p.q[0] * s * p.q[1], s * p.q[1] * s * p.q[1]};
@@ -513,6 +528,9 @@ void make_pair_consts(tcp_ctx *c) {
     k.u_p_lam = (float)(kErfcP / lam * u);
     k.u_sqrtpi_lam = (float)(kSqrtPi / lam * u);
     k.u_rshort2 = (float)(36.0 * lam * lam / (u * u));
+    k.u_close2 = (float)(close2 / (u * u));
+    k.u_inv_lam2 = (float)(u * u / (lam * lam));
+    k.u_alpha = (float)(c->alpha * u);
     for (int t = 0; t < 3; ++t) {
         k.u_inv_dx[t] = dxs[t] > 0 ? (float)(u / dxs[t]) : 0.f;
         k.u_qq_force[t] = (float)(qq[t] / (u * u));

@@ -5,19 +5,60 @@ namespace tcp {
 
 // erfc(x) = exp(-x^2) t Q(t), t = 1/(1 + kErfcP x): the factor of the
 // reciprocal argument (host constants p_alpha = kErfcP alpha, p_lam = kErfcP/lambda).
-constexpr double kErfcP = 0.4;
+constexpr double kErfcP = 0.36;
 
-// t Q(t) with the coefficients printed by fit_erfc.py (P = 0.4, degree 7).
+// Q(t) of degree kErfcDeg, coefficients printed by fit_erfc.py (highest power
+// first), listed once here for the scalar and the packed evaluations.
+constexpr int kErfcDeg = 6;
+#define TCP_ERFC_Q                                                                                  \
+    {-1.717338572e-01f, 5.984714114e-01f, -4.147594920e-01f, 4.816444120e-01f, 8.168755304e-02f,    \
+     2.231449970e-01f, 2.015448752e-01f}
+
+// t Q(t)
 __device__ __forceinline__ float erfc_poly(float t) {
-    float q = 6.807732388e-02f;
-    q = fmaf(q, t, -3.663086635e-01f);
-    q = fmaf(q, t, 6.308091155e-01f);
-    q = fmaf(q, t, -3.190751584e-01f);
-    q = fmaf(q, t, 3.760577549e-01f);
-    q = fmaf(q, t, 1.510029235e-01f);
-    q = fmaf(q, t, 2.343213173e-01f);
-    q = fmaf(q, t, 2.251152860e-01f);
+    constexpr float q_[kErfcDeg + 1] = TCP_ERFC_Q;
+    float q = q_[0];
+#pragma unroll
+    for (int k = 1; k <= kErfcDeg; ++k) q = fmaf(q, t, q_[k]);
     return q * t;
+}
+
+// Kelbg e-i pairs at r < lambda/2 with alpha r < 1/2: erfc(alpha r) and
+// g = exp(-r^2/lambda^2) both tend to 1 as r -> 0, and the force numerator
+// erfc(x) + 2x/sqrt(pi) e^{-x^2} - g (x = alpha r) is left with the FP32
+// rounding of its terms divided by its own size (~ r^2/lambda^2).  Rewritten as
+//   (1 - g) + h(x),  h(x) = 2x/sqrt(pi) e^{-x^2} - erf(x) = x^3 H(x^2),
+// and the energy numerator erfc(x) - g as (1 - g) - erf(x), erf(x) = x E(x^2),
+// with Taylor series for 1 - e^{-y} (y = r^2/lambda^2 <= 1/4, six terms,
+// 5e-8 relative), h (eight terms, 1e-8 for x <= 1/2) and erf (eight terms,
+// 2e-11), every part keeps its relative accuracy.  Arguments y = r^2/lambda^2,
+// x = alpha r; returns r * (force numerator) and r * (energy numerator
+// without the sqrt(pi)/lambda erfc(r/lambda) term).
+__device__ __forceinline__ void kelbg_close(float y, float x, float &num_f, float &num_e) {
+    const float z = x * x;
+    const float one_m_g =
+        y * fmaf(fmaf(fmaf(fmaf(fmaf(-1.0f / 720.0f, y, 1.0f / 120.0f), y, -1.0f / 24.0f), y, 1.0f / 6.0f), y, -0.5f),
+                 y, 1.0f);
+    // coefficients of x^(2n+1), n = 1..8: (-1)^n (2/sqrt(pi)) 2n / ((2n+1) n!)
+    float hz = 2.63393830e-05f;
+    hz = fmaf(hz, z, -2.08959105e-04f);
+    hz = fmaf(hz, z, 1.44663996e-03f);
+    hz = fmaf(hz, z, -8.54832702e-03f);
+    hz = fmaf(hz, z, 4.17918210e-02f);
+    hz = fmaf(hz, z, -1.61197024e-01f);
+    hz = fmaf(hz, z, 4.51351667e-01f);
+    hz = fmaf(hz, z, -7.52252778e-01f);
+    num_f = fmaf(x * z, hz, one_m_g);
+    // erf(x) = 2/sqrt(pi) x sum_n (-1)^n z^n / (n! (2n+1)), n = 0..7
+    float ez = -1.32275132e-05f;
+    ez = fmaf(ez, z, 1.06837607e-04f);
+    ez = fmaf(ez, z, -7.57575758e-04f);
+    ez = fmaf(ez, z, 4.62962963e-03f);
+    ez = fmaf(ez, z, -2.38095238e-02f);
+    ez = fmaf(ez, z, 1.00000000e-01f);
+    ez = fmaf(ez, z, -3.33333333e-01f);
+    ez = fmaf(ez, z, 1.0f);
+    num_e = fmaf(-1.1283791671f * x, ez, one_m_g);
 }
 
 }  // namespace tcp

@@ -66,10 +66,18 @@ __device__ __forceinline__ float n3_pair(const PairConsts &c, float r2, bool ok,
         const bool near = ok && (r2s < c.u_rshort2);
         const float g = near ? ex2_approx(c.u_c_lam * r2s) : 0.0f;   // exp(-r^2/lambda^2)
         s = fmaf(-g, rinv, s);
+        float erfc_rl = 0.0f;
         if (ENERGY) {
             const float t2 = rcp_approx(fmaf(c.u_p_lam, r, 1.0f));
-            const float erfc_rl = g * erfc_poly(t2);      // erfc(r/lambda)
+            erfc_rl = g * erfc_poly(t2);                  // erfc(r/lambda)
             u += fmaf(c.u_sqrtpi_lam, erfc_rl, -g * rinv);
+        }
+        const bool close = near && (r2s < c.u_close2);
+        if (__any_sync(0xffffffffu, close) && close) {    // series form, kelbg_close
+            float nf, ne;
+            kelbg_close(r2s * c.u_inv_lam2, r * c.u_alpha, nf, ne);
+            s = nf * rinv;
+            if (ENERGY) u = fmaf(c.u_sqrtpi_lam, erfc_rl, ne * rinv);
         }
     }
     if (ENERGY) pe += u;
@@ -146,33 +154,25 @@ __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 
 // The coefficients as (c, c) pairs in constant memory, so the packed FMAs can
 // take them as 64-bit constant operands instead of register pairs.
-__constant__ float2 kErfcQ2[8] = {{6.807732388e-02f, 6.807732388e-02f},   {-3.663086635e-01f, -3.663086635e-01f},
-                                  {6.308091155e-01f, 6.308091155e-01f},   {-3.190751584e-01f, -3.190751584e-01f},
-                                  {3.760577549e-01f, 3.760577549e-01f},   {1.510029235e-01f, 1.510029235e-01f},
-                                  {2.343213173e-01f, 2.343213173e-01f},   {2.251152860e-01f, 2.251152860e-01f}};
+struct ErfcQ2Table {
+    float2 q[kErfcDeg + 1];
+};
+static constexpr ErfcQ2Table make_erfc_q2() {
+    constexpr float q_[kErfcDeg + 1] = TCP_ERFC_Q;
+    ErfcQ2Table t{};
+    for (int k = 0; k <= kErfcDeg; ++k) t.q[k] = float2{q_[k], q_[k]};
+    return t;
+}
+__constant__ ErfcQ2Table kErfcQ2 = make_erfc_q2();
 
 __device__ __forceinline__ float2 erfc_poly2(float2 t) {
-    float2 q = kErfcQ2[0];
+    float2 q = kErfcQ2.q[0];
 #pragma unroll
-    for (int k = 1; k < 8; ++k) q = __ffma2_rn(q, t, kErfcQ2[k]);
+    for (int k = 1; k <= kErfcDeg; ++k) q = __ffma2_rn(q, t, kErfcQ2.q[k]);
     return __fmul2_rn(q, t);
 }
 
-// Estrin's scheme for the same polynomial: 2 more operations, dependency
-// depth 4 instead of 8 (kErfcQ2[k] holds the coefficient of t^(7-k)).
-__device__ __forceinline__ float2 erfc_poly2_estrin(float2 t) {
-    const float2 t2 = __fmul2_rn(t, t);
-    const float2 t4 = __fmul2_rn(t2, t2);
-    const float2 a0 = __ffma2_rn(kErfcQ2[6], t, kErfcQ2[7]);
-    const float2 a1 = __ffma2_rn(kErfcQ2[4], t, kErfcQ2[5]);
-    const float2 a2 = __ffma2_rn(kErfcQ2[2], t, kErfcQ2[3]);
-    const float2 a3 = __ffma2_rn(kErfcQ2[0], t, kErfcQ2[1]);
-    const float2 b0 = __ffma2_rn(a1, t2, a0);
-    const float2 b1 = __ffma2_rn(a3, t2, a2);
-    return __fmul2_rn(__ffma2_rn(b1, t4, b0), t);
-}
-
-template <int KIND, bool ENERGY, bool MASKED, bool EST>
+template <int KIND, bool ENERGY, bool MASKED>
 __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, bool ok0, bool ok1, bool near_any,
                                              float2 &pe) {
     const float2 r2s = MASKED ? make_float2(ok0 ? r2.x : 1.0f, ok1 ? r2.y : 1.0f) : r2;
@@ -183,7 +183,7 @@ __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, boo
     const float2 t = make_float2(rcp_approx(ta.x), rcp_approx(ta.y));
     const float2 ea = __fmul2_rn(f2(c.u_c_exp), r2s);
     const float2 e = make_float2(ex2_approx(ea.x), ex2_approx(ea.y));
-    const float2 er = __fmul2_rn(__fmul2_rn(e, EST ? erfc_poly2_estrin(t) : erfc_poly2(t)), rinv_m);   // erfc(ar)/r
+    const float2 er = __fmul2_rn(__fmul2_rn(e, erfc_poly2(t)), rinv_m);   // erfc(ar)/r
     float2 s = __ffma2_rn(f2(c.u_c_gauss), e, er);
     float2 u = er;
     if (KIND == 1) {                                      // Deutsch, force.f90:136-139
@@ -198,11 +198,26 @@ __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, boo
         const float2 g = make_float2(n0 ? ex2_approx(ga.x) : 0.0f, n1 ? ex2_approx(ga.y) : 0.0f);
         const float2 nrinv = __fmul2_rn(rinv, f2(-1.0f));
         s = __ffma2_rn(g, nrinv, s);
+        float2 erfc_rl = f2(0.0f);
         if (ENERGY) {
             const float2 t2a = __ffma2_rn(f2(c.u_p_lam), r, f2(1.0f));
             const float2 t2 = make_float2(rcp_approx(t2a.x), rcp_approx(t2a.y));
-            const float2 erfc_rl = __fmul2_rn(g, EST ? erfc_poly2_estrin(t2) : erfc_poly2(t2));   // erfc(r/lambda)
+            erfc_rl = __fmul2_rn(g, erfc_poly2(t2));      // erfc(r/lambda)
             u = __fadd2_rn(u, __ffma2_rn(f2(c.u_sqrtpi_lam), erfc_rl, __fmul2_rn(g, nrinv)));
+        }
+        const bool c0 = n0 && (r2s.x < c.u_close2), c1 = n1 && (r2s.y < c.u_close2);
+        if (__any_sync(0xffffffffu, c0 || c1)) {          // series form, kelbg_close
+            float nf, ne;
+            if (c0) {
+                kelbg_close(r2s.x * c.u_inv_lam2, r.x * c.u_alpha, nf, ne);
+                s.x = nf * rinv.x;
+                if (ENERGY) u.x = fmaf(c.u_sqrtpi_lam, erfc_rl.x, ne * rinv.x);
+            }
+            if (c1) {
+                kelbg_close(r2s.y * c.u_inv_lam2, r.y * c.u_alpha, nf, ne);
+                s.y = nf * rinv.y;
+                if (ENERGY) u.y = fmaf(c.u_sqrtpi_lam, erfc_rl.y, ne * rinv.y);
+            }
         }
     }
     if (ENERGY) pe = __fadd2_rn(pe, u);
@@ -211,7 +226,7 @@ __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, boo
 
 __device__ __forceinline__ float idiff(int a, int b) { return (float)(int)((unsigned)a - (unsigned)b); }
 
-template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R, bool EST>
+template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R>
 __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__restrict__ tj, int cnt, int jstart,
                                            const int4 (&xi)[R], int ibase, int iend,
                                            float (*sjacc)[3], float (&p)[R][3], float &pe) {
@@ -251,7 +266,7 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
             if (KIND == 2) near_any = __any_sync(0xffffffffu, r2min < c.u_rshort2);
 #pragma unroll
             for (int g = 0; g < G; ++g) {
-                const float2 w = n3_pair_x2<KIND, ENERGY, MASKED, EST>(c, r2[g], ok[2 * g], ok[2 * g + 1], near_any, pe2);
+                const float2 w = n3_pair_x2<KIND, ENERGY, MASKED>(c, r2[g], ok[2 * g], ok[2 * g + 1], near_any, pe2);
                 pg[g][0] = __ffma2_rn(w, d[g][0], pg[g][0]);
                 pg[g][1] = __ffma2_rn(w, d[g][1], pg[g][1]);
                 pg[g][2] = __ffma2_rn(w, d[g][2], pg[g][2]);
@@ -285,8 +300,8 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
     pe = pe2.x + pe2.y;
 }
 
-// MODE 0: scalar FP32, i-force accumulators in registers; 1: packed FP32x2
-// (Horner erfc), accumulators in shared memory; 2: as 1 with Estrin's erfc.
+// MODE 0: scalar FP32, i-force accumulators in registers; 1: packed FP32x2,
+// accumulators in shared memory.
 // W: warps per CTA (i-tile = 32 R W particles).
 template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH, int MODE = 0, int W = kN3Warps>
 __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
@@ -409,7 +424,7 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
 #define TCP_N3_ITEM(KIND, MASKED)                                                                      \
     do {                                                                                                \
         if (X2)                                                                                         \
-            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R, MODE == 2>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe); \
+            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe); \
         else                                                                                            \
             n3_item<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe);    \
     } while (0)

@@ -38,6 +38,8 @@ struct PairConsts {
     float p_lam;               // P/lambda
     float sqrtpi_lam;          // sqrt(pi)/lambda
     float rshort2;             // (6 lambda)^2: Kelbg Gaussian terms below FP64 resolution beyond
+    float close2;              // Kelbg close pairs (series form, kelbg_close): min(lambda^2/4, 1/(4 alpha^2))
+    float inv_lam2f, alphaf;   // 1/lambda^2, alpha
     float inv_dx[3];           // RDF 1/dx per pair type ee|ei|ii
     float qqf[3];              // q_i q_j s^2 per pair type (energy/force sign and scale)
     // the same constants for cubic boxes in units of u = L/2^32 (the fixed-point
@@ -45,6 +47,7 @@ struct PairConsts {
     // (force) and q_i q_j / u (energy)
     int cubic;
     float u_rc2, u_p_alpha, u_c_exp, u_c_gauss, u_c_rs, u_inv_rs, u_c_lam, u_p_lam, u_sqrtpi_lam, u_rshort2;
+    float u_close2, u_inv_lam2, u_alpha;
     float u_inv_dx[3], u_qq_force[3], u_qq_energy[3];
     // FP64 path
     double box[3];

@@ -103,7 +103,8 @@ def mb_velocities(count: int, T: float, m: float, rng: np.random.Generator) -> n
     if count == 0:
         return np.zeros((0, 3))
     v = rng.normal(0.0, math.sqrt(T / m), size=(count, 3))
-    v -= v.mean(axis=0)
+    if count > 1:               # (a lone particle keeps its direction: removing the mean would stop it)
+        v -= v.mean(axis=0)
     T0 = m * np.sum(v * v) / (3.0 * count)
     return v * math.sqrt(T / T0)
 

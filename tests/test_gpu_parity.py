@@ -367,3 +367,31 @@ def test_deterministic_flag_is_bitwise_reproducible(precision):
         _, _, f2, _ = c.download(x=False, v=False, f=True)
     assert np.array_equal(f1, f2)
     assert e1["Ur"] == e2["Ur"] and e1["Um"] == e2["Um"]
+
+
+@pytest.mark.parametrize("variant", [0, 1, 6])
+@pytest.mark.parametrize("r_over_lam", [1e-3, 1e-2, 0.1, 0.3, 0.49, 0.8, 2.0])
+def test_kelbg_close_pair_accuracy(monkeypatch, variant, r_over_lam):
+    """One electron and one ion at r = (1e-3 .. 2) lambda: the Kelbg e-i force
+    and energy of the FP32C kernels (ordered, scalar and packed Newton-3)
+    against the FP64 oracle.  Below lambda/2 the force numerator
+    erfc(ar) + 2ar/sqrt(pi) e^{-a^2r^2} - e^{-r^2/lambda^2} is of order
+    r^2/lambda^2 while each term is of order 1; the series form keeps the
+    FP32 relative accuracy there."""
+    monkeypatch.setenv("TCP_PAIR_VARIANT", str(variant))
+    s = T.make_system(2, gamma=1.0, lam=0.5, seed=1, alpha_rc=3.1, K=8, order=4)
+    assert s.nel == 1 and s.nion == 1
+    lam = s.lambda_ei
+    u = np.array([0.48, -0.6, 0.64])
+    u /= np.linalg.norm(u)
+    x = np.zeros((2, 3))
+    x[1] = r_over_lam * lam * u
+    o = oracle.Oracle.from_system(s, ei="kelbg")
+    fo, uo = o.force_direct(x)
+    with T.Context(T.params_for(s, precision="fp32c", ei="kelbg", recip="none"), 1, 1) as c:
+        c.EWALD_SELF()
+        c.upload(x=x, v=np.zeros((2, 3)))
+        ur = c.Force_direct_self()
+        _, _, f, _ = c.download(x=False, v=False, f=True)
+    assert np.linalg.norm(f - fo) / np.linalg.norm(fo) < 2e-5
+    assert ur == pytest.approx(uo, rel=2e-5, abs=1e-6 * abs(uo) + 1e-12)
