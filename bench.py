@@ -244,6 +244,7 @@ def run_gpu(args, world, rank, local, dist):
     ctx.upload(x=s.x, v=s.v)
     e0 = ctx.force()                        # initial forces (restart-style start, main.f90:49-54)
     tune = ctx.autotune_report()
+    reserve, reserve_ms = ctx.overlap_report()
     _, _, f32, _ = ctx.download(x=False, v=False, f=True)
 
     ctx64 = T.Context(p64, s.nel, s.nion, device=local)
@@ -348,7 +349,8 @@ def run_gpu(args, world, rank, local, dist):
             "recipe": f"{recipe} FP32/ALU-pipe ops + {RECIPE_SFU_OPS} SFU ops per {runit}",
             "peak_source": "measured FFMA issue rate (tcp_fp32_peak) on this GPU, not MEASURED_PEAKS.json "
                            "(which has HBM and bf16 only)",
-            "sfu_frac": sfu_frac, "pair_kernel_ms": pair_ms}
+            "sfu_frac": sfu_frac, "pair_kernel_ms": pair_ms,
+            "grid_reserve": reserve, "reserve_ms": reserve_ms}
 
     # CPU baseline (rank 0, N = 1 only) and the FP32C force error vs the oracle
     cpu = None

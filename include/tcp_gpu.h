@@ -282,6 +282,12 @@ int tcp_time_steps(tcp_ctx *ctx, double dt, int nsteps, int flush_l2, double *ou
  * ordered pairs, >= 1 = Newton-3 variants) and the per-candidate times in ms
  * (ms[k] for variant k, 0 when not timed), up to nmax entries. */
 int tcp_autotune_report(tcp_ctx *ctx, int *variant, double *ms, int nmax);
+/* The number of CTAs the autotuner left out of the persistent Newton-3 grid
+ * so that the reciprocal chain, which runs beside the pair kernel in a step,
+ * finds room on the SMs; the candidates and the time of the pair kernel with
+ * the chain beside it for each (ms, 0 when not timed), up to nmax entries.
+ * TCP_PAIR_RESERVE=k forces k. */
+int tcp_overlap_report(tcp_ctx *ctx, int *reserve, int *candidates, double *ms, int nmax);
 /* Kernel launches issued by the context so far (all kernels of this library). */
 int tcp_launch_count(tcp_ctx *ctx, long long *count);
 /* Measured FP32 FFMA issue rate of the device: a calibration kernel of

@@ -218,6 +218,16 @@ class Context:
                   "tcp_autotune_report")
         return v.value, ms
 
+    def overlap_report(self):
+        """(CTAs left out of the Newton-3 grid, {candidate: ms of the pair kernel with the
+        reciprocal chain beside it})."""
+        r = C.c_int()
+        cand = np.zeros(8, dtype=np.int32)
+        ms = np.zeros(8)
+        self._chk(self.lib.tcp_overlap_report(self.h, C.byref(r), cand.ctypes.data_as(C.POINTER(C.c_int)),
+                                              ms.ctypes.data_as(C.POINTER(C.c_double)), 8), "tcp_overlap_report")
+        return r.value, {int(k): float(t) for k, t in zip(cand, ms) if t > 0}
+
     def launch_count(self):
         n = C.c_longlong()
         self._chk(self.lib.tcp_launch_count(self.h, C.byref(n)), "tcp_launch_count")

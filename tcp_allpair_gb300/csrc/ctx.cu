@@ -118,13 +118,43 @@ static int recip_fork(tcp_ctx *c) {
     c->rstream = c->stream2;
     const int rc = recip_launch(c);
     c->rstream = c->stream;
+    c->recip_beside = rc == TCP_OK;
     return rc;
 }
 
 static int recip_join(tcp_ctx *c) {
+    c->recip_beside = false;
     if (c->p.reciprocal == TCP_RECIP_NONE) return TCP_OK;
     TCP_CUDA(cudaEventRecord(c->ev_join, c->stream2));
     TCP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+    return TCP_OK;
+}
+
+// Mean time of the real-space launch with the reciprocal chain beside it on
+// stream2, as inside a step (the autotuner's measure for the grid reserve).
+int time_pair_with_recip(tcp_ctx *c, int reps, double *ms) {
+    cudaEvent_t e0, e1;
+    TCP_CUDA(cudaEventCreate(&e0));
+    TCP_CUDA(cudaEventCreate(&e1));
+    int rc = TCP_OK;
+    auto once = [&]() -> int {
+        int r = recip_fork(c);
+        if (!r) r = launch_pair(c, energy_on(c), false);
+        if (int j = recip_join(c)) return j;
+        return r;
+    };
+    rc = once();
+    cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < reps && !rc; ++r) rc = once();
+    cudaEventRecord(e1, c->stream);
+    cudaEventSynchronize(e1);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / std::max(reps, 1);
+    if (rc) return rc;
+    TCP_CUDA(cudaGetLastError());
     return TCP_OK;
 }
 

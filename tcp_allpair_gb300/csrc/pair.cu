@@ -905,9 +905,9 @@ static int cache_lookup(const char *path, const std::string &key) {
     return v;
 }
 
-int autotune_pair(tcp_ctx *c) {
-    if (c->p.precision != TCP_PREC_FP32C || c->tuned) return TCP_OK;
-    c->tuned = true;
+// Real-space kernel of an FP32C context: the variant with the shortest
+// pair-kernel time (TCP_PAIR_VARIANT forces one).
+static int choose_variant(tcp_ctx *c, const char *cache, const std::string &key) {
     const int nv = c->pc.cubic ? std::min(n3_variant_count(), 15) : 0;
     c->pair_variant = c->pc.cubic ? 1 : 0;
     if (const char *forced = getenv("TCP_PAIR_VARIANT")) {
@@ -916,8 +916,6 @@ int autotune_pair(tcp_ctx *c) {
     }
     if (const char *off = getenv("TCP_AUTOTUNE"))
         if (atoi(off) == 0) return TCP_OK;
-    const char *cache = getenv("TCP_AUTOTUNE_CACHE");
-    const std::string key = tune_key(c);
     if (cache) {
         const int v = cache_lookup(cache, key);
         if (v >= 0 && v <= nv) {
@@ -958,6 +956,65 @@ int autotune_pair(tcp_ctx *c) {
             fclose(f);
         }
     }
+    return TCP_OK;
+}
+
+// CTAs left out of the persistent Newton-3 grid.  In a step the reciprocal
+// chain runs on a second stream beside the pair kernel; with every SM holding
+// its full share of pair CTAs, the chain's kernels (cuFFT's among them) find no
+// registers free and wait for the pair kernel's tail.  Each candidate is timed
+// as the pair kernel with the chain beside it (TCP_PAIR_RESERVE forces one).
+static constexpr int kReserveCandidates[] = {0, 8, 16, 32, 64};
+static int choose_reserve(tcp_ctx *c, const char *cache, const std::string &key) {
+    c->pair_reserve = 0;
+    if (const char *forced = getenv("TCP_PAIR_RESERVE")) {
+        c->pair_reserve = std::max(atoi(forced), 0);
+        return TCP_OK;
+    }
+    if (c->p.reciprocal == TCP_RECIP_NONE || !n3_applicable(c)) return TCP_OK;
+    if (const char *off = getenv("TCP_AUTOTUNE"))
+        if (atoi(off) == 0) return TCP_OK;
+    const std::string rkey = key + " reserve";
+    if (cache) {
+        const int r = cache_lookup(cache, rkey);
+        if (r >= 0) {
+            c->pair_reserve = r;
+            return TCP_OK;
+        }
+    }
+    double best = 1e300;
+    int best_r = 0, k = 0;
+    for (const int r : kReserveCandidates) {
+        c->pair_reserve = r;
+        double ms = 0.0;
+        const long long before = c->launches;
+        const int rc = time_pair_with_recip(c, 2, &ms);
+        c->launches = before;
+        if (rc) return rc;
+        c->pair_reserve_ms[k++] = ms;
+        if (ms < best) {
+            best = ms;
+            best_r = r;
+        }
+    }
+    c->pair_reserve = best_r;
+    if (cache) {
+        if (FILE *f = fopen(cache, "a")) {
+            fprintf(f, "%s %d\n", rkey.c_str(), best_r);
+            fclose(f);
+        }
+    }
+    return TCP_OK;
+}
+
+int autotune_pair(tcp_ctx *c) {
+    if (c->p.precision != TCP_PREC_FP32C || c->tuned) return TCP_OK;
+    c->tuned = true;
+    const char *cache = getenv("TCP_AUTOTUNE_CACHE");
+    const std::string key = tune_key(c);
+    int rc = choose_variant(c, cache, key);
+    if (!rc) rc = choose_reserve(c, cache, key);
+    if (rc) return rc;
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;
 }
@@ -969,5 +1026,17 @@ extern "C" int tcp_autotune_report(tcp_ctx *c, int *variant, double *ms, int nma
     if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
     if (variant) *variant = c->pair_variant;
     for (int k = 0; ms && k < nmax && k < 16; ++k) ms[k] = c->pair_variant_ms[k];
+    return TCP_OK;
+}
+
+extern "C" int tcp_overlap_report(tcp_ctx *c, int *reserve, int *candidates, double *ms, int nmax) {
+    using namespace tcp;
+    if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
+    if (reserve) *reserve = c->pair_reserve;
+    constexpr int nc = (int)(sizeof kReserveCandidates / sizeof kReserveCandidates[0]);
+    for (int k = 0; k < nmax && k < nc; ++k) {
+        if (candidates) candidates[k] = kReserveCandidates[k];
+        if (ms) ms[k] = c->pair_reserve_ms[k];
+    }
     return TCP_OK;
 }

@@ -226,10 +226,13 @@ __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, boo
 
 __device__ __forceinline__ float idiff(int a, int b) { return (float)(int)((unsigned)a - (unsigned)b); }
 
-template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R>
+// LDSJ: j positions read from a warp-private copy of the chunk written twice
+// in a row (jb[64]), so that step s reads jb[lane + s] with one shared load
+// instead of rotating them with three shuffles; the reactions still rotate.
+template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R, bool LDSJ = false>
 __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__restrict__ tj, int cnt, int jstart,
                                            const int4 (&xi)[R], int ibase, int iend,
-                                           float (*sjacc)[3], float (&p)[R][3], float &pe) {
+                                           float (*sjacc)[3], float (&p)[R][3], float &pe, int4 *jb = nullptr) {
     static_assert(R % 2 == 0, "paired form needs an even number of i-particles per lane");
     constexpr int G = R / 2;
     const int lane = threadIdx.x & 31;
@@ -240,9 +243,16 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
     for (int g = 0; g < G; ++g) pg[g][0] = pg[g][1] = pg[g][2] = f2(0.0f);
     for (int ch = 0; ch * 32 < cnt; ++ch) {
         int4 xj = tj[ch * 32 + lane];
+        if (LDSJ) {
+            __syncwarp();                // the previous chunk's reads of jb are done
+            jb[lane] = xj;
+            jb[lane + 32] = xj;
+            __syncwarp();
+        }
         float2 jx = f2(0.0f), jy = f2(0.0f), jz = f2(0.0f);
 #pragma unroll UNROLL
         for (int s = 0; s < 32; ++s) {
+            if (LDSJ) xj = jb[lane + s];
             float2 d[G][3], r2[G];
             bool ok[R];
             float r2min = 3.0e38f;
@@ -275,9 +285,11 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
                 jz = __ffma2_rn(w, d[g][2], jz);
             }
             // rotate j (position and both halves of the reaction) to the next lane
-            xj.x = __shfl_sync(0xffffffffu, xj.x, src);
-            xj.y = __shfl_sync(0xffffffffu, xj.y, src);
-            xj.z = __shfl_sync(0xffffffffu, xj.z, src);
+            if (!LDSJ) {
+                xj.x = __shfl_sync(0xffffffffu, xj.x, src);
+                xj.y = __shfl_sync(0xffffffffu, xj.y, src);
+                xj.z = __shfl_sync(0xffffffffu, xj.z, src);
+            }
             jx.x = __shfl_sync(0xffffffffu, jx.x, src);
             jx.y = __shfl_sync(0xffffffffu, jx.y, src);
             jy.x = __shfl_sync(0xffffffffu, jy.x, src);
@@ -301,7 +313,8 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
 }
 
 // MODE 0: scalar FP32, i-force accumulators in registers; 1: packed FP32x2,
-// accumulators in shared memory.
+// accumulators in shared memory; 2: as 1 with j positions read from shared
+// memory (LDSJ).
 // W: warps per CTA (i-tile = 32 R W particles).
 template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH, int MODE = 0, int W = kN3Warps>
 __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
@@ -320,6 +333,7 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
     // in shared memory ([slot][thread], conflict-free) for the packed forms,
     // whose constant pairs need the registers
     __shared__ float sacc[SACC ? 2 * 3 * R : 1][SACC ? NT : 1];
+    __shared__ __align__(16) int4 jbuf[MODE == 2 ? W : 1][MODE == 2 ? 64 : 1];
     float hi[SACC ? 1 : R][3], lo[SACC ? 1 : R][3];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -424,7 +438,7 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
 #define TCP_N3_ITEM(KIND, MASKED)                                                                      \
     do {                                                                                                \
         if (X2)                                                                                         \
-            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe); \
+            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R, MODE == 2>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe, jbuf[MODE == 2 ? warp : 0]); \
         else                                                                                            \
             n3_item<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe);    \
     } while (0)
@@ -541,6 +555,8 @@ static const N3Variant kVariants[] = {
     {pair_n3_kernel<true, 2, 2, 3, false, 1>, pair_n3_kernel<false, 2, 2, 3, false, 1>, 2, 8, "n3_r2_u2_b3_x2"},
     {pair_n3_kernel<true, 4, 1, 5, false, 1, 4>, pair_n3_kernel<false, 4, 1, 5, false, 1, 4>, 4, 4, "n3_r4_u1_w4b5_x2"},
     {pair_n3_kernel<true, 4, 1, 3, false, 1>, pair_n3_kernel<false, 4, 1, 3, false, 1>, 4, 8, "n3_r4_u1_b3_x2"},
+    {pair_n3_kernel<true, 4, 1, 2, false, 2>, pair_n3_kernel<false, 4, 1, 2, false, 2>, 4, 8, "n3_r4_u1_b2_x2l"},
+    {pair_n3_kernel<true, 4, 1, 3, false, 2>, pair_n3_kernel<false, 4, 1, 3, false, 2>, 4, 8, "n3_r4_u1_b3_x2l"},
 };
 constexpr int kN3Variants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -595,7 +611,9 @@ int launch_pair_n3(tcp_ctx *c, bool energy) {
     a.counter = c->counter;
     a.c = c->pc;
     a.inject_skip = inject_fault("tile_wait") ? 1 : 0;
-    const int grid = (int)std::min<long long>(n3_grid_for(c, v), total);
+    // CTAs left free for the reciprocal chain when it runs beside this launch
+    const int reserve = c->recip_beside ? c->pair_reserve : 0;
+    const int grid = (int)std::min<long long>(std::max(1, n3_grid_for(c, v) - reserve), total);
     if (grid > c->n_upart) return set_error(TCP_ERR_STATE, "energy partial buffer smaller than the Newton-3 grid");
     TCP_CUDA(cudaMemsetAsync(c->fpart, 0, sizeof(double) * 3 * (size_t)c->n, c->stream));
     TCP_CUDA(cudaMemsetAsync(c->counter, 0, sizeof(unsigned), c->stream));
@@ -623,6 +641,8 @@ static const N3BatchVariant kBatchVariants[] = {
     {pair_n3_kernel<true, 4, 1, 2, true, 1>, pair_n3_kernel<false, 4, 1, 2, true, 1>, 4, 8, "b_r4_u1_b2_x2"},
     {pair_n3_kernel<true, 2, 2, 3, true, 1>, pair_n3_kernel<false, 2, 2, 3, true, 1>, 2, 8, "b_r2_u2_b3_x2"},
     {pair_n3_kernel<true, 4, 1, 3, true, 1>, pair_n3_kernel<false, 4, 1, 3, true, 1>, 4, 8, "b_r4_u1_b3_x2"},
+    {pair_n3_kernel<true, 4, 1, 3, true, 2>, pair_n3_kernel<false, 4, 1, 3, true, 2>, 4, 8, "b_r4_u1_b3_x2l"},
+    {pair_n3_kernel<true, 2, 2, 3, true, 2>, pair_n3_kernel<false, 2, 2, 3, true, 2>, 2, 8, "b_r2_u2_b3_x2l"},
 };
 constexpr int kN3BatchVariants = sizeof(kBatchVariants) / sizeof(kBatchVariants[0]);
 

@@ -94,6 +94,12 @@ struct tcp_ctx {
     int pair_variant = 1;      // FP32C real-space kernel: 0 ordered pairs, >= 1 Newton-3 variant
     bool tuned = false;        // autotuner ran for the current parameters
     double pair_variant_ms[16] = {};   // autotuner timings per variant
+    // CTAs of the persistent Newton-3 grid left free so that the reciprocal
+    // chain, which runs beside the pair kernel in a step, finds room on the
+    // SMs (chosen by the autotuner from kReserveCandidates)
+    int pair_reserve = 0;
+    double pair_reserve_ms[8] = {};
+    bool recip_beside = false;          // the reciprocal chain is running on stream2
     double *fpart = nullptr;   // [jsplit][3][n]
     double *upart = nullptr;   // energy partial per pair block
     int n_upart = 0;
@@ -208,6 +214,7 @@ int n3_grid(const tcp_ctx *c);
 int n3_variant_count();
 const char *n3_variant_name(int v);
 int autotune_pair(tcp_ctx *c);
+int time_pair_with_recip(tcp_ctx *c, int reps, double *ms);   // ctx.cu
 int launch_pair_n3(tcp_ctx *c, bool energy);
 int n3_batch_variant_count();
 const char *n3_batch_variant_name(int v);

@@ -66,3 +66,24 @@ def test_batch_rejects_unsupported():
     p = T.params_for(s, precision="fp64", recip="spme")
     with pytest.raises(T.TcpError):
         T.Batch([p], [s.nel], [s.nion])
+
+
+@pytest.mark.parametrize("variant", list(range(6)))
+def test_batch_pair_variants_match_oracle(monkeypatch, variant):
+    """Every batched real-space variant (TCP_BATCH_VARIANT) against the oracle's
+    total force and the energies."""
+    monkeypatch.setenv("TCP_BATCH_VARIANT", str(variant))
+    ss = systems()[:3]
+    params = [T.params_for(s, precision="fp32c", ei="kelbg", recip="spme") for s in ss]
+    with T.Batch(params, [s.nel for s in ss], [s.nion for s in ss]) as b:
+        b.EWALD_SELF()
+        for r, s in enumerate(ss):
+            b.upload(r, x=s.x, v=s.v)
+        eb = b.force()
+        chosen, _ = b.autotune_report()
+        fb = [b.download(r, x=False, v=False)[2] for r in range(len(ss))]
+    assert chosen == variant
+    for r, s in enumerate(ss):
+        fo, uro, umo = oracle.Oracle.from_system(s, ei="kelbg").force_total(s.x)
+        assert oracle.rms_rel(fb[r], fo) < 2e-6
+        assert eb[r]["Ur"] == pytest.approx(uro, rel=2e-5)

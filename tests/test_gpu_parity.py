@@ -265,7 +265,7 @@ def test_large_fp32c_rows_sample():
     assert np.linalg.norm(f.sum(0)) < 1e-6 * np.abs(f).sum()
 
 
-@pytest.mark.parametrize("variant", list(range(10)))
+@pytest.mark.parametrize("variant", list(range(12)))
 @pytest.mark.parametrize("ei,n", [("kelbg", 2048), ("deutsch", 1536), ("kelbg", 1000)])
 def test_fp32c_kernel_variants(monkeypatch, variant, ei, n):
     """Every real-space kernel the autotuner can pick (0 = ordered pairs,
@@ -289,8 +289,32 @@ def test_autotuner_picks_a_timed_variant(monkeypatch):
     with ctx_for(s, precision="fp32c", ei="kelbg", recip="none") as c:
         c.Force_direct_self()
         v, ms = c.autotune_report()
-    assert 0 <= v <= 9
+    assert 0 <= v <= 11
     assert ms[v] > 0 and ms[v] == min(m for m in ms if m > 0)
+
+
+def test_grid_reserve_for_the_overlapped_reciprocal_chain(monkeypatch):
+    """With SPME the autotuner also times the pair kernel with the reciprocal
+    chain beside it for a few grid reserves and keeps the fastest;
+    TCP_PAIR_RESERVE forces one, and the forces do not depend on it."""
+    monkeypatch.delenv("TCP_PAIR_VARIANT", raising=False)
+    monkeypatch.delenv("TCP_PAIR_RESERVE", raising=False)
+    s = make(8192, seed=41, K=32, order=5)
+    with ctx_for(s, precision="fp32c", ei="kelbg", recip="spme") as c:
+        c.force()
+        r, cand = c.overlap_report()
+    assert set(cand) == {0, 8, 16, 32, 64}
+    assert r in cand and cand[r] == min(cand.values())
+    forces = []
+    for forced in ("0", "40"):
+        monkeypatch.setenv("TCP_PAIR_RESERVE", forced)
+        with ctx_for(s, precision="fp32c", ei="kelbg", recip="spme") as c:
+            e = c.force()
+            _, _, f, _ = c.download(x=False, v=False, f=True)
+            assert c.overlap_report() == (int(forced), {})
+        forces.append((f, e["Ur"]))
+    assert oracle.rms_rel(forces[1][0], forces[0][0]) < 1e-6
+    assert forces[1][1] == pytest.approx(forces[0][1], rel=1e-6)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32c"])
