@@ -18,7 +18,11 @@
 // warp takes the subtile in chunks of 32: lane l loads j = l, and for 32
 // steps computes the R pairs (i_r, j) and rotates j's position and reaction
 // accumulator to the next lane with shuffles, so after 32 steps every lane
-// holds the reaction of its own j again.  Reactions are summed over the
+// holds the reaction of its own j again (the LDSJ variants read j's position
+// from a warp-private doubled copy of the chunk instead of rotating it).
+// The autotuner picks the variant; with a reciprocal sum running beside the
+// launch, c->pair_reserve CTAs may be left out of the persistent grid.
+// Reactions are summed over the
 // warps in shared memory and added to the global FP64 force with one atomic
 // per j and component per item; i-forces are folded per item into TwoSum
 // (hi, lo) accumulators and added with atomics when the CTA leaves the row.
@@ -26,8 +30,9 @@
 // mask i < j; all others run unmasked except for the cut-off.
 //
 // Pair arithmetic is that of pair_fp32c_kernel (fixed-point differences in
-// units of L/2^32, SFU rsqrt/rcp/ex2, erfc = exp(-x^2) t Q(t)).  Cubic boxes
-// only; other boxes use the ordered-pair kernel.
+// units of L/2^32, SFU rsqrt/rcp/ex2, erfc = exp(-x^2) t Q(t), the series
+// form of kelbg_close for close Kelbg pairs).  Cubic boxes only; other boxes
+// use the ordered-pair kernel.
 #include <algorithm>
 #include <cstring>
 
