@@ -172,7 +172,14 @@ __global__ void __launch_bounds__(kAdjThreads) adj_pair_kernel(const AdjArgs a) 
             T G1, G2, dl, gl;
             if (F32) {
                 float g1, g2, d, g;
-                if (type == 1 && EIK == 1) radial_f32<1>(a, (float)r2, g1, g2, d, g);
+                if (type == 1 && EIK == 2 && (float)r2 < a.c.close2) {
+                    // close Kelbg pairs: the FP32 terms of G1, G2 cancel to order
+                    // r^2/lambda^2 (the force kernels use the series of kelbg_close);
+                    // these rare pairs take the FP64 radial functions
+                    double h1, h2, hd, hg;
+                    radial_f64<2>(a, (double)r2, h1, h2, hd, hg);
+                    g1 = (float)h1; g2 = (float)h2; d = (float)hd; g = (float)hg;
+                } else if (type == 1 && EIK == 1) radial_f32<1>(a, (float)r2, g1, g2, d, g);
                 else if (type == 1 && EIK == 2) radial_f32<2>(a, (float)r2, g1, g2, d, g);
                 else radial_f32<0>(a, (float)r2, g1, g2, d, g);
                 G1 = g1; G2 = g2; dl = d; gl = g;

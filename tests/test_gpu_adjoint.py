@@ -219,3 +219,22 @@ def test_reverse_md_rejects_thermostat():
     with ctx_for(s, precision="fp64", thermo="isokin") as c:
         with pytest.raises(T.TcpError):
             c.reverse_md(s.dt, 4, 2)
+
+
+@pytest.mark.parametrize("r_over_lam", [1e-2, 0.1, 0.3, 1.0])
+def test_hvp_fp32c_close_kelbg_pair(r_over_lam):
+    """One electron and one ion at r = (0.01 .. 1) lambda: the FP32C
+    Hessian-vector product and dF/dlambda.w against the oracle (close pairs
+    take the FP64 radial functions; their FP32 form cancels to r^2/lambda^2)."""
+    s = T.make_system(2, gamma=1.0, lam=0.5, seed=1, alpha_rc=3.1, K=8, order=4)
+    u = np.array([0.48, -0.6, 0.64])
+    x = np.zeros((2, 3))
+    x[1] = r_over_lam * s.lambda_ei * u / np.linalg.norm(u)
+    w = np.array([[0.3, -0.2, 0.9], [-0.5, 0.4, 0.1]])
+    hw_o, dfl_o = oracle.Oracle.from_system(s, ei="kelbg").hvp(x, w, recip="none")
+    with T.Context(T.params_for(s, precision="fp32c", ei="kelbg", recip="none"), 1, 1) as c:
+        c.EWALD_SELF()
+        c.upload(x=x, v=np.zeros((2, 3)))
+        hw, dfl = c.hvp(w)
+    assert oracle.rms_rel(hw, hw_o) < 2e-5
+    assert dfl == pytest.approx(dfl_o, rel=2e-5)
