@@ -313,9 +313,12 @@ __global__ void spme_influence_kernel(cufftDoubleComplex *__restrict__ Qk, const
 // mode: FP32 mesh and weights, the per-particle sum in FP32, force in FP64).
 template <int P, typename T>
 __global__ void spme_gather_kernel(const SpmeArgs a, const T *__restrict__ phi, double coef,
-                                   double *__restrict__ frec) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= a.n) return;
+                                   double *__restrict__ frec, const int *__restrict__ order) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n) return;
+    // particles in the cell-sort order of the spread: the lanes of a warp share
+    // their (y, z) mesh columns, so their mesh rows are read together
+    const int m = order ? order[t] : t;
     const double q = m < a.nel ? a.q0 : a.q1;
     const double L[3] = {a.box0, a.box1, a.box2};
     const int K[3] = {a.K1, a.K2, a.K3};
@@ -325,27 +328,31 @@ __global__ void spme_gather_kernel(const SpmeArgs a, const T *__restrict__ phi, 
     for (int d = 0; d < 3; ++d) {
         const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];
         spline_w<P, T>(u, W[d], dW[d]);
-        base[d] = (int)trunc(u) - (P - 3);
+        base[d] = wrapi((int)trunc(u) - (P - 3), K[d]);    // first mesh index, wrapped once
     }
     T gx = 0, gy = 0, gz = 0;
+    int iz = base[2];
 #pragma unroll 1
     for (int k = 0; k < P; ++k) {
-        const int iz = wrapi(base[2] + k, a.K3);
+        int iy = base[1];
 #pragma unroll 1
         for (int j = 0; j < P; ++j) {
-            const int iy = wrapi(base[1] + j, a.K2);
             const T *row = phi + (size_t)a.K1 * (iy + (size_t)a.K2 * iz);
             T sx = 0, sd = 0;
+            int ix = base[0];
 #pragma unroll
             for (int i = 0; i < P; ++i) {
-                const T ph = row[wrapi(base[0] + i, a.K1)];
+                const T ph = row[ix];
                 sx += dW[0][i] * ph;
                 sd += W[0][i] * ph;
+                ix = ix + 1 == a.K1 ? 0 : ix + 1;
             }
             gx += sx * W[1][j] * W[2][k];
             gy += sd * dW[1][j] * W[2][k];
             gz += sd * W[1][j] * dW[2][k];
+            iy = iy + 1 == a.K2 ? 0 : iy + 1;
         }
+        iz = iz + 1 == a.K3 ? 0 : iz + 1;
     }
     // F = -eps/(pi V) q (K_d/L_d) sum dW W W phi
     frec[m] = -coef * q * (double)gx * ((double)a.K1 / a.box0);
@@ -353,25 +360,33 @@ __global__ void spme_gather_kernel(const SpmeArgs a, const T *__restrict__ phi, 
     frec[2 * (size_t)a.n + m] = -coef * q * (double)gz * ((double)a.K3 / a.box2);
 }
 
-// FP32C influence multiply; the energy sum is kept in FP64
-__global__ void spme_influence_f_kernel(cufftComplex *__restrict__ Qk, const float *__restrict__ infl, long total,
+// FP32C influence multiply.  Energy terms are summed in FP32 per thread (a
+// few elements each) and in FP64 across threads and blocks.  The half-spectrum
+// column kx of element idx advances by the grid stride modulo Kh, so no
+// division runs per element.
+__global__ void spme_influence_f_kernel(cufftComplex *__restrict__ Qk, const float *__restrict__ infl, int total,
                                         int Kh, int K1, double *__restrict__ epart, bool energy) {
     __shared__ double red[32];
-    double e = 0.0;
-    for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+    float e = 0.0f;
+    const int stride = gridDim.x * blockDim.x;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    int kx = idx % Kh;
+    const int dkx = stride % Kh;
+    for (; idx < total; idx += stride) {
         const float g = infl[idx];
         cufftComplex z = Qk[idx];
         if (energy) {
-            const int kx = (int)(idx % Kh);
-            const double wgt = (kx == 0 || (2 * kx == K1)) ? 1.0 : 2.0;
-            e += wgt * (double)g * ((double)z.x * z.x + (double)z.y * z.y);
+            const float wgt = (kx == 0 || (2 * kx == K1)) ? 1.0f : 2.0f;
+            e = fmaf(wgt * g, fmaf(z.x, z.x, z.y * z.y), e);
         }
         z.x *= g;
         z.y *= g;
         Qk[idx] = z;
+        kx += dkx;
+        if (kx >= Kh) kx -= Kh;
     }
     if (energy) {
-        const double t = block_sum(e, red);
+        const double t = block_sum((double)e, red);
         if (threadIdx.x == 0) epart[blockIdx.x] = t;
     }
 }
@@ -493,9 +508,11 @@ int spme_free(tcp_ctx *c) {
     return TCP_OK;
 }
 
+// blocks of 256 threads for the influence multiply: about four elements per
+// thread, at most 4096 blocks (the size of the energy partial array)
 static int spme_energy_blocks(const tcp_ctx *c) {
     const long total = (long)c->K3 * c->K2 * c->Kh;
-    return (int)std::min<long>((total + 255) / 256, 4096);
+    return (int)std::max<long>(1, std::min<long>((total + 1023) / 1024, 4096));
 }
 
 static int prepare_cell_spread(tcp_ctx *c);
@@ -683,10 +700,11 @@ static int cell_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Qf) {
 template <int P>
 static void launch_gather(tcp_ctx *c, const SpmeArgs &a, double coef) {
     const int threads = 128, blocks = (c->n + threads - 1) / threads;
+    const int *order = c->bin_list;      // the spread of this chain sorted the particles
     if (c->spme_fp32)
-        spme_gather_kernel<P, float><<<blocks, threads, 0, c->rstream>>>(a, c->Qf, coef, c->frec);
+        spme_gather_kernel<P, float><<<blocks, threads, 0, c->rstream>>>(a, c->Qf, coef, c->frec, order);
     else
-        spme_gather_kernel<P, double><<<blocks, threads, 0, c->rstream>>>(a, c->Q, coef, c->frec);
+        spme_gather_kernel<P, double><<<blocks, threads, 0, c->rstream>>>(a, c->Q, coef, c->frec, order);
 }
 
 static void gather(tcp_ctx *c, const SpmeArgs &a, double coef) {
@@ -714,7 +732,7 @@ int launch_spme(tcp_ctx *c, bool energy) {
     cufftSetStream(c->plan_b, c->rstream);
     if (c->spme_fp32) {
         if (cufftExecR2C(c->plan_f, c->Qf, c->Qkf) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecR2C failed");
-        spme_influence_f_kernel<<<eb, 256, 0, c->rstream>>>(c->Qkf, c->infl_f, total, c->Kh, c->K1, epart, energy);
+        spme_influence_f_kernel<<<eb, 256, 0, c->rstream>>>(c->Qkf, c->infl_f, (int)total, c->Kh, c->K1, epart, energy);
         c->launches++;
         if (cufftExecC2R(c->plan_b, c->Qkf, c->Qf) != CUFFT_SUCCESS) return set_error(TCP_ERR_CUFFT, "cufftExecC2R failed");
     } else {
