@@ -451,6 +451,7 @@ def run_batch(args):
         for r, s in enumerate(ss):
             b.upload(r, x=s.x, v=s.v)
         b.force()
+        bvar, bms = b.autotune_report()
         b.md_steps(dt, args.warmup)
         ms_batch = b.time_steps(dt, args.steps)
     # looping single-system contexts (each its own graph), same steps
@@ -475,7 +476,8 @@ def run_batch(args):
            "value": pairs / (ms_batch * 1e-3), "unit": "pair-int/s", "ms_per_step": ms_batch,
            "loop_single_contexts": {"value": pairs / (ms_loop * 1e-3), "ms_per_step": ms_loop},
            "speedup_batch_over_loop": ms_loop / ms_batch, "replicas": len(ss),
-           "particles": sum(s.n for s in ss), "steps": args.steps, "warmup": args.warmup}
+           "particles": sum(s.n for s in ss), "steps": args.steps, "warmup": args.warmup,
+           "batch_variant": int(bvar), "batch_variant_ms": [round(float(x), 4) for x in bms if x > 0]}
     print(json.dumps(out))
     return 0
 

@@ -256,26 +256,36 @@ __global__ void b_influence_kernel(cufftComplex *__restrict__ Qk, const float *_
     }
     const BRep &R = reps[lo];
     const int nb = blk0[lo + 1] - blk0[lo], lb = blockIdx.x - blk0[lo];
-    const long total = (long)R.K[2] * R.K[1] * R.Kh;
-    double e = 0.0;
-    for (long idx = (long)lb * blockDim.x + threadIdx.x; idx < total; idx += (long)nb * blockDim.x) {
+    const int total = R.K[2] * R.K[1] * R.Kh;
+    // energy terms in FP32 per thread, FP64 across threads; the half-spectrum
+    // column advances by the stride modulo Kh (no division per element)
+    float e = 0.0f;
+    const int stride = nb * blockDim.x;
+    int idx = lb * blockDim.x + threadIdx.x;
+    int kx = idx % R.Kh;
+    const int dkx = stride % R.Kh;
+    for (; idx < total; idx += stride) {
         const float g = infl[R.half_off + idx];
         cufftComplex z = Qk[R.half_off + idx];
-        const int kx = (int)(idx % R.Kh);
-        const double wgt = (kx == 0 || (2 * kx == R.K[0])) ? 1.0 : 2.0;
-        e += wgt * (double)g * ((double)z.x * z.x + (double)z.y * z.y);
+        const float wgt = (kx == 0 || (2 * kx == R.K[0])) ? 1.0f : 2.0f;
+        e = fmaf(wgt * g, fmaf(z.x, z.x, z.y * z.y), e);
         z.x *= g;
         z.y *= g;
         Qk[R.half_off + idx] = z;
+        kx += dkx;
+        if (kx >= R.Kh) kx -= R.Kh;
     }
-    const double t = block_sum(e, red);
+    const double t = block_sum((double)e, red);
     if (threadIdx.x == 0) atomicAdd(&um[lo], t * kEps / (2.0 * kPi * R.V));
 }
 
+// Particles in the cell-sort order of the spread (order[t]): the lanes of a
+// warp share replicas and mesh columns; mesh indices wrap by comparison.
 template <int P>
-__global__ void b_gather_kernel(const BParticles a, const float *__restrict__ phi) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.ntot) return;
+__global__ void b_gather_kernel(const BParticles a, const float *__restrict__ phi, const int *__restrict__ order) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.ntot) return;
+    const int i = order[t];
     const BRep &R = a.reps[a.rep_of[i]];
     const double q = (i - R.off) < R.nel ? R.q[0] : R.q[1];
     float W[3][P], dW[3][P];
@@ -283,28 +293,32 @@ __global__ void b_gather_kernel(const BParticles a, const float *__restrict__ ph
     for (int d = 0; d < 3; ++d) {
         const double u = (double)R.K[d] * (a.x[(size_t)d * a.ntot + i] + R.L[d] * .5) / R.L[d];
         spline_w<P, float>(u, W[d], dW[d]);
-        base[d] = (int)trunc(u) - (P - 3);
+        base[d] = wrapi((int)trunc(u) - (P - 3), R.K[d]);
     }
     const float *mesh = phi + R.mesh_off;
     float gx = 0.f, gy = 0.f, gz = 0.f;
+    int iz = base[2];
 #pragma unroll 1
     for (int k = 0; k < P; ++k) {
-        const int iz = wrapi(base[2] + k, R.K[2]);
+        int iy = base[1];
 #pragma unroll 1
         for (int j = 0; j < P; ++j) {
-            const int iy = wrapi(base[1] + j, R.K[1]);
             const float *row = mesh + (size_t)R.K[0] * (iy + (size_t)R.K[1] * iz);
             float sx = 0.f, sd = 0.f;
+            int ix = base[0];
 #pragma unroll
             for (int ii = 0; ii < P; ++ii) {
-                const float ph = row[wrapi(base[0] + ii, R.K[0])];
+                const float ph = row[ix];
                 sx += dW[0][ii] * ph;
                 sd += W[0][ii] * ph;
+                ix = ix + 1 == R.K[0] ? 0 : ix + 1;
             }
             gx += sx * W[1][j] * W[2][k];
             gy += sd * dW[1][j] * W[2][k];
             gz += sd * W[1][j] * dW[2][k];
+            iy = iy + 1 == R.K[1] ? 0 : iy + 1;
         }
+        iz = iz + 1 == R.K[2] ? 0 : iz + 1;
     }
     const double coef = kEps / (kPi * R.V);
     a.frec[i] = -coef * q * (double)gx * ((double)R.K[0] / R.L[0]);
@@ -477,7 +491,7 @@ template <int P>
 static void b_spme_launch(tcp_batch *b, bool gather, cudaStream_t st) {
     const int blocks = (b->ntot + 127) / 128;
     if (gather) {
-        b_gather_kernel<P><<<blocks, 128, 0, st>>>(parts(b), b->Qf);
+        b_gather_kernel<P><<<blocks, 128, 0, st>>>(parts(b), b->Qf, b->bin_list);   // sorted by the spread
         return;
     }
     const SpreadBins bins = b_bins(b);

@@ -648,6 +648,8 @@ static const N3BatchVariant kBatchVariants[] = {
     {pair_n3_kernel<true, 4, 1, 3, true, 1>, pair_n3_kernel<false, 4, 1, 3, true, 1>, 4, 8, "b_r4_u1_b3_x2"},
     {pair_n3_kernel<true, 4, 1, 3, true, 2>, pair_n3_kernel<false, 4, 1, 3, true, 2>, 4, 8, "b_r4_u1_b3_x2l"},
     {pair_n3_kernel<true, 2, 2, 3, true, 2>, pair_n3_kernel<false, 2, 2, 3, true, 2>, 2, 8, "b_r2_u2_b3_x2l"},
+    {pair_n3_kernel<true, 2, 2, 6, true, 2, 4>, pair_n3_kernel<false, 2, 2, 6, true, 2, 4>, 2, 4, "b_r2_u2_w4b6_x2l"},
+    {pair_n3_kernel<true, 4, 1, 6, true, 2, 4>, pair_n3_kernel<false, 4, 1, 6, true, 2, 4>, 4, 4, "b_r4_u1_w4b6_x2l"},
 };
 constexpr int kN3BatchVariants = sizeof(kBatchVariants) / sizeof(kBatchVariants[0]);
 
