@@ -20,7 +20,10 @@
 // 1/r^3), G2 -= y (3/(rs r^2) + 3/r^3 + 1/(rs^2 r))/r^2, dl = -y/rs^2,
 // gl = -y/(rs^3 r), y = exp(-r/rs).
 //
-// The real-space kernel visits every ordered pair (i, j) once: thread i sums
+// The default real-space kernel (adj_n3_kernel) visits every unique pair once
+// on the Newton-3 item schedule of the force kernels and adds +t to row i and
+// -t to row j.  With TCP_FLAG_DETERMINISTIC the ordered-pair kernel visits
+// every ordered pair (i, j) once: thread i sums
 // (H w)_i = sum_j qq (-G1 dw + G2 (u.dw) u), dw = w_i - w_j, and the scalars
 // dE/dlambda = 1/2 sum qq dl and dF/dlambda . w = sum qq gl (u.w_i).  The
 // j-range is split over gridDim.y; rows are added to hw with FP64 atomics.
@@ -34,6 +37,7 @@
 
 #include "device_util.cuh"
 #include "pair_math.cuh"
+#include "pair_n3.cuh"
 #include "tcp_internal.h"
 
 namespace tcp {
@@ -221,6 +225,200 @@ __global__ void __launch_bounds__(kAdjThreads) adj_pair_kernel(const AdjArgs a) 
     }
 }
 
+// ---- Newton-3 form -------------------------------------------------------------
+// The same sums over unique pairs (i < j), on the item schedule of the Newton-3
+// force kernels (pair_n3.cuh: i-tiles of kAdjN3Tile particles x j-subtiles of
+// kN3Sub, every item taken from an atomic counter).  A lane holds one
+// i-particle; the j position, w_j and the reaction (H w)_j rotate through the
+// warp with shuffles.  Per unique pair with t = qq (-G1 dw + G2 (u.dw) u):
+// (H w)_i += t, (H w)_j -= t; dE/dlambda += qq dl; dF/dlambda . w += qq gl (u.dw)
+// (the ordered-pair sums counted each of these twice or split them over i, j).
+constexpr int kAdjN3Warps = 8;
+constexpr int kAdjN3Threads = 32 * kAdjN3Warps;
+constexpr int kAdjN3Tile = kAdjN3Threads;     // one i-particle per lane
+
+__device__ __forceinline__ void adj_radial_t(const AdjArgs &a, int type, int eik, float r2, float &G1, float &G2,
+                                             float &dl, float &gl) {
+    if (type == 1 && eik == 2 && r2 < a.c.close2) {   // close Kelbg pairs, as in adj_pair_kernel
+        double h1, h2, hd, hg;
+        radial_f64<2>(a, (double)r2, h1, h2, hd, hg);
+        G1 = (float)h1;
+        G2 = (float)h2;
+        dl = (float)hd;
+        gl = (float)hg;
+        return;
+    }
+    if (type == 1 && eik == 1) radial_f32<1>(a, r2, G1, G2, dl, gl);
+    else if (type == 1 && eik == 2) radial_f32<2>(a, r2, G1, G2, dl, gl);
+    else radial_f32<0>(a, r2, G1, G2, dl, gl);
+}
+
+__device__ __forceinline__ void adj_radial_t(const AdjArgs &a, int type, int eik, double r2, double &G1,
+                                             double &G2, double &dl, double &gl) {
+    if (type == 1 && eik == 1) radial_f64<1>(a, r2, G1, G2, dl, gl);
+    else if (type == 1 && eik == 2) radial_f64<2>(a, r2, G1, G2, dl, gl);
+    else radial_f64<0>(a, r2, G1, G2, dl, gl);
+}
+
+template <bool F32, int EIK, bool HVP>
+__global__ void __launch_bounds__(kAdjN3Threads) adj_n3_kernel(const AdjArgs a, const N3Geom g, long long total,
+                                                                 unsigned *counter) {
+    using T = typename std::conditional<F32, float, double>::type;
+    __shared__ int4 sxq[F32 ? kN3Sub : 1];
+    __shared__ double4_32a sxd[F32 ? 1 : kN3Sub];
+    __shared__ double sw[3][HVP ? kN3Sub : 1];
+    __shared__ double sh[HVP ? kN3Sub : 1][3];
+    __shared__ double red[32];
+    __shared__ long long s_next;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int src = (lane + 1) & 31;
+    for (int k = tid; k < (HVP ? kN3Sub : 1) * 3; k += kAdjN3Threads) (&sh[0][0])[k] = 0.0;
+
+    int curI = -1, istart = 0, iend = 0, isp = 0, ifirst = 0, ibase = 0;
+    int4 xqi = make_int4(0, 0, 0, 0);
+    double3 xdi = make_double3(0.0, 0.0, 0.0);
+    T wi[3] = {0, 0, 0};
+    double hi[3] = {0.0, 0.0, 0.0};
+    double el = 0.0, fl = 0.0;
+
+    auto flush_i = [&]() {
+        if (HVP && curI >= 0 && ibase < iend)
+            for (int d = 0; d < 3; ++d) atomicAdd(a.hw + (size_t)d * a.n + ibase, hi[d]);
+        hi[0] = hi[1] = hi[2] = 0.0;
+    };
+
+    while (true) {
+        if (tid == 0) s_next = (long long)atomicAdd(counter, 1u);
+        __syncthreads();
+        const long long it = s_next;
+        if (it >= total) break;
+        int I, S;
+        n3_decode<kAdjN3Tile>(g, it, I, S);
+        if (I != curI) {
+            flush_i();
+            curI = I;
+            n3_itile<kAdjN3Tile>(g, I, istart, iend, isp, ifirst);
+            ibase = istart + warp * 32 + lane;
+            const int ir = ibase < iend ? ibase : istart;
+            if (F32) {
+                xqi = a.xq[ir];
+            } else {
+                const double4_32a t = a.xd[ir];
+                xdi = make_double3(t.x, t.y, t.z);
+            }
+            if (HVP)
+                for (int d = 0; d < 3; ++d) wi[d] = (T)a.w[(size_t)d * a.n + ir];
+        }
+        int jstart, cnt, jsp;
+        n3_sub(g, S, jstart, cnt, jsp);
+        for (int k = tid; k < cnt; k += kAdjN3Threads) {
+            if (F32) sxq[k] = a.xq[jstart + k];
+            else sxd[k] = a.xd[jstart + k];
+            if (HVP)
+                for (int d = 0; d < 3; ++d) sw[d][k] = a.w[(size_t)d * a.n + jstart + k];
+        }
+        __syncthreads();
+        const bool masked = (S < ifirst + kAdjN3Tile / kN3Sub && jsp == isp) || cnt < kN3Sub || (iend - istart) < kAdjN3Tile;
+        const int type = isp + jsp;
+        const T qq = F32 ? (T)(a.c.qqf[type] * (float)kEps) : (T)(a.c.qq[type] * kEps);
+        T ti0 = 0, ti1 = 0, ti2 = 0, te = 0, tf = 0;   // per-item partials (FP32 in FP32C mode)
+        for (int ch = 0; ch * 32 < cnt; ++ch) {
+            const int jl = ch * 32 + lane;
+            const bool jv = jl < cnt;
+            int4 xqj = make_int4(0, 0, 0, 0);
+            double xj0 = 0.0, xj1 = 0.0, xj2 = 0.0;
+            if (jv) {
+                if (F32) {
+                    xqj = sxq[jl];
+                } else {
+                    xj0 = sxd[jl].x;
+                    xj1 = sxd[jl].y;
+                    xj2 = sxd[jl].z;
+                }
+            }
+            T wj0 = HVP && jv ? (T)sw[0][jl] : (T)0, wj1 = HVP && jv ? (T)sw[1][jl] : (T)0,
+              wj2 = HVP && jv ? (T)sw[2][jl] : (T)0;
+            T hj0 = 0, hj1 = 0, hj2 = 0;
+#pragma unroll 1
+            for (int s = 0; s < 32; ++s) {
+                const int jo = ch * 32 + ((lane + s) & 31);
+                T u0, u1, u2;
+                if (F32) {
+                    u0 = (T)(float)(int)((unsigned)xqi.x - (unsigned)xqj.x) * (T)a.c.sx;
+                    u1 = (T)(float)(int)((unsigned)xqi.y - (unsigned)xqj.y) * (T)a.c.sy;
+                    u2 = (T)(float)(int)((unsigned)xqi.z - (unsigned)xqj.z) * (T)a.c.sz;
+                } else {
+                    u0 = (T)fma(-a.c.box[0], rint((xdi.x - xj0) * a.c.inv_box[0]), xdi.x - xj0);
+                    u1 = (T)fma(-a.c.box[1], rint((xdi.y - xj1) * a.c.inv_box[1]), xdi.y - xj1);
+                    u2 = (T)fma(-a.c.box[2], rint((xdi.z - xj2) * a.c.inv_box[2]), xdi.z - xj2);
+                }
+                const T r2 = u0 * u0 + u1 * u1 + u2 * u2;
+                bool ok = r2 < (F32 ? (T)a.c.rc2f : (T)a.c.rc2) && r2 > (T)0;
+                if (masked) ok = ok && ibase < iend && jo < cnt && ibase < jstart + jo;
+                if (ok) {
+                    T G1, G2, dl, gl;
+                    adj_radial_t(a, type, EIK, r2, G1, G2, dl, gl);
+                    te += qq * dl;
+                    if (HVP) {
+                        const T dw0 = wi[0] - wj0, dw1 = wi[1] - wj1, dw2 = wi[2] - wj2;
+                        const T ud = u0 * dw0 + u1 * dw1 + u2 * dw2;
+                        const T a1 = -qq * G1, a2 = qq * G2 * ud;
+                        const T t0 = a1 * dw0 + a2 * u0, t1 = a1 * dw1 + a2 * u1, t2 = a1 * dw2 + a2 * u2;
+                        ti0 += t0;
+                        ti1 += t1;
+                        ti2 += t2;
+                        hj0 -= t0;
+                        hj1 -= t1;
+                        hj2 -= t2;
+                        tf += qq * gl * ud;
+                    }
+                }
+                // rotate j (position, w and reaction) to the next lane
+                if (F32) {
+                    xqj.x = __shfl_sync(0xffffffffu, xqj.x, src);
+                    xqj.y = __shfl_sync(0xffffffffu, xqj.y, src);
+                    xqj.z = __shfl_sync(0xffffffffu, xqj.z, src);
+                } else {
+                    xj0 = __shfl_sync(0xffffffffu, xj0, src);
+                    xj1 = __shfl_sync(0xffffffffu, xj1, src);
+                    xj2 = __shfl_sync(0xffffffffu, xj2, src);
+                }
+                if (HVP) {
+                    wj0 = __shfl_sync(0xffffffffu, wj0, src);
+                    wj1 = __shfl_sync(0xffffffffu, wj1, src);
+                    wj2 = __shfl_sync(0xffffffffu, wj2, src);
+                    hj0 = __shfl_sync(0xffffffffu, hj0, src);
+                    hj1 = __shfl_sync(0xffffffffu, hj1, src);
+                    hj2 = __shfl_sync(0xffffffffu, hj2, src);
+                }
+            }
+            if (HVP && jv) {
+                atomicAdd(&sh[jl][0], (double)hj0);
+                atomicAdd(&sh[jl][1], (double)hj1);
+                atomicAdd(&sh[jl][2], (double)hj2);
+            }
+        }
+        hi[0] += (double)ti0;
+        hi[1] += (double)ti1;
+        hi[2] += (double)ti2;
+        el += (double)te;
+        fl += (double)tf;
+        __syncthreads();                   // reactions of this subtile complete; tiles free
+        if (HVP && tid < cnt)
+            for (int d = 0; d < 3; ++d) {
+                atomicAdd(a.hw + (size_t)d * a.n + jstart + tid, sh[tid][d]);
+                sh[tid][d] = 0.0;
+            }
+    }
+    flush_i();
+    el = block_sum(el, red);
+    fl = block_sum(fl, red);
+    if (tid == 0) {
+        atomicAdd(a.scal + kAdjDEdl, el);
+        if (HVP) atomicAdd(a.scal + kAdjDFdl, fl);
+    }
+}
+
 // ---- host-layout transposes ---------------------------------------------------
 __global__ void aos_to_soa_kernel(const double *__restrict__ in, double *__restrict__ out, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -370,9 +568,55 @@ static AdjArgs adj_args(tcp_ctx *c, const double *w, double *hw) {
     return a;
 }
 
-// Real-space part: hw += H_real w (when w), scalars into adj_scal.
+template <bool F32, int EIK, bool HVP>
+static int launch_adj_n3_t(tcp_ctx *c, const AdjArgs &a) {
+    long long total = 0;
+    const N3Geom g = n3_geometry(0, c->nel, c->nion, kAdjN3Tile, 0, &total);
+    int bps = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, adj_n3_kernel<F32, EIK, HVP>, kAdjN3Threads, 0);
+    const int grid = (int)std::max<long long>(1, std::min<long long>((long long)c->num_sms * std::max(bps, 1), total));
+    TCP_CUDA(cudaMemsetAsync(c->counter, 0, sizeof(unsigned), c->stream));
+    adj_n3_kernel<F32, EIK, HVP><<<grid, kAdjN3Threads, 0, c->stream>>>(a, g, total, c->counter);
+    return TCP_OK;
+}
+
+// Real-space part: hw += H_real w (when w), scalars into adj_scal.  The
+// Newton-3 form unless TCP_FLAG_DETERMINISTIC asks for the ordered-pair sums
+// (which add their rows in a fixed pattern).
 static int launch_adj_pair(tcp_ctx *c, const double *w, double *hw) {
     AdjArgs a = adj_args(c, w, hw);
+    if (!(c->flags & TCP_FLAG_DETERMINISTIC)) {
+        const bool f32 = c->p.precision == TCP_PREC_FP32C;
+        const int eik = c->p.ei_model == TCP_EI_DEUTSCH ? 1 : (c->p.ei_model == TCP_EI_KELBG ? 2 : 0);
+        int rc;
+#define ADJ_N3(F, E, H) rc = launch_adj_n3_t<F, E, H>(c, a)
+        if (w) {
+            if (f32) {
+                if (eik == 1) ADJ_N3(true, 1, true);
+                else if (eik == 2) ADJ_N3(true, 2, true);
+                else ADJ_N3(true, 0, true);
+            } else {
+                if (eik == 1) ADJ_N3(false, 1, true);
+                else if (eik == 2) ADJ_N3(false, 2, true);
+                else ADJ_N3(false, 0, true);
+            }
+        } else {
+            if (f32) {
+                if (eik == 1) ADJ_N3(true, 1, false);
+                else if (eik == 2) ADJ_N3(true, 2, false);
+                else ADJ_N3(true, 0, false);
+            } else {
+                if (eik == 1) ADJ_N3(false, 1, false);
+                else if (eik == 2) ADJ_N3(false, 2, false);
+                else ADJ_N3(false, 0, false);
+            }
+        }
+#undef ADJ_N3
+        if (rc) return rc;
+        c->launches++;
+        TCP_CUDA(cudaGetLastError());
+        return TCP_OK;
+    }
     const int bx = (c->n + kAdjThreads - 1) / kAdjThreads;
     const int by = (c->n + a.jchunk - 1) / a.jchunk;
     const dim3 grid(bx, by);

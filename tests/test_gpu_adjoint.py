@@ -238,3 +238,29 @@ def test_hvp_fp32c_close_kelbg_pair(r_over_lam):
         hw, dfl = c.hvp(w)
     assert oracle.rms_rel(hw, hw_o) < 2e-5
     assert dfl == pytest.approx(dfl_o, rel=2e-5)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+@pytest.mark.parametrize("ei", ["kelbg", "deutsch", "coulomb"])
+def test_newton3_adjoint_matches_ordered(precision, ei):
+    """The Newton-3 real-space H w / dE/dlambda / dF/dlambda.w (default)
+    against the ordered-pair sums (TCP_FLAG_DETERMINISTIC) on 700 electrons
+    and 300 ions (ragged tiles, unequal species)."""
+    s = T.make_system(1000, gamma=1.0, lam=0.5, seed=12, alpha_rc=3.1, K=16, order=4)
+    s.nel, s.nion = 700, 300
+    w = np.random.default_rng(5).normal(size=(s.n, 3))
+    out = {}
+    for det in (False, True):
+        with ctx_for(s, precision=precision, ei=ei, recip="none") as c:
+            if det:
+                c.set_flags(T.FLAG_ENERGY | T.FLAG_DETERMINISTIC)
+            hw, dfl = c.hvp(w)
+            _, dl, _ = c.adjoint_energy()
+        out[det] = (hw, dfl, dl)
+    tol = 1e-12 if precision == "fp64" else 2e-6
+    assert oracle.rms_rel(out[False][0], out[True][0]) < tol
+    if ei == "coulomb":
+        assert out[False][1] == 0.0 and out[False][2] == 0.0
+    else:
+        assert out[False][1] == pytest.approx(out[True][1], rel=tol)
+        assert out[False][2] == pytest.approx(out[True][2], rel=tol)
