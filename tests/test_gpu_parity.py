@@ -69,7 +69,7 @@ def test_spme_vs_oracle(order, K):
 
 @pytest.mark.parametrize("order,K", [(4, 16), (5, 32), (6, 24)])
 def test_spme_fp32_mode_vs_oracle(order, K):
-    """FP32C mode: FP64 charge accumulation, FP32 transforms and gather."""
+    """FP32C mode: compensated-FP32 charge accumulation, FP32 transforms and gather."""
     s = make(2000, seed=4, K=K, order=order)
     o = oracle.Oracle.from_system(s, ei="kelbg")
     fo, umo = o.force_spme(s.x)
@@ -419,3 +419,21 @@ def test_kelbg_close_pair_accuracy(monkeypatch, variant, r_over_lam):
         _, _, f, _ = c.download(x=False, v=False, f=True)
     assert np.linalg.norm(f - fo) / np.linalg.norm(fo) < 2e-5
     assert ur == pytest.approx(uo, rel=2e-5, abs=1e-6 * abs(uo) + 1e-12)
+
+
+@pytest.mark.parametrize("variant", [6, 9, 11])
+@pytest.mark.parametrize("nel,nion", [(1, 300), (257, 0), (700, 333), (1030, 2)])
+def test_fp32c_newton3_ragged_species(monkeypatch, variant, nel, nion):
+    """Packed Newton-3 variants with a single electron, one species only, and
+    species counts that leave partial i-tiles and j-subtiles, against the
+    oracle (Kelbg, real-space sum)."""
+    monkeypatch.setenv("TCP_PAIR_VARIANT", str(variant))
+    s = T.make_system(nel + nion, gamma=1.0, lam=0.5, seed=21, alpha_rc=3.1, K=16, order=4)
+    s.nel, s.nion = nel, nion
+    fo, uo = oracle.Oracle.from_system(s, ei="kelbg").force_direct(s.x)
+    with ctx_for(s, precision="fp32c", ei="kelbg", recip="none") as c:
+        ur = c.Force_direct_self()
+        _, _, f, _ = c.download(x=False, v=False, f=True)
+        assert c.autotune_report()[0] == variant
+    assert oracle.rms_rel(f, fo) < FP32_FORCE_RMS
+    assert ur == pytest.approx(uo, rel=2e-5, abs=1e-9)
