@@ -225,7 +225,8 @@ def config_dict(s):
             "lambda_ei_over_a": 0.5, "ei_model": "kelbg", "box_A": s.box, "rc": "L/2",
             "ewald_alpha_rc": s.alpha * s.rc, "spme_mesh": s.K, "spline_order": s.order, "ensemble": "NVE",
             "dt_over_wpe": 0.01, "units": "reference (A, eV, amu, 10.18 fs)",
-            "precision": "FP32 pair arithmetic with compensated accumulation; FP64 integration, SPME, reductions",
+            "precision": "FP32 pair arithmetic with compensated accumulation; SPME on a compensated-FP32 mesh "
+                         "with FP32 transforms; FP64 integration and reductions",
             "l2": "flushed between timed steps (a 2x L2 buffer is written outside the timed spans)"}
 
 
