@@ -321,6 +321,7 @@ int tcp_create(const tcp_params *p_in, int nel, int nion, int device, tcp_ctx **
     TCP_ALLOC(c->frec, sizeof(double) * 3 * n);
     TCP_ALLOC(c->xq, sizeof(int4) * n);
     TCP_ALLOC(c->xd, sizeof(double4_32a) * n);
+    TCP_ALLOC(c->xl, sizeof(longlong4_32a) * n);
     c->red_cap = red_capacity(c->n, 8192 + 65536);
     TCP_ALLOC(c->red, sizeof(double) * (size_t)c->red_cap);
     TCP_ALLOC(c->scal, sizeof(double) * kScalCount);
@@ -360,6 +361,7 @@ int tcp_destroy(tcp_ctx *c) {
     cudaFree(c->frec);
     cudaFree(c->xq);
     cudaFree(c->xd);
+    cudaFree(c->xl);
     cudaFree(c->fpart);
     cudaFree(c->upart);
     cudaFree(c->red);

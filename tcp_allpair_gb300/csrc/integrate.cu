@@ -29,10 +29,21 @@ __device__ __forceinline__ int fixed_coord(double x, double iL) {
     return (int)(unsigned)(u & 0xffffffffull);
 }
 
+// 2^64 units per box length (the FP64 Newton-3 kernel): the wrapped int64
+// difference is the minimum image, exact before its conversion to FP64.
+__device__ __forceinline__ long long fixed_coord64(double x, double iL) {
+    double t = fma(x, iL, 0.5);
+    t -= floor(t);                                  // [0, 1)
+    const double s = t * 18446744073709551616.0;    // [0, 2^64]
+    const unsigned long long u = s >= 18446744073709551615.0 ? 0ull : (unsigned long long)s;
+    return (long long)u;
+}
+
 struct IntArgs {
     double *x, *v, *f;
     int4 *xq;
     double4_32a *xd;
+    longlong4_32a *xl;
     int nel, n;
     double xm0, xm1;
     double L0, L1, L2;
@@ -45,6 +56,12 @@ __device__ __forceinline__ void store_pos(const IntArgs &a, int i, double x0, do
     a.x[2 * (size_t)a.n + i] = x2;
     a.xq[i] = make_int4(fixed_coord(x0, a.iL0), fixed_coord(x1, a.iL1), fixed_coord(x2, a.iL2), 0);
     a.xd[i] = make_double4_32a(x0, x1, x2, 0.0);
+    longlong4_32a q;
+    q.x = fixed_coord64(x0, a.iL0);
+    q.y = fixed_coord64(x1, a.iL1);
+    q.z = fixed_coord64(x2, a.iL2);
+    q.w = 0;
+    a.xl[i] = q;
 }
 
 // x - L DNINT(x/L) (vverlet.f90:153); x/L from the reciprocal with one FMA
@@ -418,6 +435,7 @@ static IntArgs int_args(tcp_ctx *c) {
     a.f = c->f;
     a.xq = c->xq;
     a.xd = c->xd;
+    a.xl = c->xl;
     a.nel = c->nel;
     a.n = c->n;
     a.xm0 = c->p.xm[0];

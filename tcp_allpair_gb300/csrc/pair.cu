@@ -539,6 +539,7 @@ void make_pair_consts(tcp_ctx *c) {
     for (int d = 0; d < 3; ++d) {
         k.box[d] = p.box[d];
         k.inv_box[d] = 1.0 / p.box[d];
+        k.sl[d] = p.box[d] / 18446744073709551616.0;
     }
     k.rc2 = c->rc2;
     k.alpha = c->alpha;

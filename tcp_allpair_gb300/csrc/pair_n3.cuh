@@ -34,7 +34,8 @@ struct N3Rep {
 
 struct N3Args {
     const int4 *xq;                // fixed-point positions (FP32C kernels)
-    const double4_32a *xd;         // FP64 positions (FP64 kernel)
+    const double4_32a *xd;         // FP64 positions
+    const longlong4_32a *xl;       // 64-bit fixed-point positions (FP64 kernel)
     long long total;      // items (all systems)
     long long nstatic;    // items [0, nstatic) split statically
     int ntot;             // stride of facc

@@ -14,10 +14,12 @@
 // vary in the last bits; TCP_FLAG_DETERMINISTIC selects the ordered-pair
 // kernel with its fixed-order reduction instead.
 //
-// Pair arithmetic follows force.f90:87-141 in FP64 without divisions: minimum
-// image by multiplication with 1/box and round-to-nearest (force.f90:92 rounds
-// half away from zero; the two differ only at |d| = box/2 exactly, where
-// r >= rc), 1/r and 1/r^3 from one rsqrt, and erfc(alpha r) from the Gaussian
+// Pair arithmetic follows force.f90:87-141 in FP64 without divisions: the
+// minimum image (force.f90:92) is the wrapped difference of 64-bit fixed-point
+// coordinates (2^64 per box length, refreshed with every position update),
+// exact and then rounded once to FP64 (the sign choice at |d| = box/2 exactly
+// differs from DNINT's, where r >= rc), 1/r and 1/r^3 come from one rsqrt,
+// and erfc(alpha r) from the Gaussian
 // exp(-alpha^2 r^2) that the force needs anyway times a polynomial
 // (erfc_gauss; 4e-15 relative, fit_erfc64.py), where the reference takes
 // 1 - erf(alpha r).
@@ -99,33 +101,35 @@ __device__ __forceinline__ double n3_pair_f64(const PairConsts &c, double r2, bo
     return ok ? s * (rinv * rinv * rinv) : 0.0;
 }
 
-__device__ __forceinline__ double min_image(double d, double box, double inv_box) {
-    return fma(-box, rint(d * inv_box), d);
+// minimum-image separation from 64-bit fixed-point coordinates (2^64 per box
+// length): the wrapped integer difference, exact, then one rounding to FP64
+__device__ __forceinline__ double fixed_diff(long long a, long long b, double scale) {
+    return (double)(long long)((unsigned long long)a - (unsigned long long)b) * scale;
 }
 
 // One item: the R i-particles of this lane against a j-subtile in shared
 // memory.  MASKED: apply validity and i < j index masks.
 template <int KIND, bool ENERGY, bool MASKED, int R>
-__device__ __forceinline__ void n3_item_f64(const PairConsts &c, const double4_32a *__restrict__ tj, int cnt,
-                                            int jstart, const double3 (&xi)[R], int ibase, int iend,
+__device__ __forceinline__ void n3_item_f64(const PairConsts &c, const longlong4_32a *__restrict__ tj, int cnt,
+                                            int jstart, const longlong3 (&xi)[R], int ibase, int iend,
                                             double (*sjacc)[3], double (&p)[R][3], double &pe) {
     const int lane = threadIdx.x & 31;
     const int src = (lane + 1) & 31;
     for (int ch = 0; ch * 32 < cnt; ++ch) {
         const int jl = ch * 32 + lane;
-        double3 xj = make_double3(0.0, 0.0, 0.0);        // padding lanes: finite, masked below
+        longlong3 xj = make_longlong3(0, 0, 0);           // padding lanes: masked below
         if (jl < cnt) {
-            const double4_32a t = tj[jl];
-            xj = make_double3(t.x, t.y, t.z);
+            const longlong4_32a t = tj[jl];
+            xj = make_longlong3(t.x, t.y, t.z);
         }
         double jx = 0.0, jy = 0.0, jz = 0.0;
 #pragma unroll 1
         for (int s = 0; s < 32; ++s) {
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const double dx = min_image(xi[r].x - xj.x, c.box[0], c.inv_box[0]);
-                const double dy = min_image(xi[r].y - xj.y, c.box[1], c.inv_box[1]);
-                const double dz = min_image(xi[r].z - xj.z, c.box[2], c.inv_box[2]);
+                const double dx = fixed_diff(xi[r].x, xj.x, c.sl[0]);
+                const double dy = fixed_diff(xi[r].y, xj.y, c.sl[1]);
+                const double dz = fixed_diff(xi[r].z, xj.z, c.sl[2]);
                 const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
                 bool ok = r2 < c.rc2 && r2 > 0.0;
                 if (MASKED) {
@@ -160,7 +164,7 @@ __device__ __forceinline__ void n3_item_f64(const PairConsts &c, const double4_3
 template <bool ENERGY, int R>
 __global__ void __launch_bounds__(kN3Threads) pair_n3_f64_kernel(const N3Args a) {
     constexpr int TILE = 32 * R * kN3Warps;
-    __shared__ __align__(128) double4_32a tiles[kN3Stages][kN3Sub];
+    __shared__ __align__(128) longlong4_32a tiles[kN3Stages][kN3Sub];
     __shared__ __align__(8) uint64_t bars[kN3Stages];
     __shared__ double sjacc[kN3Sub][3];
     __shared__ double red[32];
@@ -184,9 +188,9 @@ __global__ void __launch_bounds__(kN3Threads) pair_n3_f64_kernel(const N3Args a)
         n3_locate<TILE, false>(a, it, rep, I_, S_);
         int js, jc, jsp;
         n3_sub(a.g, S_, js, jc, jsp);
-        const uint32_t bytes = (uint32_t)jc * sizeof(double4_32a);
+        const uint32_t bytes = (uint32_t)jc * sizeof(longlong4_32a);
         mbar_arrive_expect_tx(&bars[stage], bytes);
-        bulk_g2s(tiles[stage], a.xd + js, bytes, &bars[stage]);
+        bulk_g2s(tiles[stage], a.xl + js, bytes, &bars[stage]);
     };
     if (tid == 0)
         for (int k = 0; k < min(kN3Stages, nst); ++k)
@@ -194,12 +198,12 @@ __global__ void __launch_bounds__(kN3Threads) pair_n3_f64_kernel(const N3Args a)
 
     double etot = 0.0;
     int curI = -1, istart = 0, iend = 0, isp = 0, ifirst = 0;
-    double3 xi[R];
+    longlong3 xi[R];
     double fi[R][3];
     int ibase = 0;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-        xi[r] = make_double3(0.0, 0.0, 0.0);
+        xi[r] = make_longlong3(0, 0, 0);
         fi[r][0] = fi[r][1] = fi[r][2] = 0.0;
     }
 
@@ -225,8 +229,8 @@ __global__ void __launch_bounds__(kN3Threads) pair_n3_f64_kernel(const N3Args a)
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int ir = ibase + 32 * r;
-                const double4_32a t = a.xd[ir < iend ? ir : istart];
-                xi[r] = make_double3(t.x, t.y, t.z);
+                const longlong4_32a t = a.xl[ir < iend ? ir : istart];
+                xi[r] = make_longlong3(t.x, t.y, t.z);
             }
         }
         int jstart, cnt, jsp;
@@ -337,7 +341,7 @@ int launch_pair_n3_f64(tcp_ctx *c, bool energy) {
     std::memset(&a, 0, sizeof a);
     long long total = 0;
     a.g = n3_geometry(0, c->nel, c->nion, tile, 0, &total);
-    a.xd = c->xd;
+    a.xl = c->xl;
     a.total = total;
     // all items from the counter: an FP64 item takes milliseconds, so the
     // per-item copy latency is negligible and the tail is at most one item

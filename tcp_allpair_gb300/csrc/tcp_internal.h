@@ -53,6 +53,7 @@ struct PairConsts {
     double box[3];
     double rc2, alpha, rs, lambda;
     double inv_box[3];         // 1/box (minimum image by multiplication)
+    double sl[3];              // box / 2^64: the 64-bit fixed-point difference in A
     double alpha2;             // alpha^2
     double c_gauss_d;          // 2 alpha / sqrt(pi)
     double inv_rs_d;           // 1/rs
@@ -88,6 +89,7 @@ struct tcp_ctx {
     double *x = nullptr, *v = nullptr, *f = nullptr, *frec = nullptr;
     int4 *xq = nullptr;        // fixed-point positions for the FP32 pair kernel
     double4_32a *xd = nullptr;     // FP64 positions for the FP64 pair kernel
+    longlong4_32a *xl = nullptr;   // 64-bit fixed-point positions (2^64 per box length) for the FP64 Newton-3 kernel
     // pair-kernel partials
     int jsplit = 1;
     int fpart_splits = 1;      // splits written by the last pair launch
