@@ -48,6 +48,7 @@ enum { kAdjDEdl = 0, kAdjDFdl = 1, kAdjJ = 2, kAdjCount = 8 };
 struct AdjArgs {
     const int4 *xq;
     const double4_32a *xd;
+    const longlong4_32a *xl;   // 64-bit fixed-point positions (FP64 Newton-3 form)
     const double *w;      // [3][n] (HVP) or nullptr
     double *hw;           // [3][n], atomic adds
     double *scal;         // kAdj*
@@ -60,25 +61,26 @@ struct AdjArgs {
 template <int KIND>
 __device__ __forceinline__ void radial_f64(const AdjArgs &a, double r2, double &G1, double &G2, double &dl,
                                            double &gl) {
-    const double r = sqrt(r2), rinv = 1.0 / r, rinv2 = rinv * rinv;
+    // no divisions (GB300's FP64 rate): 1/r from rsqrt, erfc from the Gaussians
+    const double rinv = rsqrt(r2), r = r2 * rinv, rinv2 = rinv * rinv;
     const double al = a.c.alpha;
-    const double e = exp(-al * al * r2);
-    const double w0 = (erfc(al * r) * rinv + (2.0 * al / kSqrtPi) * e) * rinv2;
+    const double e = exp(-a.c.alpha2 * r2);
+    const double w0 = (erfc_gauss(al * r, e) * rinv + a.c.c_gauss_d * e) * rinv2;
     G1 = w0;
     G2 = (3.0 * w0 + a.c2a * e) * rinv2;
     dl = 0.0;
     gl = 0.0;
     if (KIND == 1) {
-        const double irs = 1.0 / a.c.rs, y = exp(-r * irs);
+        const double irs = a.c.inv_rs_d, y = exp(-r * irs);
         G1 -= y * (irs + rinv) * rinv2;
         G2 -= y * (3.0 * irs * rinv2 + 3.0 * rinv2 * rinv + a.inv_rs2 * rinv) * rinv2;
         dl = -y * a.inv_rs2;
         gl = -y * a.inv_rs3 * rinv;
     } else if (KIND == 2) {
-        const double l = a.c.lambda, g = exp(-r2 / (l * l));
+        const double g = exp(-r2 * a.c.inv_lam2);
         G1 -= g * rinv2 * rinv;
         G2 -= g * (3.0 * rinv2 * rinv + a.k_l2 * rinv) * rinv2;
-        dl = -a.k_dl * erfc(r / l);
+        dl = -a.k_dl * erfc_gauss(r * a.c.inv_lam, g);   // erfc(r/l), exp(-(r/l)^2) = g
         gl = -a.k_gl * g * rinv;
     }
 }
@@ -265,7 +267,7 @@ __global__ void __launch_bounds__(kAdjN3Threads) adj_n3_kernel(const AdjArgs a, 
                                                                  unsigned *counter) {
     using T = typename std::conditional<F32, float, double>::type;
     __shared__ int4 sxq[F32 ? kN3Sub : 1];
-    __shared__ double4_32a sxd[F32 ? 1 : kN3Sub];
+    __shared__ longlong4_32a sxl[F32 ? 1 : kN3Sub];
     __shared__ double sw[3][HVP ? kN3Sub : 1];
     __shared__ double sh[HVP ? kN3Sub : 1][3];
     __shared__ double red[32];
@@ -276,7 +278,7 @@ __global__ void __launch_bounds__(kAdjN3Threads) adj_n3_kernel(const AdjArgs a, 
 
     int curI = -1, istart = 0, iend = 0, isp = 0, ifirst = 0, ibase = 0;
     int4 xqi = make_int4(0, 0, 0, 0);
-    double3 xdi = make_double3(0.0, 0.0, 0.0);
+    longlong3 xli = make_longlong3(0, 0, 0);
     T wi[3] = {0, 0, 0};
     double hi[3] = {0.0, 0.0, 0.0};
     double el = 0.0, fl = 0.0;
@@ -303,8 +305,8 @@ __global__ void __launch_bounds__(kAdjN3Threads) adj_n3_kernel(const AdjArgs a, 
             if (F32) {
                 xqi = a.xq[ir];
             } else {
-                const double4_32a t = a.xd[ir];
-                xdi = make_double3(t.x, t.y, t.z);
+                const longlong4_32a t = a.xl[ir];
+                xli = make_longlong3(t.x, t.y, t.z);
             }
             if (HVP)
                 for (int d = 0; d < 3; ++d) wi[d] = (T)a.w[(size_t)d * a.n + ir];
@@ -313,7 +315,7 @@ __global__ void __launch_bounds__(kAdjN3Threads) adj_n3_kernel(const AdjArgs a, 
         n3_sub(g, S, jstart, cnt, jsp);
         for (int k = tid; k < cnt; k += kAdjN3Threads) {
             if (F32) sxq[k] = a.xq[jstart + k];
-            else sxd[k] = a.xd[jstart + k];
+            else sxl[k] = a.xl[jstart + k];
             if (HVP)
                 for (int d = 0; d < 3; ++d) sw[d][k] = a.w[(size_t)d * a.n + jstart + k];
         }
@@ -326,14 +328,14 @@ __global__ void __launch_bounds__(kAdjN3Threads) adj_n3_kernel(const AdjArgs a, 
             const int jl = ch * 32 + lane;
             const bool jv = jl < cnt;
             int4 xqj = make_int4(0, 0, 0, 0);
-            double xj0 = 0.0, xj1 = 0.0, xj2 = 0.0;
+            long long xj0 = 0, xj1 = 0, xj2 = 0;
             if (jv) {
                 if (F32) {
                     xqj = sxq[jl];
                 } else {
-                    xj0 = sxd[jl].x;
-                    xj1 = sxd[jl].y;
-                    xj2 = sxd[jl].z;
+                    xj0 = sxl[jl].x;
+                    xj1 = sxl[jl].y;
+                    xj2 = sxl[jl].z;
                 }
             }
             T wj0 = HVP && jv ? (T)sw[0][jl] : (T)0, wj1 = HVP && jv ? (T)sw[1][jl] : (T)0,
@@ -347,10 +349,10 @@ __global__ void __launch_bounds__(kAdjN3Threads) adj_n3_kernel(const AdjArgs a, 
                     u0 = (T)(float)(int)((unsigned)xqi.x - (unsigned)xqj.x) * (T)a.c.sx;
                     u1 = (T)(float)(int)((unsigned)xqi.y - (unsigned)xqj.y) * (T)a.c.sy;
                     u2 = (T)(float)(int)((unsigned)xqi.z - (unsigned)xqj.z) * (T)a.c.sz;
-                } else {
-                    u0 = (T)fma(-a.c.box[0], rint((xdi.x - xj0) * a.c.inv_box[0]), xdi.x - xj0);
-                    u1 = (T)fma(-a.c.box[1], rint((xdi.y - xj1) * a.c.inv_box[1]), xdi.y - xj1);
-                    u2 = (T)fma(-a.c.box[2], rint((xdi.z - xj2) * a.c.inv_box[2]), xdi.z - xj2);
+                } else {   // wrapped 64-bit fixed-point difference = minimum image
+                    u0 = (T)((double)(long long)((unsigned long long)xli.x - (unsigned long long)xj0) * a.c.sl[0]);
+                    u1 = (T)((double)(long long)((unsigned long long)xli.y - (unsigned long long)xj1) * a.c.sl[1]);
+                    u2 = (T)((double)(long long)((unsigned long long)xli.z - (unsigned long long)xj2) * a.c.sl[2]);
                 }
                 const T r2 = u0 * u0 + u1 * u1 + u2 * u2;
                 bool ok = r2 < (F32 ? (T)a.c.rc2f : (T)a.c.rc2) && r2 > (T)0;
@@ -541,6 +543,7 @@ static AdjArgs adj_args(tcp_ctx *c, const double *w, double *hw) {
     AdjArgs a;
     a.xq = c->xq;
     a.xd = c->xd;
+    a.xl = c->xl;
     a.w = w;
     a.hw = hw;
     a.scal = c->adj_scal;
