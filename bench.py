@@ -351,6 +351,9 @@ def run_gpu(args, world, rank, local, dist):
             "peak_source": "measured FFMA issue rate (tcp_fp32_peak) on this GPU, not MEASURED_PEAKS.json "
                            "(which has HBM and bf16 only)",
             "sfu_frac": sfu_frac, "pair_kernel_ms": pair_ms,
+            # the same launch timed by the autotuner alone (no reciprocal chain beside it)
+            "pair_kernel_alone_ms": float(variant_ms[variant]),
+            "frac_alone": recipe * units / (float(variant_ms[variant]) * 1e-3) / peak if variant_ms[variant] > 0 else None,
             "grid_reserve": reserve, "reserve_ms": reserve_ms}
 
     # CPU baseline (rank 0, N = 1 only) and the FP32C force error vs the oracle

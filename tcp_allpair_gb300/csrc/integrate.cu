@@ -44,24 +44,33 @@ struct IntArgs {
     int4 *xq;
     double4_32a *xd;
     longlong4_32a *xl;
+    int copies;              // pair-kernel copies to refresh: kCopyXq | kCopyXd | kCopyXl
     int nel, n;
     double xm0, xm1;
     double L0, L1, L2;
     double iL0, iL1, iL2;    // 1/L
 };
 
+// The copies a context's kernels read: the FP32C kernels the 32-bit fixed
+// point, the FP64 kernels the doubles (ordered-pair and derivative kernels) and
+// the 64-bit fixed point (Newton-3 kernels).
+enum { kCopyXq = 1, kCopyXd = 2, kCopyXl = 4 };
+
 __device__ __forceinline__ void store_pos(const IntArgs &a, int i, double x0, double x1, double x2) {
     a.x[i] = x0;
     a.x[(size_t)a.n + i] = x1;
     a.x[2 * (size_t)a.n + i] = x2;
-    a.xq[i] = make_int4(fixed_coord(x0, a.iL0), fixed_coord(x1, a.iL1), fixed_coord(x2, a.iL2), 0);
-    a.xd[i] = make_double4_32a(x0, x1, x2, 0.0);
-    longlong4_32a q;
-    q.x = fixed_coord64(x0, a.iL0);
-    q.y = fixed_coord64(x1, a.iL1);
-    q.z = fixed_coord64(x2, a.iL2);
-    q.w = 0;
-    a.xl[i] = q;
+    if (a.copies & kCopyXq)
+        a.xq[i] = make_int4(fixed_coord(x0, a.iL0), fixed_coord(x1, a.iL1), fixed_coord(x2, a.iL2), 0);
+    if (a.copies & kCopyXd) a.xd[i] = make_double4_32a(x0, x1, x2, 0.0);
+    if (a.copies & kCopyXl) {
+        longlong4_32a q;
+        q.x = fixed_coord64(x0, a.iL0);
+        q.y = fixed_coord64(x1, a.iL1);
+        q.z = fixed_coord64(x2, a.iL2);
+        q.w = 0;
+        a.xl[i] = q;
+    }
 }
 
 // x - L DNINT(x/L) (vverlet.f90:153); x/L from the reciprocal with one FMA
@@ -436,6 +445,7 @@ static IntArgs int_args(tcp_ctx *c) {
     a.xq = c->xq;
     a.xd = c->xd;
     a.xl = c->xl;
+    a.copies = c->p.precision == TCP_PREC_FP32C ? kCopyXq : (kCopyXd | kCopyXl);
     a.nel = c->nel;
     a.n = c->n;
     a.xm0 = c->p.xm[0];
