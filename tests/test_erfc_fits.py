@@ -1,0 +1,82 @@
+"""The erfc approximations compiled into the pair kernels, read from their
+source tables and evaluated on the CPU against scipy's erfc: the FP32 fit
+(pair_math.cuh TCP_ERFC_Q, float32 Horner as the kernels evaluate it) and the
+FP64 fit (kErfc64Q, the Gaussian factor times t Q(s))."""
+import pathlib
+import re
+
+import numpy as np
+import pytest
+from scipy.special import erfc
+
+CSRC = pathlib.Path(__file__).resolve().parents[1] / "tcp_allpair_gb300" / "csrc"
+SRC = (CSRC / "pair_math.cuh").read_text()
+
+
+def _floats(block):
+    return [float(v.rstrip("f")) for v in re.findall(r"-?\d+\.\d+e[-+]\d+f?|-?\d+\.\d+", block)]
+
+
+def fp32_table():
+    p = float(re.search(r"constexpr double kErfcP = ([0-9.]+);", SRC).group(1))
+    deg = int(re.search(r"constexpr int kErfcDeg = (\d+);", SRC).group(1))
+    block = re.search(r"#define TCP_ERFC_Q\s*\\\s*\{(.*?)\}", SRC, re.S).group(1)
+    c = _floats(block)
+    assert len(c) == deg + 1
+    return p, c
+
+
+def fp64_table():
+    block = re.search(r"kErfc64Q\[17\] = \{(.*?)\};", SRC, re.S).group(1)
+    c = _floats(block)
+    p = float(re.search(r"kErfc64P = ([0-9.]+)", SRC).group(1))
+    xmax = float(re.search(r"kErfc64XMax = ([0-9.]+)", SRC).group(1))
+    return p, xmax, c
+
+
+def test_fp32_fit_in_float32():
+    p, c = fp32_table()
+    x = np.linspace(0.0, 4.5, 100001).astype(np.float32)
+    t = (np.float32(1.0) / (np.float32(1.0) + np.float32(p) * x)).astype(np.float32)
+    q = np.full_like(t, np.float32(c[0]))
+    for ck in c[1:]:   # fused multiply-add: exact product, one rounding
+        q = (q.astype(np.float64) * t.astype(np.float64) + np.float64(np.float32(ck))).astype(np.float32)
+    approx = np.exp(-x.astype(np.float64) ** 2) * (t.astype(np.float64) * q.astype(np.float64))
+    ref = erfc(x.astype(np.float64))
+    rel = np.abs(approx - ref) / ref
+    assert rel.max() < 6e-7
+    assert np.sqrt(np.mean(rel ** 2)) < 2e-7
+
+
+def test_fp64_fit():
+    p, xmax, c = fp64_table()
+    assert len(c) == 17
+    t0 = 1.0 / (1.0 + p * xmax)
+    x = np.linspace(0.0, xmax, 20001)
+    t = 1.0 / (1.0 + p * x)
+    s = (2.0 * t - (1.0 + t0)) / (1.0 - t0)
+    q = np.full_like(s, c[-1])
+    for ck in c[-2::-1]:
+        q = q * s + ck
+    approx = np.exp(-x * x) * t * q
+    rel = np.abs(approx - erfc(x)) / erfc(x)
+    assert rel.max() < 6e-15
+
+
+@pytest.mark.parametrize("y", [1e-6, 0.01, 0.1, 0.25])
+def test_kelbg_close_series(y):
+    """The Taylor forms of kelbg_close (pair_math.cuh) against direct FP64."""
+    from scipy.special import erf
+    z = np.linspace(1e-6, 0.25, 200)
+    x = np.sqrt(z)
+    one_m_g = -np.expm1(-y)
+    ser = y * (((((-y / 720 + 1 / 120) * y - 1 / 24) * y + 1 / 6) * y - 0.5) * y + 1)
+    assert abs(ser - one_m_g) / one_m_g < 1e-7
+    H = [2.63393830e-05, -2.08959105e-04, 1.44663996e-03, -8.54832702e-03, 4.17918210e-02,
+         -1.61197024e-01, 4.51351667e-01, -7.52252778e-01]
+    block = re.search(r"float hz = (.*?)num_f", SRC, re.S).group(1)
+    assert _floats(block) == pytest.approx(H, rel=1e-8)
+    hz = np.polyval(H, z)
+    h = x * z * hz
+    href = 2 / np.sqrt(np.pi) * x * np.exp(-z) - erf(x)
+    assert np.max(np.abs(h - href) / np.abs(href)) < 1e-7
