@@ -618,9 +618,9 @@ int pair_setup(tcp_ctx *c) {
 
 int launch_pair(tcp_ctx *c, bool energy, bool rdf) {
     const bool fp64 = c->p.precision == TCP_PREC_FP64;
-    if (!rdf && n3_applicable(c)) {
+    if (n3_applicable(c)) {
         c->fpart_splits = 1;
-        return launch_pair_n3(c, energy);
+        return launch_pair_n3(c, energy, rdf);
     }
     if (!rdf && n3_f64_applicable(c)) {
         c->fpart_splits = 1;

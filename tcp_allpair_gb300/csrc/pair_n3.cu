@@ -177,13 +177,25 @@ __device__ __forceinline__ float2 erfc_poly2(float2 t) {
     return __fmul2_rn(q, t);
 }
 
-template <int KIND, bool ENERGY, bool MASKED>
+// RDF: +2 per unique pair inside rc in bin INT(r/dx) <= kNdist of this pair
+// type (the ordered-pair kernels add 1 from each side), in a CTA histogram
+template <bool RDF>
+__device__ __forceinline__ void rdf_add(unsigned *hist, float inv_dx, float r, bool ok) {
+    if (RDF && ok) {
+        const int bin = (int)(r * inv_dx);
+        if (bin <= kNdist) atomicAdd(&hist[bin], 2u);
+    }
+}
+
+template <int KIND, bool ENERGY, bool MASKED, bool RDF = false>
 __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, bool ok0, bool ok1, bool near_any,
-                                             float2 &pe) {
+                                             float2 &pe, unsigned *hist = nullptr, float inv_dx = 0.f) {
     const float2 r2s = MASKED ? make_float2(ok0 ? r2.x : 1.0f, ok1 ? r2.y : 1.0f) : r2;
     const float2 rinv = make_float2(rsqrt_approx(r2s.x), rsqrt_approx(r2s.y));
     const float2 rinv_m = make_float2(ok0 ? rinv.x : 0.0f, ok1 ? rinv.y : 0.0f);
     const float2 r = __fmul2_rn(r2s, rinv);
+    rdf_add<RDF>(hist, inv_dx, r.x, ok0);
+    rdf_add<RDF>(hist, inv_dx, r.y, ok1);
     const float2 ta = __ffma2_rn(f2(c.u_p_alpha), r, f2(1.0f));
     const float2 t = make_float2(rcp_approx(ta.x), rcp_approx(ta.y));
     const float2 ea = __fmul2_rn(f2(c.u_c_exp), r2s);
@@ -234,10 +246,11 @@ __device__ __forceinline__ float idiff(int a, int b) { return (float)(int)((unsi
 // LDSJ: j positions read from a warp-private copy of the chunk written twice
 // in a row (jb[64]), so that step s reads jb[lane + s] with one shared load
 // instead of rotating them with three shuffles; the reactions still rotate.
-template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R, bool LDSJ = false>
+template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R, bool LDSJ = false, bool RDF = false>
 __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__restrict__ tj, int cnt, int jstart,
                                            const int4 (&xi)[R], int ibase, int iend,
-                                           float (*sjacc)[3], float (&p)[R][3], float &pe, int4 *jb = nullptr) {
+                                           float (*sjacc)[3], float (&p)[R][3], float &pe, int4 *jb = nullptr,
+                                           unsigned *hist = nullptr, float inv_dx = 0.f) {
     static_assert(R % 2 == 0, "paired form needs an even number of i-particles per lane");
     constexpr int G = R / 2;
     const int lane = threadIdx.x & 31;
@@ -281,7 +294,8 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
             if (KIND == 2) near_any = __any_sync(0xffffffffu, r2min < c.u_rshort2);
 #pragma unroll
             for (int g = 0; g < G; ++g) {
-                const float2 w = n3_pair_x2<KIND, ENERGY, MASKED>(c, r2[g], ok[2 * g], ok[2 * g + 1], near_any, pe2);
+                const float2 w = n3_pair_x2<KIND, ENERGY, MASKED, RDF>(c, r2[g], ok[2 * g], ok[2 * g + 1], near_any,
+                                                                     pe2, hist, inv_dx);
                 pg[g][0] = __ffma2_rn(w, d[g][0], pg[g][0]);
                 pg[g][1] = __ffma2_rn(w, d[g][1], pg[g][1]);
                 pg[g][2] = __ffma2_rn(w, d[g][2], pg[g][2]);
@@ -321,9 +335,10 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
 // accumulators in shared memory; 2: as 1 with j positions read from shared
 // memory (LDSJ).
 // W: warps per CTA (i-tile = 32 R W particles).
-template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH, int MODE = 0, int W = kN3Warps>
+template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH, int MODE = 0, int W = kN3Warps, bool RDF = false>
 __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
     static_assert(W >= 4, "the reaction flush needs at least kN3Sub threads");
+    static_assert(!RDF || (MODE >= 1 && !BATCH), "RDF histograms: packed single-system forms");
     constexpr int NT = 32 * W;
     constexpr bool X2 = MODE >= 1;
     constexpr bool SACC = MODE >= 1;
@@ -334,6 +349,7 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
     __shared__ float sjacc[kN3Sub][3];
     __shared__ double red[32];
     __shared__ long long s_next;
+    __shared__ unsigned hist[RDF ? 3 * kNbin : 1];
     // per-thread TwoSum (hi, lo) i-force accumulators, touched once per item:
     // in shared memory ([slot][thread], conflict-free) for the packed forms,
     // whose constant pairs need the registers
@@ -347,6 +363,8 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
     const int nst = (int)(it1 - it0);
 
     for (int k = tid; k < kN3Sub * 3; k += NT) (&sjacc[0][0])[k] = 0.f;
+    if (RDF)
+        for (int k = tid; k < 3 * kNbin; k += NT) hist[k] = 0u;
     if (tid == 0) {
         for (int s = 0; s < kN3Stages; ++s) mbar_init(&bars[s], 1);
         fence_mbar_init();
@@ -443,7 +461,7 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
 #define TCP_N3_ITEM(KIND, MASKED)                                                                      \
     do {                                                                                                \
         if (X2)                                                                                         \
-            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R, MODE == 2>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe, jbuf[MODE == 2 ? warp : 0]); \
+            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R, MODE == 2, RDF>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe, jbuf[MODE == 2 ? warp : 0], RDF ? hist + pt * kNbin : nullptr, RDF ? c.u_inv_dx[pt] : 0.f); \
         else                                                                                            \
             n3_item<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe);    \
     } while (0)
@@ -532,6 +550,11 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
         const double tot = block_sum(etot, red);
         if (tid == 0) a.upart[blockIdx.x] = tot;
     }
+    if (RDF) {
+        __syncthreads();
+        for (int q = tid; q < 3 * kNbin; q += NT)
+            if (hist[q]) atomicAdd(&a.rdf[q], (unsigned long long)hist[q]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -565,6 +588,17 @@ static const N3Variant kVariants[] = {
 };
 constexpr int kN3Variants = sizeof(kVariants) / sizeof(kVariants[0]);
 
+// Forms that also accumulate the RDF histograms (steps with TCP_FLAG_RDF,
+// which the reference accumulates in every force call): the two best packed
+// forms of the variants above; TCP_RDF_VARIANT=k picks one (default 0).
+static const N3Variant kRdfVariants[] = {
+    {pair_n3_kernel<true, 4, 1, 3, false, 2, 8, true>, pair_n3_kernel<false, 4, 1, 3, false, 2, 8, true>, 4, 8,
+     "n3_r4_u1_b3_x2l_rdf"},
+    {pair_n3_kernel<true, 4, 1, 2, false, 1, 8, true>, pair_n3_kernel<false, 4, 1, 2, false, 1, 8, true>, 4, 8,
+     "n3_r4_u1_b2_x2_rdf"},
+};
+constexpr int kN3RdfVariants = sizeof(kRdfVariants) / sizeof(kRdfVariants[0]);
+
 int n3_variant_count() { return kN3Variants; }
 const char *n3_variant_name(int v) { return v >= 1 && v <= kN3Variants ? kVariants[v - 1].name : "ordered"; }
 
@@ -574,9 +608,16 @@ int n3_grid_for(const tcp_ctx *c, int v) {
     return std::max(1, c->num_sms * std::max(1, bps));
 }
 
+static int kernel_grid(const tcp_ctx *c, N3Kernel k, int threads) {
+    int bps = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, threads, 0);
+    return std::max(1, c->num_sms * std::max(1, bps));
+}
+
 int n3_grid(const tcp_ctx *c) {
     int g = 1;
     for (int v = 1; v <= kN3Variants; ++v) g = std::max(g, n3_grid_for(c, v));
+    for (int v = 0; v < kN3RdfVariants; ++v) g = std::max(g, kernel_grid(c, kRdfVariants[v].energy, 32 * kRdfVariants[v].W));
     return g;
 }
 
@@ -598,10 +639,13 @@ N3Geom n3_geometry(int off, int nel, int nion, int tile, long long item0, long l
     return g;
 }
 
-int launch_pair_n3(tcp_ctx *c, bool energy) {
+int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf) {
+    int rv = 0;
+    if (const char *forced = getenv("TCP_RDF_VARIANT")) rv = std::min(std::max(atoi(forced), 0), kN3RdfVariants - 1);
     const int v = std::min(std::max(c->pair_variant, 1), kN3Variants);
-    const int tile = 32 * kVariants[v - 1].R * kVariants[v - 1].W;
-    const int nt = 32 * kVariants[v - 1].W;
+    const N3Variant &K = rdf ? kRdfVariants[rv] : kVariants[v - 1];
+    const int tile = 32 * K.R * K.W;
+    const int nt = 32 * K.W;
     N3Args a;
     std::memset(&a, 0, sizeof a);
     long long total = 0;
@@ -616,17 +660,19 @@ int launch_pair_n3(tcp_ctx *c, bool energy) {
     a.counter = c->counter;
     a.c = c->pc;
     a.inject_skip = inject_fault("tile_wait") ? 1 : 0;
+    a.rdf = c->rdf;
     // CTAs left free for the reciprocal chain when it runs beside this launch
     const int reserve = c->recip_beside ? c->pair_reserve : 0;
-    const int grid = (int)std::min<long long>(std::max(1, n3_grid_for(c, v) - reserve), total);
+    const int full = rdf ? kernel_grid(c, K.energy, nt) : n3_grid_for(c, v);
+    const int grid = (int)std::min<long long>(std::max(1, full - reserve), total);
     if (grid > c->n_upart) return set_error(TCP_ERR_STATE, "energy partial buffer smaller than the Newton-3 grid");
     TCP_CUDA(cudaMemsetAsync(c->fpart, 0, sizeof(double) * 3 * (size_t)c->n, c->stream));
     TCP_CUDA(cudaMemsetAsync(c->counter, 0, sizeof(unsigned), c->stream));
     if (energy) {
         TCP_CUDA(cudaMemsetAsync(c->upart, 0, sizeof(double) * (size_t)c->n_upart, c->stream));
-        kVariants[v - 1].energy<<<grid, nt, 0, c->stream>>>(a);
+        K.energy<<<grid, nt, 0, c->stream>>>(a);
     } else {
-        kVariants[v - 1].plain<<<grid, nt, 0, c->stream>>>(a);
+        K.plain<<<grid, nt, 0, c->stream>>>(a);
     }
     c->launches++;
     TCP_CUDA(cudaGetLastError());

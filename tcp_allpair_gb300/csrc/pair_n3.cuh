@@ -49,6 +49,7 @@ struct N3Args {
     int nrep;
     double *ur_rep;       // batch: Ur per replica (zeroed before the launch)
     int inject_skip;      // test hook: CTA 0 never issues the copy of its first item (its bounded wait runs out)
+    unsigned long long *rdf;   // RDF variants: [3][kNbin] pair counts, +2 per unique pair (force.f90:99-103)
 };
 
 template <int TILE>

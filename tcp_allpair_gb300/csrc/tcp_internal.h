@@ -217,7 +217,7 @@ int n3_variant_count();
 const char *n3_variant_name(int v);
 int autotune_pair(tcp_ctx *c);
 int time_pair_with_recip(tcp_ctx *c, int reps, double *ms);   // ctx.cu
-int launch_pair_n3(tcp_ctx *c, bool energy);
+int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf);
 int n3_batch_variant_count();
 const char *n3_batch_variant_name(int v);
 int n3_batch_tile(int variant);

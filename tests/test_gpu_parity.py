@@ -437,3 +437,28 @@ def test_fp32c_newton3_ragged_species(monkeypatch, variant, nel, nion):
         assert c.autotune_report()[0] == variant
     assert oracle.rms_rel(f, fo) < FP32_FORCE_RMS
     assert ur == pytest.approx(uo, rel=2e-5, abs=1e-9)
+
+
+@pytest.mark.parametrize("rdf_variant", [0, 1])
+def test_fp32c_newton3_rdf_histograms(monkeypatch, rdf_variant):
+    """RDF counts of the packed Newton-3 forms (+2 per unique pair inside rc,
+    force.f90:99-103) against the FP64 oracle's: an FP32 separation (relative
+    error ~1e-7) moves a pair within that distance of a bin edge to the
+    neighbouring bin (about 3e-5 of the pairs here, 500 bins), so the totals
+    per pair type agree to a few pairs (those at rc) and the bins to 1e-4 of the
+    counts; forces and energy as without the histograms."""
+    monkeypatch.setenv("TCP_PAIR_VARIANT", "11")
+    monkeypatch.setenv("TCP_RDF_VARIANT", str(rdf_variant))
+    s = make(4096, seed=13, K=16)
+    o = oracle.Oracle.from_system(s, ei="kelbg")
+    fo, uo, h = o.force_direct(s.x, rdf=True)
+    with ctx_for(s, precision="fp32c", ei="kelbg", recip="none") as c:
+        c.set_flags(T.FLAG_ENERGY | T.FLAG_RDF)
+        ur = c.Force_direct_self()
+        _, _, f, _ = c.download(x=False, v=False, f=True)
+        rdf, _ = c.histograms(reset=True)
+    for t in range(3):
+        assert abs(int(rdf[t].sum()) - int(h[t].sum())) <= 8
+    assert np.abs(rdf.astype(np.int64) - h.astype(np.int64)).sum() <= 1e-4 * h.sum()
+    assert oracle.rms_rel(f, fo) < FP32_FORCE_RMS
+    assert ur == pytest.approx(uo, rel=2e-5)
