@@ -622,9 +622,9 @@ int launch_pair(tcp_ctx *c, bool energy, bool rdf) {
         c->fpart_splits = 1;
         return launch_pair_n3(c, energy, rdf);
     }
-    if (!rdf && n3_f64_applicable(c)) {
+    if (n3_f64_applicable(c)) {
         c->fpart_splits = 1;
-        return launch_pair_n3_f64(c, energy);
+        return launch_pair_n3_f64(c, energy, rdf);
     }
     c->fpart_splits = c->jsplit;
     Geometry g = geometry(c, fp64);

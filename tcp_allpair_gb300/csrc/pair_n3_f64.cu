@@ -78,10 +78,13 @@ __device__ __forceinline__ double fixed_diff(long long a, long long b, double sc
 
 // One item: the R i-particles of this lane against a j-subtile in shared
 // memory.  MASKED: apply validity and i < j index masks.
-template <int KIND, bool ENERGY, bool MASKED, int R>
+// RDF: +2 per unique pair inside rc in bin INT(r/dx) of its type, r from sqrt
+// as in the ordered FP64 kernel (force.f90:99-103)
+template <int KIND, bool ENERGY, bool MASKED, int R, bool RDF = false>
 __device__ __forceinline__ void n3_item_f64(const PairConsts &c, const longlong4_32a *__restrict__ tj, int cnt,
                                             int jstart, const longlong3 (&xi)[R], int ibase, int iend,
-                                            double (*sjacc)[3], double (&p)[R][3], double &pe) {
+                                            double (*sjacc)[3], double (&p)[R][3], double &pe,
+                                            unsigned *hist = nullptr, double inv_dx = 0.0) {
     const int lane = threadIdx.x & 31;
     const int src = (lane + 1) & 31;
     for (int ch = 0; ch * 32 < cnt; ++ch) {
@@ -105,6 +108,10 @@ __device__ __forceinline__ void n3_item_f64(const PairConsts &c, const longlong4
                     const int jo = ch * 32 + ((lane + s) & 31);
                     const int ir = ibase + 32 * r;
                     ok = ok && (ir < iend) && (jo < cnt) && (ir < jstart + jo);
+                }
+                if (RDF && ok) {
+                    const double tb = sqrt(r2) * inv_dx;
+                    if (tb < (double)kNbin) atomicAdd(&hist[(int)tb], 2u);
                 }
                 const double w = n3_pair_f64<KIND, ENERGY>(c, ok ? r2 : 1.0, ok, pe);
                 p[r][0] = fma(w, dx, p[r][0]);
@@ -130,7 +137,7 @@ __device__ __forceinline__ void n3_item_f64(const PairConsts &c, const longlong4
     }
 }
 
-template <bool ENERGY, int R>
+template <bool ENERGY, int R, bool RDF = false>
 __global__ void __launch_bounds__(kN3Threads) pair_n3_f64_kernel(const N3Args a) {
     constexpr int TILE = 32 * R * kN3Warps;
     __shared__ __align__(128) longlong4_32a tiles[kN3Stages][kN3Sub];
@@ -138,7 +145,10 @@ __global__ void __launch_bounds__(kN3Threads) pair_n3_f64_kernel(const N3Args a)
     __shared__ double sjacc[kN3Sub][3];
     __shared__ double red[32];
     __shared__ long long s_next;
+    __shared__ unsigned hist[RDF ? 3 * kNbin : 1];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (RDF)
+        for (int k = tid; k < 3 * kNbin; k += kN3Threads) hist[k] = 0u;
 
     const long long it0 = a.nstatic * (long long)blockIdx.x / gridDim.x;
     const long long it1 = a.nstatic * (long long)(blockIdx.x + 1) / gridDim.x;
@@ -215,7 +225,8 @@ __global__ void __launch_bounds__(kN3Threads) pair_n3_f64_kernel(const N3Args a)
         const int kind = pt == 1 ? (c.ei_model == TCP_EI_DEUTSCH ? 1 : (c.ei_model == TCP_EI_KELBG ? 2 : 0)) : 0;
         if (ok) {
 #define TCP_N3D_ITEM(KIND, MASKED) \
-    n3_item_f64<KIND, ENERGY, MASKED, R>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe)
+    n3_item_f64<KIND, ENERGY, MASKED, R, RDF>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe, \
+                                              RDF ? hist + pt * kNbin : nullptr, RDF ? c.inv_dxd[pt] : 0.0)
             if (masked) {
                 if (kind == 1) TCP_N3D_ITEM(1, true);
                 else if (kind == 2) TCP_N3D_ITEM(2, true);
@@ -291,6 +302,11 @@ __global__ void __launch_bounds__(kN3Threads) pair_n3_f64_kernel(const N3Args a)
         const double tot = block_sum(etot, red);
         if (tid == 0) a.upart[blockIdx.x] = tot;
     }
+    if (RDF) {
+        __syncthreads();
+        for (int q = tid; q < 3 * kNbin; q += kN3Threads)
+            if (hist[q]) atomicAdd(&a.rdf[q], (unsigned long long)hist[q]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -304,7 +320,7 @@ int n3_f64_grid(const tcp_ctx *c) {
     return std::max(1, c->num_sms * std::max(1, bps));
 }
 
-int launch_pair_n3_f64(tcp_ctx *c, bool energy) {
+int launch_pair_n3_f64(tcp_ctx *c, bool energy, bool rdf) {
     constexpr int tile = 32 * kF64R * kN3Warps;
     N3Args a;
     std::memset(&a, 0, sizeof a);
@@ -322,15 +338,18 @@ int launch_pair_n3_f64(tcp_ctx *c, bool energy) {
     a.counter = c->counter;
     a.c = c->pc;
     a.inject_skip = inject_fault("tile_wait") ? 1 : 0;
+    a.rdf = c->rdf;
     const int grid = (int)std::min<long long>(n3_f64_grid(c), total);
     if (grid > c->n_upart) return set_error(TCP_ERR_STATE, "energy partial buffer smaller than the Newton-3 grid");
     TCP_CUDA(cudaMemsetAsync(c->fpart, 0, sizeof(double) * 3 * (size_t)c->n, c->stream));
     TCP_CUDA(cudaMemsetAsync(c->counter, 0, sizeof(unsigned), c->stream));
     if (energy) {
         TCP_CUDA(cudaMemsetAsync(c->upart, 0, sizeof(double) * (size_t)c->n_upart, c->stream));
-        pair_n3_f64_kernel<true, kF64R><<<grid, kN3Threads, 0, c->stream>>>(a);
+        if (rdf) pair_n3_f64_kernel<true, kF64R, true><<<grid, kN3Threads, 0, c->stream>>>(a);
+        else pair_n3_f64_kernel<true, kF64R><<<grid, kN3Threads, 0, c->stream>>>(a);
     } else {
-        pair_n3_f64_kernel<false, kF64R><<<grid, kN3Threads, 0, c->stream>>>(a);
+        if (rdf) pair_n3_f64_kernel<false, kF64R, true><<<grid, kN3Threads, 0, c->stream>>>(a);
+        else pair_n3_f64_kernel<false, kF64R><<<grid, kN3Threads, 0, c->stream>>>(a);
     }
     c->launches++;
     TCP_CUDA(cudaGetLastError());

@@ -211,7 +211,7 @@ int launch_force_finalize(tcp_ctx *c, bool add_rec);
 bool n3_applicable(const tcp_ctx *c);
 bool n3_f64_applicable(const tcp_ctx *c);
 int n3_f64_grid(const tcp_ctx *c);
-int launch_pair_n3_f64(tcp_ctx *c, bool energy);
+int launch_pair_n3_f64(tcp_ctx *c, bool energy, bool rdf);
 int n3_grid(const tcp_ctx *c);
 int n3_variant_count();
 const char *n3_variant_name(int v);
