@@ -28,6 +28,10 @@ MODULE TCP_GPU
 
   TYPE(C_PTR), SAVE :: ctx = C_NULL_PTR
 
+  ! tcp_set_flags bits (include/tcp_gpu.h)
+  INTEGER(C_INT), PARAMETER :: TCP_FLAG_RDF = 1, TCP_FLAG_VDF = 2, TCP_FLAG_ENERGY = 4, &
+       TCP_FLAG_DETERMINISTIC = 8
+
   INTERFACE
      INTEGER(C_INT) FUNCTION tcp_create(p, nel, nion, device, out) BIND(C, NAME='tcp_create')
        IMPORT :: C_INT, C_PTR, tcp_params
@@ -80,6 +84,11 @@ MODULE TCP_GPU
        TYPE(C_PTR), VALUE :: c
        REAL(C_DOUBLE), VALUE :: dt
        REAL(C_DOUBLE), INTENT(OUT) :: mv2el, mv2ion
+     END FUNCTION
+     INTEGER(C_INT) FUNCTION tcp_set_flags(c, flags) BIND(C, NAME='tcp_set_flags')
+       IMPORT :: C_INT, C_PTR
+       TYPE(C_PTR), VALUE :: c
+       INTEGER(C_INT), VALUE :: flags
      END FUNCTION
      INTEGER(C_INT) FUNCTION tcp_histograms(c, rdf, vdf, reset) BIND(C, NAME='tcp_histograms')
        IMPORT :: C_INT, C_PTR, C_DOUBLE
@@ -143,6 +152,22 @@ CONTAINS
          "tcp_upload")
   END SUBROUTINE
 
+  ! NS%RDF_* / NS%VDF_* += the device histograms since the last pull, which are
+  ! then zeroed; called before DUMP (main.f90:155-157), which reads and
+  ! resets the NS arrays (result.f90:209-278)
+  SUBROUTINE tcp_pull_histograms(NS)
+    TYPE(NM) :: NS
+    REAL(C_DOUBLE) :: rdf(3 * SIZE(NS%RDF_ee)), vdf(2 * SIZE(NS%VDF_e))
+    INTEGER :: m
+    m = SIZE(NS%RDF_ee)
+    CALL tcp_stop_on(tcp_histograms(ctx, rdf, vdf, 1_C_INT), "tcp_histograms")
+    NS%RDF_ee = NS%RDF_ee + rdf(1:m)
+    NS%RDF_ei = NS%RDF_ei + rdf(m + 1:2 * m)
+    NS%RDF_ii = NS%RDF_ii + rdf(2 * m + 1:3 * m)
+    NS%VDF_e = NS%VDF_e + vdf(1:m)
+    NS%VDF_i = NS%VDF_i + vdf(m + 1:2 * m)
+  END SUBROUTINE
+
   SUBROUTINE tcp_pull(species, rec, n)
     INTEGER, INTENT(IN) :: species, n
     TYPE(PT), TARGET, INTENT(INOUT) :: rec(n)
@@ -179,7 +204,11 @@ SUBROUTINE EWALD_SELF(NS, param, sys, PSI, COMM)
   IF (param%thermo == 'ISOKIN') p%thermo = 1
   IF (param%thermo == 'BEREND') p%thermo = 2
   IF (param%thermo == 'STOCH ') p%thermo = 3
-  IF (.NOT. C_ASSOCIATED(ctx)) CALL tcp_stop_on(tcp_create(p, NS%NTel, NS%NTion, 0, ctx), "tcp_create")
+  IF (.NOT. C_ASSOCIATED(ctx)) THEN
+    CALL tcp_stop_on(tcp_create(p, NS%NTel, NS%NTion, 0, ctx), "tcp_create")
+    ! the reference accumulates RDF and VDF in every force call and kick
+    CALL tcp_stop_on(tcp_set_flags(ctx, IOR(IOR(TCP_FLAG_RDF, TCP_FLAG_VDF), TCP_FLAG_ENERGY)), "tcp_set_flags")
+  END IF
   CALL tcp_stop_on(tcp_ewald_self(ctx, a, uo), "EWALD_SELF")
   param%a = a
   param%rc2 = param%rc**2
