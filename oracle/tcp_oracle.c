@@ -93,7 +93,7 @@ static inline double pair_deutsch(double a, double rs, double qq, double r2, dou
     return qq * (x - y) / r;
 }
 
-/* Kelbg e-i pair (BASELINE model, not in the reference):
+/* Kelbg e-i pair (an extension of the reference, which has Deutsch):
  *   V = qq [erfc(ar)/r - exp(-r^2/l^2)/r + sqrt(pi) erfc(r/l)/l]
  *   -dV/dr / r = qq [erfc(ar) + 2ar/sqrt(pi) exp(-a^2 r^2) - exp(-r^2/l^2)] / r^3 */
 static inline double pair_kelbg(double a, double lam, double qq, double r2, double r, double *df) {
