@@ -178,24 +178,28 @@ __device__ __forceinline__ float2 erfc_poly2(float2 t) {
 }
 
 // RDF: +2 per unique pair inside rc in bin INT(r/dx) <= kNdist of this pair
-// type (the ordered-pair kernels add 1 from each side), in a CTA histogram
+// type (the ordered-pair kernels add 1 from each side), in a CTA histogram.
+// Branch-free: a pair that does not count adds to its lane's spare slot
+// (kRdfSpare + lane, never flushed), so every lane issues the same atomic.
+constexpr int kRdfSpare = 3 * kNbin;
 template <bool RDF>
-__device__ __forceinline__ void rdf_add(unsigned *hist, float inv_dx, float r, bool ok) {
-    if (RDF && ok) {
+__device__ __forceinline__ void rdf_add(unsigned *hist, int off, float inv_dx, float r, bool ok) {
+    if (RDF) {
         const int bin = (int)(r * inv_dx);
-        if (bin <= kNdist) atomicAdd(&hist[bin], 2u);
+        const int idx = (ok && bin <= kNdist) ? off + bin : kRdfSpare + (int)(threadIdx.x & 31);
+        atomicAdd(&hist[idx], 2u);
     }
 }
 
 template <int KIND, bool ENERGY, bool MASKED, bool RDF = false>
 __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, bool ok0, bool ok1, bool near_any,
-                                             float2 &pe, unsigned *hist = nullptr, float inv_dx = 0.f) {
+                                             float2 &pe, unsigned *hist = nullptr, int hoff = 0, float inv_dx = 0.f) {
     const float2 r2s = MASKED ? make_float2(ok0 ? r2.x : 1.0f, ok1 ? r2.y : 1.0f) : r2;
     const float2 rinv = make_float2(rsqrt_approx(r2s.x), rsqrt_approx(r2s.y));
     const float2 rinv_m = make_float2(ok0 ? rinv.x : 0.0f, ok1 ? rinv.y : 0.0f);
     const float2 r = __fmul2_rn(r2s, rinv);
-    rdf_add<RDF>(hist, inv_dx, r.x, ok0);
-    rdf_add<RDF>(hist, inv_dx, r.y, ok1);
+    rdf_add<RDF>(hist, hoff, inv_dx, r.x, ok0);
+    rdf_add<RDF>(hist, hoff, inv_dx, r.y, ok1);
     const float2 ta = __ffma2_rn(f2(c.u_p_alpha), r, f2(1.0f));
     const float2 t = make_float2(rcp_approx(ta.x), rcp_approx(ta.y));
     const float2 ea = __fmul2_rn(f2(c.u_c_exp), r2s);
@@ -250,7 +254,7 @@ template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R, bool LDSJ = fal
 __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__restrict__ tj, int cnt, int jstart,
                                            const int4 (&xi)[R], int ibase, int iend,
                                            float (*sjacc)[3], float (&p)[R][3], float &pe, int4 *jb = nullptr,
-                                           unsigned *hist = nullptr, float inv_dx = 0.f) {
+                                           unsigned *hist = nullptr, int hoff = 0, float inv_dx = 0.f) {
     static_assert(R % 2 == 0, "paired form needs an even number of i-particles per lane");
     constexpr int G = R / 2;
     const int lane = threadIdx.x & 31;
@@ -295,7 +299,7 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
 #pragma unroll
             for (int g = 0; g < G; ++g) {
                 const float2 w = n3_pair_x2<KIND, ENERGY, MASKED, RDF>(c, r2[g], ok[2 * g], ok[2 * g + 1], near_any,
-                                                                     pe2, hist, inv_dx);
+                                                                     pe2, hist, hoff, inv_dx);
                 pg[g][0] = __ffma2_rn(w, d[g][0], pg[g][0]);
                 pg[g][1] = __ffma2_rn(w, d[g][1], pg[g][1]);
                 pg[g][2] = __ffma2_rn(w, d[g][2], pg[g][2]);
@@ -349,7 +353,7 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
     __shared__ float sjacc[kN3Sub][3];
     __shared__ double red[32];
     __shared__ long long s_next;
-    __shared__ unsigned hist[RDF ? 3 * kNbin : 1];
+    __shared__ unsigned hist[RDF ? kRdfSpare + 32 : 1];
     // per-thread TwoSum (hi, lo) i-force accumulators, touched once per item:
     // in shared memory ([slot][thread], conflict-free) for the packed forms,
     // whose constant pairs need the registers
@@ -364,7 +368,7 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
 
     for (int k = tid; k < kN3Sub * 3; k += NT) (&sjacc[0][0])[k] = 0.f;
     if (RDF)
-        for (int k = tid; k < 3 * kNbin; k += NT) hist[k] = 0u;
+        for (int k = tid; k < kRdfSpare + 32; k += NT) hist[k] = 0u;
     if (tid == 0) {
         for (int s = 0; s < kN3Stages; ++s) mbar_init(&bars[s], 1);
         fence_mbar_init();
@@ -461,7 +465,7 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
 #define TCP_N3_ITEM(KIND, MASKED)                                                                      \
     do {                                                                                                \
         if (X2)                                                                                         \
-            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R, MODE == 2, RDF>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe, jbuf[MODE == 2 ? warp : 0], RDF ? hist + pt * kNbin : nullptr, RDF ? c.u_inv_dx[pt] : 0.f); \
+            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R, MODE == 2, RDF>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe, jbuf[MODE == 2 ? warp : 0], RDF ? hist : nullptr, pt * kNbin, RDF ? c.u_inv_dx[pt] : 0.f); \
         else                                                                                            \
             n3_item<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe);    \
     } while (0)
