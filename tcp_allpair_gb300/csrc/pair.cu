@@ -316,38 +316,42 @@ template <int KIND, bool ENERGY, bool RDF, int TPP>
 __device__ __forceinline__ void tile_f64(const double4_32a *__restrict__ tj, int cnt, int sub, double4_32a xi,
                                          const PairConsts &c, double qq, double &fx, double &fy,
                                          double &fz, double &ue, unsigned *hist, double inv_dx) {
+    // The expressions of force.f90 without divisions (GB300 issues FP64 at 1/64
+    // of the FP32 rate): DNINT of d/box by multiplication with 1/box, 1/r from
+    // rsqrt, and erfc(ar) (the reference's 1 - erf(ar)) and erfc(r/lambda) from
+    // the Gaussians exp(-a^2 r^2) and exp(-r^2/lambda^2) that the force needs
+    // anyway (erfc_gauss, pair_math.cuh).
     const double a = c.alpha;
     for (int jj = sub; jj < cnt; jj += TPP) {
         const double4_32a xj = tj[jj];
         double xr0 = xi.x - xj.x, xr1 = xi.y - xj.y, xr2 = xi.z - xj.z;
-        xr0 = xr0 - c.box[0] * round(xr0 / c.box[0]);    // force.f90:92 (DNINT)
-        xr1 = xr1 - c.box[1] * round(xr1 / c.box[1]);
-        xr2 = xr2 - c.box[2] * round(xr2 / c.box[2]);
+        xr0 = fma(-c.box[0], round(xr0 * c.inv_box[0]), xr0);   // force.f90:92 (DNINT)
+        xr1 = fma(-c.box[1], round(xr1 * c.inv_box[1]), xr1);
+        xr2 = fma(-c.box[2], round(xr2 * c.inv_box[2]), xr2);
         const double r2 = xr0 * xr0 + xr1 * xr1 + xr2 * xr2;
         if (r2 < c.rc2 && r2 > 0.0) {
-            const double r = sqrt(r2);
+            const double rinv = rsqrt(r2), r = r2 * rinv, rinv3 = rinv * rinv * rinv;
+            const double e = exp(-c.alpha2 * r2);
+            const double x = erfc_gauss(a * r, e);
             double df, u;
             if (KIND == 0) {                                   // force.f90:104-106
-                const double x = 1.0 - erf(a * r);
-                df = kEps * qq * (2.0 * exp(-a * a * r2) * a * r / kSqrtPi + x) / r2 / r;
-                u = qq * x / r;
+                df = kEps * qq * fma(c.c_gauss_d * r, e, x) * rinv3;
+                u = qq * x * rinv;
             } else if (KIND == 1) {                            // force.f90:135-139
-                const double x = 1.0 - erf(a * r);
-                const double y = exp(-r / c.rs);
-                df = kEps * qq * ((2.0 * exp(-a * a * r2) * a * r / kSqrtPi + x - y) / r2 / r - y / r2 / c.rs);
-                u = qq * (x - y) / r;
+                const double y = exp(-r * c.inv_rs_d);
+                df = kEps * qq * (fma(c.c_gauss_d * r, e, x) - y - y * r * c.inv_rs_d) * rinv3;
+                u = qq * (x - y) * rinv;
             } else {                                           // Kelbg
-                const double x = erfc(a * r);
-                const double g = exp(-r2 / (c.lambda * c.lambda));
-                df = kEps * qq * (x + 2.0 * a * r / kSqrtPi * exp(-a * a * r2) - g) / (r2 * r);
-                u = qq * (x / r - g / r + kSqrtPi * erfc(r / c.lambda) / c.lambda);
+                const double g = exp(-r2 * c.inv_lam2);
+                df = kEps * qq * (fma(c.c_gauss_d * r, e, x) - g) * rinv3;
+                u = qq * ((x - g) * rinv + c.sqrtpi_lam_d * erfc_gauss(r * c.inv_lam, g));
             }
             fx += df * xr0;
             fy += df * xr1;
             fz += df * xr2;
             if (ENERGY) ue += u;
             if (RDF) {
-                const double tb = r * inv_dx;
+                const double tb = sqrt(r2) * inv_dx;             // INT(r/dx) from the rounded sqrt
                 if (tb < (double)kNbin) atomicAdd(&hist[(int)tb], 1u);
             }
         }
