@@ -198,6 +198,16 @@ int tcp_finit(tcp_ctx *ctx, double dt, tcp_energies *e);
  * removal, vverlet2+thermostat), captured once as a CUDA graph and replayed.
  * e receives the energies of the last step (NULL: not read back). */
 int tcp_md_steps(tcp_ctx *ctx, double dt, int nsteps, tcp_energies *e);
+/* The same steps on the caller's PT records, which main.f90:81-153 updates in
+ * place: the fields given (xx, xv, ff as for tcp_upload; NULL skips one) are
+ * read from the qel and qion records, nsteps steps run, and the same fields
+ * are written back.  Equal to tcp_upload(0) + tcp_upload(1) + tcp_md_steps +
+ * tcp_download(0) + tcp_download(1) with one wait for the device instead of
+ * five.  Every argument is checked before anything runs. */
+int tcp_md_steps_records(tcp_ctx *ctx, double dt, int nsteps,
+                         double *el_xx, double *el_xv, double *el_ff, long el_stride_bytes,
+                         double *ion_xx, double *ion_xv, double *ion_ff, long ion_stride_bytes,
+                         tcp_energies *e);
 /* Energies of the most recent evaluation without launching anything. */
 int tcp_energies_get(tcp_ctx *ctx, tcp_energies *e);
 

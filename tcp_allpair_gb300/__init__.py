@@ -147,6 +147,21 @@ class Context:
         self._chk(self.lib.tcp_md_steps(self.h, dt, nsteps, C.byref(e)), "tcp_md_steps")
         return e.as_dict()
 
+    def md_steps_pt(self, dt, nsteps, qel: np.ndarray, qion: np.ndarray, fields=("xx", "xv", "ff")):
+        """nsteps steps on PT records (data.f90:32-35) updated in place, as
+        main.f90:81-153 updates qel / qion: upload_pt + md_steps + download_pt
+        in one call with one wait for the device."""
+        ptr = []
+        for arr in (qel, qion):
+            offs = {k: arr.dtype.fields[k][1] for k in ("xx", "xv", "ff")}
+            base = arr.ctypes.data
+            live = len(arr) > 0
+            ptr += [C.c_void_p(base + offs[k]) if (live and k in fields) else None for k in ("xx", "xv", "ff")]
+            ptr.append(arr.strides[0] if live else 24)
+        e = TcpEnergies()
+        self._chk(self.lib.tcp_md_steps_records(self.h, dt, nsteps, *ptr, C.byref(e)), "tcp_md_steps_records")
+        return e.as_dict()
+
     def set_flags(self, flags):
         self._chk(self.lib.tcp_set_flags(self.h, flags), "tcp_set_flags")
 

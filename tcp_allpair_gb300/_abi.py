@@ -75,6 +75,8 @@ SIGNATURES = {
     "tcp_vverlet2": (C.c_int, [_CTX, C.c_double, _P, _P]),
     "tcp_finit": (C.c_int, [_CTX, C.c_double, C.POINTER(TcpEnergies)]),
     "tcp_md_steps": (C.c_int, [_CTX, C.c_double, C.c_int, C.POINTER(TcpEnergies)]),
+    "tcp_md_steps_records": (C.c_int, [_CTX, C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_long,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.POINTER(TcpEnergies)]),
     "tcp_energies_get": (C.c_int, [_CTX, C.POINTER(TcpEnergies)]),
     "tcp_histograms": (C.c_int, [_CTX, _P, _P, C.c_int]),
     "tcp_time_component": (C.c_int, [_CTX, C.c_int, C.c_int, C.c_double, _P]),

@@ -443,65 +443,66 @@ int tcp_set_flags(tcp_ctx *c, unsigned flags) {
 }
 
 // ---- transfers ---------------------------------------------------------------
-int tcp_upload(tcp_ctx *c, int species, const double *xx, const double *xv, const double *ff, long stride) {
-    TCP_TRACE("tcp_upload");
-    if (!c || (species != 0 && species != 1)) return set_error(TCP_ERR_BAD_PARAM, "bad ctx or species");
-    cudaSetDevice(c->device);
-    const int count = species == 0 ? c->nel : c->nion, first = species == 0 ? 0 : c->nel;
-    if (count == 0 || (!xx && !xv && !ff)) return TCP_OK;
+// One species' fields in its records: the lowest field address, the byte
+// offset of xx, xv, ff from it (-1: skipped) and the span of bytes touched.
+struct RecSpan {
+    const char *base = nullptr;
+    long off[3] = {-1, -1, -1};
+    size_t span = 0;
+};
+
+static int record_span(int count, const double *xx, const double *xv, const double *ff, long stride, RecSpan &rs) {
+    rs = RecSpan();
     const double *ptrs[3] = {xx, xv, ff};
-    const char *base = nullptr, *top = nullptr;
+    const char *top = nullptr;
     for (const double *q : ptrs)
         if (q) {
             const char *b = reinterpret_cast<const char *>(q);
-            if (!base || b < base) base = b;
+            if (!rs.base || b < rs.base) rs.base = b;
             if (!top || b > top) top = b;
         }
-    if (stride < 24 || stride % 8 || (top - base) + 24 > (count > 1 ? stride : (top - base) + 24))
+    if (!rs.base || count == 0) return TCP_OK;
+    if (stride < 24 || stride % 8 || (top - rs.base) + 24 > (count > 1 ? stride : (top - rs.base) + 24))
         return set_error(TCP_ERR_BAD_PARAM, "stride must be a multiple of 8 and cover the three fields");
-    long off[3];
     for (int k = 0; k < 3; ++k) {
-        off[k] = ptrs[k] ? (long)(reinterpret_cast<const char *>(ptrs[k]) - base) : -1;
-        if (off[k] >= 0 && off[k] % 8) return set_error(TCP_ERR_BAD_PARAM, "fields must be 8-byte aligned");
+        rs.off[k] = ptrs[k] ? (long)(reinterpret_cast<const char *>(ptrs[k]) - rs.base) : -1;
+        if (rs.off[k] >= 0 && rs.off[k] % 8) return set_error(TCP_ERR_BAD_PARAM, "fields must be 8-byte aligned");
     }
-    const size_t span = (size_t)(count - 1) * stride + (size_t)(top - base) + 24;
-    int rc;
-    const unsigned char *src = reinterpret_cast<const unsigned char *>(base);
-    if (!c->host_direct) {      // staged: one copy of the record span, then the same gather
-        if ((rc = ensure_stage(c, span))) return rc;
-        TCP_CUDA(cudaMemcpyAsync(c->d_stage, base, span, cudaMemcpyHostToDevice, c->stream));
-        src = c->d_stage;
-    }
-    if ((rc = launch_extract(c, src, first, count, stride, off[0], off[1], off[2]))) return rc;   // refreshes xq, xd
-    // the step graph reads the device arrays in place: new data needs no new graph
-    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    rs.span = (size_t)(count - 1) * stride + (size_t)(top - rs.base) + 24;
     return TCP_OK;
 }
 
-int tcp_download(tcp_ctx *c, int species, double *xx, double *xv, double *ff, long stride) {
-    TCP_TRACE("tcp_download");
-    if (!c || (species != 0 && species != 1)) return set_error(TCP_ERR_BAD_PARAM, "bad ctx or species");
-    cudaSetDevice(c->device);
-    const int count = species == 0 ? c->nel : c->nion, first = species == 0 ? 0 : c->nel;
-    if (count == 0 || (!xx && !xv && !ff)) return TCP_OK;
-    if (stride < 24 || stride % 8) return set_error(TCP_ERR_BAD_PARAM, "bad stride");
-    int nf = 0, rc;
-    if (c->host_direct) {       // the device writes the caller's records in place
-        const double *ptrs[3] = {xx, xv, ff};
-        const char *base = nullptr;
-        for (const double *q : ptrs)
-            if (q && (!base || reinterpret_cast<const char *>(q) < base)) base = reinterpret_cast<const char *>(q);
-        long off[3];
-        for (int k = 0; k < 3; ++k) {
-            off[k] = ptrs[k] ? (long)(reinterpret_cast<const char *>(ptrs[k]) - base) : -1;
-            if (off[k] >= 0 && off[k] % 8) return set_error(TCP_ERR_BAD_PARAM, "fields must be 8-byte aligned");
-        }
-        if ((rc = launch_scatter(c, reinterpret_cast<unsigned char *>(const_cast<char *>(base)), first, count, stride,
-                                 off[0], off[1], off[2], c->f)))
-            return rc;
-        TCP_CUDA(cudaStreamSynchronize(c->stream));
-        return TCP_OK;
+static int species_range(const tcp_ctx *c, int species, int &first, int &count) {
+    if (species != 0 && species != 1) return set_error(TCP_ERR_BAD_PARAM, "bad species");
+    count = species == 0 ? c->nel : c->nion;
+    first = species == 0 ? 0 : c->nel;
+    return TCP_OK;
+}
+
+// records -> device arrays, queued on the stream (no wait)
+static int enqueue_upload(tcp_ctx *c, int first, int count, const RecSpan &rs, long stride) {
+    if (count == 0 || !rs.base) return TCP_OK;
+    const unsigned char *src = reinterpret_cast<const unsigned char *>(rs.base);
+    int rc;
+    if (!c->host_direct) {      // staged: one copy of the record span, then the same gather
+        if ((rc = ensure_stage(c, rs.span))) return rc;
+        TCP_CUDA(cudaMemcpyAsync(c->d_stage, rs.base, rs.span, cudaMemcpyHostToDevice, c->stream));
+        src = c->d_stage;
     }
+    return launch_extract(c, src, first, count, stride, rs.off[0], rs.off[1], rs.off[2]);   // refreshes xq, xd
+}
+
+// device arrays -> records the device writes in place (host_direct), queued
+static int enqueue_download_direct(tcp_ctx *c, int first, int count, const RecSpan &rs, long stride) {
+    if (count == 0 || !rs.base) return TCP_OK;
+    return launch_scatter(c, reinterpret_cast<unsigned char *>(const_cast<char *>(rs.base)), first, count, stride,
+                          rs.off[0], rs.off[1], rs.off[2], c->f);
+}
+
+// device arrays -> records through the pinned stage; waits for the device
+static int download_staged(tcp_ctx *c, int first, int count, double *xx, double *xv, double *ff, long stride) {
+    if (count == 0 || (!xx && !xv && !ff)) return TCP_OK;
+    int nf = 0, rc;
     if ((rc = ensure_stage(c, (size_t)count * 4 * 3 * sizeof(double)))) return rc;
     if ((rc = launch_pack(c, first, count, xx != nullptr, xv != nullptr, ff != nullptr, false, &nf))) return rc;
     TCP_CUDA(cudaMemcpyAsync(c->h_stage, c->d_stage, (size_t)count * nf * 3 * sizeof(double), cudaMemcpyDeviceToHost,
@@ -516,6 +517,34 @@ int tcp_download(tcp_ctx *c, int species, double *xx, double *xv, double *ff, lo
             std::memcpy(b + (size_t)r * stride, c->h_stage + ((size_t)r * nf + slot) * 3, 3 * sizeof(double));
         ++slot;
     }
+    return TCP_OK;
+}
+
+int tcp_upload(tcp_ctx *c, int species, const double *xx, const double *xv, const double *ff, long stride) {
+    TCP_TRACE("tcp_upload");
+    if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
+    cudaSetDevice(c->device);
+    int first, count, rc;
+    RecSpan rs;
+    if ((rc = species_range(c, species, first, count))) return rc;
+    if ((rc = record_span(count, xx, xv, ff, stride, rs))) return rc;
+    if ((rc = enqueue_upload(c, first, count, rs, stride))) return rc;
+    // the step graph reads the device arrays in place: new data needs no new graph
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
+    return TCP_OK;
+}
+
+int tcp_download(tcp_ctx *c, int species, double *xx, double *xv, double *ff, long stride) {
+    TCP_TRACE("tcp_download");
+    if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
+    cudaSetDevice(c->device);
+    int first, count, rc;
+    RecSpan rs;
+    if ((rc = species_range(c, species, first, count))) return rc;
+    if ((rc = record_span(count, xx, xv, ff, stride, rs))) return rc;
+    if (!c->host_direct) return download_staged(c, first, count, xx, xv, ff, stride);
+    if ((rc = enqueue_download_direct(c, first, count, rs, stride))) return rc;   // written in place
+    TCP_CUDA(cudaStreamSynchronize(c->stream));
     return TCP_OK;
 }
 
@@ -732,6 +761,38 @@ int tcp_md_steps(tcp_ctx *c, double dt, int nsteps, tcp_energies *e) {
     for (int s = 0; s < nsteps; ++s)
         if ((rc = launch_step(c, dt))) return rc;
     if ((rc = sync_scalars(c))) return rc;
+    fill_energies(c, nullptr);
+    c->last.mv2el = c->h_scal[kScalMv2e];
+    c->last.mv2ion = c->h_scal[kScalMv2i];
+    if (e) *e = c->last;
+    return TCP_OK;
+}
+
+int tcp_md_steps_records(tcp_ctx *c, double dt, int nsteps, double *el_xx, double *el_xv, double *el_ff,
+                         long el_stride, double *ion_xx, double *ion_xv, double *ion_ff, long ion_stride,
+                         tcp_energies *e) {
+    TCP_TRACE("tcp_md_steps_records");
+    TCP_REQUIRE_READY(c);
+    if (nsteps < 0) return set_error(TCP_ERR_BAD_PARAM, "nsteps < 0");
+    RecSpan rs[2];
+    int rc;
+    // every argument is checked before anything is queued
+    if ((rc = record_span(c->nel, el_xx, el_xv, el_ff, el_stride, rs[0]))) return rc;
+    if ((rc = record_span(c->nion, ion_xx, ion_xv, ion_ff, ion_stride, rs[1]))) return rc;
+    if ((rc = enqueue_upload(c, 0, c->nel, rs[0], el_stride))) return rc;
+    if ((rc = enqueue_upload(c, c->nel, c->nion, rs[1], ion_stride))) return rc;
+    if ((rc = ensure_graph(c, dt))) return rc;
+    for (int s = 0; s < nsteps; ++s)
+        if ((rc = launch_step(c, dt))) return rc;
+    if (c->host_direct) {       // written in place before the one wait below
+        if ((rc = enqueue_download_direct(c, 0, c->nel, rs[0], el_stride))) return rc;
+        if ((rc = enqueue_download_direct(c, c->nel, c->nion, rs[1], ion_stride))) return rc;
+    }
+    if ((rc = sync_scalars(c))) return rc;
+    if (!c->host_direct) {
+        if ((rc = download_staged(c, 0, c->nel, el_xx, el_xv, el_ff, el_stride))) return rc;
+        if ((rc = download_staged(c, c->nel, c->nion, ion_xx, ion_xv, ion_ff, ion_stride))) return rc;
+    }
     fill_energies(c, nullptr);
     c->last.mv2el = c->h_scal[kScalMv2e];
     c->last.mv2ion = c->h_scal[kScalMv2i];

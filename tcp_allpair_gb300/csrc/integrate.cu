@@ -361,10 +361,22 @@ __global__ void __launch_bounds__(kIntThreads) extract_kernel(const unsigned cha
     const int r0 = blockIdx.x * kIntThreads;
     const int nr = min(kIntThreads, count - r0);
     const int nw = 3 * fl.nf;
-    for (int w = threadIdx.x; w < nr * nw; w += kIntThreads) {
-        const int r = w / nw, q = w - r * nw, k = q / 3;
-        const long off = k == 0 ? fl.off[0] : (k == 1 ? fl.off[1] : fl.off[2]);
-        buf[w] = reinterpret_cast<const double *>(stage + (size_t)(r0 + r) * stride + off)[q - 3 * k];
+    // all of a thread's (at most 9) loads are issued before the first is
+    // used: over the host link each round trip takes microseconds
+    double word[9];
+#pragma unroll
+    for (int u = 0; u < 9; ++u) {
+        const int w = threadIdx.x + u * kIntThreads;
+        if (w < nr * nw) {
+            const int r = w / nw, q = w - r * nw, k = q / 3;
+            const long off = k == 0 ? fl.off[0] : (k == 1 ? fl.off[1] : fl.off[2]);
+            word[u] = reinterpret_cast<const double *>(stage + (size_t)(r0 + r) * stride + off)[q - 3 * k];
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < 9; ++u) {
+        const int w = threadIdx.x + u * kIntThreads;
+        if (w < nr * nw) buf[w] = word[u];
     }
     __syncthreads();
     const int r = threadIdx.x;

@@ -315,12 +315,14 @@ __global__ void __launch_bounds__(kPairThreads) pair_fp32c_kernel(const PairArgs
 template <int KIND, bool ENERGY, bool RDF, int TPP>
 __device__ __forceinline__ void tile_f64(const double4_32a *__restrict__ tj, int cnt, int sub, double4_32a xi,
                                          const PairConsts &c, double qq, double &fx, double &fy,
-                                         double &fz, double &ue, unsigned *hist, double inv_dx) {
+                                         double &fz, double &ue, unsigned *hist, double inv_dx,
+                                         const F64Tab &tb) {
     // The expressions of force.f90 without divisions (GB300 issues FP64 at 1/64
     // of the FP32 rate): DNINT of d/box by multiplication with 1/box, 1/r from
-    // rsqrt, and erfc(ar) (the reference's 1 - erf(ar)) and erfc(r/lambda) from
-    // the Gaussians exp(-a^2 r^2) and exp(-r^2/lambda^2) that the force needs
-    // anyway (erfc_gauss, pair_math.cuh).
+    // rsqrt_nr, the exponentials from the table-driven exp_neg_tab, and
+    // erfc(ar) (the reference's 1 - erf(ar)) and erfc(r/lambda) from the
+    // Gaussians exp(-a^2 r^2) and exp(-r^2/lambda^2) that the force needs anyway
+    // (erfc_tab; pair_math.cuh).
     const double a = c.alpha;
     for (int jj = sub; jj < cnt; jj += TPP) {
         const double4_32a xj = tj[jj];
@@ -330,21 +332,21 @@ __device__ __forceinline__ void tile_f64(const double4_32a *__restrict__ tj, int
         xr2 = fma(-c.box[2], round(xr2 * c.inv_box[2]), xr2);
         const double r2 = xr0 * xr0 + xr1 * xr1 + xr2 * xr2;
         if (r2 < c.rc2 && r2 > 0.0) {
-            const double rinv = rsqrt(r2), r = r2 * rinv, rinv3 = rinv * rinv * rinv;
-            const double e = exp(-c.alpha2 * r2);
-            const double x = erfc_gauss(a * r, e);
+            const double rinv = rsqrt_nr(r2), r = r2 * rinv, rinv3 = rinv * rinv * rinv;
+            const double e = exp_neg_tab(c.alpha2 * r2, tb);
+            const double x = erfc_tab(a * r, e, tb);
             double df, u;
             if (KIND == 0) {                                   // force.f90:104-106
                 df = kEps * qq * fma(c.c_gauss_d * r, e, x) * rinv3;
                 u = qq * x * rinv;
             } else if (KIND == 1) {                            // force.f90:135-139
-                const double y = exp(-r * c.inv_rs_d);
+                const double y = exp_neg_tab(r * c.inv_rs_d, tb);
                 df = kEps * qq * (fma(c.c_gauss_d * r, e, x) - y - y * r * c.inv_rs_d) * rinv3;
                 u = qq * (x - y) * rinv;
             } else {                                           // Kelbg
-                const double g = exp(-r2 * c.inv_lam2);
+                const double g = exp_neg_tab(r2 * c.inv_lam2, tb);
                 df = kEps * qq * (fma(c.c_gauss_d * r, e, x) - g) * rinv3;
-                u = qq * ((x - g) * rinv + c.sqrtpi_lam_d * erfc_gauss(r * c.inv_lam, g));
+                u = qq * ((x - g) * rinv + c.sqrtpi_lam_d * erfc_tab(r * c.inv_lam, g, tb));
             }
             fx += df * xr0;
             fy += df * xr1;
@@ -365,6 +367,7 @@ __global__ void __launch_bounds__(kPairThreads) pair_fp64_kernel(const PairArgs 
     __shared__ __align__(8) uint64_t bars[kStagesD];
     __shared__ unsigned hist[RDF ? 3 * kNbin : 1];
     __shared__ double red[32];
+    __shared__ F64Tab tab;
 
     const int tid = threadIdx.x;
     const int b = blockIdx.x;
@@ -391,6 +394,7 @@ __global__ void __launch_bounds__(kPairThreads) pair_fp64_kernel(const PairArgs 
     }
     if (RDF)
         for (int k = tid; k < 3 * kNbin; k += blockDim.x) hist[k] = 0u;
+    load_f64_tab(tab);
     __syncthreads();
     if (tid == 0) {
         for (int k = 0; k < min(kStagesD, nt); ++k) {
@@ -413,11 +417,11 @@ __global__ void __launch_bounds__(kPairThreads) pair_fp64_kernel(const PairArgs 
         const double inv_dx = RDF ? a.c.inv_dxd[pt] : 0.0;
         const double qq = a.c.qq[pt];
         if (pt == 1 && EIKIND == 1)
-            tile_f64<1, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx);
+            tile_f64<1, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx, tab);
         else if (pt == 1 && EIKIND == 2)
-            tile_f64<2, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx);
+            tile_f64<2, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx, tab);
         else
-            tile_f64<0, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx);
+            tile_f64<0, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx, tab);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicOr(a.status, kStatusTmaTimeout);
             break;
@@ -555,6 +559,7 @@ void make_pair_consts(tcp_ctx *c) {
     k.inv_lam2 = 1.0 / (lam * lam);
     k.inv_lam = 1.0 / lam;
     k.sqrtpi_lam_d = kSqrtPi / lam;
+    k.kelbg_far2 = (8.5 * lam) * (8.5 * lam);
     k.ei_model = p.ei_model;
 }
 

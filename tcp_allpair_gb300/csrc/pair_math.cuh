@@ -95,4 +95,75 @@ __device__ __forceinline__ double erfc_gauss(double x, double g) {
     for (int k = 15; k >= 0; --k) q = fma(q, s, kErfc64Q[k]);
     return g * (t * q);
 }
+
+// ---- FP64, table-driven (the FP64 pair kernels) ------------------------------
+// The tables of fit_erfcx64.py, copied once per CTA into shared memory, where
+// each lane indexes them by its own argument.
+#include "erfcx64_table.inc"
+
+struct F64Tab {
+    double erfcx[kErfcxDeg + 1][kErfcxSeg];   // [k][j]: lanes on different segments use different banks
+    double exp2[64];
+};
+
+// all threads of the CTA; the caller synchronises before first use
+__device__ __forceinline__ void load_f64_tab(F64Tab &t) {
+    for (int i = threadIdx.x; i < (kErfcxDeg + 1) * kErfcxSeg; i += blockDim.x)
+        (&t.erfcx[0][0])[i] = (&kErfcxTab[0][0])[i];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) t.exp2[i] = kExp2Tab[i];
+}
+
+constexpr double kRound52 = 6755399441055744.0;   // 1.5 * 2^52: x + kRound52 holds rint(x) in its low word
+
+// exp(-z) for 0 <= z < 700 (0 beyond): -z = k ln2/64 + f with k = rint(-64 z/ln2)
+// and |f| <= ln2/128, exp(-z) = 2^(k >> 6) 2^((k & 63)/64) (1 + p(f)), p the
+// degree-5 Taylor polynomial of exp(f) - 1 (truncation 4e-17).  The first
+// reduction step is exact (one FMA of a 13-bit k), ln2/64 is split in two
+// doubles; relative error 2e-16.  10 FP64 operations.
+__device__ __forceinline__ double exp_neg_tab(double z, const F64Tab &t) {
+    constexpr double kInvLn2x64 = 92.33248261689366;
+    constexpr double kLn2d64Hi = 0.010830424696249145, kLn2d64Lo = 3.623510646634843e-19;
+    const double kd = fma(z, -kInvLn2x64, kRound52);
+    const int k = __double2loint(kd);
+    const double kf = kd - kRound52;
+    double f = fma(-kf, kLn2d64Hi, -z);
+    f = fma(-kf, kLn2d64Lo, f);
+    double q = fma(f, 1.0 / 120.0, 1.0 / 24.0);
+    q = fma(q, f, 1.0 / 6.0);
+    q = fma(q, f, 0.5);
+    q = fma(q, f, 1.0);
+    const double tk = t.exp2[k & 63];
+    const double v = fma(tk, q * f, tk);
+    // times 2^(k >> 6) by the exponent field; the result stays normal for z < 700
+    const double sc = __hiloint2double((int)((unsigned)__double2hiint(v) + ((unsigned)(k >> 6) << 20)),
+                                       __double2loint(v));
+    return __double2hiint(z) < 0x4085E000 ? sc : 0.0;   // z < 700 (z >= 0: the high words order as z)
+}
+
+// erfc(x) = g erfcx(x) for x >= 0 with g = exp(-x^2) from the caller: for
+// x <= 9, x = j/8 + h with |h| <= 1/16 and erfcx by the degree-9 segment
+// polynomial j in h (relative error about 3e-16 with a correctly rounded g);
+// beyond 9 (erfc < 5e-37) and for NaN, 0.  No branch: the segment index of an
+// argument out of range is replaced by 0 and its value discarded.
+__device__ __forceinline__ double erfc_tab(double x, double g, const F64Tab &t) {
+    const bool in = (unsigned)__double2hiint(x) <= 0x40220000u;   // x <= 9 on the high word (x >= 0)
+    const double kd = fma(x, 8.0, kRound52);
+    const int j = in ? __double2loint(kd) : 0;
+    const double h = fma(kd - kRound52, -0.125, x);
+    double q = t.erfcx[kErfcxDeg][j];
+#pragma unroll
+    for (int k = kErfcxDeg - 1; k >= 0; --k) q = fma(q, h, t.erfcx[k][j]);
+    return in ? g * q : 0.0;
+}
+
+// 1/sqrt(x) for positive normal x: the hardware approximation
+// (rsqrt.approx.ftz.f64) and two Newton steps y += y (1 - x y^2)/2 written as
+// y = fma(y, 0.5 - (x/2) y^2, y).  7 FP64 operations.
+__device__ __forceinline__ double rsqrt_nr(double x) {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    const double hx = 0.5 * x;
+    y = fma(y, fma(-hx, y * y, 0.5), y);
+    return fma(y, fma(-hx, y * y, 0.5), y);
+}
 }  // namespace tcp

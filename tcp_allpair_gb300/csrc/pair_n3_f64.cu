@@ -41,25 +41,25 @@ constexpr double kKelbgFar = 8.5;
 // One pair at squared distance r2 (> 0).  Returns the force weight w, with the
 // force on i = eps qq w d, and adds the energy term (energy = qq pe) with ENERGY.
 template <int KIND, bool ENERGY>
-__device__ __forceinline__ double n3_pair_f64(const PairConsts &c, double r2, bool ok, double &pe) {
-    const double rinv = rsqrt(r2);
+__device__ __forceinline__ double n3_pair_f64(const PairConsts &c, double r2, bool ok, double &pe, const F64Tab &tb) {
+    const double rinv = rsqrt_nr(r2);
     const double r = r2 * rinv;
-    const double e = exp(-c.alpha2 * r2);
+    const double e = exp_neg_tab(c.alpha2 * r2, tb);
     double s, u = 0.0;
     if (KIND == 2) {                                      // Kelbg, e-i pairs
-        const double x = erfc_gauss(c.alpha * r, e);
+        const double x = erfc_tab(c.alpha * r, e, tb);
         s = fma(c.c_gauss_d * r, e, x);                   // erfc(ar) + 2ar/sqrt(pi) exp(-a^2 r^2)
         if (ENERGY) u = x * rinv;
-        if (r2 < kKelbgFar * kKelbgFar * c.lambda * c.lambda) {
-            const double g = exp(-r2 * c.inv_lam2);
+        if (__double_as_longlong(r2) < __double_as_longlong(c.kelbg_far2)) {   // r < 8.5 lambda
+            const double g = exp_neg_tab(r2 * c.inv_lam2, tb);
             s -= g;
-            if (ENERGY) u += c.sqrtpi_lam_d * erfc(r * c.inv_lam) - g * rinv;
+            if (ENERGY) u += c.sqrtpi_lam_d * erfc_tab(r * c.inv_lam, g, tb) - g * rinv;
         }
     } else {
-        const double x = erfc_gauss(c.alpha * r, e);      // 1 - erf(ar), force.f90:104 / 135
+        const double x = erfc_tab(c.alpha * r, e, tb);    // 1 - erf(ar), force.f90:104 / 135
         s = fma(c.c_gauss_d * r, e, x);
         if (KIND == 1) {                                  // Deutsch, force.f90:136-139
-            const double y = exp(-r * c.inv_rs_d);
+            const double y = exp_neg_tab(r * c.inv_rs_d, tb);
             s = s - y - y * r * c.inv_rs_d;
             if (ENERGY) u = (x - y) * rinv;
         } else if (ENERGY) {
@@ -84,7 +84,7 @@ template <int KIND, bool ENERGY, bool MASKED, int R, bool RDF = false>
 __device__ __forceinline__ void n3_item_f64(const PairConsts &c, const longlong4_32a *__restrict__ tj, int cnt,
                                             int jstart, const longlong3 (&xi)[R], int ibase, int iend,
                                             double (*sjacc)[3], double (&p)[R][3], double &pe,
-                                            unsigned *hist = nullptr, double inv_dx = 0.0) {
+                                            const F64Tab &tb, unsigned *hist = nullptr, double inv_dx = 0.0) {
     const int lane = threadIdx.x & 31;
     const int src = (lane + 1) & 31;
     for (int ch = 0; ch * 32 < cnt; ++ch) {
@@ -103,7 +103,9 @@ __device__ __forceinline__ void n3_item_f64(const PairConsts &c, const longlong4
                 const double dy = fixed_diff(xi[r].y, xj.y, c.sl[1]);
                 const double dz = fixed_diff(xi[r].z, xj.z, c.sl[2]);
                 const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
-                bool ok = r2 < c.rc2 && r2 > 0.0;
+                // 0 < r2 < rc^2 on the bit patterns (r2 >= 0: they order as the values)
+                const long long rb = __double_as_longlong(r2);
+                bool ok = rb > 0 && rb < __double_as_longlong(c.rc2);
                 if (MASKED) {
                     const int jo = ch * 32 + ((lane + s) & 31);
                     const int ir = ibase + 32 * r;
@@ -113,7 +115,7 @@ __device__ __forceinline__ void n3_item_f64(const PairConsts &c, const longlong4
                     const double tb = sqrt(r2) * inv_dx;
                     if (tb < (double)kNbin) atomicAdd(&hist[(int)tb], 2u);
                 }
-                const double w = n3_pair_f64<KIND, ENERGY>(c, ok ? r2 : 1.0, ok, pe);
+                const double w = n3_pair_f64<KIND, ENERGY>(c, ok ? r2 : 1.0, ok, pe, tb);
                 p[r][0] = fma(w, dx, p[r][0]);
                 p[r][1] = fma(w, dy, p[r][1]);
                 p[r][2] = fma(w, dz, p[r][2]);
@@ -138,7 +140,7 @@ __device__ __forceinline__ void n3_item_f64(const PairConsts &c, const longlong4
 }
 
 template <bool ENERGY, int R, bool RDF = false>
-__global__ void __launch_bounds__(kN3Threads) pair_n3_f64_kernel(const N3Args a) {
+__global__ void __launch_bounds__(kN3Threads, 2) pair_n3_f64_kernel(const N3Args a) {
     constexpr int TILE = 32 * R * kN3Warps;
     __shared__ __align__(128) longlong4_32a tiles[kN3Stages][kN3Sub];
     __shared__ __align__(8) uint64_t bars[kN3Stages];
@@ -146,6 +148,7 @@ __global__ void __launch_bounds__(kN3Threads) pair_n3_f64_kernel(const N3Args a)
     __shared__ double red[32];
     __shared__ long long s_next;
     __shared__ unsigned hist[RDF ? 3 * kNbin : 1];
+    __shared__ F64Tab tab;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (RDF)
         for (int k = tid; k < 3 * kNbin; k += kN3Threads) hist[k] = 0u;
@@ -155,6 +158,7 @@ __global__ void __launch_bounds__(kN3Threads) pair_n3_f64_kernel(const N3Args a)
     const int nst = (int)(it1 - it0);
 
     for (int k = tid; k < kN3Sub * 3; k += kN3Threads) (&sjacc[0][0])[k] = 0.0;
+    load_f64_tab(tab);
     if (tid == 0) {
         for (int s = 0; s < kN3Stages; ++s) mbar_init(&bars[s], 1);
         fence_mbar_init();
@@ -225,7 +229,7 @@ __global__ void __launch_bounds__(kN3Threads) pair_n3_f64_kernel(const N3Args a)
         const int kind = pt == 1 ? (c.ei_model == TCP_EI_DEUTSCH ? 1 : (c.ei_model == TCP_EI_KELBG ? 2 : 0)) : 0;
         if (ok) {
 #define TCP_N3D_ITEM(KIND, MASKED) \
-    n3_item_f64<KIND, ENERGY, MASKED, R, RDF>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe, \
+    n3_item_f64<KIND, ENERGY, MASKED, R, RDF>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe, tab, \
                                               RDF ? hist + pt * kNbin : nullptr, RDF ? c.inv_dxd[pt] : 0.0)
             if (masked) {
                 if (kind == 1) TCP_N3D_ITEM(1, true);

@@ -60,6 +60,7 @@ struct PairConsts {
     double inv_lam2;           // 1/lambda^2
     double inv_lam;            // 1/lambda
     double sqrtpi_lam_d;       // sqrt(pi)/lambda
+    double kelbg_far2;         // (8.5 lambda)^2: beyond, the Kelbg Gaussian terms are below 1e-31
     double inv_dxd[3];
     double qq[3];
     int ei_model;

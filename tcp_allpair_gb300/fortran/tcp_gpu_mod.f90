@@ -103,6 +103,15 @@ MODULE TCP_GPU
        INTEGER(C_INT), VALUE :: nsteps
        TYPE(tcp_energies), INTENT(OUT) :: e
      END FUNCTION
+     INTEGER(C_INT) FUNCTION tcp_md_steps_records(c, dt, nsteps, exx, exv, eff, estride, ixx, ixv, iff, istride, e) &
+          BIND(C, NAME='tcp_md_steps_records')
+       IMPORT :: C_INT, C_PTR, C_DOUBLE, C_LONG, tcp_energies
+       TYPE(C_PTR), VALUE :: c, exx, exv, eff, ixx, ixv, iff
+       REAL(C_DOUBLE), VALUE :: dt
+       INTEGER(C_INT), VALUE :: nsteps
+       INTEGER(C_LONG), VALUE :: estride, istride
+       TYPE(tcp_energies), INTENT(OUT) :: e
+     END FUNCTION
      ! derivatives (no counterpart in the reference)
      INTEGER(C_INT) FUNCTION tcp_adjoint_energy(c, e, dedl, deds) BIND(C, NAME='tcp_adjoint_energy')
        IMPORT :: C_INT, C_PTR, C_DOUBLE
@@ -150,6 +159,31 @@ CONTAINS
     IF (n > 1) stride = TRANSFER(C_LOC(rec(2)), 0_C_LONG) - TRANSFER(C_LOC(rec(1)), 0_C_LONG)
     CALL tcp_stop_on(tcp_upload(ctx, species, C_LOC(rec(1)%xx), C_LOC(rec(1)%xv), C_LOC(rec(1)%ff), stride), &
          "tcp_upload")
+  END SUBROUTINE
+
+  ! nsteps MD steps on qel / qion updated in place (the body of main.f90:81-153
+  ! with the records read before and written after, one wait for the device)
+  SUBROUTINE tcp_steps_records(dt, nsteps, qel, nel, qion, nion, e)
+    REAL(C_DOUBLE), INTENT(IN) :: dt
+    INTEGER, INTENT(IN) :: nsteps, nel, nion
+    TYPE(PT), TARGET, INTENT(INOUT) :: qel(nel), qion(nion)
+    TYPE(tcp_energies), INTENT(OUT) :: e
+    INTEGER(C_LONG) :: estr, istr
+    TYPE(C_PTR) :: exx, exv, eff, ixx, ixv, iff
+    estr = 104
+    istr = 104
+    exx = C_NULL_PTR; exv = C_NULL_PTR; eff = C_NULL_PTR
+    ixx = C_NULL_PTR; ixv = C_NULL_PTR; iff = C_NULL_PTR
+    IF (nel > 0) THEN
+      exx = C_LOC(qel(1)%xx); exv = C_LOC(qel(1)%xv); eff = C_LOC(qel(1)%ff)
+      IF (nel > 1) estr = TRANSFER(C_LOC(qel(2)), 0_C_LONG) - TRANSFER(C_LOC(qel(1)), 0_C_LONG)
+    END IF
+    IF (nion > 0) THEN
+      ixx = C_LOC(qion(1)%xx); ixv = C_LOC(qion(1)%xv); iff = C_LOC(qion(1)%ff)
+      IF (nion > 1) istr = TRANSFER(C_LOC(qion(2)), 0_C_LONG) - TRANSFER(C_LOC(qion(1)), 0_C_LONG)
+    END IF
+    CALL tcp_stop_on(tcp_md_steps_records(ctx, dt, INT(nsteps, C_INT), exx, exv, eff, estr, ixx, ixv, iff, istr, e), &
+         "tcp_md_steps_records")
   END SUBROUTINE
 
   ! NS%RDF_* / NS%VDF_* += the device histograms since the last pull, which are

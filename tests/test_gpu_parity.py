@@ -4,11 +4,14 @@ Tolerances: the FP64 kernels agree with the oracle to summation-order
 rounding (1e-11 relative); the compensated-FP32 pair kernel meets the
 RMS relative force error bound 2e-6 of the FP32 path.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
 import oracle
 import tcp_allpair_gb300 as T
+from tcp_allpair_gb300 import _abi
 
 pytestmark = pytest.mark.gpu
 
@@ -235,6 +238,58 @@ def test_transfer_paths(direct, monkeypatch):
     assert np.all(a["id"] == 5) and np.all(b["id"] == 6)
     assert np.array_equal(x, s.x) and np.array_equal(v, s.v)
     assert np.array_equal(x2, s.x[::-1]) and np.array_equal(v2, s.v) and np.array_equal(f2, 2 * f)
+
+
+@pytest.mark.parametrize("direct", ["1", "0"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_md_steps_records_equals_separate_calls(direct, precision, monkeypatch):
+    """tcp_md_steps_records (records read, steps, records written, one wait)
+    against tcp_upload x2 + tcp_md_steps + tcp_download x2 on the same records:
+    bitwise, through both transfer paths; other record fields untouched."""
+    monkeypatch.setenv("TCP_HOST_DIRECT", direct)
+    s = make(600, seed=21, K=16)
+    p = T.params_for(s, precision=precision, recip="spme")
+    out = []
+    for fused in (False, True):
+        qel, qion = s.to_pt()
+        qel["id"], qion["id"] = 3, 4
+        with T.Context(p, s.nel, s.nion) as c:
+            c.EWALD_SELF()
+            c.set_flags(T.FLAG_ENERGY | T.FLAG_DETERMINISTIC)    # fixed-order sums: bitwise comparable
+            c.upload_pt(qel, qion, fields=("xx", "xv"))
+            c.force()
+            c.download_pt(qel, qion, fields=("ff",))
+            for _ in range(3):
+                if fused:
+                    e = c.md_steps_pt(s.dt, 2, qel, qion)
+                else:
+                    c.upload_pt(qel, qion)
+                    e = c.md_steps(s.dt, 2)
+                    c.download_pt(qel, qion)
+        out.append((qel, qion, e))
+    (a_el, a_ion, ea), (b_el, b_ion, eb) = out
+    for k in ("xx", "xv", "ff"):
+        assert np.array_equal(a_el[k], b_el[k]) and np.array_equal(a_ion[k], b_ion[k])
+    assert np.all(b_el["id"] == 3) and np.all(b_ion["id"] == 4)
+    assert ea == eb
+
+
+def test_md_steps_records_rejects_bad_strides():
+    s = make(64, seed=2, K=16)
+    qel, qion = s.to_pt()
+    p = T.params_for(s, precision="fp64", recip="spme")
+    with T.Context(p, s.nel, s.nion) as c:
+        c.EWALD_SELF()
+        c.upload_pt(qel, qion)
+        x0, _, _, _ = c.download(x=True, v=False, f=False)
+        base = qel.ctypes.data
+        off = {k: qel.dtype.fields[k][1] for k in ("xx", "xv", "ff")}
+        ptr = [C.c_void_p(base + off[k]) for k in ("xx", "xv", "ff")]
+        e = T.TcpEnergies()
+        rc = c.lib.tcp_md_steps_records(c.h, s.dt, 1, *ptr, 20, None, None, None, 104, C.byref(e))
+        assert rc == _abi.TCP_ERR_BAD_PARAM
+        x1, _, _, _ = c.download(x=True, v=False, f=False)
+    assert np.array_equal(x0, x1)                 # nothing ran
 
 
 def test_errors():
