@@ -59,28 +59,29 @@ struct AdjArgs {
 };
 
 template <int KIND>
-__device__ __forceinline__ void radial_f64(const AdjArgs &a, double r2, double &G1, double &G2, double &dl,
-                                           double &gl) {
-    // no divisions (GB300's FP64 rate): 1/r from rsqrt, erfc from the Gaussians
-    const double rinv = rsqrt(r2), r = r2 * rinv, rinv2 = rinv * rinv;
+__device__ __forceinline__ void radial_f64(const AdjArgs &a, const F64Tab &tb, double r2, double &G1, double &G2,
+                                           double &dl, double &gl) {
+    // no divisions (GB300's FP64 rate): 1/r from rsqrt_nr, the table-driven
+    // exponentials, erfc from the Gaussians (pair_math.cuh)
+    const double rinv = rsqrt_nr(r2), r = r2 * rinv, rinv2 = rinv * rinv;
     const double al = a.c.alpha;
-    const double e = exp(-a.c.alpha2 * r2);
-    const double w0 = (erfc_gauss(al * r, e) * rinv + a.c.c_gauss_d * e) * rinv2;
+    const double e = exp_neg_tab(a.c.alpha2 * r2, tb);
+    const double w0 = (erfc_tab(al * r, e, tb) * rinv + a.c.c_gauss_d * e) * rinv2;
     G1 = w0;
     G2 = (3.0 * w0 + a.c2a * e) * rinv2;
     dl = 0.0;
     gl = 0.0;
     if (KIND == 1) {
-        const double irs = a.c.inv_rs_d, y = exp(-r * irs);
+        const double irs = a.c.inv_rs_d, y = exp_neg_tab(r * irs, tb);
         G1 -= y * (irs + rinv) * rinv2;
         G2 -= y * (3.0 * irs * rinv2 + 3.0 * rinv2 * rinv + a.inv_rs2 * rinv) * rinv2;
         dl = -y * a.inv_rs2;
         gl = -y * a.inv_rs3 * rinv;
     } else if (KIND == 2) {
-        const double g = exp(-r2 * a.c.inv_lam2);
+        const double g = exp_neg_tab(r2 * a.c.inv_lam2, tb);
         G1 -= g * rinv2 * rinv;
         G2 -= g * (3.0 * rinv2 * rinv + a.k_l2 * rinv) * rinv2;
-        dl = -a.k_dl * erfc_gauss(r * a.c.inv_lam, g);   // erfc(r/l), exp(-(r/l)^2) = g
+        dl = -a.k_dl * erfc_tab(r * a.c.inv_lam, g, tb);   // erfc(r/l), exp(-(r/l)^2) = g
         gl = -a.k_gl * g * rinv;
     }
 }
@@ -119,6 +120,8 @@ __global__ void __launch_bounds__(kAdjThreads) adj_pair_kernel(const AdjArgs a) 
     __shared__ int4 sxq[F32 ? kAdjThreads : 1];
     __shared__ double4_32a sxd[F32 ? 1 : kAdjThreads];
     __shared__ double red[32];
+    __shared__ F64Tab tab;
+    load_f64_tab(tab);     // ordered before first use by the tile loop's barrier
     const int tid = threadIdx.x;
     const int i = blockIdx.x * kAdjThreads + tid;
     const bool vi = i < a.n;
@@ -183,7 +186,7 @@ __global__ void __launch_bounds__(kAdjThreads) adj_pair_kernel(const AdjArgs a) 
                     // r^2/lambda^2 (the force kernels use the series of kelbg_close);
                     // these rare pairs take the FP64 radial functions
                     double h1, h2, hd, hg;
-                    radial_f64<2>(a, (double)r2, h1, h2, hd, hg);
+                    radial_f64<2>(a, tab, (double)r2, h1, h2, hd, hg);
                     g1 = (float)h1; g2 = (float)h2; d = (float)hd; g = (float)hg;
                 } else if (type == 1 && EIK == 1) radial_f32<1>(a, (float)r2, g1, g2, d, g);
                 else if (type == 1 && EIK == 2) radial_f32<2>(a, (float)r2, g1, g2, d, g);
@@ -191,9 +194,9 @@ __global__ void __launch_bounds__(kAdjThreads) adj_pair_kernel(const AdjArgs a) 
                 G1 = g1; G2 = g2; dl = d; gl = g;
             } else {
                 double g1, g2, d, g;
-                if (type == 1 && EIK == 1) radial_f64<1>(a, (double)r2, g1, g2, d, g);
-                else if (type == 1 && EIK == 2) radial_f64<2>(a, (double)r2, g1, g2, d, g);
-                else radial_f64<0>(a, (double)r2, g1, g2, d, g);
+                if (type == 1 && EIK == 1) radial_f64<1>(a, tab, (double)r2, g1, g2, d, g);
+                else if (type == 1 && EIK == 2) radial_f64<2>(a, tab, (double)r2, g1, g2, d, g);
+                else radial_f64<0>(a, tab, (double)r2, g1, g2, d, g);
                 G1 = g1; G2 = g2; dl = d; gl = g;
             }
             const T qq = F32 ? (T)(a.c.qqf[type] * (float)kEps) : (T)(a.c.qq[type] * kEps);
@@ -239,11 +242,11 @@ constexpr int kAdjN3Warps = 8;
 constexpr int kAdjN3Threads = 32 * kAdjN3Warps;
 constexpr int kAdjN3Tile = kAdjN3Threads;     // one i-particle per lane
 
-__device__ __forceinline__ void adj_radial_t(const AdjArgs &a, int type, int eik, float r2, float &G1, float &G2,
-                                             float &dl, float &gl) {
+__device__ __forceinline__ void adj_radial_t(const AdjArgs &a, const F64Tab &tb, int type, int eik, float r2,
+                                             float &G1, float &G2, float &dl, float &gl) {
     if (type == 1 && eik == 2 && r2 < a.c.close2) {   // close Kelbg pairs, as in adj_pair_kernel
         double h1, h2, hd, hg;
-        radial_f64<2>(a, (double)r2, h1, h2, hd, hg);
+        radial_f64<2>(a, tb, (double)r2, h1, h2, hd, hg);
         G1 = (float)h1;
         G2 = (float)h2;
         dl = (float)hd;
@@ -255,11 +258,11 @@ __device__ __forceinline__ void adj_radial_t(const AdjArgs &a, int type, int eik
     else radial_f32<0>(a, r2, G1, G2, dl, gl);
 }
 
-__device__ __forceinline__ void adj_radial_t(const AdjArgs &a, int type, int eik, double r2, double &G1,
-                                             double &G2, double &dl, double &gl) {
-    if (type == 1 && eik == 1) radial_f64<1>(a, r2, G1, G2, dl, gl);
-    else if (type == 1 && eik == 2) radial_f64<2>(a, r2, G1, G2, dl, gl);
-    else radial_f64<0>(a, r2, G1, G2, dl, gl);
+__device__ __forceinline__ void adj_radial_t(const AdjArgs &a, const F64Tab &tb, int type, int eik, double r2,
+                                             double &G1, double &G2, double &dl, double &gl) {
+    if (type == 1 && eik == 1) radial_f64<1>(a, tb, r2, G1, G2, dl, gl);
+    else if (type == 1 && eik == 2) radial_f64<2>(a, tb, r2, G1, G2, dl, gl);
+    else radial_f64<0>(a, tb, r2, G1, G2, dl, gl);
 }
 
 template <bool F32, int EIK, bool HVP>
@@ -272,9 +275,11 @@ __global__ void __launch_bounds__(kAdjN3Threads) adj_n3_kernel(const AdjArgs a, 
     __shared__ double sh[HVP ? kN3Sub : 1][3];
     __shared__ double red[32];
     __shared__ long long s_next;
+    __shared__ F64Tab tab;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int src = (lane + 1) & 31;
     for (int k = tid; k < (HVP ? kN3Sub : 1) * 3; k += kAdjN3Threads) (&sh[0][0])[k] = 0.0;
+    load_f64_tab(tab);     // ordered before first use by the item loop's barrier
 
     int curI = -1, istart = 0, iend = 0, isp = 0, ifirst = 0, ibase = 0;
     int4 xqi = make_int4(0, 0, 0, 0);
@@ -359,7 +364,7 @@ __global__ void __launch_bounds__(kAdjN3Threads) adj_n3_kernel(const AdjArgs a, 
                 if (masked) ok = ok && ibase < iend && jo < cnt && ibase < jstart + jo;
                 if (ok) {
                     T G1, G2, dl, gl;
-                    adj_radial_t(a, type, EIK, r2, G1, G2, dl, gl);
+                    adj_radial_t(a, tab, type, EIK, r2, G1, G2, dl, gl);
                     te += qq * dl;
                     if (HVP) {
                         const T dw0 = wi[0] - wj0, dw1 = wi[1] - wj1, dw2 = wi[2] - wj2;

@@ -63,40 +63,7 @@ __device__ __forceinline__ void kelbg_close(float y, float x, float &num_f, floa
     num_e = fmaf(-1.1283791671f * x, ez, one_m_g);
 }
 
-// ---- FP64 ----------------------------------------------------------------------
-// erfc(x) = g t Q(s) for 0 <= x <= 6 with g = exp(-x^2), t = 1/(1 + 0.3 x),
-// s = (2t - (1 + t0))/(1 - t0), t0 = 1/2.8 (coefficients of s^k, k = 0..16,
-// printed by fit_erfc64.py; FP64 relative error 4.2e-15 on [0, 6]); beyond 6,
-// CUDA's erfc.
-static __constant__ double kErfc64Q[17] = {
-    0.45555520140889583,     0.30607916747347613,     0.15698996500388523,    0.061053316559926858,
-    0.017220474968784219,    0.0030594945415118834,   0.00013619148512448821, -8.0956163342312334e-05,
-    -1.5369868692330893e-05, 1.8383498117058095e-06,  7.6697409474484379e-07, -5.8913282295749855e-08,
-    -3.6736788304988968e-08, 3.4415628100951905e-09,  1.7561301609804529e-09, -2.1041881319352887e-10,
-    -7.0680541191474699e-11};
-constexpr double kErfc64P = 0.3, kErfc64XMax = 6.0;
-
-// 1/y for y in [1, 2.8]: FP32 reciprocal seed, two Newton steps (error e -> e^2)
-__device__ __forceinline__ double recip_newton(double y) {
-    double t = (double)rcp_approx((float)y);
-    double e = fma(-y, t, 1.0);
-    t = fma(t, e, t);
-    e = fma(-y, t, 1.0);
-    return fma(t, e, t);
-}
-
-__device__ __forceinline__ double erfc_gauss(double x, double g) {
-    if (x > kErfc64XMax) return erfc(x);
-    constexpr double t0 = 1.0 / (1.0 + kErfc64P * kErfc64XMax);
-    const double t = recip_newton(fma(kErfc64P, x, 1.0));
-    const double s = fma(t, 2.0 / (1.0 - t0), -(1.0 + t0) / (1.0 - t0));
-    double q = kErfc64Q[16];
-#pragma unroll
-    for (int k = 15; k >= 0; --k) q = fma(q, s, kErfc64Q[k]);
-    return g * (t * q);
-}
-
-// ---- FP64, table-driven (the FP64 pair kernels) ------------------------------
+// ---- FP64, table-driven (the FP64 pair and adjoint kernels) ----------------------
 // The tables of fit_erfcx64.py, copied once per CTA into shared memory, where
 // each lane indexes them by its own argument.
 #include "erfcx64_table.inc"

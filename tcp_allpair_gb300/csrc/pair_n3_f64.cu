@@ -18,11 +18,13 @@
 // minimum image (force.f90:92) is the wrapped difference of 64-bit fixed-point
 // coordinates (2^64 per box length, refreshed with every position update),
 // exact and then rounded once to FP64 (the sign choice at |d| = box/2 exactly
-// differs from DNINT's, where r >= rc), 1/r and 1/r^3 come from one rsqrt,
-// and erfc(alpha r) from the Gaussian
-// exp(-alpha^2 r^2) that the force needs anyway times a polynomial
-// (erfc_gauss; 4e-15 relative, fit_erfc64.py), where the reference takes
-// 1 - erf(alpha r).
+// differs from DNINT's, where r >= rc), 1/r and 1/r^3 come from one
+// rsqrt_nr, the exponentials from the table-driven exp_neg_tab (2e-16
+// relative), and erfc(alpha r) from the Gaussian exp(-alpha^2 r^2) that the
+// force needs anyway times the segment polynomial of erfcx (erfc_tab; 3e-16
+// relative, fit_erfcx64.py), where the reference takes 1 - erf(alpha r).  The
+// cut-off and Kelbg range tests compare the bit patterns of non-negative
+// doubles, which order as their values.
 #include <algorithm>
 #include <cstring>
 

@@ -1,7 +1,7 @@
-"""The erfc approximations compiled into the pair kernels, read from their
-source tables and evaluated on the CPU against scipy's erfc: the FP32 fit
-(pair_math.cuh TCP_ERFC_Q, float32 Horner as the kernels evaluate it) and the
-FP64 fit (kErfc64Q, the Gaussian factor times t Q(s))."""
+"""The erfc and exp approximations compiled into the pair kernels, read from
+their source tables and evaluated on the CPU against scipy / numpy: the FP32
+fit (pair_math.cuh TCP_ERFC_Q, float32 Horner as the kernels evaluate it), and
+the FP64 segment erfcx and 2^(i/64) tables (erfcx64_table.inc)."""
 import pathlib
 import re
 
@@ -26,14 +26,6 @@ def fp32_table():
     return p, c
 
 
-def fp64_table():
-    block = re.search(r"kErfc64Q\[17\] = \{(.*?)\};", SRC, re.S).group(1)
-    c = _floats(block)
-    p = float(re.search(r"kErfc64P = ([0-9.]+)", SRC).group(1))
-    xmax = float(re.search(r"kErfc64XMax = ([0-9.]+)", SRC).group(1))
-    return p, xmax, c
-
-
 def test_fp32_fit_in_float32():
     p, c = fp32_table()
     x = np.linspace(0.0, 4.5, 100001).astype(np.float32)
@@ -46,21 +38,6 @@ def test_fp32_fit_in_float32():
     rel = np.abs(approx - ref) / ref
     assert rel.max() < 6e-7
     assert np.sqrt(np.mean(rel ** 2)) < 2e-7
-
-
-def test_fp64_fit():
-    p, xmax, c = fp64_table()
-    assert len(c) == 17
-    t0 = 1.0 / (1.0 + p * xmax)
-    x = np.linspace(0.0, xmax, 20001)
-    t = 1.0 / (1.0 + p * x)
-    s = (2.0 * t - (1.0 + t0)) / (1.0 - t0)
-    q = np.full_like(s, c[-1])
-    for ck in c[-2::-1]:
-        q = q * s + ck
-    approx = np.exp(-x * x) * t * q
-    rel = np.abs(approx - erfc(x)) / erfc(x)
-    assert rel.max() < 6e-15
 
 
 @pytest.mark.parametrize("y", [1e-6, 0.01, 0.1, 0.25])
