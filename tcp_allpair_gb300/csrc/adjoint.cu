@@ -66,7 +66,7 @@ __device__ __forceinline__ void radial_f64(const AdjArgs &a, const F64Tab &tb, d
     const double rinv = rsqrt_nr(r2), r = r2 * rinv, rinv2 = rinv * rinv;
     const double al = a.c.alpha;
     const double e = exp_neg_tab(a.c.alpha2 * r2, tb);
-    const double w0 = (erfc_tab(al * r, e, tb) * rinv + a.c.c_gauss_d * e) * rinv2;
+    const double w0 = e * ewald_q(al * r, tb) * rinv * rinv2;   // (erfc(ar)/r + 2a/sqrt(pi) e)/r^2
     G1 = w0;
     G2 = (3.0 * w0 + a.c2a * e) * rinv2;
     dl = 0.0;

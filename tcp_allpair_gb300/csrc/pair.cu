@@ -319,10 +319,10 @@ __device__ __forceinline__ void tile_f64(const double4_32a *__restrict__ tj, int
                                          const F64Tab &tb) {
     // The expressions of force.f90 without divisions (GB300 issues FP64 at 1/64
     // of the FP32 rate): DNINT of d/box by multiplication with 1/box, 1/r from
-    // rsqrt_nr, the exponentials from the table-driven exp_neg_tab, and
-    // erfc(ar) (the reference's 1 - erf(ar)) and erfc(r/lambda) from the
-    // Gaussians exp(-a^2 r^2) and exp(-r^2/lambda^2) that the force needs anyway
-    // (erfc_tab; pair_math.cuh).
+    // rsqrt_nr, the exponentials from the table-driven exp_neg_tab, the Ewald
+    // force term erfc(ar) + 2ar/sqrt(pi) exp(-a^2 r^2) (the reference's
+    // 1 - erf(ar)) as exp(-a^2 r^2) ewald_q(ar), and erfc(r/lambda) from the
+    // Kelbg Gaussian exp(-r^2/lambda^2) (erfc_tab; pair_math.cuh).
     const double a = c.alpha;
     for (int jj = sub; jj < cnt; jj += TPP) {
         const double4_32a xj = tj[jj];
@@ -334,19 +334,20 @@ __device__ __forceinline__ void tile_f64(const double4_32a *__restrict__ tj, int
         if (r2 < c.rc2 && r2 > 0.0) {
             const double rinv = rsqrt_nr(r2), r = r2 * rinv, rinv3 = rinv * rinv * rinv;
             const double e = exp_neg_tab(c.alpha2 * r2, tb);
-            const double x = erfc_tab(a * r, e, tb);
+            const double sq = e * ewald_q(a * r, tb);          // erfc(ar) + 2ar/sqrt(pi) exp(-a^2 r^2)
+            const double er = fma(sq, rinv, -c.c_gauss_d * e);  // erfc(ar)/r
             double df, u;
             if (KIND == 0) {                                   // force.f90:104-106
-                df = kEps * qq * fma(c.c_gauss_d * r, e, x) * rinv3;
-                u = qq * x * rinv;
+                df = kEps * qq * sq * rinv3;
+                u = qq * er;
             } else if (KIND == 1) {                            // force.f90:135-139
                 const double y = exp_neg_tab(r * c.inv_rs_d, tb);
-                df = kEps * qq * (fma(c.c_gauss_d * r, e, x) - y - y * r * c.inv_rs_d) * rinv3;
-                u = qq * (x - y) * rinv;
+                df = kEps * qq * (sq - y - y * r * c.inv_rs_d) * rinv3;
+                u = qq * (er - y * rinv);
             } else {                                           // Kelbg
                 const double g = exp_neg_tab(r2 * c.inv_lam2, tb);
-                df = kEps * qq * (fma(c.c_gauss_d * r, e, x) - g) * rinv3;
-                u = qq * ((x - g) * rinv + c.sqrtpi_lam_d * erfc_tab(r * c.inv_lam, g, tb));
+                df = kEps * qq * (sq - g) * rinv3;
+                u = qq * ((er - g * rinv) + c.sqrtpi_lam_d * erfc_tab(r * c.inv_lam, g, tb));
             }
             fx += df * xr0;
             fy += df * xr1;

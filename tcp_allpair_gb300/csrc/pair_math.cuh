@@ -69,58 +69,66 @@ __device__ __forceinline__ void kelbg_close(float y, float x, float &num_f, floa
 #include "erfcx64_table.inc"
 
 struct F64Tab {
-    double erfcx[kErfcxDeg + 1][kErfcxSeg];   // [k][j]: lanes on different segments use different banks
-    double exp2[64];
+    double ewq[kEwqDeg + 1][kEwqSeg];   // [k][j]: lanes on different segments use different banks
+    double exp2[kExpTab];
 };
 
 // all threads of the CTA; the caller synchronises before first use
 __device__ __forceinline__ void load_f64_tab(F64Tab &t) {
-    for (int i = threadIdx.x; i < (kErfcxDeg + 1) * kErfcxSeg; i += blockDim.x)
-        (&t.erfcx[0][0])[i] = (&kErfcxTab[0][0])[i];
-    for (int i = threadIdx.x; i < 64; i += blockDim.x) t.exp2[i] = kExp2Tab[i];
+    for (int i = threadIdx.x; i < (kEwqDeg + 1) * kEwqSeg; i += blockDim.x) (&t.ewq[0][0])[i] = (&kEwqTab[0][0])[i];
+    for (int i = threadIdx.x; i < kExpTab; i += blockDim.x) t.exp2[i] = kExp2Tab[i];
 }
 
 constexpr double kRound52 = 6755399441055744.0;   // 1.5 * 2^52: x + kRound52 holds rint(x) in its low word
+constexpr double kTwoOverSqrtPi = 1.1283791670955126;
 
-// exp(-z) for 0 <= z < 700 (0 beyond): -z = k ln2/64 + f with k = rint(-64 z/ln2)
-// and |f| <= ln2/128, exp(-z) = 2^(k >> 6) 2^((k & 63)/64) (1 + p(f)), p the
-// degree-5 Taylor polynomial of exp(f) - 1 (truncation 4e-17).  The first
-// reduction step is exact (one FMA of a 13-bit k), ln2/64 is split in two
-// doubles; relative error 2e-16.  10 FP64 operations.
+// exp(-z) for 0 <= z < 700 (0 beyond): -z = k ln2/256 + f with
+// k = rint(-256 z/ln2) and |f| <= ln2/512, exp(-z) = 2^(k >> 8) 2^((k & 255)/256)
+// (1 + p(f)), p the degree-4 Taylor polynomial of exp(f) - 1 (truncation
+// 4e-17).  The first reduction step is exact (one FMA of a 16-bit k), ln2/256
+// is split in two doubles; relative error 2e-16.  9 FP64 operations.
 __device__ __forceinline__ double exp_neg_tab(double z, const F64Tab &t) {
-    constexpr double kInvLn2x64 = 92.33248261689366;
-    constexpr double kLn2d64Hi = 0.010830424696249145, kLn2d64Lo = 3.623510646634843e-19;
-    const double kd = fma(z, -kInvLn2x64, kRound52);
+    constexpr double kInvLn2x256 = 369.3299304675746;
+    constexpr double kLn2d256Hi = 0.0027076061740622863, kLn2d256Lo = 9.058776616587108e-20;
+    const double kd = fma(z, -kInvLn2x256, kRound52);
     const int k = __double2loint(kd);
     const double kf = kd - kRound52;
-    double f = fma(-kf, kLn2d64Hi, -z);
-    f = fma(-kf, kLn2d64Lo, f);
-    double q = fma(f, 1.0 / 120.0, 1.0 / 24.0);
-    q = fma(q, f, 1.0 / 6.0);
+    double f = fma(-kf, kLn2d256Hi, -z);
+    f = fma(-kf, kLn2d256Lo, f);
+    double q = fma(f, 1.0 / 24.0, 1.0 / 6.0);
     q = fma(q, f, 0.5);
     q = fma(q, f, 1.0);
-    const double tk = t.exp2[k & 63];
+    const double tk = t.exp2[k & (kExpTab - 1)];
     const double v = fma(tk, q * f, tk);
-    // times 2^(k >> 6) by the exponent field; the result stays normal for z < 700
-    const double sc = __hiloint2double((int)((unsigned)__double2hiint(v) + ((unsigned)(k >> 6) << 20)),
+    // times 2^(k >> 8) by the exponent field; the result stays normal for z < 700
+    const double sc = __hiloint2double((int)((unsigned)__double2hiint(v) + ((unsigned)(k >> 8) << 20)),
                                        __double2loint(v));
     return __double2hiint(z) < 0x4085E000 ? sc : 0.0;   // z < 700 (z >= 0: the high words order as z)
 }
 
-// erfc(x) = g erfcx(x) for x >= 0 with g = exp(-x^2) from the caller: for
-// x <= 9, x = j/8 + h with |h| <= 1/16 and erfcx by the degree-9 segment
-// polynomial j in h (relative error about 3e-16 with a correctly rounded g);
-// beyond 9 (erfc < 5e-37) and for NaN, 0.  No branch: the segment index of an
-// argument out of range is replaced by 0 and its value discarded.
-__device__ __forceinline__ double erfc_tab(double x, double g, const F64Tab &t) {
+// Q(x) = erfcx(x) + 2x/sqrt(pi) for x >= 0, so that the Ewald real-space force
+// term erfc(x) + 2x/sqrt(pi) exp(-x^2) is exp(-x^2) Q(x): for x <= 9,
+// x = j/8 + h with |h| <= 1/16 and Q by the degree-9 segment polynomial j in h
+// (relative error 2e-16); beyond 9 (where exp(-x^2) < 7e-36) and for NaN, 0.
+// No branch: the segment index of an argument out of range is replaced by 0
+// and its value discarded.  13 FP64 operations.
+__device__ __forceinline__ double ewald_q(double x, const F64Tab &t) {
     const bool in = (unsigned)__double2hiint(x) <= 0x40220000u;   // x <= 9 on the high word (x >= 0)
     const double kd = fma(x, 8.0, kRound52);
     const int j = in ? __double2loint(kd) : 0;
     const double h = fma(kd - kRound52, -0.125, x);
-    double q = t.erfcx[kErfcxDeg][j];
+    double q = t.ewq[kEwqDeg][j];
 #pragma unroll
-    for (int k = kErfcxDeg - 1; k >= 0; --k) q = fma(q, h, t.erfcx[k][j]);
-    return in ? g * q : 0.0;
+    for (int k = kEwqDeg - 1; k >= 0; --k) q = fma(q, h, t.ewq[k][j]);
+    return in ? q : 0.0;
+}
+
+// erfc(x) = g (Q(x) - 2x/sqrt(pi)) for x >= 0 with g = exp(-x^2) from the
+// caller (relative error 1e-14 at x = 6 from the cancellation, absolute below
+// 2e-16 g Q(x)); 0 beyond 9 (erfc < 5e-37).
+__device__ __forceinline__ double erfc_tab(double x, double g, const F64Tab &t) {
+    const double v = g * fma(-kTwoOverSqrtPi, x, ewald_q(x, t));
+    return (unsigned)__double2hiint(x) <= 0x40220000u ? v : 0.0;
 }
 
 // 1/sqrt(x) for positive normal x: the hardware approximation

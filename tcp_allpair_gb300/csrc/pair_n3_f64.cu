@@ -20,9 +20,10 @@
 // exact and then rounded once to FP64 (the sign choice at |d| = box/2 exactly
 // differs from DNINT's, where r >= rc), 1/r and 1/r^3 come from one
 // rsqrt_nr, the exponentials from the table-driven exp_neg_tab (2e-16
-// relative), and erfc(alpha r) from the Gaussian exp(-alpha^2 r^2) that the
-// force needs anyway times the segment polynomial of erfcx (erfc_tab; 3e-16
-// relative, fit_erfcx64.py), where the reference takes 1 - erf(alpha r).  The
+// relative), and the Ewald force term erfc(ar) + 2ar/sqrt(pi) exp(-a^2 r^2)
+// (the reference's 1 - erf(ar)) is the Gaussian exp(-a^2 r^2), which the force
+// needs anyway, times the segment polynomial of erfcx(x) + 2x/sqrt(pi)
+// (ewald_q; 2e-16 relative, fit_erfcx64.py).  The
 // cut-off and Kelbg range tests compare the bit patterns of non-negative
 // doubles, which order as their values.
 #include <algorithm>
@@ -46,30 +47,23 @@ template <int KIND, bool ENERGY>
 __device__ __forceinline__ double n3_pair_f64(const PairConsts &c, double r2, bool ok, double &pe, const F64Tab &tb) {
     const double rinv = rsqrt_nr(r2);
     const double r = r2 * rinv;
+    const double rinv_m = ok ? rinv : 0.0;
     const double e = exp_neg_tab(c.alpha2 * r2, tb);
-    double s, u = 0.0;
+    double s = e * ewald_q(c.alpha * r, tb);              // erfc(ar) + 2ar/sqrt(pi) exp(-a^2 r^2), force.f90:104-106
+    // the Ewald energy term erfc(ar)/r (force.f90:105, 1 - erf) = s/r - 2a/sqrt(pi) exp(-a^2 r^2)
+    if (ENERGY) pe = fma(s, rinv_m, fma(-c.c_gauss_d, ok ? e : 0.0, pe));
     if (KIND == 2) {                                      // Kelbg, e-i pairs
-        const double x = erfc_tab(c.alpha * r, e, tb);
-        s = fma(c.c_gauss_d * r, e, x);                   // erfc(ar) + 2ar/sqrt(pi) exp(-a^2 r^2)
-        if (ENERGY) u = x * rinv;
         if (__double_as_longlong(r2) < __double_as_longlong(c.kelbg_far2)) {   // r < 8.5 lambda
             const double g = exp_neg_tab(r2 * c.inv_lam2, tb);
             s -= g;
-            if (ENERGY) u += c.sqrtpi_lam_d * erfc_tab(r * c.inv_lam, g, tb) - g * rinv;
+            if (ENERGY && ok) pe += c.sqrtpi_lam_d * erfc_tab(r * c.inv_lam, g, tb) - g * rinv;
         }
-    } else {
-        const double x = erfc_tab(c.alpha * r, e, tb);    // 1 - erf(ar), force.f90:104 / 135
-        s = fma(c.c_gauss_d * r, e, x);
-        if (KIND == 1) {                                  // Deutsch, force.f90:136-139
-            const double y = exp_neg_tab(r * c.inv_rs_d, tb);
-            s = s - y - y * r * c.inv_rs_d;
-            if (ENERGY) u = (x - y) * rinv;
-        } else if (ENERGY) {
-            u = x * rinv;
-        }
+    } else if (KIND == 1) {                               // Deutsch, force.f90:136-139
+        const double y = exp_neg_tab(r * c.inv_rs_d, tb);
+        s = s - y - y * r * c.inv_rs_d;
+        if (ENERGY) pe = fma(-y, rinv_m, pe);
     }
-    if (ENERGY && ok) pe += u;
-    return ok ? s * (rinv * rinv * rinv) : 0.0;
+    return s * (rinv_m * rinv * rinv);
 }
 
 // minimum-image separation from 64-bit fixed-point coordinates (2^64 per box

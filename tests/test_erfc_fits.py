@@ -61,19 +61,23 @@ def test_kelbg_close_series(y):
 
 def fp64_segment_tables():
     inc = (CSRC / "erfcx64_table.inc").read_text()
-    deg = int(re.search(r"kErfcxDeg = (\d+)", inc).group(1))
-    nseg = int(re.search(r"kErfcxSeg = (\d+)", inc).group(1))
-    block = re.search(r"kErfcxTab\[\d+\]\[\d+\] = \{(.*?)\};", inc, re.S).group(1)
+    deg = int(re.search(r"kEwqDeg = (\d+)", inc).group(1))
+    nseg = int(re.search(r"kEwqSeg = (\d+)", inc).group(1))
+    nexp = int(re.search(r"kExpTab = (\d+)", inc).group(1))
+    block = re.search(r"kEwqTab\[\d+\]\[\d+\] = \{(.*?)\};", inc, re.S).group(1)
     rows = re.findall(r"\{([^{}]*)\}", block)
     tab = np.array([[float(v) for v in r.split(",")] for r in rows])
     assert tab.shape == (deg + 1, nseg)
-    e2 = np.array([float(v) for v in re.search(r"kExp2Tab\[64\] = \{(.*?)\};", inc, re.S).group(1).split(",")])
+    e2 = np.array([float(v) for v in
+                   re.search(r"kExp2Tab\[\d+\] = \{(.*?)\};", inc, re.S).group(1).split(",")])
+    assert len(e2) == nexp
     return tab, e2
 
 
-def test_fp64_segment_erfc():
-    """erfc_tab (pair_math.cuh): erfc(x) = exp(-x^2) * the degree-9 segment
-    polynomial of erfcx at the nearest multiple of 1/8, on [0, 9]."""
+def test_fp64_segment_ewald_q():
+    """ewald_q (pair_math.cuh): Q(x) = erfcx(x) + 2x/sqrt(pi) by the degree-9
+    segment polynomial at the nearest multiple of 1/8 on [0, 9]; the Ewald force
+    term exp(-x^2) Q(x) and erfc(x) = exp(-x^2) (Q(x) - 2x/sqrt(pi))."""
     tab, _ = fp64_segment_tables()
     x = np.concatenate([np.linspace(0.0, 9.0, 40001), [9.0 + 1e-13]])
     j = np.rint(8.0 * x).astype(int)
@@ -82,9 +86,12 @@ def test_fp64_segment_erfc():
     q = tab[-1, j]
     for k in range(tab.shape[0] - 2, -1, -1):
         q = q * h + tab[k, j]
-    approx = np.exp(-x * x) * q
-    ref = erfc(x)
-    assert np.max(np.abs(approx - ref) / ref) < 2e-15
+    g = np.exp(-x * x)
+    c = 2.0 / np.sqrt(np.pi)
+    force = erfc(x) + c * x * g
+    assert np.max(np.abs(g * q - force) / force) < 2e-15
+    sel = x <= 6.0
+    assert np.max(np.abs(g * (q - c * x) - erfc(x))[sel] / erfc(x)[sel]) < 5e-14
 
 
 def _fma(a, b, c):
@@ -95,23 +102,23 @@ def _fma(a, b, c):
 
 def test_fp64_table_exp():
     """exp_neg_tab (pair_math.cuh) step by step with fused multiply-adds:
-    2^(k/64) (1 + p(f)) with the 2^(i/64) table, against numpy's exp on [0, 700)."""
+    2^(k/256) (1 + p(f)) with the 2^(i/256) table, against numpy's exp on [0, 700)."""
     _, e2 = fp64_segment_tables()
-    assert np.max(np.abs(e2 / np.exp2(np.arange(64) / 64.0) - 1)) < 2.3e-16
+    n = len(e2)
+    assert n == 256 and np.max(np.abs(e2 / np.exp2(np.arange(n) / n) - 1)) < 2.3e-16
     rng = np.random.default_rng(5)
     M = 6755399441055744.0
-    hi, lo = 0.010830424696249145, 3.623510646634843e-19
+    hi, lo = 0.0027076061740622863, 9.058776616587108e-20
     worst = 0.0
     for z in np.concatenate([rng.uniform(0.0, 80.0, 1500), rng.uniform(80.0, 699.0, 500), [0.0, 1e-300]]):
-        kd = _fma(z, -92.33248261689366, M)
+        kd = _fma(z, -369.3299304675746, M)
         k = int(kd - M)
         kf = kd - M
         f = _fma(-kf, hi, -z)
         f = _fma(-kf, lo, f)
-        q = _fma(f, 1.0 / 120.0, 1.0 / 24.0)
-        q = _fma(q, f, 1.0 / 6.0)
+        q = _fma(f, 1.0 / 24.0, 1.0 / 6.0)
         q = _fma(q, f, 0.5)
         q = _fma(q, f, 1.0)
-        v = _fma(e2[k & 63], q * f, e2[k & 63]) * 2.0 ** (k >> 6)
+        v = _fma(e2[k & 255], q * f, e2[k & 255]) * 2.0 ** (k >> 8)
         worst = max(worst, abs(v / np.exp(-z) - 1))
     assert worst < 5e-16
