@@ -550,6 +550,7 @@ void make_pair_consts(tcp_ctx *c) {
         k.inv_box[d] = 1.0 / p.box[d];
         k.sl[d] = p.box[d] / 18446744073709551616.0;
     }
+    k.sl2 = k.sl[0] * k.sl[0];
     k.rc2 = c->rc2;
     k.alpha = c->alpha;
     k.rs = rs;

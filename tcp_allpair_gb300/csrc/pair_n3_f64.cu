@@ -73,10 +73,12 @@ __device__ __forceinline__ double fixed_diff(long long a, long long b, double sc
 }
 
 // One item: the R i-particles of this lane against a j-subtile in shared
-// memory.  MASKED: apply validity and i < j index masks.
+// memory.  MASKED: apply validity and i < j index masks.  CUBIC: the
+// separations stay in units of L/2^64 (r^2 scaled once, the force and reaction
+// sums once per item by the caller) instead of three scalings per pair.
 // RDF: +2 per unique pair inside rc in bin INT(r/dx) of its type, r from sqrt
 // as in the ordered FP64 kernel (force.f90:99-103)
-template <int KIND, bool ENERGY, bool MASKED, int R, bool RDF = false>
+template <int KIND, bool ENERGY, bool MASKED, int R, bool RDF, bool CUBIC>
 __device__ __forceinline__ void n3_item_f64(const PairConsts &c, const longlong4_32a *__restrict__ tj, int cnt,
                                             int jstart, const longlong3 (&xi)[R], int ibase, int iend,
                                             double (*sjacc)[3], double (&p)[R][3], double &pe,
@@ -95,10 +97,10 @@ __device__ __forceinline__ void n3_item_f64(const PairConsts &c, const longlong4
         for (int s = 0; s < 32; ++s) {
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const double dx = fixed_diff(xi[r].x, xj.x, c.sl[0]);
-                const double dy = fixed_diff(xi[r].y, xj.y, c.sl[1]);
-                const double dz = fixed_diff(xi[r].z, xj.z, c.sl[2]);
-                const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+                const double dx = fixed_diff(xi[r].x, xj.x, CUBIC ? 1.0 : c.sl[0]);
+                const double dy = fixed_diff(xi[r].y, xj.y, CUBIC ? 1.0 : c.sl[1]);
+                const double dz = fixed_diff(xi[r].z, xj.z, CUBIC ? 1.0 : c.sl[2]);
+                const double r2 = CUBIC ? fma(dx, dx, fma(dy, dy, dz * dz)) * c.sl2 : fma(dx, dx, fma(dy, dy, dz * dz));
                 // 0 < r2 < rc^2 on the bit patterns (r2 >= 0: they order as the values)
                 const long long rb = __double_as_longlong(r2);
                 bool ok = rb > 0 && rb < __double_as_longlong(c.rc2);
@@ -224,9 +226,16 @@ __global__ void __launch_bounds__(kN3Threads, 2) pair_n3_f64_kernel(const N3Args
         for (int r = 0; r < R; ++r) p[r][0] = p[r][1] = p[r][2] = 0.0;
         const int kind = pt == 1 ? (c.ei_model == TCP_EI_DEUTSCH ? 1 : (c.ei_model == TCP_EI_KELBG ? 2 : 0)) : 0;
         if (ok) {
+#define TCP_N3D_ITEM2(KIND, MASKED, CUBIC) \
+    n3_item_f64<KIND, ENERGY, MASKED, R, RDF, CUBIC>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe, \
+                                                     tab, RDF ? hist + pt * kNbin : nullptr, RDF ? c.inv_dxd[pt] : 0.0)
 #define TCP_N3D_ITEM(KIND, MASKED) \
-    n3_item_f64<KIND, ENERGY, MASKED, R, RDF>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe, tab, \
-                                              RDF ? hist + pt * kNbin : nullptr, RDF ? c.inv_dxd[pt] : 0.0)
+    do {                                   \
+        if (c.cubic)                       \
+            TCP_N3D_ITEM2(KIND, MASKED, true); \
+        else                               \
+            TCP_N3D_ITEM2(KIND, MASKED, false); \
+    } while (0)
             if (masked) {
                 if (kind == 1) TCP_N3D_ITEM(1, true);
                 else if (kind == 2) TCP_N3D_ITEM(2, true);
@@ -237,17 +246,19 @@ __global__ void __launch_bounds__(kN3Threads, 2) pair_n3_f64_kernel(const N3Args
                 else TCP_N3D_ITEM(0, false);
             }
 #undef TCP_N3D_ITEM
+#undef TCP_N3D_ITEM2
         }
         const double qq = c.qq[pt];
+        const double us = c.cubic ? c.sl[0] : 1.0;   // units of the item's sums
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
-            for (int kk = 0; kk < 3; ++kk) fi[r][kk] = fma(qq, p[r][kk], fi[r][kk]);
+            for (int kk = 0; kk < 3; ++kk) fi[r][kk] = fma(qq * us, p[r][kk], fi[r][kk]);
         if (ENERGY) etot = fma(qq, pe, etot);
         // all warps are done with this subtile and its reaction sums
         const bool timeout = __syncthreads_or(!ok);
         if (!timeout && tid < cnt) {
-            const double sc = -kEps * qq;
+            const double sc = -kEps * qq * us;
             const size_t j = (size_t)jstart + tid;
             atomicAdd(&a.facc[j], sc * sjacc[tid][0]);
             atomicAdd(&a.facc[(size_t)a.ntot + j], sc * sjacc[tid][1]);

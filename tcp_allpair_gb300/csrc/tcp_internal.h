@@ -54,6 +54,7 @@ struct PairConsts {
     double rc2, alpha, rs, lambda;
     double inv_box[3];         // 1/box (minimum image by multiplication)
     double sl[3];              // box / 2^64: the 64-bit fixed-point difference in A
+    double sl2;                // sl[0]^2 (cubic boxes: r^2 from the unscaled differences)
     double alpha2;             // alpha^2
     double c_gauss_d;          // 2 alpha / sqrt(pi)
     double inv_rs_d;           // 1/rs
