@@ -44,6 +44,26 @@ def test_direct_fp64(ei, n):
     assert oracle.rms_rel(f, fo) < FP64_REL
 
 
+@pytest.mark.parametrize("deterministic", [False, True])
+@pytest.mark.parametrize("ei", ["deutsch", "kelbg"])
+def test_direct_fp64_at_rounding_level(ei, deterministic):
+    """The FP64 kernels' table-driven exp / erfc and Newton rsqrt (about
+    2e-16 relative each) keep the direct sum at FP64 rounding level: RMS force
+    and energy within 1e-13 of the oracle (math-library erfc / exp / sqrt),
+    a hundred times tighter than the general FP64 bound."""
+    s = make(2048, seed=31, lam=0.3)
+    o = oracle.Oracle.from_system(s, ei=ei)
+    fo, uo = o.force_direct(s.x)
+    with ctx_for(s, precision="fp64", ei=ei, recip="none") as c:
+        if deterministic:
+            c.set_flags(T.FLAG_ENERGY | T.FLAG_DETERMINISTIC)
+        ur = c.Force_direct_self()
+        _, _, f, _ = c.download(x=False, v=False, f=True)
+    err = oracle.rms_rel(f, fo)
+    assert err < 1e-13, err
+    assert ur == pytest.approx(uo, rel=1e-13)
+
+
 @pytest.mark.parametrize("ei", ["deutsch", "kelbg", "coulomb"])
 @pytest.mark.parametrize("n", [1024, 4096, 777])
 def test_direct_fp32c(ei, n):
