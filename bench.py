@@ -77,10 +77,18 @@ class Clocks:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except (FileNotFoundError, OSError):
             self.proc = None
+            return self
+        # the timed region starts once the sampler writes (nvidia-smi takes a moment to start)
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 3.0 and self.proc.poll() is None:
+            if pathlib.Path(self.f.name).stat().st_size > 0:
+                break
+            time.sleep(0.02)
+        self.skip = pathlib.Path(self.f.name).read_text().count("\n")   # samples taken before the region
         return self
 
     def __exit__(self, *exc):
@@ -96,6 +104,7 @@ class Clocks:
             return None
         self.f.flush()
         rows = [r.split(",") for r in pathlib.Path(self.f.name).read_text().splitlines() if r.strip()]
+        rows = rows[getattr(self, "skip", 0):] or rows[-1:]
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in rows:
