@@ -15,12 +15,25 @@ e2e        the same metric through the C ABI with host PT records: every step
            back (tcp_md_steps_records); `separate_calls` times the same work
            as tcp_upload x2 + tcp_md_steps + tcp_download x2.
 fp64       the plain FP64 drop-in step at the same configuration.
+recip_fp64_option
+           the FP32C step with the whole SPME chain in FP64 (TCP_PREC_FP32C_R64).
 roofline   the real-space pair kernel against the measured FP32 FFMA issue rate.
+force_error / energy_error
+           at the seeded start: RMS relative error of the real-space,
+           reciprocal and total force and the largest per-particle error, and
+           the relative errors of Ur, Um, Uo and Etot, FP32C against the FP64
+           GPU path and every GPU path against the FP64 restatement (all rows).
+nve_drift / nve_drift_fp64
+           total-energy drift over 500 NVE steps, FP32C and FP64.
+c2         the N = 16,384 isokinetic workload (Gamma 2, lambda 0.4 a, SPME
+           64^3 order 4, rescale every 10 steps, 1000 steps): FP64 and FP32C
+           step times, errors against the restatement, Etot difference.
+batch      64 replicas (N log-uniform in [512, 8192]) in one persistent launch
+           per step against looping one context per replica.
 cpu_baseline / --impl reference
            the FP64 CPU restatement (oracle/, OpenMP on all host cores; the
-           Fortran/MPI reference cannot be built on this machine) on a bounded
-           sample: R i-rows of the direct sum against all j, one full SPME and
-           one integrator pass, the direct-sum time scaled to N(N-1)/2 pairs.
+           Fortran/MPI reference cannot be built on this machine): full MD steps
+           (direct sum over all pairs, SPME, integrator).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -45,6 +58,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "pair-int/s, steps/s @N=65536: FP32-comp vs FP64 on 1 GB300, ≤2e-6 force err"
 WORKLOAD = "n65536_spme128"
+EPS = 14.399644154020082      # eV*A, data.f90:21
 # Source-level op recipe of the FP32C real-space kernels (pair.cu tile_f32,
 # pair_n3.cu n3_pair/n3_item), Coulomb pair with energy, cubic box: 3 integer
 # subtractions + 3 int->float conversions (minimum image), r^2 (3), cut-off
@@ -165,31 +179,77 @@ def profile_traffic():
 
 
 # ---------------------------------------------------------------------------
-# CPU leg: the FP64 restatement on a bounded sample
-def cpu_sample(s, rows_per_species: int, threads: int):
+# CPU leg: full MD steps of the FP64 restatement
+def kinetic(s):
+    """(1/2) sum m v^2 of the seeded start (eV), the same for every arm."""
+    m = np.concatenate([np.full(s.nel, s.xm[0]), np.full(s.nion, s.xm[1])])
+    return 0.5 * float(np.sum(m[:, None] * s.v * s.v))
+
+
+def oracle_components(o, x):
+    """Real-space, reciprocal and total forces (REMOVE_RIGIDMTN applied to the
+    total, main.f90:141) and the energies of the FP64 restatement at x."""
+    f_real, ur = o.force_direct(x)
+    f_rec, um = o.force_spme(x)
+    f_tot = f_real + f_rec
+    f_tot -= f_tot.mean(axis=0)
+    return dict(real=f_real, recip=f_rec, total=f_tot, Ur=ur, Um=um, Uo=o.Uo, Epot=(ur + o.Uo) * EPS)
+
+
+def gpu_components(ctx):
+    """The same quantities from a context at its current positions: the direct
+    sum alone (tcp_force_direct), then the whole evaluation (tcp_force), whose
+    reciprocal forces stay readable as frec."""
+    ctx.Force_direct_self()
+    _, _, f_real, _ = ctx.download(x=False, v=False, f=True)
+    e = ctx.force()
+    _, _, f_tot, f_rec = ctx.download(x=False, v=False, f=True, frec=True)
+    return dict(real=f_real, recip=f_rec, total=f_tot, Ur=e["Ur"], Um=e["Um"], Uo=e["Uo"], Epot=e["Epot"])
+
+
+def force_errors(a, ref):
+    """RMS relative error of the real-space, reciprocal and total force, and the
+    largest per-particle error of the total, relative to that particle's force
+    and to the RMS force."""
+    import oracle
+    d = np.linalg.norm(a["total"] - ref["total"], axis=1)
+    fr = np.linalg.norm(ref["total"], axis=1)
+    rms = float(np.sqrt(np.mean(fr ** 2)))
+    return {"real": oracle.rms_rel(a["real"], ref["real"]), "recip": oracle.rms_rel(a["recip"], ref["recip"]),
+            "total": oracle.rms_rel(a["total"], ref["total"]),
+            "max_particle_rel": float(np.max(d / np.maximum(fr, 1e-300))),
+            "max_particle_over_rms": float(np.max(d) / rms)}
+
+
+def energy_errors(a, ref, ekin):
+    """Relative errors of Ur, Um, Uo and Etot = Ekin + Epot + Um (the ener files)."""
+    def rel(x, y):
+        return abs(x - y) / abs(y) if y != 0 else abs(x - y)
+    et_a, et_r = ekin + a["Epot"] + a["Um"], ekin + ref["Epot"] + ref["Um"]
+    return {"Ur": rel(a["Ur"], ref["Ur"]), "Um": rel(a["Um"], ref["Um"]), "Uo": rel(a["Uo"], ref["Uo"]),
+            "Etot": rel(et_a, et_r)}
+
+
+def cpu_steps(s, nsteps: int, threads: int, warmup: int = 0):
+    """Full MD steps of the FP64 restatement (OpenMP on `threads` cores): the
+    initial force evaluation (kept for the error figures), `warmup` untimed
+    steps, then `nsteps` timed steps, each vverlet1 + direct sum over all
+    pairs + SPME + vverlet2 (main.f90:81-153)."""
     import oracle
     o = oracle.Oracle.from_system(s, ei="kelbg", nthreads=threads)
-    n = s.n
     t0 = time.perf_counter()
-    fa, _ = o.force_direct_rows(s.x, 0, rows_per_species)
-    fb, _ = o.force_direct_rows(s.x, s.nel, s.nel + rows_per_species)
-    t_rows = time.perf_counter() - t0
+    comp = oracle_components(o, s.x)
+    t_first = time.perf_counter() - t0
+    x, v, f = s.x.copy(), s.v.copy(), comp["total"].copy()
+    for _ in range(warmup):
+        o.md_step(x, v, f, s.dt)
     t0 = time.perf_counter()
-    frec, um = o.force_spme(s.x)
-    t_spme = time.perf_counter() - t0
-    x, v = s.x.copy(), s.v.copy()
-    f = np.zeros_like(x)
-    t0 = time.perf_counter()
-    o.vverlet1(x, v, f, s.dt)
-    o.vverlet2(v, f, s.dt)
-    t_int = time.perf_counter() - t0
-    rows = 2 * rows_per_species
-    pairs = n * (n - 1) / 2
-    t_step = t_rows / (rows * (n - 1)) * pairs + t_spme + t_int
-    sample_rows = np.r_[0:rows_per_species, s.nel:s.nel + rows_per_species]
-    f_rows = np.concatenate([fa, fb]) + frec[sample_rows]
-    return dict(t_step=t_step, value=pairs / t_step, t_rows=t_rows, t_spme=t_spme, t_int=t_int,
-                rows=rows, f_rows=f_rows, sample_rows=sample_rows, um=um)
+    for _ in range(nsteps):
+        o.md_step(x, v, f, s.dt)
+    t_steps = time.perf_counter() - t0
+    pairs = s.n * (s.n - 1) / 2
+    t_step = t_steps / max(nsteps, 1)
+    return dict(t_step=t_step, value=pairs / t_step, t_first=t_first, t_steps=t_steps, comp=comp)
 
 
 def run_reference(args, world, rank, dist):
@@ -201,19 +261,14 @@ def run_reference(args, world, rank, dist):
     oracle.build()
     s = make_config_system(WORKLOAD, seed=0)
     threads = os.cpu_count() or 1
-    R = args.ref_rows
-    for _ in range(args.warmup):
-        cpu_sample(s, R // 2, threads)
     t0 = time.perf_counter()
-    est = []
-    for _ in range(args.steps):
-        est.append(cpu_sample(s, R // 2, threads)["t_step"])
+    cs = cpu_steps(s, args.steps, threads, warmup=args.warmup)
     wall = time.perf_counter() - t0
-    t_step = float(np.mean(est))
+    t_step = cs["t_step"]
     n = s.n
     value = n * (n - 1) / 2 / t_step
-    sample = (f"{R} of {n} i-rows x all j (FP64, OpenMP) + one SPME 128^3 p5 + one integrator pass per step; "
-              f"direct-sum time scaled to N(N-1)/2 pairs")
+    sample = (f"{args.steps} full MD steps after {args.warmup} untimed ones: direct sum over all N(N-1)/2 pairs "
+              f"(FP64, OpenMP), SPME 128^3 p5, integrator")
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "pair-int/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "steps_per_s": 1.0 / t_step,
@@ -223,7 +278,8 @@ def run_reference(args, world, rank, dist):
         "reference_note": "the Fortran 90 + MPI + FFTE reference cannot be built here or on the GPU box "
                           "(no Fortran compiler, no MPI, FFTE not vendored); timed is the FP64 C restatement "
                           "of force.f90/vverlet.f90 in oracle/",
-        "cpu_baseline": {"value": value, "unit": "pair-int/s", "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "pair-int/s", "cores": threads, "kind": "port", "sample": sample,
+                         "timed_s": cs["t_steps"]},
         "e2e": {"value": value, "unit": "pair-int/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": wall,
     }
@@ -241,6 +297,123 @@ def config_dict(s):
             "l2": "flushed between timed steps (a 2x L2 buffer is written outside the timed spans)"}
 
 
+def nve_drift(T, p, s, nsteps, device, precision):
+    """Relative total-energy drift over nsteps NVE steps from the seeded start,
+    Etot = (mv2el + mv2ion)/2 + Epot + Um as in the ener files, sampled ten times."""
+    with T.Context(p, s.nel, s.nion, device=device) as c:
+        c.EWALD_SELF()
+        c.upload(x=s.x, v=s.v)
+        c.force()
+
+        def etot(e):
+            return 0.5 * (e["mv2el"] + e["mv2ion"]) + e["Epot"] + e["Um"]
+
+        e = c.md_steps(s.dt, 1)
+        E0 = etot(e)
+        worst, done = 0.0, 1
+        every = max(1, nsteps // 10)
+        t0 = time.perf_counter()
+        while done < nsteps:
+            k = min(every, nsteps - done)
+            e = c.md_steps(s.dt, k)
+            done += k
+            worst = max(worst, abs(etot(e) - E0) / abs(E0))
+        wall = time.perf_counter() - t0
+    return {"steps": nsteps, "E_step1_eV": E0, "rel_drift_end": abs(etot(e) - E0) / abs(E0),
+            "rel_drift_max_sampled": worst, "sampled_every": every, "precision": precision,
+            "wall_s": wall}
+
+
+def run_c2(T, args, device, threads):
+    """The N = 16,384 workload: Gamma 2, lambda 0.4 a, SPME 64^3 order 4, the
+    isokinetic rescale to T = 0.5 every 10 steps (vverlet.f90:301-372), run
+    `args.c2_steps` steps in FP64 and in FP32C from the same start.  Reports
+    both step times, the force and energy errors of both at the start against
+    the FP64 restatement, and the FP32C - FP64 total-energy difference along
+    the run (the thermostat does not conserve energy, so no drift figure)."""
+    import oracle
+    from tcp_allpair_gb300.system import make_config_system
+    s = make_config_system("n16384_spme64", seed=0)
+    o = oracle.Oracle.from_system(s, ei="kelbg", nthreads=threads)
+    ref = oracle_components(o, s.x)
+    ek = kinetic(s)
+    pairs = s.n * (s.n - 1) / 2
+    out = {"workload": "n16384_spme64_kelbg_isokin10", "N": s.n, "gamma": 2.0, "lambda_ei_over_a": 0.4,
+           "spme_mesh": s.K, "spline_order": s.order, "thermostat": "isokin every 10 steps to T = 0.5",
+           "steps": args.c2_steps}
+    traj = {}
+    for prec in ("fp64", "fp32c"):
+        p = T.params_for(s, precision=prec, ei="kelbg", recip="spme", thermo="isokin", thermo_period=10)
+        with T.Context(p, s.nel, s.nion, device=device) as c:
+            c.EWALD_SELF()
+            c.upload(x=s.x, v=s.v)
+            comp = gpu_components(c)
+            t = c.time_steps(s.dt, 20, flush_l2=True)        # device time of one step
+            # the run itself from the seeded start, Etot sampled every tenth of it
+            c.upload(x=s.x, v=s.v)
+            c.force()
+            every = max(1, args.c2_steps // 10)
+            et = []
+            t0 = time.perf_counter()
+            for _ in range(args.c2_steps // every):
+                e = c.md_steps(s.dt, every)
+                et.append(0.5 * (e["mv2el"] + e["mv2ion"]) + e["Epot"] + e["Um"])
+            wall = time.perf_counter() - t0
+        ms = t["step"] / t["nsteps"]
+        out[prec] = {"ms_per_step": ms, "value": pairs / (ms * 1e-3), "run_wall_s": wall,
+                     "force_error_vs_oracle": force_errors(comp, ref),
+                     "energy_error_vs_oracle": energy_errors(comp, ref, ek)}
+        traj[prec] = np.array(et)
+    out["speedup_fp32c_over_fp64"] = out["fp64"]["ms_per_step"] / out["fp32c"]["ms_per_step"]
+    d = np.abs(traj["fp32c"] - traj["fp64"]) / np.abs(traj["fp64"])
+    out["etot_fp32c_vs_fp64"] = {"rel_diff_max_sampled": float(d.max()), "rel_diff_end": float(d[-1]),
+                                 "sampled_every": max(1, args.c2_steps // 10)}
+    return out
+
+
+def run_batch_leg(T, args, device):
+    """The batched-replica workload: 64 independent systems (N log-uniform in
+    [512, 8192], Gamma log-uniform in [0.1, 10], lambda uniform in [0.2a, 0.8a],
+    own box, alpha and SPME mesh) stepped together in one graph per step,
+    against looping one context per replica over the same steps."""
+    from tcp_allpair_gb300.system import make_batch_systems
+    ss = make_batch_systems(args.batch_reps, seed=0)
+    params = [T.params_for(s, precision="fp32c", ei="kelbg", recip="spme") for s in ss]
+    pairs = sum(s.n * (s.n - 1) / 2 for s in ss)
+    dt = ss[0].dt
+    with T.Batch(params, [s.nel for s in ss], [s.nion for s in ss], device=device) as b:
+        b.EWALD_SELF()
+        for r, s in enumerate(ss):
+            b.upload(r, x=s.x, v=s.v)
+        b.force()
+        bvar, bms = b.autotune_report()
+        b.md_steps(dt, args.warmup)
+        ms_batch = b.time_steps(dt, args.steps)
+    ctxs = []
+    for p_, s in zip(params, ss):
+        c = T.Context(p_, s.nel, s.nion, device=device)
+        c.EWALD_SELF()
+        c.upload(x=s.x, v=s.v)
+        c.force()
+        c.md_steps(dt, args.warmup)
+        ctxs.append(c)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for c in ctxs:
+            c.lib.tcp_md_steps(c.h, dt, 1, None)
+    for c in ctxs:
+        c.md_steps(dt, 0)          # synchronise every stream
+    ms_loop = (time.perf_counter() - t0) * 1e3 / args.steps
+    for c in ctxs:
+        c.close()
+    return {"metric": "aggregate pair-int/s, batched replicas", "workload": f"batch{len(ss)}_n512-8192",
+            "value": pairs / (ms_batch * 1e-3), "unit": "pair-int/s", "ms_per_step": ms_batch,
+            "loop_single_contexts": {"value": pairs / (ms_loop * 1e-3), "ms_per_step": ms_loop},
+            "speedup_batch_over_loop": ms_loop / ms_batch, "replicas": len(ss),
+            "particles": sum(s.n for s in ss), "steps": args.steps, "warmup": args.warmup,
+            "batch_variant": int(bvar), "batch_variant_ms": [round(float(x), 4) for x in bms if x > 0]}
+
+
 def run_gpu(args, world, rank, local, dist):
     import oracle
     import tcp_allpair_gb300 as T
@@ -249,22 +422,26 @@ def run_gpu(args, world, rank, local, dist):
     s = make_config_system(WORKLOAD, seed=rank)
     n = s.n
     pairs = n * (n - 1) / 2
+    ek = kinetic(s)
     p32 = T.params_for(s, precision="fp32c", ei="kelbg", recip="spme", thermo="notemp")
     p64 = T.params_for(s, precision="fp64", ei="kelbg", recip="spme", thermo="notemp")
+    pr64 = T.params_for(s, precision="fp32c_r64", ei="kelbg", recip="spme", thermo="notemp")
     ctx = T.Context(p32, s.nel, s.nion, device=local)
     ctx.EWALD_SELF()
     ctx.upload(x=s.x, v=s.v)
     e0 = ctx.force()                        # initial forces (restart-style start, main.f90:49-54)
     tune = ctx.autotune_report()
     reserve, reserve_ms = ctx.overlap_report()
-    _, _, f32, _ = ctx.download(x=False, v=False, f=True)
+    comp32 = gpu_components(ctx)
+    ctx.upload(x=s.x, v=s.v)
+    ctx.force()
 
     ctx64 = T.Context(p64, s.nel, s.nion, device=local)
     ctx64.EWALD_SELF()
     ctx64.upload(x=s.x, v=s.v)
+    comp64 = gpu_components(ctx64)
+    ctx64.upload(x=s.x, v=s.v)
     ctx64.force()
-    _, _, f64, _ = ctx64.download(x=False, v=False, f=True)
-    err_vs_fp64 = oracle.rms_rel(f32, f64)
 
     # warm-up, then the timed steps (device-resident)
     ctx.md_steps(s.dt, args.warmup)
@@ -288,30 +465,30 @@ def run_gpu(args, world, rank, local, dist):
     step64_ms = t64["step"] / t64["nsteps"]
     ctx64.close()
 
-    # NVE energy drift of the FP32C step over the headline run length (500 steps),
-    # total energy Etot = (mv2el + mv2ion)/2 + Epot + Um as in the ener files
-    drift = None
-    if args.nve_steps > 0 and rank == 0:
-        ctx_d = T.Context(p32, s.nel, s.nion, device=local)
-        ctx_d.EWALD_SELF()
-        ctx_d.upload(x=s.x, v=s.v)
-        ctx_d.force()
+    # the FP32C step with the whole reciprocal chain in FP64 (TCP_PREC_FP32C_R64)
+    with T.Context(pr64, s.nel, s.nion, device=local) as cr:
+        cr.EWALD_SELF()
+        cr.upload(x=s.x, v=s.v)
+        comp_r64 = gpu_components(cr)
+        cr.upload(x=s.x, v=s.v)
+        cr.force()
+        cr.md_steps(s.dt, args.warmup)
+        tr = cr.time_steps(s.dt, args.steps, flush_l2=True)
+        recip64_alone_ms = cr.time_component(1, 5)
+    r64_ms = tr["step"] / tr["nsteps"]
+    recip_fp64 = {"ms_per_step": r64_ms, "value": pairs / (r64_ms * 1e-3),
+                  "pair_kernel_ms": tr["pair"] / tr["nsteps"], "recip_concurrent_wall": tr["recip"] / tr["nsteps"],
+                  "recip_alone_ms": recip64_alone_ms, "step_time_ratio_vs_fp32c_recip": r64_ms / step_ms,
+                  "note": "TCP_PREC_FP32C_R64: the FP32C real-space sum with the SPME spread, transforms, "
+                          "influence multiply and gather in FP64, on the second stream beside the pair kernel"}
 
-        def etot(e):
-            return 0.5 * (e["mv2el"] + e["mv2ion"]) + e["Epot"] + e["Um"]
-
-        e = ctx_d.md_steps(s.dt, 1)
-        E0 = etot(e)
-        worst, done = 0.0, 1
-        every = max(1, args.nve_steps // 10)
-        while done < args.nve_steps:
-            k = min(every, args.nve_steps - done)
-            e = ctx_d.md_steps(s.dt, k)
-            done += k
-            worst = max(worst, abs(etot(e) - E0) / abs(E0))
-        drift = {"steps": args.nve_steps, "E_step1_eV": E0, "rel_drift_end": abs(etot(e) - E0) / abs(E0),
-                 "rel_drift_max_sampled": worst, "sampled_every": every, "precision": "fp32c"}
-        ctx_d.close()
+    # NVE energy drift over the headline run length (500 steps), FP32C and FP64
+    drift = drift64 = None
+    if rank == 0:
+        if args.nve_steps > 0:
+            drift = nve_drift(T, p32, s, args.nve_steps, local, "fp32c")
+        if args.nve_fp64_steps > 0:
+            drift64 = nve_drift(T, p64, s, args.nve_fp64_steps, local, "fp64")
 
     # e2e through the C ABI with host PT records
     qel, qion = s.to_pt()
@@ -362,7 +539,7 @@ def run_gpu(args, world, rank, local, dist):
     traffic = profile_traffic()
     roof = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "Top/s",
             "frac": achieved / peak, "traffic": traffic,
-            "kernel": kname, "autotune_ms": [round(x, 4) for x in variant_ms.tolist() if x > 0],
+            "kernel": kname, "autotune_ms": {str(k): round(x, 4) for k, x in enumerate(variant_ms.tolist()) if x > 0},
             "recipe": f"{recipe} FP32/ALU-pipe ops + {RECIPE_SFU_OPS} SFU ops per {runit}",
             "peak_source": "measured FFMA issue rate (tcp_fp32_peak) on this GPU, not MEASURED_PEAKS.json "
                            "(which has HBM and bf16 only)",
@@ -372,18 +549,34 @@ def run_gpu(args, world, rank, local, dist):
             "frac_alone": recipe * units / (float(variant_ms[variant]) * 1e-3) / peak if variant_ms[variant] > 0 else None,
             "grid_reserve": reserve, "reserve_ms": reserve_ms}
 
-    # CPU baseline (rank 0, N = 1 only) and the FP32C force error vs the oracle
+    # CPU baseline (rank 0, N = 1 only): full steps of the FP64 restatement, whose
+    # initial evaluation is also the reference of the force and energy errors
     cpu = None
-    err_vs_oracle = None
+    ferr = {"bound_total_rms": 2e-6,
+            "definition": "RMS relative sqrt(sum|F-F_ref|^2 / sum|F_ref|^2) per component over all particles; "
+                          "max_particle_rel = max_i |dF_i|/|F_ref_i|, max_particle_over_rms = max_i |dF_i| / "
+                          "RMS|F_ref|; total includes REMOVE_RIGIDMTN",
+            "fp32c_vs_fp64_gpu": force_errors(comp32, comp64)}
+    eerr = {"fp32c_vs_fp64_gpu": energy_errors(comp32, comp64, ek)}
+    c2 = batch = None
     if rank == 0 and world == 1:
         threads = os.cpu_count() or 1
-        cs = cpu_sample(s, args.ref_rows // 2, threads)
+        cs = cpu_steps(s, args.cpu_steps, threads)
+        ref = cs["comp"]
         cpu = {"value": cs["value"], "unit": "pair-int/s", "cores": threads, "kind": "port",
-               "sample": f"{cs['rows']} of {n} i-rows x all j (FP64, OpenMP) + one SPME + one integrator pass, "
-                         f"direct-sum time scaled to N(N-1)/2 pairs ({cs['t_rows'] + cs['t_spme']:.1f} s CPU)",
+               "sample": f"{args.cpu_steps} full MD steps of the FP64 restatement (direct sum over all "
+                         f"N(N-1)/2 pairs with OpenMP, SPME 128^3 p5, integrator), {cs['t_steps']:.1f} s timed",
                "ms_per_step": cs["t_step"] * 1e3}
-        # FP32C total force vs the FP64 oracle on the sampled rows
-        err_vs_oracle = oracle.rms_rel(f32[cs["sample_rows"]], cs["f_rows"])
+        ferr["fp32c_vs_oracle"] = force_errors(comp32, ref)
+        ferr["fp64_gpu_vs_oracle"] = force_errors(comp64, ref)
+        ferr["fp32c_r64_vs_oracle"] = force_errors(comp_r64, ref)
+        eerr["fp32c_vs_oracle"] = energy_errors(comp32, ref, ek)
+        eerr["fp64_gpu_vs_oracle"] = energy_errors(comp64, ref, ek)
+        eerr["fp32c_r64_vs_oracle"] = energy_errors(comp_r64, ref, ek)
+        if args.c2_steps > 0:
+            c2 = run_c2(T, args, local, threads)
+        if args.batch_reps > 0:
+            batch = run_batch_leg(T, args, local)
 
     ctx.close()
     clocks = clk.summary()
@@ -401,10 +594,12 @@ def run_gpu(args, world, rank, local, dist):
                                           "the same chain timed by itself"},
         "fp64": {"ms_per_step": step64_ms, "value": pairs / (step64_ms * 1e-3), "steps": args.fp64_steps,
                  "speedup_fp32c_over_fp64": step64_ms / step_ms},
-        "force_error": {"rms_rel_fp32c_vs_fp64_gpu": err_vs_fp64, "rms_rel_fp32c_vs_fp64_oracle_rows": err_vs_oracle,
-                        "bound": 2e-6},
+        "recip_fp64_option": recip_fp64,
+        "force_error": ferr,
+        "energy_error": eerr,
         "energies_initial": {"Ur": e0["Ur"], "Um": e0["Um"], "Uo": e0["Uo"]},
         "nve_drift": drift,
+        "nve_drift_fp64": drift64,
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "pair-int/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
@@ -417,6 +612,8 @@ def run_gpu(args, world, rank, local, dist):
                                                         "md_steps": ph[1] / args.steps * 1e3,
                                                         "download": ph[2] / args.steps * 1e3},
                                    "path": "tcp_upload x2 + tcp_md_steps(1) + tcp_download x2"}},
+        "c2": c2,
+        "batch": batch,
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
@@ -427,8 +624,8 @@ def run_gpu(args, world, rank, local, dist):
 
 def run_pair_only(args):
     """Launch the real-space pair kernel alone on an N-particle version of the
-    headline system (profiling target: `ncu -k regex:pair_ ... python bench.py
-    --pair-only N`)."""
+    headline system (profiling target: `ncu --clock-control none -k regex:pair_
+    -c 1 ... python bench.py --pair-only N`)."""
     import tcp_allpair_gb300 as T
     n = args.pair_only
     s = T.make_system(n, gamma=1.0, lam=0.5, seed=0, ewald_rel_err=1e-6, K=64, order=5)
@@ -445,7 +642,8 @@ def run_pair_only(args):
 
 def run_recip_only(args):
     """Launch the SPME chain alone on the headline system with N particles
-    (profiling target: `ncu -k regex:spme ... python bench.py --recip-only N`)."""
+    (profiling target: `ncu --clock-control none -k regex:spme -c 3 ... python
+    bench.py --recip-only N`)."""
     import tcp_allpair_gb300 as T
     from tcp_allpair_gb300.system import make_config_system
     s = make_config_system(WORKLOAD, n=args.recip_only)
@@ -461,49 +659,9 @@ def run_recip_only(args):
 
 
 def run_batch(args):
-    """The batched-replica workload: 64 independent systems (N log-uniform in
-    [512, 8192], Gamma log-uniform in [0.1, 10], lambda uniform in [0.2a, 0.8a],
-    own box, alpha and SPME mesh) stepped together in one graph per step,
-    against looping one context per replica over the same steps."""
+    """--batch: the batched-replica leg alone."""
     import tcp_allpair_gb300 as T
-    from tcp_allpair_gb300.system import make_batch_systems
-    ss = make_batch_systems(args.batch_reps, seed=0)
-    params = [T.params_for(s, precision="fp32c", ei="kelbg", recip="spme") for s in ss]
-    pairs = sum(s.n * (s.n - 1) / 2 for s in ss)
-    dt = ss[0].dt
-    with T.Batch(params, [s.nel for s in ss], [s.nion for s in ss]) as b:
-        b.EWALD_SELF()
-        for r, s in enumerate(ss):
-            b.upload(r, x=s.x, v=s.v)
-        b.force()
-        bvar, bms = b.autotune_report()
-        b.md_steps(dt, args.warmup)
-        ms_batch = b.time_steps(dt, args.steps)
-    # looping single-system contexts (each its own graph), same steps
-    ctxs = []
-    for p_, s in zip(params, ss):
-        c = T.Context(p_, s.nel, s.nion)
-        c.EWALD_SELF()
-        c.upload(x=s.x, v=s.v)
-        c.force()
-        c.md_steps(dt, args.warmup)
-        ctxs.append(c)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        for c in ctxs:
-            c.lib.tcp_md_steps(c.h, dt, 1, None)
-    for c in ctxs:
-        c.md_steps(dt, 0)          # synchronise every stream
-    ms_loop = (time.perf_counter() - t0) * 1e3 / args.steps
-    for c in ctxs:
-        c.close()
-    out = {"metric": "aggregate pair-int/s, batched replicas", "workload": f"batch{len(ss)}_n512-8192",
-           "value": pairs / (ms_batch * 1e-3), "unit": "pair-int/s", "ms_per_step": ms_batch,
-           "loop_single_contexts": {"value": pairs / (ms_loop * 1e-3), "ms_per_step": ms_loop},
-           "speedup_batch_over_loop": ms_loop / ms_batch, "replicas": len(ss),
-           "particles": sum(s.n for s in ss), "steps": args.steps, "warmup": args.warmup,
-           "batch_variant": int(bvar), "batch_variant_ms": [round(float(x), 4) for x in bms if x > 0]}
-    print(json.dumps(out))
+    print(json.dumps(run_batch_leg(T, args, 0)))
     return 0
 
 
@@ -514,13 +672,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--ref-rows", type=int, default=4096)
+    ap.add_argument("--cpu-steps", type=int, default=3, help="full CPU steps of the cpu_baseline leg")
     ap.add_argument("--nve-steps", type=int, default=500, help="FP32C NVE energy-drift run (0: skip)")
+    ap.add_argument("--nve-fp64-steps", type=int, default=500, help="FP64 NVE energy-drift run (0: skip)")
+    ap.add_argument("--c2-steps", type=int, default=1000, help="N = 16,384 isokinetic run (0: skip)")
     ap.add_argument("--pair-only", type=int, default=0, help="profile target: pair kernel alone at this N")
     ap.add_argument("--recip-only", type=int, default=0, help="profile target: SPME chain alone at this N")
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--batch", action="store_true", help="batched-replica workload instead of the headline")
-    ap.add_argument("--batch-reps", type=int, default=64)
+    ap.add_argument("--batch-reps", type=int, default=64, help="replicas of the batched leg (0: skip)")
     args = ap.parse_args()
     if args.batch:
         return run_batch(args)

@@ -49,6 +49,9 @@ extern "C" {
 /* ---- enumerations ------------------------------------------------------ */
 #define TCP_PREC_FP64 0         /* plain FP64 pair kernel (the drop-in)        */
 #define TCP_PREC_FP32C 1        /* FP32 pair arithmetic, compensated sums      */
+#define TCP_PREC_FP32C_R64 2    /* TCP_PREC_FP32C real-space sum with the whole
+                                 * reciprocal chain (spread, transforms,
+                                 * influence, gather) in FP64                  */
 
 #define TCP_EI_DEUTSCH 0        /* reference e-i term (erfc(ar)-exp(-r/rs))/r, force.f90:135-139 */
 #define TCP_EI_KELBG 1          /* Kelbg e-i potential with length lambda_ei   */
@@ -102,7 +105,11 @@ typedef struct tcp_params {
 /* Energies of the last force evaluation / step (TYPE ST, data.f90:89-92). */
 typedef struct tcp_energies {
     double Ur;              /* real-space energy WITHOUT eps (sys%Ur)        */
-    double Uo;              /* self energy WITHOUT eps (sys%Uo)              */
+    double Uo;              /* self energy WITHOUT eps (sys%Uo), plus the
+                             * neutralising-background energy
+                             * -pi Q^2/(2 V alpha^2) of a system with net
+                             * charge Q (0 for neutral systems; the reference
+                             * has no such term)                             */
     double Um;              /* reciprocal energy WITH eps (sys%Um)           */
     double Epot;            /* (Ur + Uo) * eps, main.f90:138                 */
     double mv2el, mv2ion;   /* sum m v^2 per species (sys%mv2el/mv2ion)      */
@@ -122,8 +129,31 @@ int tcp_version(int *major, int *minor, int *arch);
 
 /* EWALD_SELF(NS,param,sys,PSI,COMM), force.f90:4-49: checks rc <= L/2,
  * sets alpha (3.1/rc unless p->a > 0) and rc^2, fills the influence mesh and
- * returns Uo (no eps).  Must precede every force call. */
+ * returns Uo (no eps): -alpha/sqrt(pi) sum q^2 (force.f90:44-45) plus, for a
+ * net charge Q, the background term -pi Q^2/(2 V alpha^2).  Must precede
+ * every force call. */
 int tcp_ewald_self(tcp_ctx *ctx, double *alpha_out, double *Uo_out);
+
+/* The GPU build's own parameters for callers that fill tcp_params from the
+ * reference's tcp.prm (main.f90:221-294), which has no field for them; no
+ * counterpart in the reference.  Keys and values, read first from the file
+ * named by $TCP_GPU_PRM, else ./tcp_gpu.prm if it exists ("key value" or
+ * "key = value" per line, '#' or '!' starts a comment), then from the
+ * environment variables TCP_GPU_<KEY>, later ones overriding earlier ones:
+ *   precision     fp64 | fp32c | fp32c_r64      -> p->precision
+ *   ei_model      deutsch | kelbg | coulomb     -> p->ei_model
+ *   reciprocal    none | spme | ewald           -> p->reciprocal
+ *   order         4..8                          -> p->order
+ *   alpha         Ewald alpha [1/A], 0 = 3.1/rc -> p->a
+ *   lambda_ei     Kelbg length [A]              -> p->lambda_ei
+ *   ewald_nmax2, thermo_period, seed, charge_scale -> the fields of that name
+ *   device        GPU index                     -> *device (may be NULL)
+ *   sync_every    host records refreshed every n steps by the Fortran
+ *                 module's second half kick (0 = never) -> *sync_every
+ * Fields without a key are left as they are.  An unknown key, a bad value
+ * or an unreadable $TCP_GPU_PRM returns TCP_ERR_BAD_PARAM naming the line or
+ * variable.  Touches no device. */
+int tcp_params_from_env(tcp_params *p, int *device, int *sync_every);
 
 /* Updates the parameters that may change between steps (temperatures,
  * thermostat, tau, charge scale, e-i length).  Box, mesh, order, counts and
@@ -157,9 +187,11 @@ int tcp_download_soa(tcp_ctx *ctx, double *x, double *v, double *f, double *frec
  * larger n returns TCP_ERR_BAD_PARAM.  x and f are device arrays, SoA [3][n]
  * (electrons first); *Ur (host, may be NULL) gets Ur without eps.  Runs on
  * `stream` (a cudaStream_t, NULL = legacy default stream) and returns when the
- * forces are written.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current.  Calls share the
- * array: calls that overlap on the GPU race and must be serialised. */
+ * forces are written.  Every call looks up the array's device address
+ * (cudaGetSymbolAddress) with the caller's current device, which allocates
+ * nothing.  Calls share the array: calls that overlap on the GPU race and
+ * must be serialised.  After a non-zero return the contents of f are
+ * undefined. */
 int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, const double *x, double *f,
                              double *Ur, void *stream);
 

@@ -69,7 +69,12 @@ int orc_ewald_self(orc_params *p, int nel, int nion, double alpha_override,
         double s = p->charge_scale;
         double u = -(double)nel * (s * p->q[0]) * (s * p->q[0]) -
                    (double)nion * (s * p->q[1]) * (s * p->q[1]);         /* :44 */
-        *Uo = u * p->a / ORC_SQRTPI;                                     /* :45 */
+        /* net charge Q: the uniform neutralising background of the Ewald sum,
+         * -pi Q^2 / (2 V alpha^2) (not in the reference; 0 for neutral systems) */
+        double Q = (double)nel * s * p->q[0] + (double)nion * s * p->q[1];
+        double V = p->box[0] * p->box[1] * p->box[2];
+        *Uo = u * p->a / ORC_SQRTPI                                      /* :45 */
+              - ORC_PI * Q * Q / (2.0 * V * p->a * p->a);
     }
     return 0;
 }

@@ -16,6 +16,7 @@ import numpy as np
 
 from . import _abi
 from ._abi import (EI_COULOMB, EI_DEUTSCH, EI_KELBG, FLAG_DETERMINISTIC, FLAG_ENERGY, FLAG_RDF, FLAG_VDF, PREC_FP32C,
+                   PREC_FP32C_R64,
                    PREC_FP64, RECIP_EWALD, RECIP_NONE, RECIP_SPME, THERMO_BEREND, THERMO_ISOKIN,
                    THERMO_NOTEMP, THERMO_STOCH, TcpEnergies, TcpError, TcpParams)
 from .system import EPS, NDIST, PT_DTYPE, System, make_config_system, make_system
@@ -26,7 +27,7 @@ __all__ = ["Context", "Batch", "TcpParams", "TcpEnergies", "TcpError", "params_f
 _THERMO = {"notemp": THERMO_NOTEMP, "isokin": THERMO_ISOKIN, "berend": THERMO_BEREND, "stoch": THERMO_STOCH}
 _EI = {"deutsch": EI_DEUTSCH, "kelbg": EI_KELBG, "coulomb": EI_COULOMB}
 _RECIP = {"none": RECIP_NONE, "spme": RECIP_SPME, "ewald": RECIP_EWALD}
-_PREC = {"fp64": PREC_FP64, "fp32c": PREC_FP32C}
+_PREC = {"fp64": PREC_FP64, "fp32c": PREC_FP32C, "fp32c_r64": PREC_FP32C_R64}
 
 
 def params_for(sys: System, precision="fp32c", ei="kelbg", recip="spme", thermo="notemp",
@@ -228,8 +229,8 @@ class Context:
     def autotune_report(self):
         """(chosen FP32C pair-kernel variant, per-variant ms measured by the autotuner)."""
         v = C.c_int()
-        ms = np.zeros(16)
-        self._chk(self.lib.tcp_autotune_report(self.h, C.byref(v), ms.ctypes.data_as(C.POINTER(C.c_double)), 16),
+        ms = np.zeros(32)
+        self._chk(self.lib.tcp_autotune_report(self.h, C.byref(v), ms.ctypes.data_as(C.POINTER(C.c_double)), 32),
                   "tcp_autotune_report")
         return v.value, ms
 

@@ -20,7 +20,7 @@ TCP_ERR_NO_DEVICE = 6
 TCP_ERR_STATE = 7
 TCP_ERR_NOMEM = 8
 
-PREC_FP64, PREC_FP32C = 0, 1
+PREC_FP64, PREC_FP32C, PREC_FP32C_R64 = 0, 1, 2
 EI_DEUTSCH, EI_KELBG, EI_COULOMB = 0, 1, 2
 THERMO_NOTEMP, THERMO_ISOKIN, THERMO_BEREND, THERMO_STOCH = 0, 1, 2, 3
 RECIP_NONE, RECIP_SPME, RECIP_EWALD = 0, 1, 2
@@ -85,6 +85,7 @@ SIGNATURES = {
     "tcp_overlap_report": (C.c_int, [_CTX, C.POINTER(C.c_int), C.POINTER(C.c_int), _P, C.c_int]),
     "tcp_launch_count": (C.c_int, [_CTX, C.POINTER(C.c_longlong)]),
     "tcp_fp32_peak": (C.c_int, [C.c_int, _P]),
+    "tcp_params_from_env": (C.c_int, [C.POINTER(TcpParams), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "tcp_adjoint_energy": (C.c_int, [_CTX, _P, _P, _P]),
     "tcp_hvp": (C.c_int, [_CTX, C.c_void_p, C.c_void_p, _P]),
     "tcp_reverse_md": (C.c_int, [_CTX, C.c_double, C.c_int, C.c_int, _P, _P]),

@@ -415,6 +415,8 @@ struct tcp_batch {
     std::vector<tcp::BRep> h_reps;
     void *n3reps = nullptr;             // device Newton-3 table
     long long n3_items = 0;
+    long long *n3_chunks = nullptr;     // chunk table of the guided schedule (device)
+    unsigned n3_nchunks = 0;
     std::vector<tcp::PairConsts> pcs;   // per-replica pair constants (the table is refilled per variant)
     int pair_variant = 0;               // batched Newton-3 variant (batch autotuner)
     bool tuned = false;
@@ -568,7 +570,7 @@ static int b_step(tcp_batch *b, double dt) {
     b_vverlet1_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), dt);
     int rc = b_recip_fork(b, A);
     if (!rc)
-        rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
+        rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, b->n3_chunks, b->n3_nchunks, A.ur,
                                   b->status, b->counter, b->num_sms, true, b->pair_variant);
     if (int jrc = b_recip_join(b)) return jrc;
     if (rc) return rc;
@@ -586,6 +588,14 @@ static int b_fill_n3(tcp_batch *b, int v) {
     b->n3_items = n3_batch_fill(n3h.data(), b->nrep, b->off.data(), b->nel.data(), b->nion.data(), b->pcs.data(),
                                 n3_batch_tile(v));
     TCP_CUDA(cudaMemcpyAsync(b->n3reps, n3h.data(), n3h.size(), cudaMemcpyHostToDevice, b->stream));
+    std::vector<long long> chunks;
+    n3_chunk_table(b->n3_items, n3_batch_ctas(b->num_sms, v), chunks);
+    cudaFree(b->n3_chunks);
+    b->n3_chunks = nullptr;
+    TCP_CUDA(cudaMalloc(&b->n3_chunks, sizeof(long long) * chunks.size()));
+    TCP_CUDA(cudaMemcpyAsync(b->n3_chunks, chunks.data(), sizeof(long long) * chunks.size(), cudaMemcpyHostToDevice,
+                             b->stream));
+    b->n3_nchunks = (unsigned)chunks.size() - 1;
     TCP_CUDA(cudaStreamSynchronize(b->stream));
     b->pair_variant = v;
     return TCP_OK;
@@ -609,11 +619,11 @@ static int b_autotune(tcp_batch *b) {
     int best_v = 0, rc = TCP_OK;
     for (int v = 0; v < nv && v < 8 && !rc; ++v) {
         if ((rc = b_fill_n3(b, v))) break;
-        rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
+        rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, b->n3_chunks, b->n3_nchunks, A.ur,
                                   b->status, b->counter, b->num_sms, true, v);
         cudaEventRecord(e0, b->stream);
         for (int r = 0; r < 2 && !rc; ++r)
-            rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
+            rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, b->n3_chunks, b->n3_nchunks, A.ur,
                                       b->status, b->counter, b->num_sms, true, v);
         cudaEventRecord(e1, b->stream);
         cudaEventSynchronize(e1);
@@ -672,7 +682,7 @@ int tcp_batch_destroy(tcp_batch *b) {
         cufftDestroy(g.inv);
     }
     for (void *ptr : {(void *)b->x, (void *)b->v, (void *)b->f, (void *)b->frec, (void *)b->facc, (void *)b->xq,
-                      (void *)b->rep_of, (void *)b->reps, b->n3reps, (void *)b->acc, (void *)b->status,
+                      (void *)b->rep_of, (void *)b->reps, b->n3reps, (void *)b->n3_chunks, (void *)b->acc, (void *)b->status,
                       (void *)b->counter, (void *)b->Qf, (void *)b->infl, (void *)b->Qk, (void *)b->blk0,
                       (void *)b->bin_count, (void *)b->bin_start, (void *)b->bin_bsum, (void *)b->bin_rank,
                       (void *)b->bin_list, (void *)b->bin_ebx, (void *)b->bin_eby, (void *)b->bin_ew,
@@ -843,8 +853,7 @@ int tcp_batch_ewald_self(tcp_batch *b, double *Uo) {
         const double alpha = p.a > 0.0 ? p.a : 3.1 / p.rc;                     // force.f90:23
         b->alpha[r] = alpha;
         const double s = p.charge_scale;
-        b->Uo[r] = (-(double)b->nel[r] * (s * p.q[0]) * (s * p.q[0]) - (double)b->nion[r] * (s * p.q[1]) * (s * p.q[1])) *
-                   alpha / kSqrtPi;                                            // force.f90:44-45
+        b->Uo[r] = ewald_constant_energy(p, b->nel[r], b->nion[r], alpha);   // force.f90:44-45 + background
         tcp_ctx tmp;
         tmp.p = p;
         tmp.nel = b->nel[r];
@@ -968,7 +977,7 @@ int tcp_batch_force(tcp_batch *b, tcp_energies *e) {
     TCP_CUDA(cudaMemsetAsync(A.um, 0, sizeof(double) * 8 * (size_t)b->nrep, b->stream));
     int rc = b_recip_fork(b, A);
     if (!rc)
-        rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, A.ur,
+        rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, b->n3_chunks, b->n3_nchunks, A.ur,
                                   b->status, b->counter, b->num_sms, true, b->pair_variant);
     if (int jrc = b_recip_join(b)) return jrc;
     if (rc) return rc;

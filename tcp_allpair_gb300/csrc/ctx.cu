@@ -41,7 +41,7 @@ static int validate(const tcp_params *p, int nel, int nion) {
         if (!(p->box[d] > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "box lengths must be positive");
     if (!(p->rc > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "rc must be positive");
     if (!(p->xm[0] > 0.0) || !(p->xm[1] > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "masses must be positive");
-    if (p->precision != TCP_PREC_FP64 && p->precision != TCP_PREC_FP32C)
+    if (p->precision != TCP_PREC_FP64 && p->precision != TCP_PREC_FP32C && p->precision != TCP_PREC_FP32C_R64)
         return set_error(TCP_ERR_BAD_PARAM, "unknown precision");
     if (p->ei_model < TCP_EI_DEUTSCH || p->ei_model > TCP_EI_COULOMB) return set_error(TCP_ERR_BAD_PARAM, "unknown ei_model");
     if (p->ei_model == TCP_EI_DEUTSCH && !(p->rs > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "Deutsch model needs rs > 0");
@@ -286,6 +286,9 @@ int tcp_create(const tcp_params *p_in, int nel, int nion, int device, tcp_ctx **
     tcp_ctx *c = new tcp_ctx();
     c->p = *p_in;
     normalise(&c->p);
+    // TCP_PREC_FP32C_R64 is the FP32C context with an FP64 reciprocal chain
+    c->recip_fp64 = c->p.precision == TCP_PREC_FP32C_R64;
+    if (c->recip_fp64) c->p.precision = TCP_PREC_FP32C;
     c->nel = nel;
     c->nion = nion;
     c->n = nel + nion;
@@ -329,6 +332,7 @@ int tcp_create(const tcp_params *p_in, int nel, int nion, int device, tcp_ctx **
     TCP_ALLOC(c->counter, sizeof(unsigned));
     TCP_ALLOC(c->rdf, sizeof(unsigned long long) * 3 * kNbin);
     TCP_ALLOC(c->vdf, sizeof(unsigned long long) * 2 * kNbin);
+    TCP_ALLOC(c->rdf_edges, sizeof(RdfEdges));
 #undef TCP_ALLOC
     if (cudaMallocHost(&c->h_scal, sizeof(double) * (kScalCount + 1)) != cudaSuccess)
         return fail(cuda_check(cudaGetLastError(), "cudaMallocHost"));
@@ -370,6 +374,8 @@ int tcp_destroy(tcp_ctx *c) {
     cudaFree(c->counter);
     cudaFree(c->rdf);
     cudaFree(c->vdf);
+    cudaFree(c->rdf_edges);
+    cudaFree(c->n3_chunks);
     cudaFree(c->d_stage);
     cudaFree(c->kvec);
     cudaFree(c->ksum);
@@ -399,9 +405,7 @@ int tcp_ewald_self(tcp_ctx *c, double *alpha_out, double *Uo_out) {
     c->alpha = p.a > 0.0 ? p.a : 3.1 / p.rc;                                       // force.f90:23
     c->rc2 = p.rc * p.rc;                                                           // force.f90:24
     c->V = p.box[0] * p.box[1] * p.box[2];
-    const double s = p.charge_scale;
-    c->Uo = (-(double)c->nel * (s * p.q[0]) * (s * p.q[0]) - (double)c->nion * (s * p.q[1]) * (s * p.q[1])) *
-            c->alpha / kSqrtPi;                                                     // force.f90:44-45
+    c->Uo = ewald_constant_energy(p, c->nel, c->nion, c->alpha);                   // force.f90:44-45 + background
     int rc;
     if ((rc = pair_setup(c))) return rc;
     if (p.reciprocal == TCP_RECIP_SPME && (rc = spme_setup(c))) return rc;
@@ -425,8 +429,10 @@ int tcp_set_params(tcp_ctx *c, const tcp_params *p) {
     for (int d = 0; d < 3; ++d)
         if (q.box[d] != c->p.box[d] || q.K[d] != c->p.K[d])
             return set_error(TCP_ERR_BAD_PARAM, "box and mesh are fixed at tcp_create");
-    if (q.order != c->p.order || q.precision != c->p.precision || q.reciprocal != c->p.reciprocal ||
-        q.ewald_nmax2 != c->p.ewald_nmax2)
+    const bool q_r64 = q.precision == TCP_PREC_FP32C_R64;
+    if (q_r64) q.precision = TCP_PREC_FP32C;
+    if (q.order != c->p.order || q.precision != c->p.precision || q_r64 != c->recip_fp64 ||
+        q.reciprocal != c->p.reciprocal || q.ewald_nmax2 != c->p.ewald_nmax2)
         return set_error(TCP_ERR_BAD_PARAM, "order, precision and reciprocal method are fixed at tcp_create");
     const bool alpha_changed = q.a != c->p.a || q.rc != c->p.rc;
     c->p = q;

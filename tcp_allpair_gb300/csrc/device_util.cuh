@@ -79,6 +79,28 @@ __device__ __forceinline__ float ex2_approx(float x) {
     return y;
 }
 
+// ---- fixed-point coordinates ------------------------------------------------
+// 2^32 units per box length (iL = 1/L, computed once on the host); the int32
+// difference of two coordinates is the minimum-image separation.  Every
+// entry point quantises positions through this function, so that they all
+// see the same grid.
+__device__ __forceinline__ int fixed_coord(double x, double iL) {
+    double t = fma(x, iL, 0.5);
+    t -= floor(t);
+    const unsigned long long u = (unsigned long long)llrint(t * 4294967296.0);
+    return (int)(unsigned)(u & 0xffffffffull);
+}
+
+// 2^64 units per box length (the FP64 Newton-3 kernel): the wrapped int64
+// difference is the minimum image, exact before its conversion to FP64.
+__device__ __forceinline__ long long fixed_coord64(double x, double iL) {
+    double t = fma(x, iL, 0.5);
+    t -= floor(t);                                  // [0, 1)
+    const double s = t * 18446744073709551616.0;    // [0, 2^64]
+    const unsigned long long u = s >= 18446744073709551615.0 ? 0ull : (unsigned long long)s;
+    return (long long)u;
+}
+
 // ---- compensated FP32 sums -------------------------------------------------
 // Knuth's TwoSum: s + e == a + b exactly.
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {

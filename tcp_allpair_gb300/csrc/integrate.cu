@@ -20,25 +20,6 @@ constexpr int kIntThreads = 256;
 // the box length through its reciprocal (iL = 1/L, set on the host) and by
 // the mass through dt/(2m) computed once per thread.
 
-// 2^32 units per box length; the int32 difference of two coordinates is the
-// minimum-image separation.
-__device__ __forceinline__ int fixed_coord(double x, double iL) {
-    double t = fma(x, iL, 0.5);
-    t -= floor(t);
-    const unsigned long long u = (unsigned long long)llrint(t * 4294967296.0);
-    return (int)(unsigned)(u & 0xffffffffull);
-}
-
-// 2^64 units per box length (the FP64 Newton-3 kernel): the wrapped int64
-// difference is the minimum image, exact before its conversion to FP64.
-__device__ __forceinline__ long long fixed_coord64(double x, double iL) {
-    double t = fma(x, iL, 0.5);
-    t -= floor(t);                                  // [0, 1)
-    const double s = t * 18446744073709551616.0;    // [0, 2^64]
-    const unsigned long long u = s >= 18446744073709551615.0 ? 0ull : (unsigned long long)s;
-    return (long long)u;
-}
-
 struct IntArgs {
     double *x, *v, *f;
     int4 *xq;

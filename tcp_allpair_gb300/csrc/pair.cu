@@ -26,8 +26,8 @@
 // FP64 kernel: the reference's expressions (force.f90:99-110, 130-144,
 // 163-175) in double precision with CUDA's erf/erfc/exp/sqrt.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
-#include <mutex>
 #include <string>
 
 #include "device_util.cuh"
@@ -56,6 +56,7 @@ struct PairArgs {
     double *fpart;          // [gridDim.y][3][n]
     double *upart;          // [gridDim.y * gridDim.x]
     unsigned long long *rdf;
+    const RdfEdges *rdf_edges;   // exact bin edges of the FP32C RDF
     unsigned *status;
     PairConsts c;
 };
@@ -80,10 +81,14 @@ __device__ __forceinline__ void tile_range(const PairArgs &a, int t, int &j0, in
 // equal, so the fixed-point difference is used unscaled (lengths in units of
 // L/2^32) and the scale is folded into the constants and the per-tile factor
 // applied when the tile partial is folded.
+// RDF (+1 per ordered pair inside rc): the FP32 bin, or the exact one of the
+// fixed-point separation near a bin edge or rc (rdf_exact_bin); vi is false
+// for the padding lanes of a partial i-block, which count nothing.
 template <int KIND, bool ENERGY, bool RDF, int TPP, bool FULL, bool DIAG, bool CUBIC>
 __device__ __forceinline__ void tile_f32(const int4 *__restrict__ tj, int cnt, int sub, int4 xi,
                                          const PairConsts &c, float &px, float &py, float &pz,
-                                         float &pe, unsigned *hist, float inv_dx) {
+                                         float &pe, unsigned *hist, float inv_dx, bool vi = true,
+                                         const RdfEdges *E = nullptr, int pt = 0) {
     const int cnt_up = FULL ? kTjF : (cnt + TPP - 1) / TPP * TPP;   // uniform trip count per warp
     // constants in the units of this path
     const float rc2 = CUBIC ? c.u_rc2 : c.rc2f;
@@ -156,10 +161,17 @@ __device__ __forceinline__ void tile_f32(const int4 *__restrict__ tj, int cnt, i
         pz = fmaf(w, dz, pz);
         if (ENERGY) pe += u;
         if (RDF) {
-            if (ok) {
-                const int bin = (int)(r * inv_dx);
-                if (bin <= kNdist) atomicAdd(&hist[bin], 1u);
+            const bool valid = vi && (!DIAG || r2 > 0.0f) && (FULL || jj < cnt);
+            const float tb = r * inv_dx;
+            int bin = (int)tb;
+            bool okr = ok && vi;
+            if (valid && rdf_near_edge(tb, bin, r2, rc2)) {
+                if (!ok) bin = (int)(sqrtf(r2) * inv_dx);
+                bin = rdf_exact_bin<CUBIC>((int)((unsigned)xi.x - (unsigned)xj.x),
+                                           (int)((unsigned)xi.y - (unsigned)xj.y),
+                                           (int)((unsigned)xi.z - (unsigned)xj.z), E, pt, c.box, bin, okr);
             }
+            if (okr && bin <= kNdist) atomicAdd(&hist[bin], 1u);
         }
     }
 }
@@ -168,10 +180,11 @@ __device__ __forceinline__ void tile_f32(const int4 *__restrict__ tj, int cnt, i
 template <int KIND, bool ENERGY, bool RDF, bool CUBIC>
 __device__ __forceinline__ void tile_f32_any(const int4 *__restrict__ tj, int cnt, bool diag, int sub, int4 xi,
                                              const PairConsts &c, float &px, float &py, float &pz, float &pe,
-                                             unsigned *hist, float inv_dx) {
+                                             unsigned *hist, float inv_dx, bool vi, const RdfEdges *E, int pt) {
     constexpr int TPP = kTppF;
     if (RDF) {
-        tile_f32<KIND, ENERGY, RDF, TPP, false, true, CUBIC>(tj, cnt, sub, xi, c, px, py, pz, pe, hist, inv_dx);
+        tile_f32<KIND, ENERGY, RDF, TPP, false, true, CUBIC>(tj, cnt, sub, xi, c, px, py, pz, pe, hist, inv_dx, vi,
+                                                              E, pt);
     } else if (cnt == kTjF) {
         if (diag) tile_f32<KIND, ENERGY, false, TPP, true, true, CUBIC>(tj, cnt, sub, xi, c, px, py, pz, pe, hist, inv_dx);
         else tile_f32<KIND, ENERGY, false, TPP, true, false, CUBIC>(tj, cnt, sub, xi, c, px, py, pz, pe, hist, inv_dx);
@@ -239,11 +252,14 @@ __global__ void __launch_bounds__(kPairThreads) pair_fp32c_kernel(const PairArgs
         // the tile can hold the i-particles of this CTA only on the diagonal
         const bool diag = (j0 < i0 + a.bi) && (i0 < j0 + cnt);
         if (pt == 1 && EIKIND == 1)
-            tile_f32_any<1, ENERGY, RDF, CUBIC>(tiles[stage], cnt, diag, sub, xi, a.c, px, py, pz, pe, h, inv_dx);
+            tile_f32_any<1, ENERGY, RDF, CUBIC>(tiles[stage], cnt, diag, sub, xi, a.c, px, py, pz, pe, h, inv_dx,
+                                                 vi, a.rdf_edges, pt);
         else if (pt == 1 && EIKIND == 2)
-            tile_f32_any<2, ENERGY, RDF, CUBIC>(tiles[stage], cnt, diag, sub, xi, a.c, px, py, pz, pe, h, inv_dx);
+            tile_f32_any<2, ENERGY, RDF, CUBIC>(tiles[stage], cnt, diag, sub, xi, a.c, px, py, pz, pe, h, inv_dx,
+                                                 vi, a.rdf_edges, pt);
         else
-            tile_f32_any<0, ENERGY, RDF, CUBIC>(tiles[stage], cnt, diag, sub, xi, a.c, px, py, pz, pe, h, inv_dx);
+            tile_f32_any<0, ENERGY, RDF, CUBIC>(tiles[stage], cnt, diag, sub, xi, a.c, px, py, pz, pe, h, inv_dx,
+                                                 vi, a.rdf_edges, pt);
         const float qf = CUBIC ? a.c.u_qq_force[pt] : a.c.qqf[pt];
         const float qe = CUBIC ? a.c.u_qq_energy[pt] : a.c.qqf[pt];
         acc2(fxh, fxl, px * qf);
@@ -316,7 +332,7 @@ template <int KIND, bool ENERGY, bool RDF, int TPP>
 __device__ __forceinline__ void tile_f64(const double4_32a *__restrict__ tj, int cnt, int sub, double4_32a xi,
                                          const PairConsts &c, double qq, double &fx, double &fy,
                                          double &fz, double &ue, unsigned *hist, double inv_dx,
-                                         const F64Tab &tb) {
+                                         const F64Tab &tb, bool vi = true) {
     // The expressions of force.f90 without divisions (GB300 issues FP64 at 1/64
     // of the FP32 rate): DNINT of d/box by multiplication with 1/box, 1/r from
     // rsqrt_nr, the exponentials from the table-driven exp_neg_tab, the Ewald
@@ -353,7 +369,7 @@ __device__ __forceinline__ void tile_f64(const double4_32a *__restrict__ tj, int
             fy += df * xr1;
             fz += df * xr2;
             if (ENERGY) ue += u;
-            if (RDF) {
+            if (RDF && vi) {                                   // (padding lanes count nothing)
                 const double tb = sqrt(r2) * inv_dx;             // INT(r/dx) from the rounded sqrt
                 if (tb < (double)kNbin) atomicAdd(&hist[(int)tb], 1u);
             }
@@ -418,11 +434,11 @@ __global__ void __launch_bounds__(kPairThreads) pair_fp64_kernel(const PairArgs 
         const double inv_dx = RDF ? a.c.inv_dxd[pt] : 0.0;
         const double qq = a.c.qq[pt];
         if (pt == 1 && EIKIND == 1)
-            tile_f64<1, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx, tab);
+            tile_f64<1, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx, tab, vi);
         else if (pt == 1 && EIKIND == 2)
-            tile_f64<2, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx, tab);
+            tile_f64<2, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx, tab, vi);
         else
-            tile_f64<0, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx, tab);
+            tile_f64<0, ENERGY, RDF, TPP>(tiles[stage], cnt, sub, xi, a.c, qq, fx, fy, fz, ue, h, inv_dx, tab, vi);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicOr(a.status, kStatusTmaTimeout);
             break;
@@ -468,18 +484,21 @@ __global__ void __launch_bounds__(kPairThreads) pair_fp64_kernel(const PairArgs 
 // ---------------------------------------------------------------------------
 // f = sum over splits of fpart (+ frec: the SPME_SUM add of force.f90:953-964
 // fused); per-block partial sums of f for REMOVE_RIGIDMTN (force.f90:986-993).
+// When a tile wait of the pair kernel ran out (status), some partials were
+// never written: f is then left as it was and the caller reports the error.
 __global__ void force_finalize_kernel(const double *__restrict__ fpart, int nsplit,
                                       const double *__restrict__ frec, double *__restrict__ f, int n,
-                                      double *__restrict__ fsum_part) {
+                                      double *__restrict__ fsum_part, const unsigned *__restrict__ status) {
     __shared__ double red[32];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool write = !(status && (*status & kStatusTmaTimeout));
     double s[3] = {0.0, 0.0, 0.0};
     if (i < n) {
         for (int k = 0; k < 3; ++k) {
             double acc = 0.0;
             for (int sp = 0; sp < nsplit; ++sp) acc += fpart[((size_t)sp * 3 + k) * n + i];
             if (frec) acc += frec[(size_t)k * n + i];
-            f[(size_t)k * n + i] = acc;
+            if (write) f[(size_t)k * n + i] = acc;
             s[k] = acc;
         }
     }
@@ -529,6 +548,8 @@ void make_pair_consts(tcp_ctx *c) {
     const double u = p.box[0] / two32;
     k.u_rc2 = (float)(c->rc2 / (u * u));
     k.u_p_alpha = (float)(kErfcP * c->alpha * u);
+    k.u_p_alpha5 = (float)(kErfc5P * c->alpha * u);
+    k.erfc5_ok = c->alpha * std::sqrt(c->rc2) <= kErfc5Xmax ? 1 : 0;
     k.u_c_exp = (float)(-c->alpha * c->alpha * log2e * u * u);
     k.u_c_gauss = (float)(2.0 * c->alpha / kSqrtPi * u);
     k.u_c_rs = (float)(-log2e / rs * u);
@@ -601,8 +622,36 @@ static int choose_jsplit(const tcp_ctx *c, const Geometry &g, int blocks_per_sm)
     return best;
 }
 
+// Bin edges of the exact RDF test (RdfEdges): in units of u^2 for cubic
+// boxes, rounded up to integers, and in A^2 for the others.  Long double
+// keeps (k dx/u)^2 < 2^64 to within a unit wherever it differs from double.
+static void fill_rdf_edges(const tcp_ctx *c, RdfEdges &E) {
+    const double dxs[3] = {c->p.dx_ee, c->p.dx_ei, c->p.dx_ii};
+    const long double u = (long double)c->p.box[0] / 4294967296.0L;
+    auto ceil_u64 = [](long double v) -> unsigned long long {
+        if (!(v > 0.0L)) return 0ull;
+        if (v >= 18446744073709551615.0L) return ~0ull;
+        return (unsigned long long)ceill(v);
+    };
+    for (int t = 0; t < 3; ++t)
+        for (int k = 0; k <= kNbin; ++k) {
+            const long double x = (long double)k * (long double)dxs[t] / u;
+            E.e[t][k] = dxs[t] > 0.0 ? ceil_u64(x * x) : ~0ull;
+            const double d = (double)k * dxs[t];
+            E.d[t][k] = dxs[t] > 0.0 ? d * d : 1e308;
+        }
+    E.rc2 = ceil_u64((long double)c->rc2 / (u * u));
+    E.rc2d = c->rc2;
+}
+
 int pair_setup(tcp_ctx *c) {
     make_pair_consts(c);
+    if (c->rdf_edges) {
+        RdfEdges E;
+        fill_rdf_edges(c, E);
+        TCP_CUDA(cudaMemcpyAsync(c->rdf_edges, &E, sizeof E, cudaMemcpyHostToDevice, c->stream));
+        TCP_CUDA(cudaStreamSynchronize(c->stream));   // E is a stack copy
+    }
     const bool fp64 = c->p.precision == TCP_PREC_FP64;
     Geometry g = geometry(c, fp64);
     int bps = 1;
@@ -621,6 +670,8 @@ int pair_setup(tcp_ctx *c) {
     c->upart = nullptr;
     c->jsplit = js;
     c->n_upart = std::max(g.nblk * js, fp64 ? n3_f64_grid(c) : n3_grid(c));
+    if (!fp64 && c->pc.cubic)
+        if (int rc = n3_prepare_chunks(c)) return rc;
     TCP_CUDA(cudaMalloc(&c->fpart, sizeof(double) * 3 * (size_t)c->n * js));
     TCP_CUDA(cudaMalloc(&c->upart, sizeof(double) * (size_t)c->n_upart));
     TCP_CUDA(cudaMemsetAsync(c->upart, 0, sizeof(double) * (size_t)c->n_upart, c->stream));
@@ -654,6 +705,7 @@ int launch_pair(tcp_ctx *c, bool energy, bool rdf) {
     a.fpart = c->fpart;
     a.upart = c->upart;
     a.rdf = c->rdf;
+    a.rdf_edges = c->rdf_edges;
     a.status = c->status;
     a.c = c->pc;
     dim3 grid(g.nblk, c->jsplit);
@@ -693,7 +745,7 @@ int launch_force_finalize(tcp_ctx *c, bool add_rec) {
     const int threads = 256;
     const int blocks = ceil_div(c->n, threads);
     force_finalize_kernel<<<blocks, threads, 0, c->stream>>>(c->fpart, c->fpart_splits, add_rec ? c->frec : nullptr,
-                                                             c->f, c->n, c->red);
+                                                             c->f, c->n, c->red, c->status);
     c->launches++;
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;
@@ -718,6 +770,10 @@ int launch_force_finalize(tcp_ctx *c, bool add_rec) {
 // passes the positions and the force array (device memory, SoA [3][n]) and a
 // host double for Ur.
 //
+// After a non-zero return the contents of f are undefined (a timed-out tile
+// wait leaves them as they were).  The array's device address is looked up
+// on every call with the caller's device current.
+//
 // The array is shared by all calls and keeps the last call's contents; this
 // function clears what must start at zero (the status word) and overwrites
 // everything else before reading it.  Calls that overlap on the GPU (from two
@@ -727,21 +783,13 @@ namespace tcp {
 constexpr size_t kNoAllocBytes = 8u << 20;   // 8 MiB
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-__global__ void noalloc_positions_kernel(const double *__restrict__ x, int n, double L0, double L1, double L2,
+__global__ void noalloc_positions_kernel(const double *__restrict__ x, int n, double iL0, double iL1, double iL2,
                                          int4 *xq, double4_32a *xd) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double L[3] = {L0, L1, L2};
-    double y[3];
-    int q[3];
-    for (int d = 0; d < 3; ++d) {
-        y[d] = x[(size_t)d * n + i];
-        double t = y[d] / L[d] + 0.5;
-        t -= floor(t);
-        q[d] = (int)(unsigned)((unsigned long long)llrint(t * 4294967296.0) & 0xffffffffull);
-    }
-    if (xq) xq[i] = make_int4(q[0], q[1], q[2], 0);
-    if (xd) xd[i] = make_double4_32a(y[0], y[1], y[2], 0.0);
+    const double y0 = x[i], y1 = x[(size_t)n + i], y2 = x[2 * (size_t)n + i];
+    if (xq) xq[i] = make_int4(fixed_coord(y0, iL0), fixed_coord(y1, iL1), fixed_coord(y2, iL2), 0);
+    if (xd) xd[i] = make_double4_32a(y0, y1, y2, 0.0);
 }
 
 __global__ void noalloc_sum_kernel(const double *__restrict__ part, int np, double *out) {
@@ -759,8 +807,6 @@ static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 extern "C" int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, const double *x, double *f,
                                         double *Ur, void *stream) {
     using namespace tcp;
-    static std::mutex mu;
-    static void *scratch_of_device[64] = {nullptr};
     if (!p || !x || !f) return set_error(TCP_ERR_BAD_PARAM, "NULL argument");
     if (nel < 0 || nion < 0 || nel + nion < 2) return set_error(TCP_ERR_BAD_PARAM, "need nel, nion >= 0 and nel+nion >= 2");
     for (int d = 0; d < 3; ++d)
@@ -768,26 +814,22 @@ extern "C" int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, 
     if (!(p->rc > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "rc must be positive");
     if (p->rc > std::min(std::min(p->box[0], p->box[1]), p->box[2]) / 2.0)
         return set_error(TCP_ERR_CUTOFF, " *** error at cut-off radius *** (rc > min(box)/2)");
-    if (p->precision != TCP_PREC_FP64 && p->precision != TCP_PREC_FP32C)
+    if (p->precision != TCP_PREC_FP64 && p->precision != TCP_PREC_FP32C && p->precision != TCP_PREC_FP32C_R64)
         return set_error(TCP_ERR_BAD_PARAM, "unknown precision");
     if (p->ei_model < TCP_EI_DEUTSCH || p->ei_model > TCP_EI_COULOMB) return set_error(TCP_ERR_BAD_PARAM, "unknown ei_model");
     if (p->ei_model == TCP_EI_DEUTSCH && !(p->rs > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "Deutsch model needs rs > 0");
     if (p->ei_model == TCP_EI_KELBG && !(p->lambda_ei > 0.0)) return set_error(TCP_ERR_BAD_PARAM, "Kelbg model needs lambda_ei > 0");
 
-    // once per device, with that device current: the device address of the array
+    // The device address of the array, looked up on every call with the
+    // caller's device current.  The lookup allocates nothing and costs far
+    // less than the launch; a cached address could outlive the module (after
+    // cudaDeviceReset the module is loaded again and the array may move).
     int dev = 0;
     TCP_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) return set_error(TCP_ERR_BAD_PARAM, "device index >= 64");
     void *base = nullptr;
     {
-        std::lock_guard<std::mutex> lock(mu);
-        if (!scratch_of_device[dev]) {
-            void *ptr = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-            if (e != cudaSuccess) return cuda_check(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-            scratch_of_device[dev] = ptr;
-        }
-        base = scratch_of_device[dev];
+        const cudaError_t e = cudaGetSymbolAddress(&base, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_check(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
     }
 
     // the same constants and geometry as tcp_force_direct (host-side copy only)
@@ -805,9 +847,9 @@ extern "C" int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, 
     const Geometry g = geometry(&tmp, fp64);
     int bps = 1;
     if (fp64)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp64_kernel<0, true, false>, kPairThreads, 0);
+        TCP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp64_kernel<0, true, false>, kPairThreads, 0));
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp32c_kernel<2, true, false, true>, kPairThreads, 0);
+        TCP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pair_fp32c_kernel<2, true, false, true>, kPairThreads, 0));
     const size_t n = (size_t)tmp.n;
     const int nbf = ceil_div(tmp.n, 256);
     auto need = [&](int js) {
@@ -836,7 +878,7 @@ extern "C" int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     TCP_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
     noalloc_positions_kernel<<<ceil_div(tmp.n, 256), 256, 0, st>>>(
-        x, tmp.n, p->box[0], p->box[1], p->box[2], fp64 ? nullptr : static_cast<int4 *>(pos),
+        x, tmp.n, 1.0 / p->box[0], 1.0 / p->box[1], 1.0 / p->box[2], fp64 ? nullptr : static_cast<int4 *>(pos),
         fp64 ? static_cast<double4_32a *>(pos) : nullptr);
     PairArgs a;
     a.xq = fp64 ? nullptr : static_cast<const int4 *>(pos);
@@ -853,6 +895,7 @@ extern "C" int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, 
     a.fpart = fpart;
     a.upart = upart;
     a.rdf = nullptr;
+    a.rdf_edges = nullptr;
     a.status = status;
     a.c = tmp.pc;
     dim3 grid(g.nblk, js);
@@ -872,7 +915,7 @@ extern "C" int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, 
             else pair_fp32c_kernel<2, true, false, false><<<grid, kPairThreads, 0, st>>>(a);
         }
     }
-    force_finalize_kernel<<<nbf, 256, 0, st>>>(fpart, js, nullptr, f, tmp.n, fsum);
+    force_finalize_kernel<<<nbf, 256, 0, st>>>(fpart, js, nullptr, f, tmp.n, fsum, status);
     noalloc_sum_kernel<<<1, 1024, 0, st>>>(upart, g.nblk * js, fsum);   // Ur into fsum[0]
     TCP_CUDA(cudaGetLastError());
     double ur = 0.0;
@@ -920,17 +963,18 @@ static int cache_lookup(const char *path, const std::string &key) {
 // Real-space kernel of an FP32C context: the variant with the shortest
 // pair-kernel time (TCP_PAIR_VARIANT forces one).
 static int choose_variant(tcp_ctx *c, const char *cache, const std::string &key) {
-    const int nv = c->pc.cubic ? std::min(n3_variant_count(), 15) : 0;
+    const int nv = c->pc.cubic ? std::min(n3_variant_count(), 31) : 0;
     c->pair_variant = c->pc.cubic ? 1 : 0;
     if (const char *forced = getenv("TCP_PAIR_VARIANT")) {
-        c->pair_variant = std::min(std::max(atoi(forced), 0), nv);
+        const int v = std::min(std::max(atoi(forced), 0), nv);
+        c->pair_variant = v == 0 || n3_variant_usable(c, v) ? v : c->pair_variant;
         return TCP_OK;
     }
     if (const char *off = getenv("TCP_AUTOTUNE"))
         if (atoi(off) == 0) return TCP_OK;
     if (cache) {
         const int v = cache_lookup(cache, key);
-        if (v >= 0 && v <= nv) {
+        if (v == 0 || (v >= 1 && v <= nv && n3_variant_usable(c, v))) {
             c->pair_variant = v;
             return TCP_OK;
         }
@@ -942,6 +986,7 @@ static int choose_variant(tcp_ctx *c, const char *cache, const std::string &key)
     int best_v = c->pair_variant;
     int rc = TCP_OK;
     for (int v = 0; v <= nv && !rc; ++v) {
+        if (v >= 1 && !n3_variant_usable(c, v)) continue;   // ms stays 0: not timed
         c->pair_variant = v;
         const long long before = c->launches;
         rc = launch_pair(c, true, false);
@@ -1037,7 +1082,7 @@ extern "C" int tcp_autotune_report(tcp_ctx *c, int *variant, double *ms, int nma
     using namespace tcp;
     if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");
     if (variant) *variant = c->pair_variant;
-    for (int k = 0; ms && k < nmax && k < 16; ++k) ms[k] = c->pair_variant_ms[k];
+    for (int k = 0; ms && k < nmax && k < 32; ++k) ms[k] = c->pair_variant_ms[k];
     return TCP_OK;
 }
 

@@ -2,8 +2,43 @@
 #pragma once
 
 #include "device_util.cuh"
+#include "tcp_internal.h"
 
 namespace tcp {
+
+// Exact RDF bin of one pair from its fixed-point separations (RdfEdges):
+// `bin` is the FP32 estimate on entry and the exact bin on return; *ok is
+// set to whether r < rc holds exactly.  The estimate is within one bin, so
+// each loop runs at most once in practice.
+template <bool CUBIC>
+__device__ __forceinline__ int rdf_exact_bin(int d0, int d1, int d2, const RdfEdges *__restrict__ E, int t,
+                                             const double *box, int bin, bool &ok) {
+    bin = min(max(bin, 0), kNbin);
+    if (CUBIC) {
+        const long long a = d0, b = d1, c = d2;
+        const unsigned long long q =
+            (unsigned long long)(a * a) + (unsigned long long)(b * b) + (unsigned long long)(c * c);
+        ok = q < E->rc2;
+        while (bin > 0 && q < __ldg(&E->e[t][bin])) --bin;
+        while (bin < kNbin && q >= __ldg(&E->e[t][bin + 1])) ++bin;
+    } else {
+        constexpr double k2m32 = 1.0 / 4294967296.0;
+        const double a = (double)d0 * (box[0] * k2m32), b = (double)d1 * (box[1] * k2m32),
+                     c = (double)d2 * (box[2] * k2m32);
+        const double q = a * a + b * b + c * c;
+        ok = q < E->rc2d;
+        while (bin > 0 && q < __ldg(&E->d[t][bin])) --bin;
+        while (bin < kNbin && q >= __ldg(&E->d[t][bin + 1])) ++bin;
+    }
+    return bin;
+}
+
+// true when the FP32 bin estimate tb = r/dx or r^2 (against rc^2) is too
+// close to an edge to be trusted
+__device__ __forceinline__ bool rdf_near_edge(float tb, int bin, float r2, float rc2) {
+    const float fr = tb - (float)bin;
+    return fr < kRdfEdge || fr > 1.0f - kRdfEdge || fabsf(r2 - rc2) < kRdfEdge * rc2;
+}
 
 // erfc(x) = exp(-x^2) t Q(t), t = 1/(1 + kErfcP x): the factor of the
 // reciprocal argument (host constants p_alpha = kErfcP alpha, p_lam = kErfcP/lambda).
@@ -15,6 +50,19 @@ constexpr int kErfcDeg = 6;
 #define TCP_ERFC_Q                                                                                  \
     {-1.717338572e-01f, 5.984714114e-01f, -4.147594920e-01f, 4.816444120e-01f, 8.168755304e-02f,    \
      2.231449970e-01f, 2.015448752e-01f}
+
+// The Ewald term alone needs erfc(x) only for x = alpha r <= alpha rc, which
+// is 3.1 for the reference's alpha = 3.1/rc and 3.46 for a 1e-6 Ewald error.
+// On [0, kErfc5Xmax] a degree-5 Q with P = kErfc5P (fit_erfc.py --short)
+// reaches 8.5e-7 max / 3.7e-7 rms relative error in FP32 Horner form, one
+// FMA less per pair than the degree-6 fit; the host selects it when
+// alpha rc <= kErfc5Xmax.
+constexpr double kErfc5P = 0.41;
+constexpr double kErfc5Xmax = 3.6;
+constexpr int kErfc5Deg = 5;
+#define TCP_ERFC5_Q                                                                                 \
+    {-1.858996734e-01f, 6.017686447e-01f, -2.337225564e-01f, 3.931379106e-01f, 1.894349663e-01f,    \
+     2.352810149e-01f}
 
 // t Q(t)
 __device__ __forceinline__ float erfc_poly(float t) {

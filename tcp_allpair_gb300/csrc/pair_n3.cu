@@ -170,41 +170,100 @@ static constexpr ErfcQ2Table make_erfc_q2() {
 }
 __constant__ ErfcQ2Table kErfcQ2 = make_erfc_q2();
 
+struct Erfc5Q2Table {
+    float2 q[kErfc5Deg + 1];
+};
+static constexpr Erfc5Q2Table make_erfc5_q2() {
+    constexpr float q_[kErfc5Deg + 1] = TCP_ERFC5_Q;
+    Erfc5Q2Table t{};
+    for (int k = 0; k <= kErfc5Deg; ++k) t.q[k] = float2{q_[k], q_[k]};
+    return t;
+}
+__constant__ Erfc5Q2Table kErfc5Q2 = make_erfc5_q2();
+
+// Forms of the Ewald erfc polynomial of the packed kernels: degree 6 in
+// Horner form (any argument up to 4.5), degree 5 (kErfc5P, arguments up to
+// kErfc5Xmax) in Horner form, or the same degree 5 as
+// ((c5 t + c4) t^2 + (c3 t + c2)) t^2 + (c1 t + c0): one operation more and a
+// dependency chain of 3 instead of 5.
+constexpr int kErfcH6 = 6, kErfcH5 = 5, kErfcE5 = 50;
+
+template <int PD = kErfcH6>
 __device__ __forceinline__ float2 erfc_poly2(float2 t) {
-    float2 q = kErfcQ2.q[0];
+    static_assert(PD == kErfcH6 || PD == kErfcH5 || PD == kErfcE5, "erfc polynomial forms");
+    if constexpr (PD == kErfcE5) {
+        const float2 t2 = __fmul2_rn(t, t);
+        const float2 a = __ffma2_rn(kErfc5Q2.q[4], t, kErfc5Q2.q[5]);   // c1 t + c0
+        const float2 b = __ffma2_rn(kErfc5Q2.q[2], t, kErfc5Q2.q[3]);   // c3 t + c2
+        const float2 c = __ffma2_rn(kErfc5Q2.q[0], t, kErfc5Q2.q[1]);   // c5 t + c4
+        return __fmul2_rn(__ffma2_rn(__ffma2_rn(c, t2, b), t2, a), t);
+    } else {
+        float2 q = PD == kErfcH6 ? kErfcQ2.q[0] : kErfc5Q2.q[0];
 #pragma unroll
-    for (int k = 1; k <= kErfcDeg; ++k) q = __ffma2_rn(q, t, kErfcQ2.q[k]);
-    return __fmul2_rn(q, t);
+        for (int k = 1; k <= PD; ++k) q = __ffma2_rn(q, t, PD == kErfcH6 ? kErfcQ2.q[k] : kErfc5Q2.q[k]);
+        return __fmul2_rn(q, t);
+    }
 }
 
 // RDF: +2 per unique pair inside rc in bin INT(r/dx) <= kNdist of this pair
 // type (the ordered-pair kernels add 1 from each side), in a CTA histogram.
-// Branch-free: a pair that does not count adds to its lane's spare slot
-// (kRdfSpare + lane, never flushed), so every lane issues the same atomic.
+// Branch-free on the common path: a pair that does not count adds to its
+// lane's spare slot (kRdfSpare + lane, never flushed), so every lane issues
+// the same atomic.  Pairs whose FP32 r/dx or r^2 lies near a bin edge or rc
+// take the exact test of the fixed-point separation (rdf_exact_bin), so the
+// counts equal those of exact arithmetic on the fixed-point positions.
 constexpr int kRdfSpare = 3 * kNbin;
+struct N3Rdf {
+    unsigned *hist;
+    int hoff;                  // pair type * kNbin
+    int pt;                    // pair type
+    float inv_dx;              // u / dx of this pair type
+    float rc2;                 // cut-off^2 in u^2
+    const RdfEdges *E;
+};
+
+__device__ __forceinline__ int idiff_i(int a, int b) { return (int)((unsigned)a - (unsigned)b); }
+
+// r: FP32 distance (meaningless where the caller replaced r^2 by 1); r2: the
+// pair's FP32 r^2; ok: the FP32 cut-off and index mask; valid: the index mask
 template <bool RDF>
-__device__ __forceinline__ void rdf_add(unsigned *hist, int off, float inv_dx, float r, bool ok) {
+__device__ __forceinline__ void rdf_add(const N3Rdf &h, float r, float r2, bool ok, bool valid, const int4 &xa,
+                                        const int4 &xj) {
     if (RDF) {
-        const int bin = (int)(r * inv_dx);
-        const int idx = (ok && bin <= kNdist) ? off + bin : kRdfSpare + (int)(threadIdx.x & 31);
-        atomicAdd(&hist[idx], 2u);
+        const float tb = r * h.inv_dx;
+        int bin = (int)tb;
+        if (valid && rdf_near_edge(tb, bin, r2, h.rc2)) {
+            if (!ok) bin = (int)(sqrtf(r2) * h.inv_dx);
+            bin = rdf_exact_bin<true>(idiff_i(xa.x, xj.x), idiff_i(xa.y, xj.y), idiff_i(xa.z, xj.z), h.E, h.pt,
+                                      nullptr, bin, ok);
+        }
+        const int idx = (ok && bin <= kNdist) ? h.hoff + bin : kRdfSpare + (int)(threadIdx.x & 31);
+        atomicAdd(&h.hist[idx], 2u);
     }
 }
 
-template <int KIND, bool ENERGY, bool MASKED, bool RDF = false>
+// PD: form of the Ewald erfc polynomial (kErfcH6, or kErfcH5 / kErfcE5 when
+// alpha rc <= kErfc5Xmax); the Kelbg erfc(r/lambda) always uses kErfcH6.
+// RDF: h, the index masks v0, v1 and the positions xa, xb (i-particles) and
+// xj of the two pairs.
+template <int KIND, bool ENERGY, bool MASKED, bool RDF = false, int PD = kErfcH6>
 __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, bool ok0, bool ok1, bool near_any,
-                                             float2 &pe, unsigned *hist = nullptr, int hoff = 0, float inv_dx = 0.f) {
+                                             float2 &pe, const N3Rdf *h = nullptr, bool v0 = true, bool v1 = true,
+                                             const int4 *xa = nullptr, const int4 *xb = nullptr,
+                                             const int4 *xj = nullptr) {
     const float2 r2s = MASKED ? make_float2(ok0 ? r2.x : 1.0f, ok1 ? r2.y : 1.0f) : r2;
     const float2 rinv = make_float2(rsqrt_approx(r2s.x), rsqrt_approx(r2s.y));
     const float2 rinv_m = make_float2(ok0 ? rinv.x : 0.0f, ok1 ? rinv.y : 0.0f);
     const float2 r = __fmul2_rn(r2s, rinv);
-    rdf_add<RDF>(hist, hoff, inv_dx, r.x, ok0);
-    rdf_add<RDF>(hist, hoff, inv_dx, r.y, ok1);
-    const float2 ta = __ffma2_rn(f2(c.u_p_alpha), r, f2(1.0f));
+    if (RDF) {
+        rdf_add<RDF>(*h, r.x, r2.x, ok0, v0, *xa, *xj);
+        rdf_add<RDF>(*h, r.y, r2.y, ok1, v1, *xb, *xj);
+    }
+    const float2 ta = __ffma2_rn(f2(PD == kErfcH6 ? c.u_p_alpha : c.u_p_alpha5), r, f2(1.0f));
     const float2 t = make_float2(rcp_approx(ta.x), rcp_approx(ta.y));
     const float2 ea = __fmul2_rn(f2(c.u_c_exp), r2s);
     const float2 e = make_float2(ex2_approx(ea.x), ex2_approx(ea.y));
-    const float2 er = __fmul2_rn(__fmul2_rn(e, erfc_poly2(t)), rinv_m);   // erfc(ar)/r
+    const float2 er = __fmul2_rn(__fmul2_rn(e, erfc_poly2<PD>(t)), rinv_m);   // erfc(ar)/r
     float2 s = __ffma2_rn(f2(c.u_c_gauss), e, er);
     float2 u = er;
     if (KIND == 1) {                                      // Deutsch, force.f90:136-139
@@ -223,7 +282,7 @@ __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, boo
         if (ENERGY) {
             const float2 t2a = __ffma2_rn(f2(c.u_p_lam), r, f2(1.0f));
             const float2 t2 = make_float2(rcp_approx(t2a.x), rcp_approx(t2a.y));
-            erfc_rl = __fmul2_rn(g, erfc_poly2(t2));      // erfc(r/lambda)
+            erfc_rl = __fmul2_rn(g, erfc_poly2<kErfcH6>(t2));   // erfc(r/lambda)
             u = __fadd2_rn(u, __ffma2_rn(f2(c.u_sqrtpi_lam), erfc_rl, __fmul2_rn(g, nrinv)));
         }
         const bool c0 = n0 && (r2s.x < c.u_close2), c1 = n1 && (r2s.y < c.u_close2);
@@ -250,11 +309,12 @@ __device__ __forceinline__ float idiff(int a, int b) { return (float)(int)((unsi
 // LDSJ: j positions read from a warp-private copy of the chunk written twice
 // in a row (jb[64]), so that step s reads jb[lane + s] with one shared load
 // instead of rotating them with three shuffles; the reactions still rotate.
-template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R, bool LDSJ = false, bool RDF = false>
+template <int KIND, bool ENERGY, bool MASKED, int UNROLL, int R, bool LDSJ = false, bool RDF = false,
+          int PD = kErfcH6>
 __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__restrict__ tj, int cnt, int jstart,
                                            const int4 (&xi)[R], int ibase, int iend,
                                            float (*sjacc)[3], float (&p)[R][3], float &pe, int4 *jb = nullptr,
-                                           unsigned *hist = nullptr, int hoff = 0, float inv_dx = 0.f) {
+                                           const N3Rdf *rh = nullptr) {
     static_assert(R % 2 == 0, "paired form needs an even number of i-particles per lane");
     constexpr int G = R / 2;
     const int lane = threadIdx.x & 31;
@@ -276,7 +336,7 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
         for (int s = 0; s < 32; ++s) {
             if (LDSJ) xj = jb[lane + s];
             float2 d[G][3], r2[G];
-            bool ok[R];
+            bool ok[R], valid[R];
             float r2min = 3.0e38f;
 #pragma unroll
             for (int g = 0; g < G; ++g) {
@@ -284,22 +344,24 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
                 d[g][1] = make_float2(idiff(xi[2 * g].y, xj.y), idiff(xi[2 * g + 1].y, xj.y));
                 d[g][2] = make_float2(idiff(xi[2 * g].z, xj.z), idiff(xi[2 * g + 1].z, xj.z));
                 r2[g] = __ffma2_rn(d[g][0], d[g][0], __ffma2_rn(d[g][1], d[g][1], __fmul2_rn(d[g][2], d[g][2])));
-                ok[2 * g] = r2[g].x < c.u_rc2;
-                ok[2 * g + 1] = r2[g].y < c.u_rc2;
+                valid[2 * g] = valid[2 * g + 1] = true;
                 if (MASKED) {
                     const int jo = ch * 32 + ((lane + s) & 31);
                     const int i0 = ibase + 64 * g, i1 = i0 + 32;   // i-particles 2g, 2g+1 of this lane
-                    ok[2 * g] = ok[2 * g] && (i0 < iend) && (jo < cnt) && (i0 < jstart + jo);
-                    ok[2 * g + 1] = ok[2 * g + 1] && (i1 < iend) && (jo < cnt) && (i1 < jstart + jo);
+                    valid[2 * g] = (i0 < iend) && (jo < cnt) && (i0 < jstart + jo);
+                    valid[2 * g + 1] = (i1 < iend) && (jo < cnt) && (i1 < jstart + jo);
                 }
+                ok[2 * g] = (r2[g].x < c.u_rc2) && valid[2 * g];
+                ok[2 * g + 1] = (r2[g].y < c.u_rc2) && valid[2 * g + 1];
                 if (KIND == 2) r2min = fminf(r2min, fminf(r2[g].x, r2[g].y));
             }
             bool near_any = false;
             if (KIND == 2) near_any = __any_sync(0xffffffffu, r2min < c.u_rshort2);
 #pragma unroll
             for (int g = 0; g < G; ++g) {
-                const float2 w = n3_pair_x2<KIND, ENERGY, MASKED, RDF>(c, r2[g], ok[2 * g], ok[2 * g + 1], near_any,
-                                                                     pe2, hist, hoff, inv_dx);
+                const float2 w = n3_pair_x2<KIND, ENERGY, MASKED, RDF, PD>(
+                    c, r2[g], ok[2 * g], ok[2 * g + 1], near_any, pe2, rh, valid[2 * g], valid[2 * g + 1], &xi[2 * g],
+                    &xi[2 * g + 1], &xj);
                 pg[g][0] = __ffma2_rn(w, d[g][0], pg[g][0]);
                 pg[g][1] = __ffma2_rn(w, d[g][1], pg[g][1]);
                 pg[g][2] = __ffma2_rn(w, d[g][2], pg[g][2]);
@@ -338,11 +400,16 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
 // MODE 0: scalar FP32, i-force accumulators in registers; 1: packed FP32x2,
 // accumulators in shared memory; 2: as 1 with j positions read from shared
 // memory (LDSJ).
-// W: warps per CTA (i-tile = 32 R W particles).
-template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH, int MODE = 0, int W = kN3Warps, bool RDF = false>
+// W: warps per CTA (i-tile = 32 R W particles).  PD: form of the Ewald erfc
+// polynomial of the packed forms (kErfcH5 / kErfcE5 only where
+// PairConsts::erfc5_ok).
+template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH, int MODE = 0, int W = kN3Warps, bool RDF = false,
+          int PD = kErfcH6>
 __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
     static_assert(W >= 4, "the reaction flush needs at least kN3Sub threads");
     static_assert(!RDF || (MODE >= 1 && !BATCH), "RDF histograms: packed single-system forms");
+    static_assert(PD == kErfcH6 || MODE >= 1, "the degree-5 erfc exists in the packed forms");
+    static_assert((32 * R * W) % kN3Sub == 0, "i-tiles hold whole j-subtiles");
     constexpr int NT = 32 * W;
     constexpr bool X2 = MODE >= 1;
     constexpr bool SACC = MODE >= 1;
@@ -352,7 +419,8 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
     __shared__ __align__(8) uint64_t bars[kN3Stages];
     __shared__ float sjacc[kN3Sub][3];
     __shared__ double red[32];
-    __shared__ long long s_next;
+    // the item of each ring slot, decoded once by thread 0 (s_I < 0: no item)
+    __shared__ int s_rep[kN3Stages], s_I[kN3Stages], s_S[kN3Stages];
     __shared__ unsigned hist[RDF ? kRdfSpare + 32 : 1];
     // per-thread TwoSum (hi, lo) i-force accumulators, touched once per item:
     // in shared memory ([slot][thread], conflict-free) for the packed forms,
@@ -361,10 +429,6 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
     __shared__ __align__(16) int4 jbuf[MODE == 2 ? W : 1][MODE == 2 ? 64 : 1];
     float hi[SACC ? 1 : R][3], lo[SACC ? 1 : R][3];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-
-    const long long it0 = a.nstatic * (long long)blockIdx.x / gridDim.x;
-    const long long it1 = a.nstatic * (long long)(blockIdx.x + 1) / gridDim.x;
-    const int nst = (int)(it1 - it0);
 
     for (int k = tid; k < kN3Sub * 3; k += NT) (&sjacc[0][0])[k] = 0.f;
     if (RDF)
@@ -375,10 +439,37 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
     }
     __syncthreads();
 
-    // subtile copy of global item `it` into ring stage `stage` (thread 0)
-    auto issue = [&](int stage, long long it) {
+    // Guided self-scheduling: thread 0 claims chunks of consecutive items
+    // (a.chunks, shorter towards the end of the list) from the counter, so the
+    // CTAs end together whatever their items cost, and the i-tile stays in
+    // registers along the long early chunks.  It decodes each item once,
+    // publishes it in the ring slot of its subtile copy and issues the copy
+    // kN3Stages items ahead of the one being processed.
+    long long cur = 0, cend = 0;   // thread 0: the rest of the current chunk
+    bool drained = false;          // thread 0: the chunk list is exhausted
+    int last_filled = -1;          // thread 0: ring index of the last item with a copy
+    auto fill = [&](int k) {       // ring index k (slot k % kN3Stages), thread 0
+        const int stage = k % kN3Stages;
+        if (!drained && cur == cend) {
+            const unsigned j = atomicAdd(a.counter, 1u);
+            if (j < a.nchunks) {
+                cur = a.chunks[j];
+                cend = a.chunks[j + 1];
+            } else {
+                drained = true;
+            }
+        }
+        if (drained) {
+            s_I[stage] = -1;
+            return;
+        }
         int rep, I_, S_;
-        n3_locate<TILE, BATCH>(a, it, rep, I_, S_);
+        n3_locate<TILE, BATCH>(a, cur++, rep, I_, S_);
+        s_rep[stage] = rep;
+        s_I[stage] = I_;
+        s_S[stage] = S_;
+        last_filled = k;
+        if (a.inject_skip && blockIdx.x == 0 && k == 0) return;   // test hook: the copy never comes
         const N3Geom &g = n3_geom<BATCH>(a, rep);
         int js, jc, jsp;
         n3_sub(g, S_, js, jc, jsp);
@@ -387,8 +478,7 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
         bulk_g2s(tiles[stage], a.xq + g.off + js, bytes, &bars[stage]);
     };
     if (tid == 0)
-        for (int k = 0; k < min(kN3Stages, nst); ++k)
-            if (!(a.inject_skip && blockIdx.x == 0 && k == 0)) issue(k, it0 + k);
+        for (int k = 0; k < kN3Stages; ++k) fill(k);
 
     double etot = 0.0;
     int curRep = -1, curI = -1, istart = 0, iend = 0, isp = 0, ifirst = 0, ioff = 0;
@@ -433,10 +523,9 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
         eh = el = 0.f;
     };
 
-    // process global item `it` in ring slot k; false on timeout
-    auto process = [&](int k, long long it) -> bool {
-        int rep, I_, S_;
-        n3_locate<TILE, BATCH>(a, it, rep, I_, S_);
+    // process the item (replica rep, row I_, subtile S_) of ring index k;
+    // false on timeout
+    auto process = [&](int k, int rep, int I_, int S_) -> bool {
         const N3Geom &g = n3_geom<BATCH>(a, rep);
         if (I_ != curI || rep != curRep) {
             flush_i();
@@ -462,10 +551,12 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
 #pragma unroll
         for (int r = 0; r < R; ++r) p[r][0] = p[r][1] = p[r][2] = 0.f;
         const int kind = pt == 1 ? (c.ei_model == TCP_EI_DEUTSCH ? 1 : (c.ei_model == TCP_EI_KELBG ? 2 : 0)) : 0;
+        N3Rdf rh;
+        if (RDF) rh = N3Rdf{hist, pt * kNbin, pt, c.u_inv_dx[pt], c.u_rc2, a.rdf_edges};
 #define TCP_N3_ITEM(KIND, MASKED)                                                                      \
     do {                                                                                                \
         if (X2)                                                                                         \
-            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R, MODE == 2, RDF>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe, jbuf[MODE == 2 ? warp : 0], RDF ? hist : nullptr, pt * kNbin, RDF ? c.u_inv_dx[pt] : 0.f); \
+            n3_item_x2<KIND, ENERGY, MASKED, UNROLL, R, MODE == 2, RDF, PD>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe, jbuf[MODE == 2 ? warp : 0], &rh); \
         else                                                                                            \
             n3_item<KIND, ENERGY, MASKED, UNROLL, R>(c, tiles[stage], cnt, jstart, xi, ibase, iend, sjacc, p, pe);    \
     } while (0)
@@ -507,43 +598,24 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
         return !timeout;
     };
 
+    __syncthreads();   // the first slots are published
     bool good = true;
     int k = 0;
-    int issued = min(kN3Stages, nst);   // items whose subtile copy has been issued
-    // static share: contiguous items, subtiles prefetched kN3Stages ahead
-    for (; k < nst; ++k) {
-        if (!process(k, it0 + k)) {
+    for (;; ++k) {
+        const int stage = k % kN3Stages;
+        const int I_ = s_I[stage];
+        if (I_ < 0) break;
+        if (!process(k, s_rep[stage], I_, s_S[stage])) {   // ends with a CTA barrier
             good = false;
             break;
         }
-        if (k + kN3Stages < nst) {
-            if (tid == 0) issue(k % kN3Stages, it0 + k + kN3Stages);
-            issued = k + kN3Stages + 1;
-        }
+        if (tid == 0) fill(k + kN3Stages);
         __syncthreads();
-    }
-    // dynamic share: one item at a time from the counter
-    while (good) {
-        if (tid == 0) {
-            const long long it = a.nstatic + (long long)atomicAdd(a.counter, 1u);
-            s_next = it;
-            if (it < a.total && !(a.inject_skip && blockIdx.x == 0 && k == 0)) issue(k % kN3Stages, it);
-        }
-        __syncthreads();
-        const long long it = s_next;
-        if (it >= a.total) break;
-        issued = k + 1;
-        if (!process(k, it)) {
-            good = false;
-            break;
-        }
-        __syncthreads();
-        ++k;
     }
     if (!good) {
         if (tid == 0) {
             atomicOr(a.status, kStatusTmaTimeout);
-            for (int kk = k; kk < issued; ++kk)   // copies possibly still in flight
+            for (int kk = k; kk <= last_filled; ++kk)   // copies possibly still in flight
                 mbar_wait_bounded(&bars[kk % kN3Stages], (uint32_t)((kk / kN3Stages) & 1), kWaitLimitCycles);
         }
         __syncthreads();
@@ -576,6 +648,7 @@ struct N3Variant {
     N3Kernel energy, plain;
     int R, W;
     const char *name;
+    bool erfc5 = false;   // degree-5 Ewald erfc: only where PairConsts::erfc5_ok
 };
 static const N3Variant kVariants[] = {
     {pair_n3_kernel<true, 2, 2, 3, false>, pair_n3_kernel<false, 2, 2, 3, false>, 2, 8, "n3_r2_u2_b3"},
@@ -589,6 +662,18 @@ static const N3Variant kVariants[] = {
     {pair_n3_kernel<true, 4, 1, 3, false, 1>, pair_n3_kernel<false, 4, 1, 3, false, 1>, 4, 8, "n3_r4_u1_b3_x2"},
     {pair_n3_kernel<true, 4, 1, 2, false, 2>, pair_n3_kernel<false, 4, 1, 2, false, 2>, 4, 8, "n3_r4_u1_b2_x2l"},
     {pair_n3_kernel<true, 4, 1, 3, false, 2>, pair_n3_kernel<false, 4, 1, 3, false, 2>, 4, 8, "n3_r4_u1_b3_x2l"},
+    {pair_n3_kernel<true, 4, 1, 3, false, 2, 8, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 1, 3, false, 2, 8, false, kErfcH5>, 4, 8, "n3_r4_u1_b3_x2l_p5", true},
+    {pair_n3_kernel<true, 4, 1, 4, false, 2, 7>, pair_n3_kernel<false, 4, 1, 4, false, 2, 7>, 4, 7,
+     "n3_r4_u1_w7b4_x2l"},
+    {pair_n3_kernel<true, 4, 1, 4, false, 2, 7, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 1, 4, false, 2, 7, false, kErfcH5>, 4, 7, "n3_r4_u1_w7b4_x2l_p5", true},
+    {pair_n3_kernel<true, 4, 1, 6, false, 2, 4, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 1, 6, false, 2, 4, false, kErfcH5>, 4, 4, "n3_r4_u1_w4b6_x2l_p5", true},
+    {pair_n3_kernel<true, 4, 2, 3, false, 2, 8, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 2, 3, false, 2, 8, false, kErfcH5>, 4, 8, "n3_r4_u2_b3_x2l_p5", true},
+    {pair_n3_kernel<true, 4, 1, 3, false, 2, 8, false, kErfcE5>,
+     pair_n3_kernel<false, 4, 1, 3, false, 2, 8, false, kErfcE5>, 4, 8, "n3_r4_u1_b3_x2l_e5", true},
 };
 constexpr int kN3Variants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -604,6 +689,9 @@ static const N3Variant kRdfVariants[] = {
 constexpr int kN3RdfVariants = sizeof(kRdfVariants) / sizeof(kRdfVariants[0]);
 
 int n3_variant_count() { return kN3Variants; }
+bool n3_variant_usable(const tcp_ctx *c, int v) {
+    return v >= 1 && v <= kN3Variants && (!kVariants[v - 1].erfc5 || c->pc.erfc5_ok);
+}
 const char *n3_variant_name(int v) { return v >= 1 && v <= kN3Variants ? kVariants[v - 1].name : "ordered"; }
 
 int n3_grid_for(const tcp_ctx *c, int v) {
@@ -643,6 +731,42 @@ N3Geom n3_geometry(int off, int nel, int nion, int tile, long long item0, long l
     return g;
 }
 
+void n3_chunk_table(long long total, int ctas, std::vector<long long> &starts) {
+    starts.assign(1, 0);
+    const long long div = 2LL * std::max(1, ctas);
+    for (long long at = 0; at < total;) {
+        at += std::max(1LL, (total - at + div - 1) / div);
+        starts.push_back(std::min(at, total));
+    }
+}
+
+// Chunk tables of every i-tile size the variants use, in one device array
+// (c->n3_chunks; c->n3_chunk_meta holds tile, items, offset, chunks per
+// table).  Built on the host when the pair constants change, outside any
+// stream capture, for the largest persistent grid.
+int n3_prepare_chunks(tcp_ctx *c) {
+    std::vector<int> tiles;
+    for (const N3Variant &v : kVariants) tiles.push_back(32 * v.R * v.W);
+    for (const N3Variant &v : kRdfVariants) tiles.push_back(32 * v.R * v.W);
+    std::sort(tiles.begin(), tiles.end());
+    tiles.erase(std::unique(tiles.begin(), tiles.end()), tiles.end());
+    const int ctas = n3_grid(c);
+    std::vector<long long> all, meta, t;
+    for (const int tile : tiles) {
+        long long total = 0;
+        n3_geometry(0, c->nel, c->nion, tile, 0, &total);
+        n3_chunk_table(total, ctas, t);
+        meta.insert(meta.end(), {(long long)tile, total, (long long)all.size(), (long long)t.size() - 1});
+        all.insert(all.end(), t.begin(), t.end());
+    }
+    if (c->n3_chunks) cudaFree(c->n3_chunks);
+    c->n3_chunks = nullptr;
+    TCP_CUDA(cudaMalloc(&c->n3_chunks, sizeof(long long) * all.size()));
+    TCP_CUDA(cudaMemcpy(c->n3_chunks, all.data(), sizeof(long long) * all.size(), cudaMemcpyHostToDevice));
+    c->n3_chunk_meta = meta;
+    return TCP_OK;
+}
+
 int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf) {
     int rv = 0;
     if (const char *forced = getenv("TCP_RDF_VARIANT")) rv = std::min(std::max(atoi(forced), 0), kN3RdfVariants - 1);
@@ -656,7 +780,12 @@ int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf) {
     a.g = n3_geometry(0, c->nel, c->nion, tile, 0, &total);
     a.xq = c->xq;
     a.total = total;
-    a.nstatic = total - total * kN3DynPercent / 100;
+    for (size_t m = 0; m + 3 < c->n3_chunk_meta.size(); m += 4)
+        if (c->n3_chunk_meta[m] == tile && c->n3_chunk_meta[m + 1] == total) {
+            a.chunks = c->n3_chunks + c->n3_chunk_meta[m + 2];
+            a.nchunks = (unsigned)c->n3_chunk_meta[m + 3];
+        }
+    if (!a.chunks) return set_error(TCP_ERR_STATE, "no Newton-3 chunk table for this geometry");
     a.ntot = c->n;
     a.facc = c->fpart;
     a.upart = c->upart;
@@ -665,6 +794,7 @@ int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf) {
     a.c = c->pc;
     a.inject_skip = inject_fault("tile_wait") ? 1 : 0;
     a.rdf = c->rdf;
+    a.rdf_edges = c->rdf_edges;
     // CTAs left free for the reciprocal chain when it runs beside this launch
     const int reserve = c->recip_beside ? c->pair_reserve : 0;
     const int full = rdf ? kernel_grid(c, K.energy, nt) : n3_grid_for(c, v);
@@ -732,15 +862,18 @@ static int n3_batch_grid(int num_sms, int v) {
     return std::max(1, num_sms * std::max(1, bps));
 }
 
+int n3_batch_ctas(int num_sms, int v) { return n3_batch_grid(num_sms, std::min(std::max(v, 0), kN3BatchVariants - 1)); }
+
 int launch_pair_n3_batch(cudaStream_t st, const int4 *xq, int ntot, double *facc, const void *reps_dev, int nrep,
-                         long long total, double *ur_rep, unsigned *status, unsigned *counter, int num_sms,
-                         bool energy, int variant) {
+                         long long total, const long long *chunks, unsigned nchunks, double *ur_rep, unsigned *status,
+                         unsigned *counter, int num_sms, bool energy, int variant) {
     const int v = std::min(std::max(variant, 0), kN3BatchVariants - 1);
     N3Args a;
     std::memset(&a, 0, sizeof a);
     a.xq = xq;
     a.total = total;
-    a.nstatic = total - total * kN3DynPercent / 100;
+    a.chunks = chunks;
+    a.nchunks = nchunks;
     a.ntot = ntot;
     a.facc = facc;
     a.status = status;

@@ -42,7 +42,9 @@ struct N3Args {
     double *facc;         // [3][ntot], zeroed before the launch
     double *upart;        // [gridDim.x] (single system)
     unsigned *status;
-    unsigned *counter;    // dynamic item counter, zeroed before the launch
+    unsigned *counter;    // chunk counter (FP32C) / item counter (FP64), zeroed before the launch
+    const long long *chunks;   // FP32C: chunk c holds items [chunks[c], chunks[c+1])
+    unsigned nchunks;
     N3Geom g;             // single system
     PairConsts c;
     const N3Rep *reps;    // batch: one entry per replica
@@ -50,6 +52,7 @@ struct N3Args {
     double *ur_rep;       // batch: Ur per replica (zeroed before the launch)
     int inject_skip;      // test hook: CTA 0 never issues the copy of its first item (its bounded wait runs out)
     unsigned long long *rdf;   // RDF variants: [3][kNbin] pair counts, +2 per unique pair (force.f90:99-103)
+    const RdfEdges *rdf_edges; // exact bin edges (RDF variants)
 };
 
 template <int TILE>
@@ -80,21 +83,34 @@ __device__ __forceinline__ void n3_sub(const N3Geom &a, int S, int &start, int &
     }
 }
 
-// local item index of one system -> (row I, subtile S)
+// local item index of one system -> (row I, subtile S), in closed form.
+// Electron row k (k < nIe) holds nS - k SPT items and starts at item
+// k nS - SPT k (k - 1) / 2; ion row nIe + k holds n0 - k SPT items
+// (n0 = nS - nSe) and starts at E + k n0 - SPT k (k - 1) / 2, E the items of
+// the electron rows.  k comes from the root of that quadratic in FP32 and is
+// corrected by exact integer comparisons.  An item at or past the end gives
+// S = nS.
 template <int TILE>
 __device__ __forceinline__ void n3_decode(const N3Geom &a, long long it, int &I, int &S) {
-    long long acc = 0;
-    int st, en, sp, first;
-    for (I = 0; I < a.nI; ++I) {
-        n3_itile<TILE>(a, I, st, en, sp, first);
-        const long long len = a.nS - first;
-        if (it < acc + len) {
-            S = first + (int)(it - acc);
-            return;
-        }
-        acc += len;
+    constexpr int SPT = TILE / kN3Sub;
+    const long long E = (long long)a.nIe * a.nS - (long long)SPT * a.nIe * (a.nIe - 1) / 2;
+    const bool ion = it >= E;
+    const long long x = ion ? it - E : it;
+    const int n0 = ion ? a.nS - a.nSe : a.nS;
+    const int rows = ion ? a.nI - a.nIe : a.nIe;
+    auto start = [&](int k) { return (long long)k * n0 - (long long)SPT * k * (k - 1) / 2; };
+    const float b = (float)n0 + 0.5f * (float)SPT;
+    int k = (int)((b - sqrtf(fmaxf(b * b - 2.0f * (float)SPT * (float)x, 0.0f))) / (float)SPT);
+    k = max(0, min(k, rows - 1));
+    while (k > 0 && start(k) > x) --k;
+    while (k + 1 < rows && start(k + 1) <= x) ++k;
+    if (rows <= 0 || x - start(k) >= (long long)(n0 - k * SPT)) {   // past the end
+        I = a.nI;
+        S = a.nS;
+        return;
     }
-    S = a.nS;
+    I = (ion ? a.nIe : 0) + k;
+    S = (ion ? a.nSe : 0) + k * SPT + (int)(x - start(k));
 }
 
 // global item -> replica (0 for a single system), row and subtile
@@ -126,5 +142,10 @@ __device__ __forceinline__ const PairConsts &n3_consts(const N3Args &a, int rep)
 
 // Tile geometry of a system of nel + nion particles for i-tiles of `tile`.
 N3Geom n3_geometry(int off, int nel, int nion, int tile, long long item0, long long *items);
+
+// Chunk boundaries of guided self-scheduling over `total` items for up to
+// `ctas` CTAs: chunk sizes ceil(rest / (2 ctas)), at least one item, so the
+// first chunks are long runs of one row and the last ones single items.
+void n3_chunk_table(long long total, int ctas, std::vector<long long> &starts);
 
 }  // namespace tcp

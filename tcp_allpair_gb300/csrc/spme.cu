@@ -10,6 +10,8 @@
 // and written as FP32 for R2C / C2R transforms, the influence multiply
 // (energy summed in FP64) and the force gather: on GB300 FP64 runs at 1/64 of
 // the FP32 rate, which makes a 128^3 FP64 transform compute-bound.
+// TCP_PREC_FP32C_R64 keeps the FP32C real-space sum and runs this chain in
+// FP64 as in TCP_PREC_FP64.
 //
 // Normalisation: both transforms are unnormalised, so the real mesh after the
 // inverse transform is phi = K^3 Qfin of the reference; its 1/K^3 (FFTE
@@ -525,7 +527,7 @@ int spme_setup(tcp_ctx *c) {
     c->Kh = c->K1 / 2 + 1;
     const size_t nreal = (size_t)c->K1 * c->K2 * c->K3;
     const size_t nhalf = (size_t)c->Kh * c->K2 * c->K3;
-    c->spme_fp32 = c->p.precision == TCP_PREC_FP32C;
+    c->spme_fp32 = c->p.precision == TCP_PREC_FP32C && !c->recip_fp64;
     if (!c->Q) {
         const size_t nbins = (size_t)c->K2 * c->K3;
         if (cudaMalloc(&c->bin_count, sizeof(int) * (nbins + 1)) != cudaSuccess ||

@@ -24,6 +24,24 @@ constexpr int kMaxOrder = 8;
 constexpr unsigned kStatusTmaTimeout = 1u;
 
 // ---------------------------------------------------------------------------
+// Exact RDF bins of the FP32C kernels.  Bin k of pair type t (ee, ei, ii)
+// holds the pairs with k dx_t <= r < (k+1) dx_t inside rc (force.f90:99-103).
+// The kernels bin from their FP32 r and send the pairs whose r/dx_t lies
+// within kRdfEdge of an integer, or whose r^2 lies within kRdfEdge of rc^2
+// (relative), to an exact test.  In a cubic box r^2 in units of u^2
+// (u = L/2^32) is an integer, the sum of the squared fixed-point
+// separations, and is compared with e[t][k] = ceil((k dx_t/u)^2) and
+// rc2 = ceil(rc^2/u^2).  Other boxes square the separations in FP64 (the
+// scaling by L/2^32 is exact) against d[t][k] = (k dx_t)^2 and rc2d.
+constexpr float kRdfEdge = 1.0f / 4096.0f;   // 8x the FP32 error of r/dx at r/dx = 500
+struct RdfEdges {
+    unsigned long long e[3][kNbin + 1];
+    unsigned long long rc2;
+    double d[3][kNbin + 1];
+    double rc2d;
+};
+
+// ---------------------------------------------------------------------------
 // Pair-kernel constants (host-computed once per parameter change).
 struct PairConsts {
     // FP32 path: fixed-point positions are 2^32 units per box length
@@ -48,6 +66,8 @@ struct PairConsts {
     int cubic;
     float u_rc2, u_p_alpha, u_c_exp, u_c_gauss, u_c_rs, u_inv_rs, u_c_lam, u_p_lam, u_sqrtpi_lam, u_rshort2;
     float u_close2, u_inv_lam2, u_alpha;
+    float u_p_alpha5;          // kErfc5P alpha u: the degree-5 erfc of the Newton-3 kernels
+    int erfc5_ok;              // alpha rc <= kErfc5Xmax: the degree-5 fit covers the Ewald term
     float u_inv_dx[3], u_qq_force[3], u_qq_energy[3];
     // FP64 path
     double box[3];
@@ -66,6 +86,21 @@ struct PairConsts {
     double qq[3];
     int ei_model;
 };
+
+// EWALD_SELF's constant energy, without eps: the self term
+// -alpha/sqrt(pi) sum q_i^2 (force.f90:44-45) plus, for a system with net
+// charge Q = sum q_i, the energy of the uniform neutralising background that
+// the Ewald sum implies, -pi Q^2 / (2 V alpha^2).  The reference has no
+// background term; its systems are neutral, where the term is zero.  Both
+// terms are in FP64 and scale with the charge scale s squared.
+inline double ewald_constant_energy(const tcp_params &p, int nel, int nion, double alpha) {
+    const double s = p.charge_scale;
+    const double q0 = s * p.q[0], q1 = s * p.q[1];
+    const double self = (-(double)nel * q0 * q0 - (double)nion * q1 * q1) * alpha / kSqrtPi;
+    const double Q = (double)nel * q0 + (double)nion * q1;
+    const double V = p.box[0] * p.box[1] * p.box[2];
+    return self - kPi * Q * Q / (2.0 * V * alpha * alpha);
+}
 
 // ---------------------------------------------------------------------------
 struct Ctx;
@@ -97,7 +132,7 @@ struct tcp_ctx {
     int fpart_splits = 1;      // splits written by the last pair launch
     int pair_variant = 1;      // FP32C real-space kernel: 0 ordered pairs, >= 1 Newton-3 variant
     bool tuned = false;        // autotuner ran for the current parameters
-    double pair_variant_ms[16] = {};   // autotuner timings per variant
+    double pair_variant_ms[32] = {};   // autotuner timings per variant
     // CTAs of the persistent Newton-3 grid left free so that the reciprocal
     // chain, which runs beside the pair kernel in a step, finds room on the
     // SMs (chosen by the autotuner from kReserveCandidates)
@@ -116,6 +151,9 @@ struct tcp_ctx {
     unsigned *counter = nullptr;        // dynamic work counter of the Newton-3 kernel
     unsigned long long *rdf = nullptr;  // [3][kNbin]
     unsigned long long *vdf = nullptr;  // [2][kNbin]
+    tcp::RdfEdges *rdf_edges = nullptr; // exact bin edges of the FP32C RDF
+    long long *n3_chunks = nullptr;     // chunk tables of the FP32C Newton-3 schedule
+    std::vector<long long> n3_chunk_meta;   // per table: i-tile, items, offset, chunks
     // staging for host transfers
     unsigned char *d_stage = nullptr;
     size_t d_stage_bytes = 0;
@@ -134,6 +172,7 @@ struct tcp_ctx {
     cufftDoubleComplex *Qk = nullptr;   // [K3][K2][Kh]
     double *infl = nullptr;             // theta * |b|^-2 on the half mesh
     bool spme_fp32 = false;             // FP32C mode: FP32 transforms, influence and gather
+    bool recip_fp64 = false;            // TCP_PREC_FP32C_R64: p.precision is FP32C, the reciprocal chain FP64
     float *Qf = nullptr;                // FP32 real mesh [K3][K2][K1]
     cufftComplex *Qkf = nullptr;        // FP32 half spectrum
     float *infl_f = nullptr;
@@ -217,6 +256,7 @@ int launch_pair_n3_f64(tcp_ctx *c, bool energy, bool rdf);
 int n3_grid(const tcp_ctx *c);
 int n3_variant_count();
 const char *n3_variant_name(int v);
+bool n3_variant_usable(const tcp_ctx *c, int v);
 int autotune_pair(tcp_ctx *c);
 int time_pair_with_recip(tcp_ctx *c, int reps, double *ms);   // ctx.cu
 int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf);
@@ -227,8 +267,11 @@ size_t n3_rep_bytes();
 long long n3_batch_fill(void *reps_host, int nrep, const int *off, const int *nel, const int *nion,
                         const PairConsts *pc, int tile);
 int launch_pair_n3_batch(cudaStream_t st, const int4 *xq, int ntot, double *facc, const void *reps_dev, int nrep,
-                         long long total, double *ur_rep, unsigned *status, unsigned *counter, int num_sms,
-                         bool energy, int variant);
+                         long long total, const long long *chunks, unsigned nchunks, double *ur_rep, unsigned *status,
+                         unsigned *counter, int num_sms, bool energy, int variant);
+int n3_batch_ctas(int num_sms, int v);
+void n3_chunk_table(long long total, int ctas, std::vector<long long> &starts);
+int n3_prepare_chunks(tcp_ctx *c);
 // spme.cu
 int spme_setup(tcp_ctx *c);                        // meshes, plans, influence function
 std::vector<double> bspline_moduli(int order, int K);

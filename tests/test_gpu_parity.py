@@ -340,12 +340,13 @@ def test_large_fp32c_rows_sample():
     assert np.linalg.norm(f.sum(0)) < 1e-6 * np.abs(f).sum()
 
 
-@pytest.mark.parametrize("variant", list(range(12)))
+@pytest.mark.parametrize("variant", list(range(18)))
 @pytest.mark.parametrize("ei,n", [("kelbg", 2048), ("deutsch", 1536), ("kelbg", 1000)])
 def test_fp32c_kernel_variants(monkeypatch, variant, ei, n):
     """Every real-space kernel the autotuner can pick (0 = ordered pairs,
-    1..4 = Newton-3 variants, 5..9 = Newton-3 with packed FP32x2 arithmetic)
-    against the oracle, including partial tiles."""
+    1..4 = Newton-3 variants, 5..17 = Newton-3 with packed FP32x2 arithmetic,
+    12 and 14..17 with the degree-5 Ewald erfc) against the oracle, including
+    partial tiles."""
     monkeypatch.setenv("TCP_PAIR_VARIANT", str(variant))
     s = make(n, seed=30 + variant)
     o = oracle.Oracle.from_system(s, ei=ei)
@@ -364,7 +365,7 @@ def test_autotuner_picks_a_timed_variant(monkeypatch):
     with ctx_for(s, precision="fp32c", ei="kelbg", recip="none") as c:
         c.Force_direct_self()
         v, ms = c.autotune_report()
-    assert 0 <= v <= 11
+    assert 0 <= v <= 17
     assert ms[v] > 0 and ms[v] == min(m for m in ms if m > 0)
 
 
@@ -496,7 +497,7 @@ def test_kelbg_close_pair_accuracy(monkeypatch, variant, r_over_lam):
     assert ur == pytest.approx(uo, rel=2e-5, abs=1e-6 * abs(uo) + 1e-12)
 
 
-@pytest.mark.parametrize("variant", [6, 9, 11])
+@pytest.mark.parametrize("variant", [6, 9, 11, 12, 13, 15])
 @pytest.mark.parametrize("nel,nion", [(1, 300), (257, 0), (700, 333), (1030, 2)])
 def test_fp32c_newton3_ragged_species(monkeypatch, variant, nel, nion):
     """Packed Newton-3 variants with a single electron, one species only, and
@@ -514,17 +515,59 @@ def test_fp32c_newton3_ragged_species(monkeypatch, variant, nel, nion):
     assert ur == pytest.approx(uo, rel=2e-5, abs=1e-9)
 
 
+def test_fp32c_with_fp64_reciprocal_chain():
+    """TCP_PREC_FP32C_R64: the FP32C real-space sum with the SPME chain
+    (spread, transforms, influence, gather) in FP64.  Its reciprocal forces
+    and Um are the FP64 context's (the same deterministic FP64 chain), its
+    real-space forces the FP32C context's, and its whole step agrees with the
+    oracle to the FP32C bound; the precision is fixed at tcp_create."""
+    s = make(2048, seed=44, K=32, order=5)
+    comps = {}
+    for prec in ("fp64", "fp32c", "fp32c_r64"):
+        with ctx_for(s, precision=prec, ei="kelbg", recip="spme") as c:
+            ur = c.Force_direct_self()
+            _, _, fr, _ = c.download(x=False, v=False, f=True)
+            um = c.Force_SPME4()
+            _, _, _, frec = c.download(x=False, v=False, f=False, frec=True)
+            e = c.force()
+            _, _, ft, _ = c.download(x=False, v=False, f=True)
+            if prec == "fp32c_r64":
+                q = T.params_for(s, precision="fp32c", ei="kelbg", recip="spme")
+                with pytest.raises(T.TcpError):
+                    c.set_params(q)
+                c.set_params(T.params_for(s, precision="fp32c_r64", ei="kelbg", recip="spme"))
+        comps[prec] = dict(real=fr, ur=ur, recip=frec, um=um, total=ft, e=e)
+    r64, f64, f32 = comps["fp32c_r64"], comps["fp64"], comps["fp32c"]
+    assert oracle.rms_rel(r64["recip"], f64["recip"]) < 1e-13
+    assert r64["um"] == pytest.approx(f64["um"], rel=1e-13)
+    assert oracle.rms_rel(r64["real"], f32["real"]) < 1e-6
+    assert r64["ur"] == pytest.approx(f32["ur"], rel=1e-6)
+    fo, uro, umo = oracle.Oracle.from_system(s, ei="kelbg").force_total(s.x, recip="spme")
+    assert oracle.rms_rel(r64["total"], fo) < FP32_FORCE_RMS
+    assert r64["e"]["Um"] == pytest.approx(umo, rel=1e-10)
+
+
+def snap_to_grid(x, box):
+    """Positions on the fixed-point grid of the FP32C kernels (2^32 points per
+    box length), so that both the GPU and the FP64 oracle see the same
+    separations up to FP64 rounding."""
+    box = np.broadcast_to(np.asarray(box, dtype=np.float64), (3,))
+    m = np.floor((x / box + 0.5) * 2.0 ** 32) % 2.0 ** 32
+    return (m / 2.0 ** 32 - 0.5) * box
+
+
 @pytest.mark.parametrize("rdf_variant", [0, 1])
 def test_fp32c_newton3_rdf_histograms(monkeypatch, rdf_variant):
     """RDF counts of the packed Newton-3 forms (+2 per unique pair inside rc,
-    force.f90:99-103) against the FP64 oracle's: an FP32 separation (relative
-    error ~1e-7) moves a pair within that distance of a bin edge to the
-    neighbouring bin (about 3e-5 of the pairs here, 500 bins), so the totals
-    per pair type agree to a few pairs (those at rc) and the bins to 1e-4 of the
-    counts; forces and energy as without the histograms."""
+    force.f90:99-103) equal the FP64 oracle's bin for bin: pairs whose FP32
+    r/dx or r^2 lies near a bin edge or rc are binned from the exact integer
+    r^2 of their fixed-point separation.  Positions on the fixed-point grid,
+    so both sides bin the same separations; forces and energy as without the
+    histograms."""
     monkeypatch.setenv("TCP_PAIR_VARIANT", "11")
     monkeypatch.setenv("TCP_RDF_VARIANT", str(rdf_variant))
     s = make(4096, seed=13, K=16)
+    s.x = snap_to_grid(s.x, s.box)
     o = oracle.Oracle.from_system(s, ei="kelbg")
     fo, uo, h = o.force_direct(s.x, rdf=True)
     with ctx_for(s, precision="fp32c", ei="kelbg", recip="none") as c:
@@ -532,8 +575,38 @@ def test_fp32c_newton3_rdf_histograms(monkeypatch, rdf_variant):
         ur = c.Force_direct_self()
         _, _, f, _ = c.download(x=False, v=False, f=True)
         rdf, _ = c.histograms(reset=True)
-    for t in range(3):
-        assert abs(int(rdf[t].sum()) - int(h[t].sum())) <= 8
-    assert np.abs(rdf.astype(np.int64) - h.astype(np.int64)).sum() <= 1e-4 * h.sum()
+    assert np.array_equal(rdf, h)
     assert oracle.rms_rel(f, fo) < FP32_FORCE_RMS
     assert ur == pytest.approx(uo, rel=2e-5)
+
+
+@pytest.mark.parametrize("precision", ["fp32c", "fp64"])
+@pytest.mark.parametrize("box_kind", ["cubic", "noncubic"])
+def test_ordered_rdf_histograms(precision, box_kind):
+    """The ordered-pair kernels (TCP_FLAG_DETERMINISTIC; in FP32C the only
+    kernel of non-cubic boxes) count +1 from each side of a pair, FP32C with
+    the same exact binning as the Newton-3 forms: equal to the oracle's RDF.
+    700 + 333 particles leave partial i-blocks, whose padding lanes must count
+    nothing."""
+    nel, nion = 700, 333
+    s = make(nel + nion, seed=17, K=16)
+    s.nel, s.nion = nel, nion
+    box = (s.box, s.box, s.box) if box_kind == "cubic" else (s.box, 1.1 * s.box, 0.9 * s.box)
+    rng = np.random.default_rng(3)
+    x = snap_to_grid((rng.random((s.n, 3)) - 0.5) * np.array(box), box)
+    rc = 0.45 * min(box)
+    o = oracle.Oracle(nel, nion, box, rc, alpha=3.1 / rc, lambda_ei=s.lambda_ei, rs=s.lambda_ei, ei="deutsch",
+                      K=16, order=4, rdf_dx=rc / T.NDIST)
+    _, _, h = o.force_direct(x, rdf=True)
+    p = T.params_for(s, precision=precision, ei="deutsch", recip="none", rdf_dx=rc / T.NDIST)
+    for d in range(3):
+        p.box[d] = box[d]
+    p.rc = rc
+    p.a = 3.1 / rc
+    with T.Context(p, nel, nion) as c:
+        c.set_flags(T.FLAG_ENERGY | T.FLAG_RDF | T.FLAG_DETERMINISTIC)
+        c.EWALD_SELF()
+        c.upload(x=x)
+        c.Force_direct_self()
+        rdf, _ = c.histograms(reset=True)
+    assert np.array_equal(rdf, h)
