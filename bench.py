@@ -66,9 +66,11 @@ EPS = 14.399644154020082      # eV*A, data.f90:21
 # (degree 6) and products (9), force numerator (1), 1/r mask select and r^-2
 # weight (3), force accumulation (3), energy add (1) = 30 per ordered pair; the
 # Newton-3 kernel adds the reaction accumulation (3) = 33 per unique pair.
-# SFU: rsqrt, rcp, ex2 (3) per pair in both.
+# The Newton-3 variants named "_p5" evaluate a degree-5 erfc polynomial (one
+# FFMA fewer): 32 per unique pair.  SFU: rsqrt, rcp, ex2 (3) per pair in all.
 RECIPE_ORDERED = 30
 RECIPE_N3 = 33
+RECIPE_N3_P5 = 32
 RECIPE_SFU_OPS = 3
 SFU_RATE = 16.0 / 128.0       # SFU lanes per SM relative to FP32 lanes
 
@@ -431,6 +433,8 @@ def run_gpu(args, world, rank, local, dist):
     ctx.upload(x=s.x, v=s.v)
     e0 = ctx.force()                        # initial forces (restart-style start, main.f90:49-54)
     tune = ctx.autotune_report()
+    ctx_name = ctx.variant_name(tune[0])
+    ctx_names = [ctx.variant_name(k) for k in range(len(tune[1]))]
     reserve, reserve_ms = ctx.overlap_report()
     comp32 = gpu_components(ctx)
     ctx.upload(x=s.x, v=s.v)
@@ -529,7 +533,8 @@ def run_gpu(args, world, rank, local, dist):
     peak = T.fp32_peak(local) * 1e12            # FFMA/s = lane instructions/s
     variant, variant_ms = tune
     if variant >= 1:
-        units, recipe, kname = float(n) * (n - 1) / 2, RECIPE_N3, f"pair_n3_kernel (Newton-3 variant {variant})"
+        recipe = RECIPE_N3_P5 if ctx_name.endswith("_p5") else RECIPE_N3
+        units, kname = float(n) * (n - 1) / 2, f"pair_n3_kernel (Newton-3 variant {variant}: {ctx_name})"
         runit = "unique pair"
     else:
         units, recipe, kname = float(n) * (n - 1), RECIPE_ORDERED, "pair_fp32c_kernel (ordered pairs)"
@@ -539,7 +544,8 @@ def run_gpu(args, world, rank, local, dist):
     traffic = profile_traffic()
     roof = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "Top/s",
             "frac": achieved / peak, "traffic": traffic,
-            "kernel": kname, "autotune_ms": {str(k): round(x, 4) for k, x in enumerate(variant_ms.tolist()) if x > 0},
+            "kernel": kname,
+            "autotune_ms": {f"{k} {ctx_names[k]}": round(x, 4) for k, x in enumerate(variant_ms.tolist()) if x > 0},
             "recipe": f"{recipe} FP32/ALU-pipe ops + {RECIPE_SFU_OPS} SFU ops per {runit}",
             "peak_source": "measured FFMA issue rate (tcp_fp32_peak) on this GPU, not MEASURED_PEAKS.json "
                            "(which has HBM and bf16 only)",
@@ -561,18 +567,19 @@ def run_gpu(args, world, rank, local, dist):
     c2 = batch = None
     if rank == 0 and world == 1:
         threads = os.cpu_count() or 1
-        cs = cpu_steps(s, args.cpu_steps, threads)
-        ref = cs["comp"]
-        cpu = {"value": cs["value"], "unit": "pair-int/s", "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_steps} full MD steps of the FP64 restatement (direct sum over all "
-                         f"N(N-1)/2 pairs with OpenMP, SPME 128^3 p5, integrator), {cs['t_steps']:.1f} s timed",
-               "ms_per_step": cs["t_step"] * 1e3}
-        ferr["fp32c_vs_oracle"] = force_errors(comp32, ref)
-        ferr["fp64_gpu_vs_oracle"] = force_errors(comp64, ref)
-        ferr["fp32c_r64_vs_oracle"] = force_errors(comp_r64, ref)
-        eerr["fp32c_vs_oracle"] = energy_errors(comp32, ref, ek)
-        eerr["fp64_gpu_vs_oracle"] = energy_errors(comp64, ref, ek)
-        eerr["fp32c_r64_vs_oracle"] = energy_errors(comp_r64, ref, ek)
+        if args.cpu_steps > 0:          # --cpu-steps 0: no CPU leg (profiling runs)
+            cs = cpu_steps(s, args.cpu_steps, threads)
+            ref = cs["comp"]
+            cpu = {"value": cs["value"], "unit": "pair-int/s", "cores": threads, "kind": "port",
+                   "sample": f"{args.cpu_steps} full MD steps of the FP64 restatement (direct sum over all "
+                             f"N(N-1)/2 pairs with OpenMP, SPME 128^3 p5, integrator), {cs['t_steps']:.1f} s timed",
+                   "ms_per_step": cs["t_step"] * 1e3}
+            ferr["fp32c_vs_oracle"] = force_errors(comp32, ref)
+            ferr["fp64_gpu_vs_oracle"] = force_errors(comp64, ref)
+            ferr["fp32c_r64_vs_oracle"] = force_errors(comp_r64, ref)
+            eerr["fp32c_vs_oracle"] = energy_errors(comp32, ref, ek)
+            eerr["fp64_gpu_vs_oracle"] = energy_errors(comp64, ref, ek)
+            eerr["fp32c_r64_vs_oracle"] = energy_errors(comp_r64, ref, ek)
         if args.c2_steps > 0:
             c2 = run_c2(T, args, local, threads)
         if args.batch_reps > 0:

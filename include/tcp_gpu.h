@@ -324,6 +324,11 @@ int tcp_time_steps(tcp_ctx *ctx, double dt, int nsteps, int flush_l2, double *ou
  * ordered pairs, >= 1 = Newton-3 variants) and the per-candidate times in ms
  * (ms[k] for variant k, 0 when not timed), up to nmax entries. */
 int tcp_autotune_report(tcp_ctx *ctx, int *variant, double *ms, int nmax);
+/* Name of FP32C real-space variant `variant` ("ordered" for 0, NULL past the
+ * last): i-particles per lane, unroll, warps and CTAs per SM, packed forms
+ * ("x2", "x2l": shared-memory j positions) and "_p5" for the degree-5 Ewald
+ * erfc polynomial (one FMA fewer per pair than degree 6). */
+const char *tcp_pair_variant_name(int variant);
 /* The number of CTAs the autotuner left out of the persistent Newton-3 grid
  * so that the reciprocal chain, which runs beside the pair kernel in a step,
  * finds room on the SMs; the candidates and the time of the pair kernel with

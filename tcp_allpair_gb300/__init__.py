@@ -234,6 +234,11 @@ class Context:
                   "tcp_autotune_report")
         return v.value, ms
 
+    def variant_name(self, variant):
+        """Name of FP32C real-space variant `variant` (tcp_pair_variant_name)."""
+        n = self.lib.tcp_pair_variant_name(int(variant))
+        return n.decode() if n else None
+
     def overlap_report(self):
         """(CTAs left out of the Newton-3 grid, {candidate: ms of the pair kernel with the
         reciprocal chain beside it})."""

@@ -181,28 +181,19 @@ static constexpr Erfc5Q2Table make_erfc5_q2() {
 }
 __constant__ Erfc5Q2Table kErfc5Q2 = make_erfc5_q2();
 
-// Forms of the Ewald erfc polynomial of the packed kernels: degree 6 in
-// Horner form (any argument up to 4.5), degree 5 (kErfc5P, arguments up to
-// kErfc5Xmax) in Horner form, or the same degree 5 as
-// ((c5 t + c4) t^2 + (c3 t + c2)) t^2 + (c1 t + c0): one operation more and a
-// dependency chain of 3 instead of 5.
-constexpr int kErfcH6 = 6, kErfcH5 = 5, kErfcE5 = 50;
+// Forms of the Ewald erfc polynomial of the packed kernels (Horner): degree 6
+// (any argument up to 4.5), or degree 5 with kErfc5P for arguments up to
+// kErfc5Xmax.  (An Estrin form of degree 5, a dependency chain of 3 instead
+// of 5 for one operation more, was slower.)
+constexpr int kErfcH6 = 6, kErfcH5 = 5;
 
 template <int PD = kErfcH6>
 __device__ __forceinline__ float2 erfc_poly2(float2 t) {
-    static_assert(PD == kErfcH6 || PD == kErfcH5 || PD == kErfcE5, "erfc polynomial forms");
-    if constexpr (PD == kErfcE5) {
-        const float2 t2 = __fmul2_rn(t, t);
-        const float2 a = __ffma2_rn(kErfc5Q2.q[4], t, kErfc5Q2.q[5]);   // c1 t + c0
-        const float2 b = __ffma2_rn(kErfc5Q2.q[2], t, kErfc5Q2.q[3]);   // c3 t + c2
-        const float2 c = __ffma2_rn(kErfc5Q2.q[0], t, kErfc5Q2.q[1]);   // c5 t + c4
-        return __fmul2_rn(__ffma2_rn(__ffma2_rn(c, t2, b), t2, a), t);
-    } else {
-        float2 q = PD == kErfcH6 ? kErfcQ2.q[0] : kErfc5Q2.q[0];
+    static_assert(PD == kErfcH6 || PD == kErfcH5, "erfc polynomial forms");
+    float2 q = PD == kErfcH6 ? kErfcQ2.q[0] : kErfc5Q2.q[0];
 #pragma unroll
-        for (int k = 1; k <= PD; ++k) q = __ffma2_rn(q, t, PD == kErfcH6 ? kErfcQ2.q[k] : kErfc5Q2.q[k]);
-        return __fmul2_rn(q, t);
-    }
+    for (int k = 1; k <= PD; ++k) q = __ffma2_rn(q, t, PD == kErfcH6 ? kErfcQ2.q[k] : kErfc5Q2.q[k]);
+    return __fmul2_rn(q, t);
 }
 
 // RDF: +2 per unique pair inside rc in bin INT(r/dx) <= kNdist of this pair
@@ -242,7 +233,7 @@ __device__ __forceinline__ void rdf_add(const N3Rdf &h, float r, float r2, bool 
     }
 }
 
-// PD: form of the Ewald erfc polynomial (kErfcH6, or kErfcH5 / kErfcE5 when
+// PD: degree of the Ewald erfc polynomial (kErfcH6, or kErfcH5 when
 // alpha rc <= kErfc5Xmax); the Kelbg erfc(r/lambda) always uses kErfcH6.
 // RDF: h, the index masks v0, v1 and the positions xa, xb (i-particles) and
 // xj of the two pairs.
@@ -400,9 +391,8 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
 // MODE 0: scalar FP32, i-force accumulators in registers; 1: packed FP32x2,
 // accumulators in shared memory; 2: as 1 with j positions read from shared
 // memory (LDSJ).
-// W: warps per CTA (i-tile = 32 R W particles).  PD: form of the Ewald erfc
-// polynomial of the packed forms (kErfcH5 / kErfcE5 only where
-// PairConsts::erfc5_ok).
+// W: warps per CTA (i-tile = 32 R W particles).  PD: degree of the Ewald erfc
+// polynomial of the packed forms (kErfcH5 only where PairConsts::erfc5_ok).
 template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH, int MODE = 0, int W = kN3Warps, bool RDF = false,
           int PD = kErfcH6>
 __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
@@ -651,29 +641,29 @@ struct N3Variant {
     bool erfc5 = false;   // degree-5 Ewald erfc: only where PairConsts::erfc5_ok
 };
 static const N3Variant kVariants[] = {
-    {pair_n3_kernel<true, 2, 2, 3, false>, pair_n3_kernel<false, 2, 2, 3, false>, 2, 8, "n3_r2_u2_b3"},
-    {pair_n3_kernel<true, 2, 1, 3, false>, pair_n3_kernel<false, 2, 1, 3, false>, 2, 8, "n3_r2_u1_b3"},
-    {pair_n3_kernel<true, 4, 1, 2, false>, pair_n3_kernel<false, 4, 1, 2, false>, 4, 8, "n3_r4_u1_b2"},
+    // degree-6 Ewald erfc (any alpha rc)
     {pair_n3_kernel<true, 4, 2, 2, false>, pair_n3_kernel<false, 4, 2, 2, false>, 4, 8, "n3_r4_u2_b2"},
     {pair_n3_kernel<true, 4, 2, 2, false, 1>, pair_n3_kernel<false, 4, 2, 2, false, 1>, 4, 8, "n3_r4_u2_b2_x2"},
-    {pair_n3_kernel<true, 4, 1, 2, false, 1>, pair_n3_kernel<false, 4, 1, 2, false, 1>, 4, 8, "n3_r4_u1_b2_x2"},
-    {pair_n3_kernel<true, 2, 2, 3, false, 1>, pair_n3_kernel<false, 2, 2, 3, false, 1>, 2, 8, "n3_r2_u2_b3_x2"},
     {pair_n3_kernel<true, 4, 1, 5, false, 1, 4>, pair_n3_kernel<false, 4, 1, 5, false, 1, 4>, 4, 4, "n3_r4_u1_w4b5_x2"},
-    {pair_n3_kernel<true, 4, 1, 3, false, 1>, pair_n3_kernel<false, 4, 1, 3, false, 1>, 4, 8, "n3_r4_u1_b3_x2"},
-    {pair_n3_kernel<true, 4, 1, 2, false, 2>, pair_n3_kernel<false, 4, 1, 2, false, 2>, 4, 8, "n3_r4_u1_b2_x2l"},
     {pair_n3_kernel<true, 4, 1, 3, false, 2>, pair_n3_kernel<false, 4, 1, 3, false, 2>, 4, 8, "n3_r4_u1_b3_x2l"},
+    {pair_n3_kernel<true, 4, 2, 4, false, 1, 4>, pair_n3_kernel<false, 4, 2, 4, false, 1, 4>, 4, 4, "n3_r4_u2_w4b4_x2"},
+    // degree-5 Ewald erfc (alpha rc <= kErfc5Xmax)
     {pair_n3_kernel<true, 4, 1, 3, false, 2, 8, false, kErfcH5>,
      pair_n3_kernel<false, 4, 1, 3, false, 2, 8, false, kErfcH5>, 4, 8, "n3_r4_u1_b3_x2l_p5", true},
-    {pair_n3_kernel<true, 4, 1, 4, false, 2, 7>, pair_n3_kernel<false, 4, 1, 4, false, 2, 7>, 4, 7,
-     "n3_r4_u1_w7b4_x2l"},
-    {pair_n3_kernel<true, 4, 1, 4, false, 2, 7, false, kErfcH5>,
-     pair_n3_kernel<false, 4, 1, 4, false, 2, 7, false, kErfcH5>, 4, 7, "n3_r4_u1_w7b4_x2l_p5", true},
-    {pair_n3_kernel<true, 4, 1, 6, false, 2, 4, false, kErfcH5>,
-     pair_n3_kernel<false, 4, 1, 6, false, 2, 4, false, kErfcH5>, 4, 4, "n3_r4_u1_w4b6_x2l_p5", true},
-    {pair_n3_kernel<true, 4, 2, 3, false, 2, 8, false, kErfcH5>,
-     pair_n3_kernel<false, 4, 2, 3, false, 2, 8, false, kErfcH5>, 4, 8, "n3_r4_u2_b3_x2l_p5", true},
-    {pair_n3_kernel<true, 4, 1, 3, false, 2, 8, false, kErfcE5>,
-     pair_n3_kernel<false, 4, 1, 3, false, 2, 8, false, kErfcE5>, 4, 8, "n3_r4_u1_b3_x2l_e5", true},
+    {pair_n3_kernel<true, 4, 2, 2, false, 1, 8, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 2, 2, false, 1, 8, false, kErfcH5>, 4, 8, "n3_r4_u2_b2_x2_p5", true},
+    {pair_n3_kernel<true, 4, 2, 5, false, 1, 4, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 2, 5, false, 1, 4, false, kErfcH5>, 4, 4, "n3_r4_u2_w4b5_x2_p5", true},
+    {pair_n3_kernel<true, 4, 2, 5, false, 2, 4, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 2, 5, false, 2, 4, false, kErfcH5>, 4, 4, "n3_r4_u2_w4b5_x2l_p5", true},
+    {pair_n3_kernel<true, 4, 2, 4, false, 1, 4, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 2, 4, false, 1, 4, false, kErfcH5>, 4, 4, "n3_r4_u2_w4b4_x2_p5", true},
+    {pair_n3_kernel<true, 4, 4, 4, false, 1, 4, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 4, 4, false, 1, 4, false, kErfcH5>, 4, 4, "n3_r4_u4_w4b4_x2_p5", true},
+    {pair_n3_kernel<true, 6, 1, 4, false, 1, 4, false, kErfcH5>,
+     pair_n3_kernel<false, 6, 1, 4, false, 1, 4, false, kErfcH5>, 6, 4, "n3_r6_u1_w4b4_x2_p5", true},
+    {pair_n3_kernel<true, 6, 2, 3, false, 1, 4, false, kErfcH5>,
+     pair_n3_kernel<false, 6, 2, 3, false, 1, 4, false, kErfcH5>, 6, 4, "n3_r6_u2_w4b3_x2_p5", true},
 };
 constexpr int kN3Variants = sizeof(kVariants) / sizeof(kVariants[0]);
 

@@ -40,6 +40,27 @@ def test_fp32_fit_in_float32():
     assert np.sqrt(np.mean(rel ** 2)) < 2e-7
 
 
+def test_fp32_degree5_fit_on_the_ewald_range():
+    """The degree-5 Q (TCP_ERFC5_Q, kErfc5P) of the Newton-3 kernels' Ewald
+    term on [0, kErfc5Xmax], float32 Horner as the kernels evaluate it; the
+    host uses it only where alpha rc <= kErfc5Xmax."""
+    p = float(re.search(r"constexpr double kErfc5P = ([0-9.]+);", SRC).group(1))
+    xmax = float(re.search(r"constexpr double kErfc5Xmax = ([0-9.]+);", SRC).group(1))
+    deg = int(re.search(r"constexpr int kErfc5Deg = (\d+);", SRC).group(1))
+    c = _floats(re.search(r"#define TCP_ERFC5_Q\s*\\\s*\{(.*?)\}", SRC, re.S).group(1))
+    assert len(c) == deg + 1 and xmax >= 3.46          # covers alpha rc for a 1e-6 Ewald error
+    x = np.linspace(0.0, xmax, 100001).astype(np.float32)
+    t = (np.float32(1.0) / (np.float32(1.0) + np.float32(p) * x)).astype(np.float32)
+    q = np.full_like(t, np.float32(c[0]))
+    for ck in c[1:]:
+        q = (q.astype(np.float64) * t.astype(np.float64) + np.float64(np.float32(ck))).astype(np.float32)
+    approx = np.exp(-x.astype(np.float64) ** 2) * (t.astype(np.float64) * q.astype(np.float64))
+    ref = erfc(x.astype(np.float64))
+    rel = np.abs(approx - ref) / ref
+    assert rel.max() < 1e-6
+    assert np.sqrt(np.mean(rel ** 2)) < 4e-7
+
+
 @pytest.mark.parametrize("y", [1e-6, 0.01, 0.1, 0.25])
 def test_kelbg_close_series(y):
     """The Taylor forms of kelbg_close (pair_math.cuh) against direct FP64."""

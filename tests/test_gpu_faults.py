@@ -45,7 +45,7 @@ def test_injected_cufft_plan_failure(monkeypatch):
 
 def test_tile_wait_timeout_is_reported_and_context_recovers(monkeypatch):
     s = make(4096, seed=42)
-    monkeypatch.setenv("TCP_PAIR_VARIANT", "6")          # the Newton-3 kernel, no autotuning launches
+    monkeypatch.setenv("TCP_PAIR_VARIANT", "2")          # the Newton-3 kernel, no autotuning launches
     p = T.params_for(s, precision="fp32c", ei="kelbg", recip="none")
     fo, uo = oracle.Oracle.from_system(s, ei="kelbg").force_direct(s.x)
     with T.Context(p, s.nel, s.nion) as c:

@@ -90,9 +90,14 @@ def test_spme_vs_oracle(order, K):
     assert oracle.rms_rel(fr, fo) < 1e-10
 
 
-@pytest.mark.parametrize("order,K", [(4, 16), (5, 32), (6, 24)])
-def test_spme_fp32_mode_vs_oracle(order, K):
-    """FP32C mode: compensated-FP32 charge accumulation, FP32 transforms and gather."""
+@pytest.mark.parametrize("order,K,tol", [(4, 16, 6e-6), (5, 32, 1e-6), (6, 24, 1e-6)])
+def test_spme_fp32_mode_vs_oracle(order, K, tol):
+    """FP32C mode: compensated-FP32 charge accumulation, FP32 transforms and
+    gather.  The reciprocal forces come from spline-derivative sums over a
+    smooth potential, which amplify the FP32 rounding of the transforms: the
+    measured RMS errors of these three cases on GB300 were 2.9e-6, 4.6e-7 and
+    3.2e-7; the bounds are about twice that (TCP_PREC_FP32C_R64 runs the
+    chain in FP64)."""
     s = make(2000, seed=4, K=K, order=order)
     o = oracle.Oracle.from_system(s, ei="kelbg")
     fo, umo = o.force_spme(s.x)
@@ -100,7 +105,7 @@ def test_spme_fp32_mode_vs_oracle(order, K):
         um = c.Force_SPME4()
         _, _, _, fr = c.download(x=False, v=False, f=False, frec=True)
     assert um == pytest.approx(umo, rel=1e-6)
-    assert oracle.rms_rel(fr, fo) < 1e-5
+    assert oracle.rms_rel(fr, fo) < tol
 
 
 def test_ewald_ksum_vs_oracle():
@@ -340,13 +345,13 @@ def test_large_fp32c_rows_sample():
     assert np.linalg.norm(f.sum(0)) < 1e-6 * np.abs(f).sum()
 
 
-@pytest.mark.parametrize("variant", list(range(18)))
+@pytest.mark.parametrize("variant", list(range(14)))
 @pytest.mark.parametrize("ei,n", [("kelbg", 2048), ("deutsch", 1536), ("kelbg", 1000)])
 def test_fp32c_kernel_variants(monkeypatch, variant, ei, n):
     """Every real-space kernel the autotuner can pick (0 = ordered pairs,
-    1..4 = Newton-3 variants, 5..17 = Newton-3 with packed FP32x2 arithmetic,
-    12 and 14..17 with the degree-5 Ewald erfc) against the oracle, including
-    partial tiles."""
+    1 = scalar Newton-3, 2..13 = Newton-3 with packed FP32x2 arithmetic,
+    6..13 with the degree-5 Ewald erfc, 12 and 13 with six i-particles per
+    lane) against the oracle, including partial tiles."""
     monkeypatch.setenv("TCP_PAIR_VARIANT", str(variant))
     s = make(n, seed=30 + variant)
     o = oracle.Oracle.from_system(s, ei=ei)
@@ -365,7 +370,7 @@ def test_autotuner_picks_a_timed_variant(monkeypatch):
     with ctx_for(s, precision="fp32c", ei="kelbg", recip="none") as c:
         c.Force_direct_self()
         v, ms = c.autotune_report()
-    assert 0 <= v <= 17
+    assert 0 <= v <= 13
     assert ms[v] > 0 and ms[v] == min(m for m in ms if m > 0)
 
 
@@ -469,7 +474,7 @@ def test_deterministic_flag_is_bitwise_reproducible(precision):
     assert e1["Ur"] == e2["Ur"] and e1["Um"] == e2["Um"]
 
 
-@pytest.mark.parametrize("variant", [0, 1, 6])
+@pytest.mark.parametrize("variant", [0, 1, 2, 10])
 @pytest.mark.parametrize("r_over_lam", [1e-3, 1e-2, 0.1, 0.3, 0.49, 0.8, 2.0])
 def test_kelbg_close_pair_accuracy(monkeypatch, variant, r_over_lam):
     """One electron and one ion at r = (1e-3 .. 2) lambda: the Kelbg e-i force
@@ -497,7 +502,7 @@ def test_kelbg_close_pair_accuracy(monkeypatch, variant, r_over_lam):
     assert ur == pytest.approx(uo, rel=2e-5, abs=1e-6 * abs(uo) + 1e-12)
 
 
-@pytest.mark.parametrize("variant", [6, 9, 11, 12, 13, 15])
+@pytest.mark.parametrize("variant", [2, 4, 5, 10, 12, 13])
 @pytest.mark.parametrize("nel,nion", [(1, 300), (257, 0), (700, 333), (1030, 2)])
 def test_fp32c_newton3_ragged_species(monkeypatch, variant, nel, nion):
     """Packed Newton-3 variants with a single electron, one species only, and
@@ -547,6 +552,32 @@ def test_fp32c_with_fp64_reciprocal_chain():
     assert r64["e"]["Um"] == pytest.approx(umo, rel=1e-10)
 
 
+def test_charged_system_background_energy():
+    """A system with net charge (40 electrons, 24 ions): Uo carries the
+    neutralising-background energy -pi Q^2/(2 V alpha^2) exactly as the
+    oracle's, and the FP64 Ewald total (Ur + Uo) eps + Um of the plain k-sum
+    does not depend on alpha."""
+    rng = np.random.default_rng(4)
+    nel, nion, L = 40, 24, 20.0
+    x = (rng.random((nel + nion, 3)) - 0.5) * L
+    s = T.make_system(nel + nion, seed=1)
+    totals = []
+    for arc in (4.5, 5.0):
+        p = T.params_for(s, precision="fp64", ei="coulomb", recip="ewald", nmax2=400)
+        for d in range(3):
+            p.box[d] = L
+        p.rc = L / 2
+        p.a = arc / p.rc
+        o = oracle.Oracle(nel, nion, L, p.rc, alpha=p.a, ei="coulomb", K=0)
+        with T.Context(p, nel, nion) as c:
+            _, uo = c.EWALD_SELF()
+            c.upload(x=x)
+            e = c.force()
+        assert uo == pytest.approx(o.Uo, rel=1e-14)
+        totals.append(e["Epot"] + e["Um"])
+    assert totals[0] == pytest.approx(totals[1], rel=1e-9)
+
+
 def snap_to_grid(x, box):
     """Positions on the fixed-point grid of the FP32C kernels (2^32 points per
     box length), so that both the GPU and the FP64 oracle see the same
@@ -564,7 +595,7 @@ def test_fp32c_newton3_rdf_histograms(monkeypatch, rdf_variant):
     r^2 of their fixed-point separation.  Positions on the fixed-point grid,
     so both sides bin the same separations; forces and energy as without the
     histograms."""
-    monkeypatch.setenv("TCP_PAIR_VARIANT", "11")
+    monkeypatch.setenv("TCP_PAIR_VARIANT", "10")
     monkeypatch.setenv("TCP_RDF_VARIANT", str(rdf_variant))
     s = make(4096, seed=13, K=16)
     s.x = snap_to_grid(s.x, s.box)

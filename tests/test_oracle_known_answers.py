@@ -71,6 +71,35 @@ def _random_system(n, seed, gamma=1.0, lam=0.5):
     return make_system(n, gamma=gamma, lam=lam, seed=seed, alpha_rc=3.1)
 
 
+def test_background_term_makes_a_charged_ewald_sum_alpha_independent(orc):
+    """A system with net charge Q: the Ewald total (Ur + Uo) eps + Um does
+    not depend on the splitting alpha once Uo carries the neutralising-
+    background energy -pi Q^2 / (2 V alpha^2); without it the totals differ
+    by pi Q^2 / (2 V) (1/alpha_1^2 - 1/alpha_2^2) eps.  Plain Ewald k-sum and
+    real-space sum converged to 1e-9 for both alphas (alpha rc = 4.5, 5)."""
+    rng = np.random.default_rng(4)
+    nel, nion, L = 40, 24, 20.0
+    x = (rng.random((nel + nion, 3)) - 0.5) * L
+    rc = L / 2
+    Q = -(nel - nion)
+    tot, bg = [], []
+    for arc in (4.5, 5.0):
+        alpha = arc / rc
+        o = orc.Oracle(nel, nion, L, rc, alpha=alpha, ei="coulomb", K=0)
+        _, ur, uk = o.force_total(x, recip="ewald", nmax2=400)
+        tot.append((ur + o.Uo) * EPS + uk)
+        bg.append(-math.pi * Q * Q / (2 * L ** 3 * alpha ** 2))
+    assert tot[0] == pytest.approx(tot[1], rel=1e-9)
+    without = [t - b * EPS for t, b in zip(tot, bg)]
+    assert abs(without[0] - without[1]) > 1e3 * abs(tot[0] - tot[1])
+    assert abs(without[0] - without[1]) == pytest.approx(abs(bg[0] - bg[1]) * EPS, rel=1e-6)
+
+
+def test_background_term_vanishes_for_neutral_systems(orc):
+    o = orc.Oracle(50, 50, 20.0, 10.0, alpha=0.31, ei="coulomb", K=0)
+    assert o.Uo == pytest.approx(-100 * 0.31 / math.sqrt(math.pi), rel=1e-15)
+
+
 def test_newton3_sum_of_forces(orc):
     s = _random_system(256, 3)
     for ei in ("deutsch", "kelbg"):
