@@ -73,6 +73,7 @@ RECIPE_N3 = 33
 RECIPE_N3_P5 = 32
 RECIPE_SFU_OPS = 3
 SFU_RATE = 16.0 / 128.0       # SFU lanes per SM relative to FP32 lanes
+REF_MAX_STEPS = 5             # full CPU steps timed by --impl reference
 
 
 def log(*a):
@@ -173,7 +174,7 @@ def reduce_sum(dist, x: float) -> float:
 
 def profile_traffic():
     """DRAM bytes per launch of the pair kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "pair_n3_x2_kelbg_n32768.md"
+    p = ROOT / "profiles" / "pair_n3_kelbg_n65536.md"
     if not p.exists():
         return None
     m = re.search(r"dram_bytes_per_launch_full_size:\s*([0-9.eE+]+)", p.read_text())
@@ -263,17 +264,21 @@ def run_reference(args, world, rank, dist):
     oracle.build()
     s = make_config_system(WORKLOAD, seed=0)
     threads = os.cpu_count() or 1
+    # a full step takes seconds on the host cores: at most REF_MAX_STEPS timed steps after one
+    # untimed one, so that the arm ends within a minute whatever --steps asks for
+    steps, warmup = max(1, min(args.steps, REF_MAX_STEPS)), min(args.warmup, 1)
     t0 = time.perf_counter()
-    cs = cpu_steps(s, args.steps, threads, warmup=args.warmup)
+    cs = cpu_steps(s, steps, threads, warmup=warmup)
     wall = time.perf_counter() - t0
     t_step = cs["t_step"]
     n = s.n
     value = n * (n - 1) / 2 / t_step
-    sample = (f"{args.steps} full MD steps after {args.warmup} untimed ones: direct sum over all N(N-1)/2 pairs "
-              f"(FP64, OpenMP), SPME 128^3 p5, integrator")
+    sample = (f"{steps} full MD steps after {warmup} untimed one(s) ({args.steps} asked): direct sum over all "
+              f"N(N-1)/2 pairs (FP64, OpenMP), SPME 128^3 p5, integrator")
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "pair-int/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "steps_per_s": 1.0 / t_step,
+        "steps": steps, "warmup": warmup, "steps_requested": args.steps, "warmup_requested": args.warmup,
+        "ms_per_step": t_step * 1e3, "steps_per_s": 1.0 / t_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded uniform positions (0.1a rejection), Maxwell-Boltzmann velocities",
         "config": config_dict(s),
@@ -351,6 +356,7 @@ def run_c2(T, args, device, threads):
             c.upload(x=s.x, v=s.v)
             comp = gpu_components(c)
             t = c.time_steps(s.dt, 20, flush_l2=True)        # device time of one step
+            kernel = c.variant_name(c.autotune_report()[0]) if prec == "fp32c" else "pair_n3_f64_kernel"
             # the run itself from the seeded start, Etot sampled every tenth of it
             c.upload(x=s.x, v=s.v)
             c.force()
@@ -363,6 +369,9 @@ def run_c2(T, args, device, threads):
             wall = time.perf_counter() - t0
         ms = t["step"] / t["nsteps"]
         out[prec] = {"ms_per_step": ms, "value": pairs / (ms * 1e-3), "run_wall_s": wall,
+                     "breakdown_ms_per_step": {k: t[k] / t["nsteps"] for k in ("vverlet1", "pair", "recip",
+                                                                              "epilogue")},
+                     "pair_kernel": kernel,
                      "force_error_vs_oracle": force_errors(comp, ref),
                      "energy_error_vs_oracle": energy_errors(comp, ref, ek)}
         traj[prec] = np.array(et)

@@ -125,6 +125,7 @@ static int recip_fork(tcp_ctx *c) {
 static int recip_join(tcp_ctx *c) {
     c->recip_beside = false;
     if (c->p.reciprocal == TCP_RECIP_NONE) return TCP_OK;
+    if (int rc = launch_pair_n3_rejoin(c, c->stream2)) return rc;
     TCP_CUDA(cudaEventRecord(c->ev_join, c->stream2));
     TCP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     return TCP_OK;
@@ -200,7 +201,9 @@ static int mark(tcp_ctx *c, int k) { return mark_on(c, k, c->stream); }
 
 // Phase marks ev[0..4] (event nodes in the graph): 0 step start, 1 after
 // the first half kick, 2 end of the reciprocal chain (on stream2, concurrent
-// with the pair kernel), 3 end of the pair kernel, 4 step end.
+// with the pair kernel), 3 end of the real-space sum (the pair launch, the
+// reserved CTAs that rejoin it after the chain, and the chain itself), 4 step
+// end.
 static int step_chain(tcp_ctx *c, double dt, bool apply, int *pass) {
     int rc;
     if ((rc = mark(c, 0))) return rc;
@@ -213,8 +216,8 @@ static int step_chain(tcp_ctx *c, double dt, bool apply, int *pass) {
         return rc;
     }
     if ((rc = launch_pair(c, energy_on(c), (c->flags & TCP_FLAG_RDF) != 0))) return rc;
-    if ((rc = mark(c, 3))) return rc;
     if ((rc = recip_join(c))) return rc;
+    if ((rc = mark(c, 3))) return rc;
     if ((rc = launch_force_finalize(c, c->p.reciprocal != TCP_RECIP_NONE))) return rc;
     if ((rc = launch_kick2(c, dt, true, apply, (c->flags & TCP_FLAG_VDF) != 0, pass))) return rc;
     if ((rc = launch_reduce(c, (energy_on(c) ? kRedUr : 0) | kRedMv2, *pass))) return rc;
@@ -308,7 +311,8 @@ int tcp_create(const tcp_params *p_in, int nel, int nion, int device, tcp_ctx **
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(cuda_check(cudaGetLastError(), "cudaStreamCreate"));
     if (cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_pair_ready, cudaEventDisableTiming) != cudaSuccess)
         return fail(cuda_check(cudaGetLastError(), "cudaStreamCreate (reciprocal stream)"));
     c->rstream = c->stream;
     for (auto &e : c->ev)
@@ -386,6 +390,8 @@ int tcp_destroy(tcp_ctx *c) {
     cudaFree(c->l2_flush);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->ev_pair_ready) cudaEventDestroy(c->ev_pair_ready);
+    n3_free(c);
     if (c->stream2) {
         cudaStreamSynchronize(c->stream2);
         cudaStreamDestroy(c->stream2);
@@ -877,8 +883,9 @@ int tcp_time_steps(tcp_ctx *c, double dt, int nsteps, int flush_l2, double *out)
         if (flush_l2) TCP_CUDA(cudaMemsetAsync(c->l2_flush, s & 0xff, c->l2_flush_bytes, c->stream));
         if ((rc = launch_step(c, dt))) return rc;
         TCP_CUDA(cudaEventSynchronize(c->ev[4]));
-        // step; first kick (0-1); reciprocal (1-2, stream2); pair (1-3, concurrent
-        // with the reciprocal chain); epilogue (from the later of 2 and 3 to 4)
+        // step; first kick (0-1); reciprocal (1-2, stream2); pair (1-3: the pair
+        // launch with the reciprocal chain beside it, up to the join of both
+        // streams); epilogue (from the later of 2 and 3 to 4)
         float t[5], e2, e3;
         cudaEventElapsedTime(&t[0], c->ev[0], c->ev[4]);
         cudaEventElapsedTime(&t[1], c->ev[0], c->ev[1]);

@@ -1019,9 +1019,13 @@ static int choose_variant(tcp_ctx *c, const char *cache, const std::string &key)
 // CTAs left out of the persistent Newton-3 grid.  In a step the reciprocal
 // chain runs on a second stream beside the pair kernel; with every SM holding
 // its full share of pair CTAs, the chain's kernels (cuFFT's among them) find no
-// registers free and wait for the pair kernel's tail.  Each candidate is timed
-// as the pair kernel with the chain beside it (TCP_PAIR_RESERVE forces one).
-static constexpr int kReserveCandidates[] = {0, 8, 16, 32, 64};
+// registers free and wait for the pair kernel's tail.  The reserved CTAs
+// rejoin the pair launch once the chain is done (launch_pair_n3_rejoin), so a
+// large reserve costs the pair kernel only while the chain runs: where the
+// chain is long against the pair kernel (small N, or the FP64 chain) it lets
+// the chain finish first.  Each candidate is timed as the pair kernel with the
+// chain beside it, up to the join of both (TCP_PAIR_RESERVE forces one).
+static constexpr int kReserveCandidates[] = {0, 16, 32, 64, 128, 256, 512};
 static int choose_reserve(tcp_ctx *c, const char *cache, const std::string &key) {
     c->pair_reserve = 0;
     if (const char *forced = getenv("TCP_PAIR_RESERVE")) {

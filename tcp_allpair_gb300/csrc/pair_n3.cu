@@ -7,14 +7,15 @@
 // particles (W warps, R i-particles per lane) and j-subtiles of kN3Sub = 128
 // (tiles never straddle the e/i boundary).  An item is (i-tile I, j-subtile
 // S) with S at or after I's first subtile; items are enumerated row by row.
-// A persistent grid takes the first ~90 % of the list in equal contiguous
-// shares (the i-tile stays in registers along a row) and the rest one item
-// at a time from an atomic counter, which absorbs the cost differences
+// A persistent grid claims chunks of consecutive items from an atomic
+// counter, the chunks shorter towards the end of the list (guided
+// self-scheduling): the i-tile stays in registers along the long early
+// chunks, and the single items at the end absorb the cost differences
 // between items (pair types, masked items).
 //
 // A lane holds R i-particles (R i-chunks of 32 per warp).  A j-subtile is
 // copied into shared memory by the bulk-copy engine (cp.async.bulk +
-// mbarrier, kN3Stages-deep ring, prefetched along the static share).  Each
+// mbarrier, kN3Stages-deep ring, issued three items ahead).  Each
 // warp takes the subtile in chunks of 32: lane l loads j = l, and for 32
 // steps computes the R pairs (i_r, j) and rotates j's position and reaction
 // accumulator to the next lane with shuffles, so after 32 steps every lane
@@ -785,22 +786,57 @@ int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf) {
     a.inject_skip = inject_fault("tile_wait") ? 1 : 0;
     a.rdf = c->rdf;
     a.rdf_edges = c->rdf_edges;
-    // CTAs left free for the reciprocal chain when it runs beside this launch
+    // CTAs left free for the reciprocal chain when it runs beside this launch;
+    // they rejoin it after the chain (launch_pair_n3_rejoin)
+    c->n3_rejoin_pending = false;
     const int reserve = c->recip_beside ? c->pair_reserve : 0;
     const int full = rdf ? kernel_grid(c, K.energy, nt) : n3_grid_for(c, v);
     const int grid = (int)std::min<long long>(std::max(1, full - reserve), total);
-    if (grid > c->n_upart) return set_error(TCP_ERR_STATE, "energy partial buffer smaller than the Newton-3 grid");
+    const int rejoin = (int)std::min<long long>(full - grid, total - grid);
+    if (grid + std::max(rejoin, 0) > c->n_upart)
+        return set_error(TCP_ERR_STATE, "energy partial buffer smaller than the Newton-3 grid");
     TCP_CUDA(cudaMemsetAsync(c->fpart, 0, sizeof(double) * 3 * (size_t)c->n, c->stream));
     TCP_CUDA(cudaMemsetAsync(c->counter, 0, sizeof(unsigned), c->stream));
-    if (energy) {
-        TCP_CUDA(cudaMemsetAsync(c->upart, 0, sizeof(double) * (size_t)c->n_upart, c->stream));
-        K.energy<<<grid, nt, 0, c->stream>>>(a);
-    } else {
-        K.plain<<<grid, nt, 0, c->stream>>>(a);
+    if (energy) TCP_CUDA(cudaMemsetAsync(c->upart, 0, sizeof(double) * (size_t)c->n_upart, c->stream));
+    if (rejoin > 0) {
+        TCP_CUDA(cudaEventRecord(c->ev_pair_ready, c->stream));
+        if (!c->n3_rejoin) c->n3_rejoin = new N3Args;
+        *c->n3_rejoin = a;
+        c->n3_rejoin->upart = c->upart + grid;   // its CTAs' energy partials follow the first launch's
+        c->n3_rejoin->inject_skip = 0;
+        c->n3_rejoin_grid = rejoin;
+        c->n3_rejoin_threads = nt;
+        c->n3_rejoin_fn = reinterpret_cast<const void *>(energy ? K.energy : K.plain);
     }
+    if (energy)
+        K.energy<<<grid, nt, 0, c->stream>>>(a);
+    else
+        K.plain<<<grid, nt, 0, c->stream>>>(a);
     c->launches++;
     TCP_CUDA(cudaGetLastError());
+    c->n3_rejoin_pending = rejoin > 0;
     return TCP_OK;
+}
+
+// The CTAs a Newton-3 launch left to the reciprocal chain, launched on the
+// chain's stream after it: the same kernel and arguments, claiming whatever
+// chunks remain from the shared counter (none if the first launch has taken
+// them all, and its CTAs then leave at once).  It waits for the clearing of
+// the counter and accumulators that preceded the first launch.
+int launch_pair_n3_rejoin(tcp_ctx *c, cudaStream_t st) {
+    if (!c->n3_rejoin_pending) return TCP_OK;
+    c->n3_rejoin_pending = false;
+    TCP_CUDA(cudaStreamWaitEvent(st, c->ev_pair_ready, 0));
+    void *args[] = {c->n3_rejoin};
+    TCP_CUDA(cudaLaunchKernel(c->n3_rejoin_fn, dim3(c->n3_rejoin_grid), dim3(c->n3_rejoin_threads), args, 0, st));
+    c->launches++;
+    return TCP_OK;
+}
+
+void n3_free(tcp_ctx *c) {
+    delete c->n3_rejoin;
+    c->n3_rejoin = nullptr;
+    c->n3_rejoin_pending = false;
 }
 
 // ---- batch of replicas -------------------------------------------------------

@@ -16,7 +16,6 @@ constexpr int kN3Warps = 8;
 constexpr int kN3Threads = 32 * kN3Warps;
 constexpr int kN3Sub = 128;                // j-subtile
 constexpr int kN3Stages = 3;
-constexpr int kN3DynPercent = 10;          // share of the items handed out dynamically
 
 // Tile geometry of one system (a replica of a batch, or the only system).
 struct N3Geom {
@@ -37,7 +36,7 @@ struct N3Args {
     const double4_32a *xd;         // FP64 positions
     const longlong4_32a *xl;       // 64-bit fixed-point positions (FP64 kernel)
     long long total;      // items (all systems)
-    long long nstatic;    // items [0, nstatic) split statically
+    long long nstatic;    // FP64: items [0, nstatic) split statically (0: all from the counter)
     int ntot;             // stride of facc
     double *facc;         // [3][ntot], zeroed before the launch
     double *upart;        // [gridDim.x] (single system)

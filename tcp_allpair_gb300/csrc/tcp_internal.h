@@ -104,6 +104,7 @@ inline double ewald_constant_energy(const tcp_params &p, int nel, int nion, doub
 
 // ---------------------------------------------------------------------------
 struct Ctx;
+struct N3Args;
 
 }  // namespace tcp
 
@@ -117,6 +118,7 @@ struct tcp_ctx {
     // reciprocal sum concurrently with the real-space kernel (fork/join events)
     cudaStream_t rstream = nullptr, stream2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_pair_ready = nullptr;   // the Newton-3 launch's counter and accumulators are cleared
     unsigned flags = TCP_FLAG_ENERGY;
     bool ewald_ready = false;
     double alpha = 0, rc2 = 0, Uo = 0, V = 0;
@@ -139,6 +141,13 @@ struct tcp_ctx {
     int pair_reserve = 0;
     double pair_reserve_ms[8] = {};
     bool recip_beside = false;          // the reciprocal chain is running on stream2
+    // The reserved CTAs rejoin the Newton-3 launch once the chain is done: a second
+    // launch of the same kernel on stream2 after the chain, claiming the remaining
+    // chunks from the same counter (pair_n3.cu launch_pair_n3_rejoin)
+    tcp::N3Args *n3_rejoin = nullptr;
+    bool n3_rejoin_pending = false;
+    int n3_rejoin_grid = 0, n3_rejoin_threads = 0;
+    const void *n3_rejoin_fn = nullptr;
     double *fpart = nullptr;   // [jsplit][3][n]
     double *upart = nullptr;   // energy partial per pair block
     int n_upart = 0;
@@ -260,6 +269,8 @@ bool n3_variant_usable(const tcp_ctx *c, int v);
 int autotune_pair(tcp_ctx *c);
 int time_pair_with_recip(tcp_ctx *c, int reps, double *ms);   // ctx.cu
 int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf);
+int launch_pair_n3_rejoin(tcp_ctx *c, cudaStream_t st);   // on stream2, after the reciprocal chain
+void n3_free(tcp_ctx *c);
 int n3_batch_variant_count();
 const char *n3_batch_variant_name(int v);
 int n3_batch_tile(int variant);

@@ -377,14 +377,15 @@ def test_autotuner_picks_a_timed_variant(monkeypatch):
 def test_grid_reserve_for_the_overlapped_reciprocal_chain(monkeypatch):
     """With SPME the autotuner also times the pair kernel with the reciprocal
     chain beside it for a few grid reserves and keeps the fastest;
-    TCP_PAIR_RESERVE forces one, and the forces do not depend on it."""
-    monkeypatch.delenv("TCP_PAIR_VARIANT", raising=False)
+    TCP_PAIR_RESERVE forces one, and the forces do not depend on it (a
+    Newton-3 variant is forced: at this size the ordered kernel can win)."""
+    monkeypatch.setenv("TCP_PAIR_VARIANT", "10")
     monkeypatch.delenv("TCP_PAIR_RESERVE", raising=False)
     s = make(8192, seed=41, K=32, order=5)
     with ctx_for(s, precision="fp32c", ei="kelbg", recip="spme") as c:
         c.force()
         r, cand = c.overlap_report()
-    assert set(cand) == {0, 8, 16, 32, 64}
+    assert set(cand) == {0, 16, 32, 64, 128, 256, 512}
     assert r in cand and cand[r] == min(cand.values())
     forces = []
     for forced in ("0", "40"):

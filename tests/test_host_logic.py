@@ -92,3 +92,27 @@ def test_bench_reductions_over_two_gloo_ranks():
         p.join(timeout=60)
         assert p.exitcode == 0
     assert out == [(0, 2, 2.0, 3.0), (1, 2, 2.0, 3.0)]
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    """bench.py --impl reference: full MD steps of the CPU restatement, at
+    most five timed whatever --steps asks, and the JSON keys the reference
+    line carries (the workload shrunk to 1,024 particles to stay quick)."""
+    import argparse
+    import json
+
+    import bench
+    from tcp_allpair_gb300 import system
+
+    small = make_config_system("n65536_spme128", n=1024)
+    small.K = 16
+    monkeypatch.setattr(system, "make_config_system", lambda name, seed=0, n=None: small)
+    args = argparse.Namespace(steps=100, warmup=5, gpus=1)
+    assert bench.run_reference(args, 1, 0, None) == 0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["steps"] == bench.REF_MAX_STEPS and line["warmup"] == 1
+    assert line["steps_requested"] == 100 and line["unit"] == "pair-int/s" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": "pair-int/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert line["config"]["workload"] == "n65536_spme128_kelbg_nve"
