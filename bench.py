@@ -40,6 +40,7 @@ Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 from __future__ import annotations
 
 import argparse
+import atexit
 import json
 import math
 import os
@@ -357,6 +358,9 @@ def run_c2(T, args, device, threads):
             comp = gpu_components(c)
             t = c.time_steps(s.dt, 20, flush_l2=True)        # device time of one step
             kernel = c.variant_name(c.autotune_report()[0]) if prec == "fp32c" else "pair_n3_f64_kernel"
+            reserve = c.overlap_report() if prec == "fp32c" else None
+            recip_alone = c.time_component(1, 5)
+            pair_alone = c.time_component(0, 5)
             # the run itself from the seeded start, Etot sampled every tenth of it
             c.upload(x=s.x, v=s.v)
             c.force()
@@ -371,7 +375,9 @@ def run_c2(T, args, device, threads):
         out[prec] = {"ms_per_step": ms, "value": pairs / (ms * 1e-3), "run_wall_s": wall,
                      "breakdown_ms_per_step": {k: t[k] / t["nsteps"] for k in ("vverlet1", "pair", "recip",
                                                                               "epilogue")},
-                     "pair_kernel": kernel,
+                     "pair_kernel": kernel, "pair_alone_ms": pair_alone, "recip_alone_ms": recip_alone,
+                     "grid_reserve": reserve[0] if reserve else None,
+                     "reserve_ms": reserve[1] if reserve else None,
                      "force_error_vs_oracle": force_errors(comp, ref),
                      "energy_error_vs_oracle": energy_errors(comp, ref, ek)}
         traj[prec] = np.array(et)
@@ -430,6 +436,13 @@ def run_gpu(args, world, rank, local, dist):
     import tcp_allpair_gb300 as T
     from tcp_allpair_gb300.system import make_config_system
 
+    # one autotuning per workload for all contexts of this run, in a file private to the
+    # run: the e2e context runs the kernel and grid reserve that the timed context chose
+    if "TCP_AUTOTUNE_CACHE" not in os.environ:
+        fd, cache = tempfile.mkstemp(prefix="tcp_autotune_", suffix=".txt")
+        os.close(fd)
+        os.environ["TCP_AUTOTUNE_CACHE"] = cache
+        atexit.register(lambda: os.path.exists(cache) and os.unlink(cache))
     s = make_config_system(WORKLOAD, seed=rank)
     n = s.n
     pairs = n * (n - 1) / 2
@@ -531,6 +544,7 @@ def run_gpu(args, world, rank, local, dist):
         ctx_e.md_steps_pt(s.dt, 1, qel, qion)
     te = time.perf_counter() - te0
     te = reduce_max(dist, te)
+    e2e_tuning = {"variant": ctx_e.variant_name(ctx_e.autotune_report()[0]), "grid_reserve": ctx_e.overlap_report()[0]}
     ctx_e.close()
     e2e_value = reduce_sum(dist, pairs) * args.steps / te
     e2e_sep_value = reduce_sum(dist, pairs) * args.steps / te_sep
@@ -622,6 +636,7 @@ def run_gpu(args, world, rank, local, dist):
                 "ms_per_step": te / args.steps * 1e3,
                 "path": "tcp_md_steps_records(1): PT records x,v,f read, one step, x,v,f written back, "
                         "pageable host memory",
+                "tuning": e2e_tuning,
                 "separate_calls": {"ms_per_step": te_sep / args.steps * 1e3,
                                    "value": e2e_sep_value,
                                    "host_ms_per_step": {"upload": ph[0] / args.steps * 1e3,
@@ -657,12 +672,12 @@ def run_pair_only(args):
 
 
 def run_recip_only(args):
-    """Launch the SPME chain alone on the headline system with N particles
-    (profiling target: `ncu --clock-control none -k regex:spme -c 3 ... python
-    bench.py --recip-only N`)."""
+    """Launch the SPME chain alone on the `--config` system (default the
+    headline one) with N particles (profiling target: `ncu --clock-control none
+    -k regex:spme -c 3 ... python bench.py --recip-only N`)."""
     import tcp_allpair_gb300 as T
     from tcp_allpair_gb300.system import make_config_system
-    s = make_config_system(WORKLOAD, n=args.recip_only)
+    s = make_config_system(args.config, n=args.recip_only)
     p = T.params_for(s, precision=args.precision, ei="kelbg", recip="spme")
     with T.Context(p, s.nel, s.nion) as c:
         c.EWALD_SELF()
@@ -695,6 +710,7 @@ def main():
     ap.add_argument("--pair-only", type=int, default=0, help="profile target: pair kernel alone at this N")
     ap.add_argument("--recip-only", type=int, default=0, help="profile target: SPME chain alone at this N")
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
+    ap.add_argument("--config", default="n65536_spme128", help="named workload of --recip-only")
     ap.add_argument("--batch", action="store_true", help="batched-replica workload instead of the headline")
     ap.add_argument("--batch-reps", type=int, default=64, help="replicas of the batched leg (0: skip)")
     args = ap.parse_args()

@@ -331,9 +331,10 @@ int tcp_autotune_report(tcp_ctx *ctx, int *variant, double *ms, int nmax);
 const char *tcp_pair_variant_name(int variant);
 /* The number of CTAs the autotuner left out of the persistent Newton-3 grid
  * so that the reciprocal chain, which runs beside the pair kernel in a step,
- * finds room on the SMs; the candidates and the time of the pair kernel with
- * the chain beside it for each (ms, 0 when not timed), up to nmax entries.
- * TCP_PAIR_RESERVE=k forces k. */
+ * finds room on the SMs (they join the pair kernel's work once the chain is
+ * done); the candidates and the time of the pair kernel with the chain
+ * beside it for each, up to the join of both (ms, 0 when not timed), up to
+ * nmax entries.  TCP_PAIR_RESERVE=k forces k. */
 int tcp_overlap_report(tcp_ctx *ctx, int *reserve, int *candidates, double *ms, int nmax);
 /* Kernel launches issued by the context so far (all kernels of this library). */
 int tcp_launch_count(tcp_ctx *ctx, long long *count);

@@ -499,7 +499,7 @@ static void b_spme_launch(tcp_batch *b, bool gather, cudaStream_t st) {
     const SpreadBins bins = b_bins(b);
     cudaMemsetAsync(b->bin_count, 0, sizeof(int) * (size_t)b->nbins, st);
     b_bin_count_kernel<P><<<blocks, 128, 0, st>>>(parts(b), bins);
-    launch_bin_sort(st, b->ntot, b->nbins, bins);
+    b->launches += launch_bin_sort(st, b->ntot, b->nbins, bins) - 5;   // the step's count assumes five
     b_bin_weights_kernel<P><<<blocks, 128, 0, st>>>(parts(b), bins);
     const size_t sm = kBRowWarps * b_row_warp_bytes(P, b->k1max);   // attribute set at tcp_batch_create
     b_row_spread_kernel<P><<<(b->ngroups + kBRowWarps - 1) / kBRowWarps, 32 * kBRowWarps, sm, st>>>(

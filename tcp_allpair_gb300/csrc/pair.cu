@@ -709,6 +709,11 @@ int launch_pair(tcp_ctx *c, bool energy, bool rdf) {
     a.status = c->status;
     a.c = c->pc;
     dim3 grid(g.nblk, c->jsplit);
+    // the energy reduction sums all n_upart partials: clear the ones this grid
+    // does not write (an earlier Newton-3 launch may have used more CTAs)
+    if (energy && (size_t)g.nblk * c->jsplit < (size_t)c->n_upart)
+        TCP_CUDA(cudaMemsetAsync(c->upart + (size_t)g.nblk * c->jsplit, 0,
+                                 sizeof(double) * ((size_t)c->n_upart - (size_t)g.nblk * c->jsplit), c->stream));
     const int ei = c->p.ei_model == TCP_EI_DEUTSCH ? 1 : (c->p.ei_model == TCP_EI_KELBG ? 2 : 0);
 #define TCP_PAIR_DISPATCH(KERNEL, ...)                                                                   \
     do {                                                                                                 \
@@ -936,7 +941,9 @@ extern "C" int tcp_force_direct_noalloc(const tcp_params *p, int nel, int nion, 
 // context's stream, on the positions currently on the device; the fastest is
 // kept.  TCP_PAIR_VARIANT=k forces variant k; TCP_AUTOTUNE=0 keeps the default
 // (Newton-3 variant 1 for cubic boxes); TCP_AUTOTUNE_CACHE=<file> stores the
-// choice per (device, n, nel, e-i model) and reuses it without timing.
+// choice per (device, n, nel, e-i model), and the grid reserve per the same
+// and the reciprocal setting (sum, mesh, order, FP64 chain), and reuses them
+// without timing.
 namespace tcp {
 
 static std::string tune_key(const tcp_ctx *c) {
@@ -1035,7 +1042,9 @@ static int choose_reserve(tcp_ctx *c, const char *cache, const std::string &key)
     if (c->p.reciprocal == TCP_RECIP_NONE || !n3_applicable(c)) return TCP_OK;
     if (const char *off = getenv("TCP_AUTOTUNE"))
         if (atoi(off) == 0) return TCP_OK;
-    const std::string rkey = key + " reserve";
+    const std::string rkey = key + "|" + std::to_string(c->p.reciprocal) + "|" + std::to_string(c->K1) + "x" +
+                             std::to_string(c->K2) + "x" + std::to_string(c->K3) + "|" +
+                             std::to_string(c->p.order) + "|" + (c->recip_fp64 ? "r64" : "r32") + " reserve";
     if (cache) {
         const int r = cache_lookup(cache, rkey);
         if (r >= 0) {
@@ -1044,20 +1053,23 @@ static int choose_reserve(tcp_ctx *c, const char *cache, const std::string &key)
         }
     }
     double best = 1e300;
-    int best_r = 0, k = 0;
+    int k = 0;
     for (const int r : kReserveCandidates) {
         c->pair_reserve = r;
         double ms = 0.0;
         const long long before = c->launches;
-        const int rc = time_pair_with_recip(c, 2, &ms);
+        const int rc = time_pair_with_recip(c, 4, &ms);
         c->launches = before;
         if (rc) return rc;
         c->pair_reserve_ms[k++] = ms;
-        if (ms < best) {
-            best = ms;
-            best_r = r;
-        }
+        best = std::min(best, ms);
     }
+    // the smallest reserve within 0.3 % of the fastest: the candidates near the
+    // optimum differ by less than the run-to-run spread, and inside a step (L2
+    // flushed, graph-launched) the smaller ones have timed faster
+    int best_r = kReserveCandidates[0];
+    for (int j = k - 1; j >= 0; --j)
+        if (c->pair_reserve_ms[j] <= best * 1.003) best_r = kReserveCandidates[j];
     c->pair_reserve = best_r;
     if (cache) {
         if (FILE *f = fopen(cache, "a")) {

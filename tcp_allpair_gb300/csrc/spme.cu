@@ -42,8 +42,9 @@ struct SpmeArgs {
 // (y, z) mesh column of their base (bin = by + K2 bz); each bin is put in
 // particle-index order and the B-spline weights of every particle are stored
 // once, in sorted order.  The spread is then a gather by mesh rows: a warp
-// owns kRows consecutive rows (y0 .. y0 + kRows - 1, z) in shared memory and
-// visits, for jz < P, the bins (y0 - P + 1 .. y0 + kRows - 1, z - jz) -- a
+// owns ROWS consecutive rows (y0 .. y0 + ROWS - 1, z) in shared memory (ROWS
+// = 8, or 4 / 2 on small meshes) and visits, for jz < P, the bins
+// (y0 - P + 1 .. y0 + ROWS - 1, z - jz) -- a
 // contiguous (or wrapped) range of the sorted list, staged 32 particles at a
 // time.  For one particle its lanes cover the P x P points (jy, jx) of plane
 // z, so no two lanes and no two warps touch the same point: no atomics, and
@@ -53,7 +54,7 @@ struct SpmeArgs {
 // adds FP32 products in compensated two-float FP32 (TwoSum hi/lo) and writes
 // the FP32 mesh read by the FP32 transforms (GB300's FP64 rate is 1/64 of
 // FP32).
-constexpr int kRows = 8;                 // mesh rows per warp
+constexpr int kRows = 8;                 // mesh rows per warp (fewer for small meshes: spread_rows)
 constexpr int kRowWarps = 4;             // warps per CTA (fewer when the rows of a large mesh need the space)
 constexpr int kScanBlock = 1024;         // bins per block of the prefix sum
 constexpr int kSortReg = 8;              // bins up to this size are sorted in registers
@@ -104,6 +105,45 @@ __global__ void scan_block_kernel(const int *__restrict__ count, int nbins, int 
     const int incl = x + (w > 0 ? ws[w - 1] : 0);
     if (i < nbins) start[i] = incl - v;
     if (threadIdx.x == kScanBlock - 1) bsum[blockIdx.x] = incl;
+}
+
+// One CTA for up to kScanBlock * kScanPer bins: each thread sums its run of
+// consecutive bins, the CTA scans the run sums, and each thread writes its
+// run's exclusive prefix; start[nbins] = total.
+constexpr int kScanPer = 32;
+__global__ void __launch_bounds__(kScanBlock) scan_single_kernel(const int *__restrict__ count, int nbins,
+                                                                 int *__restrict__ start, int total) {
+    __shared__ int ws[32];
+    const int per = (nbins + kScanBlock - 1) / kScanBlock;
+    const int b0 = min(nbins, (int)threadIdx.x * per), b1 = min(nbins, b0 + per);
+    int v = 0;
+    for (int k = b0; k < b1; ++k) v += count[k];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int t = ws[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        ws[lane] = t;
+    }
+    __syncthreads();
+    int run = x - v + (w > 0 ? ws[w - 1] : 0);
+    for (int k = b0; k < b1; ++k) {
+        const int t = count[k];
+        start[k] = run;
+        run += t;
+    }
+    if (threadIdx.x == 0) start[nbins] = total;
 }
 
 __global__ void scan_sums_kernel(int *__restrict__ bsum, int nblocks) {
@@ -188,33 +228,33 @@ __global__ void spme_bin_weights_kernel(const SpmeArgs a, SpreadBins b) {
     static_cast<T *>(b.eq)[pos] = (T)(m < a.nel ? a.q0 : a.q1);
 }
 
-// Shared memory of one warp: kRows rows of hi (T) [and lo (float)] of K1
+// Shared memory of one warp: ROWS rows of hi (T) [and lo (float)] of K1
 // points, then 32 staged particles (bx, by, q, weights).
-template <int P, typename T>
+template <int P, typename T, int ROWS = kRows>
 __host__ __device__ constexpr size_t row_warp_bytes(int K1) {
-    return (size_t)kRows * K1 * (sizeof(T) + (sizeof(T) == 4 ? 4 : 0)) + 32 * (2 * sizeof(int) + (1 + 3 * P) * sizeof(T));
+    return (size_t)ROWS * K1 * (sizeof(T) + (sizeof(T) == 4 ? 4 : 0)) + 32 * (2 * sizeof(int) + (1 + 3 * P) * sizeof(T));
 }
 
-template <int P, typename T>
+template <int P, typename T, int ROWS>
 __global__ void __launch_bounds__(32 * kRowWarps) spme_row_spread_kernel(const SpmeArgs a, const SpreadBins b,
                                                                          double *__restrict__ Q,
                                                                          float *__restrict__ Qf) {
     constexpr bool F32 = sizeof(T) == 4;
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int ngy = (a.K2 + kRows - 1) / kRows;
+    const int ngy = (a.K2 + ROWS - 1) / ROWS;
     const long grp = (long)blockIdx.x * (blockDim.x >> 5) + warp;  // (row group, z)
     if (grp >= (long)ngy * a.K3) return;                          // warp-uniform
-    const int y0 = (int)(grp % ngy) * kRows, z = (int)(grp / ngy);
-    const int nrow = min(kRows, a.K2 - y0);
-    unsigned char *base = smem + (size_t)warp * row_warp_bytes<P, T>(a.K1);
-    T *hi = reinterpret_cast<T *>(base);                            // [kRows][K1]
-    float *lo = reinterpret_cast<float *>(base + (size_t)kRows * a.K1 * sizeof(T));
-    unsigned char *st = base + (size_t)kRows * a.K1 * (sizeof(T) + (F32 ? 4 : 0));
+    const int y0 = (int)(grp % ngy) * ROWS, z = (int)(grp / ngy);
+    const int nrow = min(ROWS, a.K2 - y0);
+    unsigned char *base = smem + (size_t)warp * row_warp_bytes<P, T, ROWS>(a.K1);
+    T *hi = reinterpret_cast<T *>(base);                            // [ROWS][K1]
+    float *lo = reinterpret_cast<float *>(base + (size_t)ROWS * a.K1 * sizeof(T));
+    unsigned char *st = base + (size_t)ROWS * a.K1 * (sizeof(T) + (F32 ? 4 : 0));
     T *sw = reinterpret_cast<T *>(st);                              // [32][3P]
     T *sq = sw + 32 * 3 * P;                                        // [32]
     int *sbx = reinterpret_cast<int *>(sq + 32), *sby = sbx + 32;   // [32], [32]
-    for (int k = lane; k < kRows * a.K1; k += 32) {
+    for (int k = lane; k < ROWS * a.K1; k += 32) {
         hi[k] = (T)0;
         if (F32) lo[k] = 0.f;
     }
@@ -614,14 +654,20 @@ static SpmeArgs spme_args(const tcp_ctx *c) {
 
 // prefix sum of the bin counts, placement by the counting-sort slots, and
 // each bin in particle-index order (shared by the single-system and batched paths)
-void launch_bin_sort(cudaStream_t st, int n, int nbins, const SpreadBins &b) {
+int launch_bin_sort(cudaStream_t st, int n, int nbins, const SpreadBins &b) {
     const int threads = 256;
     const int sblocks = (nbins + kScanBlock - 1) / kScanBlock;
-    scan_block_kernel<<<sblocks, kScanBlock, 0, st>>>(b.count, nbins, b.start, b.bsum);
-    scan_sums_kernel<<<1, 32, 0, st>>>(b.bsum, sblocks);
-    scan_add_kernel<<<(nbins + threads - 1) / threads, threads, 0, st>>>(b.start, nbins, b.bsum, n);
+    const bool single = nbins <= kScanBlock * kScanPer;   // meshes up to 181 x 181 columns: one launch
+    if (single) {
+        scan_single_kernel<<<1, kScanBlock, 0, st>>>(b.count, nbins, b.start, n);
+    } else {
+        scan_block_kernel<<<sblocks, kScanBlock, 0, st>>>(b.count, nbins, b.start, b.bsum);
+        scan_sums_kernel<<<1, 32, 0, st>>>(b.bsum, sblocks);
+        scan_add_kernel<<<(nbins + threads - 1) / threads, threads, 0, st>>>(b.start, nbins, b.bsum, n);
+    }
     spme_bin_scatter_kernel<<<(n + threads - 1) / threads, threads, 0, st>>>(n, b);
     spme_bin_sort_kernel<<<(nbins + threads - 1) / threads, threads, 0, st>>>(b, nbins);
+    return single ? 3 : 5;
 }
 
 int bin_scan_block() { return kScanBlock; }
@@ -641,6 +687,25 @@ static SpreadBins spread_bins(tcp_ctx *c) {
     return b;
 }
 
+// Mesh rows per warp of the spread: 8, or 4 / 2 on meshes of fewer (y, z)
+// columns, so that the kernel keeps about 2,048 warps (13 per SM) where a
+// small mesh would leave a few warps per SM with long serial loops.  A warp
+// visits the particles of ROWS + P - 1 bin rows for ROWS mesh rows.
+static int spread_rows(const tcp_ctx *c) {
+    const long cols = (long)c->K2 * c->K3;
+    return cols >= 16384 ? kRows : (cols >= 8192 ? 4 : 2);
+}
+
+template <int P, typename T, int ROWS>
+static void launch_row_spread(tcp_ctx *c, const SpmeArgs &a, const SpreadBins &b, double *Q, float *Qf) {
+    const long groups = (long)((c->K2 + ROWS - 1) / ROWS) * c->K3;
+    const size_t per_warp = row_warp_bytes<P, T, ROWS>(c->K1);
+    const int warps = (int)std::max<size_t>(1, std::min<size_t>(kRowWarps, (200u << 10) / per_warp));
+    const size_t sm = warps * per_warp;
+    const int rblocks = (int)((groups + warps - 1) / warps);
+    spme_row_spread_kernel<P, T, ROWS><<<rblocks, 32 * warps, sm, c->rstream>>>(a, b, Q, Qf);
+}
+
 template <int P>
 static int launch_cell_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Qf) {
     const SpreadBins b = spread_bins(c);
@@ -648,34 +713,43 @@ static int launch_cell_spread(tcp_ctx *c, const SpmeArgs &a, double *Q, float *Q
     const int nbins = c->K2 * c->K3;
     TCP_CUDA(cudaMemsetAsync(c->bin_count, 0, sizeof(int) * (size_t)nbins, c->rstream));
     spme_bin_count_kernel<P><<<pblocks, threads, 0, c->rstream>>>(a, b);
-    launch_bin_sort(c->rstream, c->n, nbins, b);
-    const long groups = (long)((c->K2 + kRows - 1) / kRows) * c->K3;
-    const size_t per_warp = Qf ? row_warp_bytes<P, float>(c->K1) : row_warp_bytes<P, double>(c->K1);
-    const int warps = (int)std::max<size_t>(1, std::min<size_t>(kRowWarps, (200u << 10) / per_warp));
-    const size_t sm = warps * per_warp;
-    const int rblocks = (int)((groups + warps - 1) / warps);
+    const int sort_kernels = launch_bin_sort(c->rstream, c->n, nbins, b);
     if (Qf) {
         spme_bin_weights_kernel<P, float><<<pblocks, threads, 0, c->rstream>>>(a, b);
-        spme_row_spread_kernel<P, float><<<rblocks, 32 * warps, sm, c->rstream>>>(a, b, nullptr, Qf);
+        switch (spread_rows(c)) {
+            case 2: launch_row_spread<P, float, 2>(c, a, b, nullptr, Qf); break;
+            case 4: launch_row_spread<P, float, 4>(c, a, b, nullptr, Qf); break;
+            default: launch_row_spread<P, float, kRows>(c, a, b, nullptr, Qf); break;
+        }
     } else {
         spme_bin_weights_kernel<P, double><<<pblocks, threads, 0, c->rstream>>>(a, b);
-        spme_row_spread_kernel<P, double><<<rblocks, 32 * warps, sm, c->rstream>>>(a, b, Q, nullptr);
+        switch (spread_rows(c)) {
+            case 2: launch_row_spread<P, double, 2>(c, a, b, Q, nullptr); break;
+            case 4: launch_row_spread<P, double, 4>(c, a, b, Q, nullptr); break;
+            default: launch_row_spread<P, double, kRows>(c, a, b, Q, nullptr); break;
+        }
     }
-    c->launches += 8;
+    c->launches += 3 + sort_kernels;
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;
 }
 
 // shared-memory limits of the spread kernels for this mesh (set once, outside
 // any stream capture; a launch uses at most kRowWarps warps' worth)
+template <int P, typename T, int ROWS>
+static int prepare_row_spread(tcp_ctx *c) {
+    const size_t s = std::min<size_t>(kRowWarps * row_warp_bytes<P, T, ROWS>(c->K1), 200u << 10);
+    TCP_CUDA(cudaFuncSetAttribute(spme_row_spread_kernel<P, T, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)std::max(s, row_warp_bytes<P, T, ROWS>(c->K1))));
+    return TCP_OK;
+}
+
 template <int P>
 static int prepare_cell_spread_p(tcp_ctx *c) {
-    const size_t sf = std::min<size_t>(kRowWarps * row_warp_bytes<P, float>(c->K1), 200u << 10);
-    const size_t sd = std::min<size_t>(kRowWarps * row_warp_bytes<P, double>(c->K1), 200u << 10);
-    TCP_CUDA(cudaFuncSetAttribute(spme_row_spread_kernel<P, float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)std::max(sf, row_warp_bytes<P, float>(c->K1))));
-    TCP_CUDA(cudaFuncSetAttribute(spme_row_spread_kernel<P, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)std::max(sd, row_warp_bytes<P, double>(c->K1))));
+    for (int rc : {prepare_row_spread<P, float, 2>(c), prepare_row_spread<P, float, 4>(c),
+                   prepare_row_spread<P, float, kRows>(c), prepare_row_spread<P, double, 2>(c),
+                   prepare_row_spread<P, double, 4>(c), prepare_row_spread<P, double, kRows>(c)})
+        if (rc) return rc;
     return TCP_OK;
 }
 

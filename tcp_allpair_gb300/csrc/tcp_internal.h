@@ -318,7 +318,7 @@ struct SpreadBins {
 };
 // start = exclusive prefix of count (plus start[nbins] = n), list = particles
 // by bin (ebx[m] holds the bin of particle m on entry), each bin index-ordered
-void launch_bin_sort(cudaStream_t st, int n, int nbins, const SpreadBins &b);
+int launch_bin_sort(cudaStream_t st, int n, int nbins, const SpreadBins &b);   // returns its kernel count
 int bin_scan_block();
 
 // ctx.cu: step and force composition for the derivative routines

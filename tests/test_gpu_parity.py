@@ -78,8 +78,11 @@ def test_direct_fp32c(ei, n):
     assert ur == pytest.approx(uo, rel=2e-5)
 
 
-@pytest.mark.parametrize("order,K", [(4, 16), (5, 32), (6, 24), (4, 30)])
+@pytest.mark.parametrize("order,K", [(4, 16), (5, 32), (6, 24), (4, 30), (5, 96), (4, 128)])
 def test_spme_vs_oracle(order, K):
+    """FP64 SPME against the oracle; the meshes take the spread's three row
+    groupings (2 rows per warp below 8,192 (y, z) columns, 4 below 16,384,
+    8 above)."""
     s = make(2000, seed=4, K=K, order=order)
     o = oracle.Oracle.from_system(s, ei="kelbg")
     fo, umo = o.force_spme(s.x)
@@ -376,7 +379,8 @@ def test_autotuner_picks_a_timed_variant(monkeypatch):
 
 def test_grid_reserve_for_the_overlapped_reciprocal_chain(monkeypatch):
     """With SPME the autotuner also times the pair kernel with the reciprocal
-    chain beside it for a few grid reserves and keeps the fastest;
+    chain beside it for a few grid reserves and keeps the smallest within
+    0.3 % of the fastest;
     TCP_PAIR_RESERVE forces one, and the forces do not depend on it (a
     Newton-3 variant is forced: at this size the ordered kernel can win)."""
     monkeypatch.setenv("TCP_PAIR_VARIANT", "10")
@@ -386,7 +390,9 @@ def test_grid_reserve_for_the_overlapped_reciprocal_chain(monkeypatch):
         c.force()
         r, cand = c.overlap_report()
     assert set(cand) == {0, 16, 32, 64, 128, 256, 512}
-    assert r in cand and cand[r] == min(cand.values())
+    # the smallest reserve within 0.3 % of the fastest
+    assert r in cand and cand[r] <= 1.003 * min(cand.values())
+    assert all(cand[q] > 1.003 * min(cand.values()) for q in cand if q < r)
     forces = []
     for forced in ("0", "40"):
         monkeypatch.setenv("TCP_PAIR_RESERVE", forced)
