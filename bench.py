@@ -404,6 +404,7 @@ def run_batch_leg(T, args, device):
             b.upload(r, x=s.x, v=s.v)
         b.force()
         bvar, bms = b.autotune_report()
+        bres, bres_ms = b.overlap_report()
         b.md_steps(dt, args.warmup)
         ms_batch = b.time_steps(dt, args.steps)
     ctxs = []
@@ -428,7 +429,8 @@ def run_batch_leg(T, args, device):
             "loop_single_contexts": {"value": pairs / (ms_loop * 1e-3), "ms_per_step": ms_loop},
             "speedup_batch_over_loop": ms_loop / ms_batch, "replicas": len(ss),
             "particles": sum(s.n for s in ss), "steps": args.steps, "warmup": args.warmup,
-            "batch_variant": int(bvar), "batch_variant_ms": [round(float(x), 4) for x in bms if x > 0]}
+            "batch_variant": int(bvar), "batch_variant_ms": [round(float(x), 4) for x in bms if x > 0],
+            "grid_reserve": bres, "reserve_ms": {k: round(v, 4) for k, v in bres_ms.items()}}
 
 
 def run_gpu(args, world, rank, local, dist):

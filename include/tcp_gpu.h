@@ -273,6 +273,13 @@ int tcp_batch_md_steps(tcp_batch *b, double dt, int nsteps, tcp_energies *e);
 /* The batched real-space kernel the batch autotuner picked (variant index) and
  * the per-candidate times in ms (0 when not timed), up to nmax entries. */
 int tcp_batch_autotune_report(tcp_batch *b, int *variant, double *ms, int nmax);
+/* The CTAs the batch autotuner left out of the persistent batched pair grid so
+ * that the replicas' SPME chains, which run beside it, find room on the SMs
+ * (they join the pair launch's work once the chains are done); the candidates
+ * and the time of the pair launch with the chains beside it for each, up to
+ * the join (ms, 0 when not timed), up to nmax entries.  TCP_BATCH_RESERVE=k
+ * forces k. */
+int tcp_batch_overlap_report(tcp_batch *b, int *reserve, int *candidates, double *ms, int nmax);
 /* Mean device time of one batched step over nsteps graph replays (CUDA events). */
 int tcp_batch_time_steps(tcp_batch *b, double dt, int nsteps, double *ms_per_step);
 

@@ -348,6 +348,17 @@ class Batch:
                   "tcp_batch_autotune_report")
         return v.value, ms
 
+    def overlap_report(self):
+        """(CTAs left out of the batched pair grid for the SPME chains, {candidate: ms of the
+        pair launch with the chains beside it})."""
+        r = C.c_int()
+        cand = np.zeros(8, dtype=np.int32)
+        ms = np.zeros(8)
+        self._chk(self.lib.tcp_batch_overlap_report(self.h, C.byref(r), cand.ctypes.data_as(C.POINTER(C.c_int)),
+                                                    ms.ctypes.data_as(C.POINTER(C.c_double)), 8),
+                  "tcp_batch_overlap_report")
+        return r.value, {int(k): float(t) for k, t in zip(cand, ms) if t > 0}
+
 
 def fp32_peak(device: int = 0) -> float:
     """Measured FP32 FFMA rate of the device in 1e12 FFMA/s."""

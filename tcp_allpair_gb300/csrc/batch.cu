@@ -408,6 +408,12 @@ struct tcp_batch {
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;     // the SPME chain of a step, beside the pair launch
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_ready = nullptr;     // the pair launch's counter and accumulators are cleared
+    // CTAs of the persistent pair grid left to the SPME chains; they rejoin the
+    // pair launch on stream2 once the chains are done (chosen by the autotuner)
+    int pair_reserve = 0;
+    double reserve_ms[8] = {};
+    tcp::N3Rejoin rejoin;
     double *x = nullptr, *v = nullptr, *f = nullptr, *frec = nullptr, *facc = nullptr;
     int4 *xq = nullptr;
     int *rep_of = nullptr;
@@ -557,6 +563,7 @@ static int b_recip_fork(tcp_batch *b, const BAcc &A) {
 }
 
 static int b_recip_join(tcp_batch *b) {
+    if (int rc = n3_rejoin_launch(b->rejoin, b->stream2, b->ev_ready, &b->launches)) return rc;
     TCP_CUDA(cudaEventRecord(b->ev_join, b->stream2));
     TCP_CUDA(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
     return TCP_OK;
@@ -571,7 +578,8 @@ static int b_step(tcp_batch *b, double dt) {
     int rc = b_recip_fork(b, A);
     if (!rc)
         rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, b->n3_chunks, b->n3_nchunks, A.ur,
-                                  b->status, b->counter, b->num_sms, true, b->pair_variant);
+                                  b->status, b->counter, b->num_sms, true, b->pair_variant, b->pair_reserve,
+                                  &b->rejoin, b->ev_ready);
     if (int jrc = b_recip_join(b)) return jrc;
     if (rc) return rc;
     b_finalize_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), A.fsum);
@@ -601,6 +609,59 @@ static int b_fill_n3(tcp_batch *b, int v) {
     return TCP_OK;
 }
 
+// CTAs of the persistent pair grid left to the SPME chains, which run beside
+// it on stream2 and find no registers free otherwise; they rejoin the pair
+// launch once the chains are done.  Each candidate is timed as the chains and
+// the pair launch beside them, up to the join, over four launches; the
+// smallest reserve within 0.3 % of the fastest is kept (TCP_BATCH_RESERVE
+// forces one).
+static constexpr int kBReserveCandidates[] = {0, 16, 32, 64, 128, 256, 512};
+static int b_choose_reserve(tcp_batch *b) {
+    b->pair_reserve = 0;
+    if (const char *forced = getenv("TCP_BATCH_RESERVE")) {
+        b->pair_reserve = std::max(atoi(forced), 0);
+        return TCP_OK;
+    }
+    const BAcc A = acc_of(b);
+    cudaEvent_t e0, e1;
+    TCP_CUDA(cudaEventCreate(&e0));
+    TCP_CUDA(cudaEventCreate(&e1));
+    int rc = TCP_OK, k = 0;
+    double best = 1e300;
+    const long long before = b->launches;
+    auto once = [&]() -> int {
+        int r = b_recip_fork(b, A);
+        if (!r)
+            r = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, b->n3_chunks,
+                                     b->n3_nchunks, A.ur, b->status, b->counter, b->num_sms, true, b->pair_variant,
+                                     b->pair_reserve, &b->rejoin, b->ev_ready);
+        if (int j = b_recip_join(b)) return j;
+        return r;
+    };
+    for (const int r : kBReserveCandidates) {
+        b->pair_reserve = r;
+        rc = once();
+        cudaEventRecord(e0, b->stream);
+        for (int t = 0; t < 4 && !rc; ++t) rc = once();
+        cudaEventRecord(e1, b->stream);
+        cudaEventSynchronize(e1);
+        if (rc) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        b->reserve_ms[k++] = ms / 4;
+        best = std::min(best, (double)ms / 4);
+    }
+    b->launches = before;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    b->pair_reserve = kBReserveCandidates[0];
+    for (int j = k - 1; j >= 0; --j)
+        if (b->reserve_ms[j] <= best * 1.003) b->pair_reserve = kBReserveCandidates[j];
+    TCP_CUDA(cudaGetLastError());
+    return TCP_OK;
+}
+
 // Batch autotuner: times every batched Newton-3 variant on this batch's items
 // (one warm-up and two timed launches each, CUDA events) and keeps the
 // fastest; TCP_BATCH_VARIANT forces one.  Runs before the step graph is captured.
@@ -608,7 +669,10 @@ static int b_autotune(tcp_batch *b) {
     if (b->tuned) return TCP_OK;
     b->tuned = true;
     const int nv = n3_batch_variant_count();
-    if (const char *forced = getenv("TCP_BATCH_VARIANT")) return b_fill_n3(b, std::min(std::max(atoi(forced), 0), nv - 1));
+    if (const char *forced = getenv("TCP_BATCH_VARIANT")) {
+        if (int rc = b_fill_n3(b, std::min(std::max(atoi(forced), 0), nv - 1))) return rc;
+        return b_choose_reserve(b);
+    }
     const BAcc A = acc_of(b);
     const int nb = (b->ntot + kBThreads - 1) / kBThreads;
     b_refresh_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b));
@@ -638,7 +702,8 @@ static int b_autotune(tcp_batch *b) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
-    return b_fill_n3(b, best_v);
+    if ((rc = b_fill_n3(b, best_v))) return rc;
+    return b_choose_reserve(b);
 }
 
 static int b_sync(tcp_batch *b) {
@@ -691,6 +756,8 @@ int tcp_batch_destroy(tcp_batch *b) {
     if (b->h_acc) cudaFreeHost(b->h_acc);
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->ev_join) cudaEventDestroy(b->ev_join);
+    if (b->ev_ready) cudaEventDestroy(b->ev_ready);
+    n3_rejoin_free(b->rejoin);
     if (b->stream2) {
         cudaStreamSynchronize(b->stream2);
         cudaStreamDestroy(b->stream2);
@@ -753,7 +820,8 @@ int tcp_batch_create(const tcp_params *params, const int *nel, const int *nion, 
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_ready, cudaEventDisableTiming) != cudaSuccess)
         return fail(cuda_check(cudaGetLastError(), "cudaStreamCreate"));
     TCP_BALLOC(b->x, sizeof(double) * 3 * n);
     TCP_BALLOC(b->v, sizeof(double) * 3 * n);
@@ -978,7 +1046,8 @@ int tcp_batch_force(tcp_batch *b, tcp_energies *e) {
     int rc = b_recip_fork(b, A);
     if (!rc)
         rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, b->n3_chunks, b->n3_nchunks, A.ur,
-                                  b->status, b->counter, b->num_sms, true, b->pair_variant);
+                                  b->status, b->counter, b->num_sms, true, b->pair_variant, b->pair_reserve,
+                                  &b->rejoin, b->ev_ready);
     if (int jrc = b_recip_join(b)) return jrc;
     if (rc) return rc;
     b_finalize_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), A.fsum);
@@ -1028,6 +1097,17 @@ int tcp_batch_autotune_report(tcp_batch *b, int *variant, double *ms, int nmax) 
     if (!b) return set_error(TCP_ERR_BAD_PARAM, "batch is NULL");
     if (variant) *variant = b->pair_variant;
     for (int k = 0; ms && k < nmax && k < 8; ++k) ms[k] = b->variant_ms[k];
+    return TCP_OK;
+}
+
+int tcp_batch_overlap_report(tcp_batch *b, int *reserve, int *candidates, double *ms, int nmax) {
+    if (!b) return set_error(TCP_ERR_BAD_PARAM, "batch is NULL");
+    if (reserve) *reserve = b->pair_reserve;
+    constexpr int nc = (int)(sizeof kBReserveCandidates / sizeof kBReserveCandidates[0]);
+    for (int k = 0; k < nmax && k < nc; ++k) {
+        if (candidates) candidates[k] = kBReserveCandidates[k];
+        if (ms) ms[k] = b->reserve_ms[k];
+    }
     return TCP_OK;
 }
 

@@ -397,7 +397,7 @@ __device__ __forceinline__ void n3_item_x2(const PairConsts &c, const int4 *__re
 template <bool ENERGY, int R, int UNROLL, int MINB, bool BATCH, int MODE = 0, int W = kN3Warps, bool RDF = false,
           int PD = kErfcH6>
 __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
-    static_assert(W >= 4, "the reaction flush needs at least kN3Sub threads");
+    static_assert(W >= 1, "at least one warp per CTA");
     static_assert(!RDF || (MODE >= 1 && !BATCH), "RDF histograms: packed single-system forms");
     static_assert(PD == kErfcH6 || MODE >= 1, "the degree-5 erfc exists in the packed forms");
     static_assert((32 * R * W) % kN3Sub == 0, "i-tiles hold whole j-subtiles");
@@ -578,14 +578,27 @@ __global__ void __launch_bounds__(32 * W, MINB) pair_n3_kernel(const N3Args a) {
         if (ENERGY) acc2(eh, el, pe * c.u_qq_energy[pt]);
         // all warps are done with this subtile and its reaction sums
         const bool timeout = __syncthreads_or(!ok);
-        if (!timeout && tid < cnt) {
-            const double sc = -kEps * (double)qf;
-            const size_t j = (size_t)ioff + jstart + tid;
-            atomicAdd(&a.facc[j], sc * (double)sjacc[tid][0]);
-            atomicAdd(&a.facc[(size_t)a.ntot + j], sc * (double)sjacc[tid][1]);
-            atomicAdd(&a.facc[2 * (size_t)a.ntot + j], sc * (double)sjacc[tid][2]);
+        if constexpr (NT >= kN3Sub) {
+            if (!timeout && tid < cnt) {
+                const double sc = -kEps * (double)qf;
+                const size_t j = (size_t)ioff + jstart + tid;
+                atomicAdd(&a.facc[j], sc * (double)sjacc[tid][0]);
+                atomicAdd(&a.facc[(size_t)a.ntot + j], sc * (double)sjacc[tid][1]);
+                atomicAdd(&a.facc[2 * (size_t)a.ntot + j], sc * (double)sjacc[tid][2]);
+            }
+            if (tid < kN3Sub) sjacc[tid][0] = sjacc[tid][1] = sjacc[tid][2] = 0.f;
+        } else {   // fewer threads than subtile particles: each flushes several
+            for (int t = tid; t < kN3Sub; t += NT) {
+                if (!timeout && t < cnt) {
+                    const double sc = -kEps * (double)qf;
+                    const size_t j = (size_t)ioff + jstart + t;
+                    atomicAdd(&a.facc[j], sc * (double)sjacc[t][0]);
+                    atomicAdd(&a.facc[(size_t)a.ntot + j], sc * (double)sjacc[t][1]);
+                    atomicAdd(&a.facc[2 * (size_t)a.ntot + j], sc * (double)sjacc[t][2]);
+                }
+                sjacc[t][0] = sjacc[t][1] = sjacc[t][2] = 0.f;
+            }
         }
-        if (tid < kN3Sub) sjacc[tid][0] = sjacc[tid][1] = sjacc[tid][2] = 0.f;
         return !timeout;
     };
 
@@ -665,6 +678,18 @@ static const N3Variant kVariants[] = {
      pair_n3_kernel<false, 6, 1, 4, false, 1, 4, false, kErfcH5>, 6, 4, "n3_r6_u1_w4b4_x2_p5", true},
     {pair_n3_kernel<true, 6, 2, 3, false, 1, 4, false, kErfcH5>,
      pair_n3_kernel<false, 6, 2, 3, false, 1, 4, false, kErfcH5>, 6, 4, "n3_r6_u2_w4b3_x2_p5", true},
+    // 2 warps per CTA: 256-particle i-tiles at the per-lane work of R = 4, so
+    // that small systems end with a short tail
+    {pair_n3_kernel<true, 4, 2, 8, false, 1, 2, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 2, 8, false, 1, 2, false, kErfcH5>, 4, 2, "n3_r4_u2_w2b8_x2_p5", true},
+    {pair_n3_kernel<true, 4, 2, 8, false, 2, 2, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 2, 8, false, 2, 2, false, kErfcH5>, 4, 2, "n3_r4_u2_w2b8_x2l_p5", true},
+    // one warp per CTA: 128-particle i-tiles, no cross-warp reaction sum
+    {pair_n3_kernel<true, 4, 2, 16, false, 1, 1, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 2, 16, false, 1, 1, false, kErfcH5>, 4, 1, "n3_r4_u2_w1b16_x2_p5", true},
+    // the 2-warp form with the degree-6 erfc (any alpha rc)
+    {pair_n3_kernel<true, 4, 2, 8, false, 1, 2>, pair_n3_kernel<false, 4, 2, 8, false, 1, 2>, 4, 2,
+     "n3_r4_u2_w2b8_x2"},
 };
 constexpr int kN3Variants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -734,16 +759,21 @@ void n3_chunk_table(long long total, int ctas, std::vector<long long> &starts) {
 // Chunk tables of every i-tile size the variants use, in one device array
 // (c->n3_chunks; c->n3_chunk_meta holds tile, items, offset, chunks per
 // table).  Built on the host when the pair constants change, outside any
-// stream capture, for the largest persistent grid.
+// stream capture, each for the largest persistent grid among the variants of
+// that i-tile.
 int n3_prepare_chunks(tcp_ctx *c) {
     std::vector<int> tiles;
     for (const N3Variant &v : kVariants) tiles.push_back(32 * v.R * v.W);
     for (const N3Variant &v : kRdfVariants) tiles.push_back(32 * v.R * v.W);
     std::sort(tiles.begin(), tiles.end());
     tiles.erase(std::unique(tiles.begin(), tiles.end()), tiles.end());
-    const int ctas = n3_grid(c);
     std::vector<long long> all, meta, t;
     for (const int tile : tiles) {
+        int ctas = 1;
+        for (int v = 1; v <= kN3Variants; ++v)
+            if (32 * kVariants[v - 1].R * kVariants[v - 1].W == tile) ctas = std::max(ctas, n3_grid_for(c, v));
+        for (const N3Variant &v : kRdfVariants)
+            if (32 * v.R * v.W == tile) ctas = std::max(ctas, kernel_grid(c, v.energy, 32 * v.W));
         long long total = 0;
         n3_geometry(0, c->nel, c->nion, tile, 0, &total);
         n3_chunk_table(total, ctas, t);
@@ -756,6 +786,16 @@ int n3_prepare_chunks(tcp_ctx *c) {
     TCP_CUDA(cudaMemcpy(c->n3_chunks, all.data(), sizeof(long long) * all.size(), cudaMemcpyHostToDevice));
     c->n3_chunk_meta = meta;
     return TCP_OK;
+}
+
+// the arguments, grid and kernel of a rejoin launch (not yet pending)
+static void n3_rejoin_set(N3Rejoin &r, const N3Args &a, int grid, int threads, const void *fn) {
+    if (!r.args) r.args = new N3Args;
+    *r.args = a;
+    r.args->inject_skip = 0;
+    r.grid = grid;
+    r.threads = threads;
+    r.fn = fn;
 }
 
 int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf) {
@@ -788,7 +828,7 @@ int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf) {
     a.rdf_edges = c->rdf_edges;
     // CTAs left free for the reciprocal chain when it runs beside this launch;
     // they rejoin it after the chain (launch_pair_n3_rejoin)
-    c->n3_rejoin_pending = false;
+    c->rejoin.pending = false;
     const int reserve = c->recip_beside ? c->pair_reserve : 0;
     const int full = rdf ? kernel_grid(c, K.energy, nt) : n3_grid_for(c, v);
     const int grid = (int)std::min<long long>(std::max(1, full - reserve), total);
@@ -800,13 +840,9 @@ int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf) {
     if (energy) TCP_CUDA(cudaMemsetAsync(c->upart, 0, sizeof(double) * (size_t)c->n_upart, c->stream));
     if (rejoin > 0) {
         TCP_CUDA(cudaEventRecord(c->ev_pair_ready, c->stream));
-        if (!c->n3_rejoin) c->n3_rejoin = new N3Args;
-        *c->n3_rejoin = a;
-        c->n3_rejoin->upart = c->upart + grid;   // its CTAs' energy partials follow the first launch's
-        c->n3_rejoin->inject_skip = 0;
-        c->n3_rejoin_grid = rejoin;
-        c->n3_rejoin_threads = nt;
-        c->n3_rejoin_fn = reinterpret_cast<const void *>(energy ? K.energy : K.plain);
+        N3Args r = a;
+        r.upart = c->upart + grid;   // its CTAs' energy partials follow the first launch's
+        n3_rejoin_set(c->rejoin, r, rejoin, nt, reinterpret_cast<const void *>(energy ? K.energy : K.plain));
     }
     if (energy)
         K.energy<<<grid, nt, 0, c->stream>>>(a);
@@ -814,7 +850,7 @@ int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf) {
         K.plain<<<grid, nt, 0, c->stream>>>(a);
     c->launches++;
     TCP_CUDA(cudaGetLastError());
-    c->n3_rejoin_pending = rejoin > 0;
+    c->rejoin.pending = rejoin > 0;
     return TCP_OK;
 }
 
@@ -823,21 +859,27 @@ int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf) {
 // chunks remain from the shared counter (none if the first launch has taken
 // them all, and its CTAs then leave at once).  It waits for the clearing of
 // the counter and accumulators that preceded the first launch.
-int launch_pair_n3_rejoin(tcp_ctx *c, cudaStream_t st) {
-    if (!c->n3_rejoin_pending) return TCP_OK;
-    c->n3_rejoin_pending = false;
-    TCP_CUDA(cudaStreamWaitEvent(st, c->ev_pair_ready, 0));
-    void *args[] = {c->n3_rejoin};
-    TCP_CUDA(cudaLaunchKernel(c->n3_rejoin_fn, dim3(c->n3_rejoin_grid), dim3(c->n3_rejoin_threads), args, 0, st));
-    c->launches++;
+int n3_rejoin_launch(N3Rejoin &r, cudaStream_t st, cudaEvent_t ready, long long *launches) {
+    if (!r.pending) return TCP_OK;
+    r.pending = false;
+    TCP_CUDA(cudaStreamWaitEvent(st, ready, 0));
+    void *args[] = {r.args};
+    TCP_CUDA(cudaLaunchKernel(r.fn, dim3(r.grid), dim3(r.threads), args, 0, st));
+    if (launches) ++*launches;
     return TCP_OK;
 }
 
-void n3_free(tcp_ctx *c) {
-    delete c->n3_rejoin;
-    c->n3_rejoin = nullptr;
-    c->n3_rejoin_pending = false;
+int launch_pair_n3_rejoin(tcp_ctx *c, cudaStream_t st) {
+    return n3_rejoin_launch(c->rejoin, st, c->ev_pair_ready, &c->launches);
 }
+
+void n3_rejoin_free(N3Rejoin &r) {
+    delete r.args;
+    r.args = nullptr;
+    r.pending = false;
+}
+
+void n3_free(tcp_ctx *c) { n3_rejoin_free(c->rejoin); }
 
 // ---- batch of replicas -------------------------------------------------------
 // Variants of the batched launch (the batch autotuner picks one per batch):
@@ -892,7 +934,8 @@ int n3_batch_ctas(int num_sms, int v) { return n3_batch_grid(num_sms, std::min(s
 
 int launch_pair_n3_batch(cudaStream_t st, const int4 *xq, int ntot, double *facc, const void *reps_dev, int nrep,
                          long long total, const long long *chunks, unsigned nchunks, double *ur_rep, unsigned *status,
-                         unsigned *counter, int num_sms, bool energy, int variant) {
+                         unsigned *counter, int num_sms, bool energy, int variant, int reserve, N3Rejoin *rejoin,
+                         cudaEvent_t ready) {
     const int v = std::min(std::max(variant, 0), kN3BatchVariants - 1);
     N3Args a;
     std::memset(&a, 0, sizeof a);
@@ -907,17 +950,26 @@ int launch_pair_n3_batch(cudaStream_t st, const int4 *xq, int ntot, double *facc
     a.reps = static_cast<const N3Rep *>(reps_dev);
     a.nrep = nrep;
     a.ur_rep = ur_rep;
-    const int grid = (int)std::min<long long>(n3_batch_grid(num_sms, v), total);
+    const int full = n3_batch_grid(num_sms, v);
+    if (rejoin) rejoin->pending = false;
+    const int res = rejoin && ready ? std::max(reserve, 0) : 0;
+    const int grid = (int)std::min<long long>(std::max(1, full - res), total);
+    const int extra = (int)std::min<long long>(full - grid, total - grid);   // rejoin CTAs
     const int nt = 32 * kBatchVariants[v].W;
     TCP_CUDA(cudaMemsetAsync(facc, 0, sizeof(double) * 3 * (size_t)ntot, st));
     TCP_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
-    if (energy) {
-        TCP_CUDA(cudaMemsetAsync(ur_rep, 0, sizeof(double) * (size_t)nrep, st));
-        kBatchVariants[v].energy<<<grid, nt, 0, st>>>(a);
-    } else {
-        kBatchVariants[v].plain<<<grid, nt, 0, st>>>(a);
+    if (energy) TCP_CUDA(cudaMemsetAsync(ur_rep, 0, sizeof(double) * (size_t)nrep, st));
+    if (res > 0 && extra > 0) {   // the batched kernels add Ur per replica by atomics
+        TCP_CUDA(cudaEventRecord(ready, st));
+        n3_rejoin_set(*rejoin, a, extra, nt,
+                      reinterpret_cast<const void *>(energy ? kBatchVariants[v].energy : kBatchVariants[v].plain));
     }
+    if (energy)
+        kBatchVariants[v].energy<<<grid, nt, 0, st>>>(a);
+    else
+        kBatchVariants[v].plain<<<grid, nt, 0, st>>>(a);
     TCP_CUDA(cudaGetLastError());
+    if (rejoin) rejoin->pending = res > 0 && extra > 0;
     return TCP_OK;
 }
 

@@ -106,6 +106,15 @@ inline double ewald_constant_energy(const tcp_params &p, int nel, int nion, doub
 struct Ctx;
 struct N3Args;
 
+// The CTAs a persistent Newton-3 launch left to the reciprocal chain, launched
+// again with the same arguments on the chain's stream after it (pair_n3.cu)
+struct N3Rejoin {
+    N3Args *args = nullptr;
+    bool pending = false;
+    int grid = 0, threads = 0;
+    const void *fn = nullptr;
+};
+
 }  // namespace tcp
 
 struct tcp_ctx {
@@ -144,10 +153,7 @@ struct tcp_ctx {
     // The reserved CTAs rejoin the Newton-3 launch once the chain is done: a second
     // launch of the same kernel on stream2 after the chain, claiming the remaining
     // chunks from the same counter (pair_n3.cu launch_pair_n3_rejoin)
-    tcp::N3Args *n3_rejoin = nullptr;
-    bool n3_rejoin_pending = false;
-    int n3_rejoin_grid = 0, n3_rejoin_threads = 0;
-    const void *n3_rejoin_fn = nullptr;
+    tcp::N3Rejoin rejoin;
     double *fpart = nullptr;   // [jsplit][3][n]
     double *upart = nullptr;   // energy partial per pair block
     int n_upart = 0;
@@ -271,15 +277,21 @@ int time_pair_with_recip(tcp_ctx *c, int reps, double *ms);   // ctx.cu
 int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf);
 int launch_pair_n3_rejoin(tcp_ctx *c, cudaStream_t st);   // on stream2, after the reciprocal chain
 void n3_free(tcp_ctx *c);
+int n3_rejoin_launch(N3Rejoin &r, cudaStream_t st, cudaEvent_t ready, long long *launches);
+void n3_rejoin_free(N3Rejoin &r);
 int n3_batch_variant_count();
 const char *n3_batch_variant_name(int v);
 int n3_batch_tile(int variant);
 size_t n3_rep_bytes();
 long long n3_batch_fill(void *reps_host, int nrep, const int *off, const int *nel, const int *nion,
                         const PairConsts *pc, int tile);
+// reserve > 0 with a rejoin: that many CTAs are left out of the persistent
+// grid for the reciprocal chain and set up in *rejoin (ready is recorded on st
+// once the launch's counter and accumulators are cleared)
 int launch_pair_n3_batch(cudaStream_t st, const int4 *xq, int ntot, double *facc, const void *reps_dev, int nrep,
                          long long total, const long long *chunks, unsigned nchunks, double *ur_rep, unsigned *status,
-                         unsigned *counter, int num_sms, bool energy, int variant);
+                         unsigned *counter, int num_sms, bool energy, int variant, int reserve = 0,
+                         N3Rejoin *rejoin = nullptr, cudaEvent_t ready = nullptr);
 int n3_batch_ctas(int num_sms, int v);
 void n3_chunk_table(long long total, int ctas, std::vector<long long> &starts);
 int n3_prepare_chunks(tcp_ctx *c);

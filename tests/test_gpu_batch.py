@@ -87,3 +87,37 @@ def test_batch_pair_variants_match_oracle(monkeypatch, variant):
         fo, uro, umo = oracle.Oracle.from_system(s, ei="kelbg").force_total(s.x)
         assert oracle.rms_rel(fb[r], fo) < 2e-6
         assert eb[r]["Ur"] == pytest.approx(uro, rel=2e-5)
+
+
+def test_batch_grid_reserve_and_rejoin(monkeypatch):
+    """The batch autotuner times the batched pair launch with the SPME chains
+    beside it for several grid reserves (the reserved CTAs rejoin the launch
+    after the chains) and keeps the smallest within 0.3 % of the fastest;
+    forced reserves give the same forces and energies."""
+    monkeypatch.delenv("TCP_BATCH_RESERVE", raising=False)
+    ss = systems()
+    params = [T.params_for(s, precision="fp32c", ei="kelbg", recip="spme") for s in ss]
+
+    def run():
+        with T.Batch(params, [s.nel for s in ss], [s.nion for s in ss]) as b:
+            b.EWALD_SELF()
+            for r, s in enumerate(ss):
+                b.upload(r, x=s.x, v=s.v)
+            e = b.force()
+            f = [b.download(r, x=False, v=False)[2] for r in range(len(ss))]
+            b.md_steps(ss[0].dt, 3)
+            x = [b.download(r, v=False, f=False)[0] for r in range(len(ss))]
+            return e, f, x, b.overlap_report()
+
+    e0, f0, x0, (r, cand) = run()
+    assert set(cand) == {0, 16, 32, 64, 128, 256, 512}
+    assert r in cand and cand[r] <= 1.003 * min(cand.values())
+    for forced in ("0", "512"):
+        monkeypatch.setenv("TCP_BATCH_RESERVE", forced)
+        e, f, x, (rr, _) = run()
+        assert rr == int(forced)
+        for k in range(len(ss)):
+            assert oracle.rms_rel(f[k], f0[k]) < 1e-6
+            assert e[k]["Ur"] == pytest.approx(e0[k]["Ur"], rel=1e-6)
+            assert e[k]["Um"] == pytest.approx(e0[k]["Um"], rel=1e-6)
+            assert np.max(np.abs(x[k] - x0[k])) < 1e-6 * ss[k].box

@@ -194,6 +194,26 @@ def test_md_steps_graph_vs_oracle(precision, tol):
     assert e["mv2el"] == pytest.approx(eo["mv2el"], rel=tol)
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32c", 2e-5)])
+def test_md_trajectory_200_steps_vs_oracle(precision, tol):
+    """200 graph-launched steps against the oracle stepped alongside from the
+    same start: positions, velocities and Epot after every 50."""
+    s = make(1024, seed=12, K=16, order=4)
+    o = oracle.Oracle.from_system(s, ei="kelbg")
+    x, v = s.x.copy(), s.v.copy()
+    f, _, _ = o.force_total(x)
+    with ctx_for(s, precision=precision, ei="kelbg", recip="spme") as c:
+        c.upload(f=f)
+        for block in range(4):
+            e = c.md_steps(s.dt, 50)
+            gx, gv, _, _ = c.download()
+            for _ in range(50):
+                eo = o.md_step(x, v, f, s.dt)
+            assert np.max(np.abs(gx - x)) < tol * s.box, block
+            assert oracle.rms_rel(gv, v) < tol, block
+            assert e["Epot"] == pytest.approx(eo["Epot"], rel=10 * tol), block
+
+
 def test_finit_vs_oracle():
     s = make(1024, seed=10, K=16)
     o = oracle.Oracle.from_system(s, ei="deutsch")
@@ -348,13 +368,14 @@ def test_large_fp32c_rows_sample():
     assert np.linalg.norm(f.sum(0)) < 1e-6 * np.abs(f).sum()
 
 
-@pytest.mark.parametrize("variant", list(range(14)))
+@pytest.mark.parametrize("variant", list(range(18)))
 @pytest.mark.parametrize("ei,n", [("kelbg", 2048), ("deutsch", 1536), ("kelbg", 1000)])
 def test_fp32c_kernel_variants(monkeypatch, variant, ei, n):
     """Every real-space kernel the autotuner can pick (0 = ordered pairs,
-    1 = scalar Newton-3, 2..13 = Newton-3 with packed FP32x2 arithmetic,
-    6..13 with the degree-5 Ewald erfc, 12 and 13 with six i-particles per
-    lane) against the oracle, including partial tiles."""
+    1 = scalar Newton-3, 2..17 = Newton-3 with packed FP32x2 arithmetic,
+    6..16 with the degree-5 Ewald erfc, 12 and 13 with six i-particles per
+    lane, 14, 15 and 17 with two warps per CTA, 16 with one) against the
+    oracle, including partial tiles."""
     monkeypatch.setenv("TCP_PAIR_VARIANT", str(variant))
     s = make(n, seed=30 + variant)
     o = oracle.Oracle.from_system(s, ei=ei)
@@ -373,7 +394,7 @@ def test_autotuner_picks_a_timed_variant(monkeypatch):
     with ctx_for(s, precision="fp32c", ei="kelbg", recip="none") as c:
         c.Force_direct_self()
         v, ms = c.autotune_report()
-    assert 0 <= v <= 13
+    assert 0 <= v <= 17
     assert ms[v] > 0 and ms[v] == min(m for m in ms if m > 0)
 
 
@@ -481,7 +502,7 @@ def test_deterministic_flag_is_bitwise_reproducible(precision):
     assert e1["Ur"] == e2["Ur"] and e1["Um"] == e2["Um"]
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 10])
+@pytest.mark.parametrize("variant", [0, 1, 2, 10, 14, 16])
 @pytest.mark.parametrize("r_over_lam", [1e-3, 1e-2, 0.1, 0.3, 0.49, 0.8, 2.0])
 def test_kelbg_close_pair_accuracy(monkeypatch, variant, r_over_lam):
     """One electron and one ion at r = (1e-3 .. 2) lambda: the Kelbg e-i force
@@ -509,7 +530,7 @@ def test_kelbg_close_pair_accuracy(monkeypatch, variant, r_over_lam):
     assert ur == pytest.approx(uo, rel=2e-5, abs=1e-6 * abs(uo) + 1e-12)
 
 
-@pytest.mark.parametrize("variant", [2, 4, 5, 10, 12, 13])
+@pytest.mark.parametrize("variant", [2, 4, 5, 10, 12, 13, 14, 15, 16, 17])
 @pytest.mark.parametrize("nel,nion", [(1, 300), (257, 0), (700, 333), (1030, 2)])
 def test_fp32c_newton3_ragged_species(monkeypatch, variant, nel, nion):
     """Packed Newton-3 variants with a single electron, one species only, and
