@@ -486,6 +486,18 @@ def run_gpu(args, world, rank, local, dist):
     # the reciprocal chain by itself (it runs concurrently with the pair kernel
     # inside a step, on a second stream)
     recip_alone_ms = ctx.time_component(1, 5)
+    # the same steps with the RDF histograms accumulated in the pair sum, as the
+    # reference's Force_direct_self does in every call (force.f90:99-103)
+    ctx.set_flags(T.FLAG_ENERGY | T.FLAG_RDF)
+    ctx.md_steps(s.dt, args.warmup)
+    t_rdf = ctx.time_steps(s.dt, args.steps, flush_l2=True)
+    ctx.set_flags(T.FLAG_ENERGY)
+    rdf_step = {"ms_per_step": t_rdf["step"] / t_rdf["nsteps"],
+                "value": pairs / (t_rdf["step"] / t_rdf["nsteps"] * 1e-3),
+                "pair_kernel_ms": t_rdf["pair"] / t_rdf["nsteps"],
+                "note": "TCP_FLAG_RDF: the ee/ei/ii pair-distance histograms of force.f90:99-103 binned in "
+                        "the pair kernel at every step (the headline steps leave them off, as the library "
+                        "does unless the caller asks)"}
 
     # FP64 drop-in step (few steps: FP64 issue rate of GB300 is ~1/64 of FP32)
     ctx64.md_steps(s.dt, 1)
@@ -627,6 +639,7 @@ def run_gpu(args, world, rank, local, dist):
         "fp64": {"ms_per_step": step64_ms, "value": pairs / (step64_ms * 1e-3), "steps": args.fp64_steps,
                  "speedup_fp32c_over_fp64": step64_ms / step_ms},
         "recip_fp64_option": recip_fp64,
+        "rdf_every_step": rdf_step,
         "force_error": ferr,
         "energy_error": eerr,
         "energies_initial": {"Ur": e0["Ur"], "Um": e0["Um"], "Uo": e0["Uo"]},

@@ -201,9 +201,11 @@ __device__ __forceinline__ float2 erfc_poly2(float2 t) {
 // type (the ordered-pair kernels add 1 from each side), in a CTA histogram.
 // Branch-free on the common path: a pair that does not count adds to its
 // lane's spare slot (kRdfSpare + lane, never flushed), so every lane issues
-// the same atomic.  Pairs whose FP32 r/dx or r^2 lies near a bin edge or rc
-// take the exact test of the fixed-point separation (rdf_exact_bin), so the
-// counts equal those of exact arithmetic on the fixed-point positions.
+// the same atomic (a predicated atomic, skipping the ~half of the pairs past
+// rc = L/2, made the RDF step 10 % slower).  Pairs whose FP32 r/dx or r^2 lies
+// near a bin edge or rc take the exact test of the fixed-point separation
+// (rdf_exact_bin), so the counts equal those of exact arithmetic on the
+// fixed-point positions.
 constexpr int kRdfSpare = 3 * kNbin;
 struct N3Rdf {
     unsigned *hist;
@@ -690,13 +692,21 @@ static const N3Variant kVariants[] = {
     // the 2-warp form with the degree-6 erfc (any alpha rc)
     {pair_n3_kernel<true, 4, 2, 8, false, 1, 2>, pair_n3_kernel<false, 4, 2, 8, false, 1, 2>, 4, 2,
      "n3_r4_u2_w2b8_x2"},
+    {pair_n3_kernel<true, 4, 4, 8, false, 1, 2, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 4, 8, false, 1, 2, false, kErfcH5>, 4, 2, "n3_r4_u4_w2b8_x2_p5", true},
 };
 constexpr int kN3Variants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 // Forms that also accumulate the RDF histograms (steps with TCP_FLAG_RDF,
-// which the reference accumulates in every force call): the two best packed
-// forms of the variants above; TCP_RDF_VARIANT=k picks one (default 0).
+// which the reference accumulates in every force call): the 2-warp form of
+// the variants above with the degree-5 (0) or degree-6 (1) erfc, and two
+// 8-warp forms, the second of which (3) is the default: RDF steps of 5.50 ms
+// at N = 65,536 against 5.55 (2) and 5.72 (0); TCP_RDF_VARIANT=k picks one.
 static const N3Variant kRdfVariants[] = {
+    {pair_n3_kernel<true, 4, 2, 8, false, 1, 2, true, kErfcH5>,
+     pair_n3_kernel<false, 4, 2, 8, false, 1, 2, true, kErfcH5>, 4, 2, "n3_r4_u2_w2b8_x2_p5_rdf", true},
+    {pair_n3_kernel<true, 4, 2, 8, false, 1, 2, true>, pair_n3_kernel<false, 4, 2, 8, false, 1, 2, true>, 4, 2,
+     "n3_r4_u2_w2b8_x2_rdf"},
     {pair_n3_kernel<true, 4, 1, 3, false, 2, 8, true>, pair_n3_kernel<false, 4, 1, 3, false, 2, 8, true>, 4, 8,
      "n3_r4_u1_b3_x2l_rdf"},
     {pair_n3_kernel<true, 4, 1, 2, false, 1, 8, true>, pair_n3_kernel<false, 4, 1, 2, false, 1, 8, true>, 4, 8,
@@ -799,8 +809,9 @@ static void n3_rejoin_set(N3Rejoin &r, const N3Args &a, int grid, int threads, c
 }
 
 int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf) {
-    int rv = 0;
+    int rv = 3;   // the 8-warp 2-CTA form: the fastest RDF step measured, no spills
     if (const char *forced = getenv("TCP_RDF_VARIANT")) rv = std::min(std::max(atoi(forced), 0), kN3RdfVariants - 1);
+    if (kRdfVariants[rv].erfc5 && !c->pc.erfc5_ok) rv = 1;
     const int v = std::min(std::max(c->pair_variant, 1), kN3Variants);
     const N3Variant &K = rdf ? kRdfVariants[rv] : kVariants[v - 1];
     const int tile = 32 * K.R * K.W;

@@ -109,8 +109,10 @@ __global__ void scan_block_kernel(const int *__restrict__ count, int nbins, int 
 
 // One CTA for up to kScanBlock * kScanPer bins: each thread sums its run of
 // consecutive bins, the CTA scans the run sums, and each thread writes its
-// run's exclusive prefix; start[nbins] = total.
-constexpr int kScanPer = 32;
+// run's exclusive prefix; start[nbins] = total.  Above 8,192 bins the runs
+// are long enough that the three-launch scan is faster (16,384 bins: 17.7
+// against 8.4 us under ncu).
+constexpr int kScanPer = 8;
 __global__ void __launch_bounds__(kScanBlock) scan_single_kernel(const int *__restrict__ count, int nbins,
                                                                  int *__restrict__ start, int total) {
     __shared__ int ws[32];
@@ -657,7 +659,7 @@ static SpmeArgs spme_args(const tcp_ctx *c) {
 int launch_bin_sort(cudaStream_t st, int n, int nbins, const SpreadBins &b) {
     const int threads = 256;
     const int sblocks = (nbins + kScanBlock - 1) / kScanBlock;
-    const bool single = nbins <= kScanBlock * kScanPer;   // meshes up to 181 x 181 columns: one launch
+    const bool single = nbins <= kScanBlock * kScanPer;   // up to 8,192 (y, z) columns: one launch
     if (single) {
         scan_single_kernel<<<1, kScanBlock, 0, st>>>(b.count, nbins, b.start, n);
     } else {

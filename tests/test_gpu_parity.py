@@ -368,14 +368,14 @@ def test_large_fp32c_rows_sample():
     assert np.linalg.norm(f.sum(0)) < 1e-6 * np.abs(f).sum()
 
 
-@pytest.mark.parametrize("variant", list(range(18)))
+@pytest.mark.parametrize("variant", list(range(19)))
 @pytest.mark.parametrize("ei,n", [("kelbg", 2048), ("deutsch", 1536), ("kelbg", 1000)])
 def test_fp32c_kernel_variants(monkeypatch, variant, ei, n):
     """Every real-space kernel the autotuner can pick (0 = ordered pairs,
-    1 = scalar Newton-3, 2..17 = Newton-3 with packed FP32x2 arithmetic,
-    6..16 with the degree-5 Ewald erfc, 12 and 13 with six i-particles per
-    lane, 14, 15 and 17 with two warps per CTA, 16 with one) against the
-    oracle, including partial tiles."""
+    1 = scalar Newton-3, 2..18 = Newton-3 with packed FP32x2 arithmetic,
+    6..16 and 18 with the degree-5 Ewald erfc, 12 and 13 with six
+    i-particles per lane, 14, 15, 17 and 18 with two warps per CTA, 16 with
+    one) against the oracle, including partial tiles."""
     monkeypatch.setenv("TCP_PAIR_VARIANT", str(variant))
     s = make(n, seed=30 + variant)
     o = oracle.Oracle.from_system(s, ei=ei)
@@ -394,7 +394,7 @@ def test_autotuner_picks_a_timed_variant(monkeypatch):
     with ctx_for(s, precision="fp32c", ei="kelbg", recip="none") as c:
         c.Force_direct_self()
         v, ms = c.autotune_report()
-    assert 0 <= v <= 17
+    assert 0 <= v <= 18
     assert ms[v] > 0 and ms[v] == min(m for m in ms if m > 0)
 
 
@@ -615,7 +615,7 @@ def snap_to_grid(x, box):
     return (m / 2.0 ** 32 - 0.5) * box
 
 
-@pytest.mark.parametrize("rdf_variant", [0, 1])
+@pytest.mark.parametrize("rdf_variant", [0, 1, 2, 3])
 def test_fp32c_newton3_rdf_histograms(monkeypatch, rdf_variant):
     """RDF counts of the packed Newton-3 forms (+2 per unique pair inside rc,
     force.f90:99-103) equal the FP64 oracle's bin for bin: pairs whose FP32
