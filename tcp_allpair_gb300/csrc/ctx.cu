@@ -492,7 +492,8 @@ static int species_range(const tcp_ctx *c, int species, int &first, int &count) 
 }
 
 // records -> device arrays, queued on the stream (no wait)
-static int enqueue_upload(tcp_ctx *c, int first, int count, const RecSpan &rs, long stride) {
+static int enqueue_upload(tcp_ctx *c, int first, int count, const RecSpan &rs, long stride,
+                          cudaStream_t st = nullptr) {
     if (count == 0 || !rs.base) return TCP_OK;
     const unsigned char *src = reinterpret_cast<const unsigned char *>(rs.base);
     int rc;
@@ -500,15 +501,36 @@ static int enqueue_upload(tcp_ctx *c, int first, int count, const RecSpan &rs, l
         if ((rc = ensure_stage(c, rs.span))) return rc;
         TCP_CUDA(cudaMemcpyAsync(c->d_stage, rs.base, rs.span, cudaMemcpyHostToDevice, c->stream));
         src = c->d_stage;
+        st = nullptr;
     }
-    return launch_extract(c, src, first, count, stride, rs.off[0], rs.off[1], rs.off[2]);   // refreshes xq, xd
+    return launch_extract(c, src, first, count, stride, rs.off[0], rs.off[1], rs.off[2], st);   // refreshes xq, xd
 }
 
 // device arrays -> records the device writes in place (host_direct), queued
-static int enqueue_download_direct(tcp_ctx *c, int first, int count, const RecSpan &rs, long stride) {
+static int enqueue_download_direct(tcp_ctx *c, int first, int count, const RecSpan &rs, long stride,
+                                   cudaStream_t st = nullptr) {
     if (count == 0 || !rs.base) return TCP_OK;
     return launch_scatter(c, reinterpret_cast<unsigned char *>(const_cast<char *>(rs.base)), first, count, stride,
-                          rs.off[0], rs.off[1], rs.off[2], c->f);
+                          rs.off[0], rs.off[1], rs.off[2], c->f, st);
+}
+
+// The two species' records read or written concurrently over the host link:
+// the electrons' on the main stream, the ions' on stream2 between a fork and a
+// join (one launch alone leaves most SMs waiting on the link)
+static int records_both(tcp_ctx *c, const RecSpan *rs, long el_stride, long ion_stride, bool upload) {
+    int rc;
+    TCP_CUDA(cudaEventRecord(c->ev_fork, c->stream));
+    TCP_CUDA(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
+    if (upload) {
+        if ((rc = enqueue_upload(c, 0, c->nel, rs[0], el_stride))) return rc;
+        if ((rc = enqueue_upload(c, c->nel, c->nion, rs[1], ion_stride, c->stream2))) return rc;
+    } else {
+        if ((rc = enqueue_download_direct(c, 0, c->nel, rs[0], el_stride))) return rc;
+        if ((rc = enqueue_download_direct(c, c->nel, c->nion, rs[1], ion_stride, c->stream2))) return rc;
+    }
+    TCP_CUDA(cudaEventRecord(c->ev_join, c->stream2));
+    TCP_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+    return TCP_OK;
 }
 
 // device arrays -> records through the pinned stage; waits for the device
@@ -791,15 +813,16 @@ int tcp_md_steps_records(tcp_ctx *c, double dt, int nsteps, double *el_xx, doubl
     // every argument is checked before anything is queued
     if ((rc = record_span(c->nel, el_xx, el_xv, el_ff, el_stride, rs[0]))) return rc;
     if ((rc = record_span(c->nion, ion_xx, ion_xv, ion_ff, ion_stride, rs[1]))) return rc;
-    if ((rc = enqueue_upload(c, 0, c->nel, rs[0], el_stride))) return rc;
-    if ((rc = enqueue_upload(c, c->nel, c->nion, rs[1], ion_stride))) return rc;
+    if (c->host_direct) {
+        if ((rc = records_both(c, rs, el_stride, ion_stride, true))) return rc;
+    } else {
+        if ((rc = enqueue_upload(c, 0, c->nel, rs[0], el_stride))) return rc;
+        if ((rc = enqueue_upload(c, c->nel, c->nion, rs[1], ion_stride))) return rc;
+    }
     if ((rc = ensure_graph(c, dt))) return rc;
     for (int s = 0; s < nsteps; ++s)
         if ((rc = launch_step(c, dt))) return rc;
-    if (c->host_direct) {       // written in place before the one wait below
-        if ((rc = enqueue_download_direct(c, 0, c->nel, rs[0], el_stride))) return rc;
-        if ((rc = enqueue_download_direct(c, c->nel, c->nion, rs[1], ion_stride))) return rc;
-    }
+    if (c->host_direct && (rc = records_both(c, rs, el_stride, ion_stride, false))) return rc;   // before the one wait below
     if ((rc = sync_scalars(c))) return rc;
     if (!c->host_direct) {
         if ((rc = download_staged(c, 0, c->nel, el_xx, el_xv, el_ff, el_stride))) return rc;

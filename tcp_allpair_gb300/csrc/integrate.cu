@@ -556,21 +556,22 @@ int launch_reduce(tcp_ctx *c, int mask, int pass) {
 }
 
 int launch_extract(tcp_ctx *c, const unsigned char *src, int first, int count, long stride, long off_x, long off_v,
-                   long off_f) {
+                   long off_f, cudaStream_t st) {
     const RecFields fl = rec_fields(off_x, off_v, off_f);
     if (fl.nf == 0 || count <= 0) return TCP_OK;
-    extract_kernel<<<nblocks(count), kIntThreads, 0, c->stream>>>(src, stride, fl, count, first, int_args(c));
+    extract_kernel<<<nblocks(count), kIntThreads, 0, st ? st : c->stream>>>(src, stride, fl, count, first,
+                                                                             int_args(c));
     c->launches++;
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;
 }
 
 int launch_scatter(tcp_ctx *c, unsigned char *dst, int first, int count, long stride, long off_x, long off_v,
-                   long off_f, const double *fsrc) {
+                   long off_f, const double *fsrc, cudaStream_t st) {
     const RecFields fl = rec_fields(off_x, off_v, off_f);
     if (fl.nf == 0 || count <= 0) return TCP_OK;
     const long long words = (long long)count * 3 * fl.nf;
-    scatter_kernel<<<(unsigned)((words + kIntThreads - 1) / kIntThreads), kIntThreads, 0, c->stream>>>(
+    scatter_kernel<<<(unsigned)((words + kIntThreads - 1) / kIntThreads), kIntThreads, 0, st ? st : c->stream>>>(
         dst, stride, fl, count, first, c->n, c->x, c->v, fsrc);
     c->launches++;
     TCP_CUDA(cudaGetLastError());

@@ -317,9 +317,9 @@ int launch_remove_rigid(tcp_ctx *c);
 int launch_kick2(tcp_ctx *c, double dt, bool remove_net, bool apply_thermo, bool vdf, int *final_pass);
 int launch_reduce(tcp_ctx *c, int mask, int pass);
 int launch_extract(tcp_ctx *c, const unsigned char *src, int first, int count, long stride, long off_x, long off_v,
-                   long off_f);
+                   long off_f, cudaStream_t st = nullptr);   // st: c->stream when null
 int launch_scatter(tcp_ctx *c, unsigned char *dst, int first, int count, long stride, long off_x, long off_v,
-                   long off_f, const double *fsrc);
+                   long off_f, const double *fsrc, cudaStream_t st = nullptr);
 int launch_pack(tcp_ctx *c, int first, int count, bool x, bool v, bool f, bool frec, int *nf);
 int launch_fp32_peak(int device, double *tffma);
 
