@@ -343,8 +343,8 @@ class Batch:
     def autotune_report(self):
         """(chosen batched pair-kernel variant, per-variant ms measured by the batch autotuner)."""
         v = C.c_int()
-        ms = np.zeros(8)
-        self._chk(self.lib.tcp_batch_autotune_report(self.h, C.byref(v), ms.ctypes.data_as(C.POINTER(C.c_double)), 8),
+        ms = np.zeros(16)
+        self._chk(self.lib.tcp_batch_autotune_report(self.h, C.byref(v), ms.ctypes.data_as(C.POINTER(C.c_double)), 16),
                   "tcp_batch_autotune_report")
         return v.value, ms
 

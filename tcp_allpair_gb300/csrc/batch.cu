@@ -31,7 +31,9 @@ namespace tcp {
 struct BRep {
     int off, n, nel;
     double L[3];
+    double iL[3], KL[3];     // 1/L, K/L (the kernels multiply: GB300's FP64 division is slow)
     double xm[2], q[2];      // masses, scaled charges
+    double ixm[2];           // 1/xm
     int K[3], Kh;
     long long mesh_off, half_off;
     int bin_off, grp_off;    // first spreading bin (K2 K3 per replica) and first 8-row group
@@ -47,13 +49,6 @@ struct BAcc {
     double *ur, *um, *mv0, *mv1, *fsum;
 };
 
-__device__ __forceinline__ int fixed_coord_b(double x, double L) {
-    double t = x / L + 0.5;
-    t -= floor(t);
-    return (int)(unsigned)((unsigned long long)llrint(t * 4294967296.0) & 0xffffffffull);
-}
-
-__device__ __forceinline__ double wrap_b(double x, double L) { return x - L * round(x / L); }
 
 // add v to acc[key] with one atomic per warp when the warp shares the key
 __device__ __forceinline__ void keyed_add(double *acc, int key, double v) {
@@ -80,15 +75,15 @@ __global__ void b_vverlet1_kernel(const BParticles a, double dt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.ntot) return;
     const BRep &R = a.reps[a.rep_of[i]];
-    const double xm = (i - R.off) < R.nel ? R.xm[0] : R.xm[1];
+    const double ixm = (i - R.off) < R.nel ? R.ixm[0] : R.ixm[1];
     int q[3];
     for (int k = 0; k < 3; ++k) {
         const size_t o = (size_t)k * a.ntot + i;
-        const double vk = a.v[o] + 0.5 * dt * a.f[o] / xm;
+        const double vk = a.v[o] + 0.5 * dt * a.f[o] * ixm;
         a.v[o] = vk;
-        const double y = wrap_b(a.x[o] + dt * vk, R.L[k]);
+        const double y = wrap_box(a.x[o] + dt * vk, R.L[k], R.iL[k]);
         a.x[o] = y;
-        q[k] = fixed_coord_b(y, R.L[k]);
+        q[k] = fixed_coord(y, R.iL[k]);
     }
     a.xq[i] = make_int4(q[0], q[1], q[2], 0);
 }
@@ -97,8 +92,8 @@ __global__ void b_refresh_kernel(const BParticles a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.ntot) return;
     const BRep &R = a.reps[a.rep_of[i]];
-    a.xq[i] = make_int4(fixed_coord_b(a.x[i], R.L[0]), fixed_coord_b(a.x[(size_t)a.ntot + i], R.L[1]),
-                        fixed_coord_b(a.x[2 * (size_t)a.ntot + i], R.L[2]), 0);
+    a.xq[i] = make_int4(fixed_coord(a.x[i], R.iL[0]), fixed_coord(a.x[(size_t)a.ntot + i], R.iL[1]),
+                        fixed_coord(a.x[2 * (size_t)a.ntot + i], R.iL[2]), 0);
 }
 
 // ---- atomic-free spreading, cell-sorted per replica ------------------------------
@@ -118,7 +113,7 @@ __global__ void b_bin_count_kernel(const BParticles a, SpreadBins bins) {
     int base[3];
 #pragma unroll
     for (int d = 1; d < 3; ++d) {
-        const double u = (double)R.K[d] * (a.x[(size_t)d * a.ntot + i] + R.L[d] * .5) / R.L[d];
+        const double u = (a.x[(size_t)d * a.ntot + i] + R.L[d] * .5) * R.KL[d];
         base[d] = wrapi((int)trunc(u) - (P - 3), R.K[d]);
     }
     const int bin = R.bin_off + base[1] + R.K[1] * base[2];
@@ -137,7 +132,7 @@ __global__ void b_bin_weights_kernel(const BParticles a, SpreadBins bins) {
     int base[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double u = (double)R.K[d] * (a.x[(size_t)d * a.ntot + i] + R.L[d] * .5) / R.L[d];
+        const double u = (a.x[(size_t)d * a.ntot + i] + R.L[d] * .5) * R.KL[d];
         spline_w<P, float>(u, W, dW);
 #pragma unroll
         for (int j = 0; j < P; ++j) w[d * P + j] = W[j];
@@ -291,7 +286,7 @@ __global__ void b_gather_kernel(const BParticles a, const float *__restrict__ ph
     float W[3][P], dW[3][P];
     int base[3];
     for (int d = 0; d < 3; ++d) {
-        const double u = (double)R.K[d] * (a.x[(size_t)d * a.ntot + i] + R.L[d] * .5) / R.L[d];
+        const double u = (a.x[(size_t)d * a.ntot + i] + R.L[d] * .5) * R.KL[d];
         spline_w<P, float>(u, W[d], dW[d]);
         base[d] = wrapi((int)trunc(u) - (P - 3), R.K[d]);
     }
@@ -321,9 +316,9 @@ __global__ void b_gather_kernel(const BParticles a, const float *__restrict__ ph
         iz = iz + 1 == R.K[2] ? 0 : iz + 1;
     }
     const double coef = kEps / (kPi * R.V);
-    a.frec[i] = -coef * q * (double)gx * ((double)R.K[0] / R.L[0]);
-    a.frec[(size_t)a.ntot + i] = -coef * q * (double)gy * ((double)R.K[1] / R.L[1]);
-    a.frec[2 * (size_t)a.ntot + i] = -coef * q * (double)gz * ((double)R.K[2] / R.L[2]);
+    a.frec[i] = -coef * q * (double)gx * R.KL[0];
+    a.frec[(size_t)a.ntot + i] = -coef * q * (double)gy * R.KL[1];
+    a.frec[2 * (size_t)a.ntot + i] = -coef * q * (double)gz * R.KL[2];
 }
 
 // f = real-space + reciprocal (SPME_SUM); per-replica sum f (REMOVE_RIGIDMTN)
@@ -354,13 +349,13 @@ __global__ void b_kick2_kernel(const BParticles a, double dt, const double *__re
     const int s = (ic - R.off) < R.nel ? 0 : 1;
     double mv2 = 0.0;
     if (valid) {
-        const double xm = R.xm[s];
+        const double xm = R.xm[s], ixm = R.ixm[s], in = 1.0 / (double)R.n;
         double vv[3];
         for (int k = 0; k < 3; ++k) {
             const size_t o = (size_t)k * a.ntot + i;
-            const double fk = a.f[o] - fsum[3 * r + k] / (double)R.n;
+            const double fk = a.f[o] - fsum[3 * r + k] * in;
             a.f[o] = fk;
-            vv[k] = a.v[o] + 0.5 * dt * fk / xm;
+            vv[k] = a.v[o] + 0.5 * dt * fk * ixm;
             a.v[o] = vv[k];
         }
         mv2 = (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]) * xm;
@@ -426,7 +421,7 @@ struct tcp_batch {
     std::vector<tcp::PairConsts> pcs;   // per-replica pair constants (the table is refilled per variant)
     int pair_variant = 0;               // batched Newton-3 variant (batch autotuner)
     bool tuned = false;
-    double variant_ms[8] = {};
+    double variant_ms[16] = {};
     double *acc = nullptr;              // accumulator block
     double *h_acc = nullptr;            // pinned copy
     unsigned *status = nullptr, *counter = nullptr;
@@ -681,7 +676,7 @@ static int b_autotune(tcp_batch *b) {
     TCP_CUDA(cudaEventCreate(&e1));
     double best = 1e300;
     int best_v = 0, rc = TCP_OK;
-    for (int v = 0; v < nv && v < 8 && !rc; ++v) {
+    for (int v = 0; v < nv && v < 16 && !rc; ++v) {
         if ((rc = b_fill_n3(b, v))) break;
         rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, b->n3_chunks, b->n3_nchunks, A.ur,
                                   b->status, b->counter, b->num_sms, true, v);
@@ -937,11 +932,15 @@ int tcp_batch_ewald_self(tcp_batch *b, double *Uo) {
         R.nel = b->nel[r];
         for (int d = 0; d < 3; ++d) {
             R.L[d] = p.box[d];
+            R.iL[d] = 1.0 / p.box[d];
             R.K[d] = p.K[d];
+            R.KL[d] = (double)p.K[d] / p.box[d];
         }
         R.Kh = p.K[0] / 2 + 1;
         R.xm[0] = p.xm[0];
         R.xm[1] = p.xm[1];
+        R.ixm[0] = 1.0 / p.xm[0];
+        R.ixm[1] = 1.0 / p.xm[1];
         R.q[0] = s * p.q[0];
         R.q[1] = s * p.q[1];
         R.V = p.box[0] * p.box[1] * p.box[2];
@@ -970,7 +969,10 @@ int tcp_batch_ewald_self(tcp_batch *b, double *Uo) {
             }
         }
         const long long half = (long long)R.Kh * p.K[1] * p.K[2];
-        blk0[r + 1] = blk0[r] + (int)std::max<long long>(1, std::min<long long>((half + 255) / 256, 512));
+        // a few blocks per replica: each block adds its energy partial to the
+        // replica's Um with one FP64 atomic, and hundreds of atomics on one
+        // address serialise (512 blocks a replica: 80 us for the 64 replicas)
+        blk0[r + 1] = blk0[r] + (int)std::max<long long>(1, std::min<long long>((half + 255) / 256, 16));
     }
     b->infl_blocks = blk0[nrep];
     b->pcs = pcs;
@@ -1096,7 +1098,7 @@ int tcp_batch_md_steps(tcp_batch *b, double dt, int nsteps, tcp_energies *e) {
 int tcp_batch_autotune_report(tcp_batch *b, int *variant, double *ms, int nmax) {
     if (!b) return set_error(TCP_ERR_BAD_PARAM, "batch is NULL");
     if (variant) *variant = b->pair_variant;
-    for (int k = 0; ms && k < nmax && k < 8; ++k) ms[k] = b->variant_ms[k];
+    for (int k = 0; ms && k < nmax && k < 16; ++k) ms[k] = b->variant_ms[k];
     return TCP_OK;
 }
 

@@ -84,6 +84,15 @@ __device__ __forceinline__ float ex2_approx(float x) {
 // difference of two coordinates is the minimum-image separation.  Every
 // entry point quantises positions through this function, so that they all
 // see the same grid.
+// x - L DNINT(x/L) (vverlet.f90:153); x/L from the reciprocal with one FMA
+// correction (the quotient to within rounding of the divided value): GB300's
+// FP64 division costs dozens of FP64 operations
+__device__ __forceinline__ double wrap_box(double x, double L, double iL) {
+    double q = x * iL;
+    q = fma(fma(-q, L, x), iL, q);
+    return x - L * round(q);
+}
+
 __device__ __forceinline__ int fixed_coord(double x, double iL) {
     double t = fma(x, iL, 0.5);
     t -= floor(t);

@@ -54,13 +54,7 @@ __device__ __forceinline__ void store_pos(const IntArgs &a, int i, double x0, do
     }
 }
 
-// x - L DNINT(x/L) (vverlet.f90:153); x/L from the reciprocal with one FMA
-// correction (the quotient to within rounding of the divided value)
-__device__ __forceinline__ double wrap(double x, double L, double iL) {
-    double q = x * iL;
-    q = fma(fma(-q, L, x), iL, q);
-    return x - L * round(q);
-}
+__device__ __forceinline__ double wrap(double x, double L, double iL) { return wrap_box(x, L, iL); }
 
 __global__ void refresh_kernel(const IntArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -79,11 +73,10 @@ __global__ void shift_kernel(const IntArgs a, double sdt) {
 }
 
 // VVerletNotemp1 (vverlet.f90:148-167) / VVerletStoch1 (vverlet.f90:34-55)
-__global__ void vverlet1_kernel(const IntArgs a, double dt, double alpha_lgv, int stoch) {
+__global__ void vverlet1_kernel(const IntArgs a, double dt, double hdm0, double hdm1, double alpha_lgv, int stoch) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    const double xm = i < a.nel ? a.xm0 : a.xm1;
-    const double hdm = 0.5 * dt / xm;                  // dt/(2m)
+    const double hdm = i < a.nel ? hdm0 : hdm1;        // dt/(2m), divided on the host
     const double damp = 1.0 - alpha_lgv * hdm;
     const double L[3] = {a.L0, a.L1, a.L2}, iL[3] = {a.iL0, a.iL1, a.iL2};
     double y[3];
@@ -132,6 +125,7 @@ __device__ __forceinline__ void gauss3(uint64_t seed, long long step, int i, dou
 struct KickArgs {
     IntArgs a;
     double dt;
+    double hdm0, hdm1;       // dt/(2m) per species (host-divided: the same correctly rounded value)
     int thermo;              // TCP_THERMO_*
     int remove_net;          // subtract sum(f)/n first (REMOVE_RIGIDMTN fused)
     const double *fsum_part; // [3][nbf]
@@ -174,7 +168,7 @@ __global__ void kick2_kernel(const KickArgs k) {
     if (i < a.n) {
         const int s = i < a.nel ? 0 : 1;
         const double xm = s == 0 ? a.xm0 : a.xm1;
-        const double hdm = 0.5 * k.dt / xm;               // dt/(2m)
+        const double hdm = s == 0 ? k.hdm0 : k.hdm1;      // dt/(2m)
         const double idamp = k.thermo == TCP_THERMO_STOCH ? 1.0 / (1.0 + k.alpha_lgv * hdm) : 1.0;
         double vv[3];
         double eta[3] = {0.0, 0.0, 0.0};
@@ -476,7 +470,8 @@ int launch_shift(tcp_ctx *c, double sdt) {
 }
 
 int launch_vverlet1(tcp_ctx *c, double dt, double) {
-    vverlet1_kernel<<<nblocks(c->n), kIntThreads, 0, c->stream>>>(int_args(c), dt, c->p.alpha_lgv,
+    vverlet1_kernel<<<nblocks(c->n), kIntThreads, 0, c->stream>>>(int_args(c), dt, 0.5 * dt / c->p.xm[0],
+                                                                  0.5 * dt / c->p.xm[1], c->p.alpha_lgv,
                                                                   c->p.thermo == TCP_THERMO_STOCH);
     c->launches++;
     TCP_CUDA(cudaGetLastError());
@@ -509,6 +504,8 @@ int launch_kick2(tcp_ctx *c, double dt, bool remove_net, bool apply_thermo, bool
     KickArgs k;
     k.a = int_args(c);
     k.dt = dt;
+    k.hdm0 = 0.5 * dt / c->p.xm[0];
+    k.hdm1 = 0.5 * dt / c->p.xm[1];
     k.thermo = c->p.thermo;
     const bool rescale = apply_thermo && (c->p.thermo == TCP_THERMO_ISOKIN || c->p.thermo == TCP_THERMO_BEREND);
     if (!apply_thermo && k.thermo != TCP_THERMO_STOCH) k.thermo = TCP_THERMO_NOTEMP;

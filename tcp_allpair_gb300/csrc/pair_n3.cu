@@ -909,6 +909,13 @@ static const N3BatchVariant kBatchVariants[] = {
     {pair_n3_kernel<true, 2, 2, 3, true, 2>, pair_n3_kernel<false, 2, 2, 3, true, 2>, 2, 8, "b_r2_u2_b3_x2l"},
     {pair_n3_kernel<true, 2, 2, 6, true, 2, 4>, pair_n3_kernel<false, 2, 2, 6, true, 2, 4>, 2, 4, "b_r2_u2_w4b6_x2l"},
     {pair_n3_kernel<true, 4, 1, 6, true, 2, 4>, pair_n3_kernel<false, 4, 1, 6, true, 2, 4>, 4, 4, "b_r4_u1_w4b6_x2l"},
+    // 1- and 2-warp CTAs: 128- and 256-particle i-tiles
+    {pair_n3_kernel<true, 4, 2, 8, true, 1, 2>, pair_n3_kernel<false, 4, 2, 8, true, 1, 2>, 4, 2, "b_r4_u2_w2b8_x2"},
+    {pair_n3_kernel<true, 2, 2, 12, true, 2, 2>, pair_n3_kernel<false, 2, 2, 12, true, 2, 2>, 2, 2,
+     "b_r2_u2_w2b12_x2l"},
+    {pair_n3_kernel<true, 2, 2, 12, true, 1, 2>, pair_n3_kernel<false, 2, 2, 12, true, 1, 2>, 2, 2,
+     "b_r2_u2_w2b12_x2"},
+    {pair_n3_kernel<true, 4, 2, 16, true, 1, 1>, pair_n3_kernel<false, 4, 2, 16, true, 1, 1>, 4, 1, "b_r4_u2_w1b16_x2"},
 };
 constexpr int kN3BatchVariants = sizeof(kBatchVariants) / sizeof(kBatchVariants[0]);
 

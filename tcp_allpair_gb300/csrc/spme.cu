@@ -33,6 +33,7 @@ struct SpmeArgs {
     int nel, n;
     double q0, q1;       // scaled charges per species
     double box0, box1, box2;
+    double kl0, kl1, kl2;   // K/L: the step's kernels multiply (GB300's FP64 division is slow)
     int K1, K2, K3;
 };
 
@@ -65,11 +66,12 @@ __global__ void spme_bin_count_kernel(const SpmeArgs a, SpreadBins b) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= a.n) return;
     const double L[3] = {a.box0, a.box1, a.box2};
+    const double KL[3] = {a.kl0, a.kl1, a.kl2};
     const int K[3] = {a.K1, a.K2, a.K3};
     int base[3];
 #pragma unroll
     for (int d = 1; d < 3; ++d) {
-        const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];   // :700-702
+        const double u = (a.x[(size_t)d * a.n + m] + L[d] * .5) * KL[d];   // force.f90:700-702, K/L precomputed
         base[d] = wrapi((int)trunc(u) - (P - 3), K[d]);
     }
     const int bin = base[1] + a.K2 * base[2];
@@ -213,13 +215,14 @@ __global__ void spme_bin_weights_kernel(const SpmeArgs a, SpreadBins b) {
     if (pos >= a.n) return;
     const int m = b.list[pos];
     const double L[3] = {a.box0, a.box1, a.box2};
+    const double KL[3] = {a.kl0, a.kl1, a.kl2};
     const int K[3] = {a.K1, a.K2, a.K3};
     T *w = static_cast<T *>(b.ew) + (size_t)pos * 3 * P;
     T W[P], dW[P];
     int base[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];
+        const double u = (a.x[(size_t)d * a.n + m] + L[d] * .5) * KL[d];
         spline_w<P, T>(u, W, dW);
 #pragma unroll
         for (int j = 0; j < P; ++j) w[d * P + j] = W[j];
@@ -365,12 +368,13 @@ __global__ void spme_gather_kernel(const SpmeArgs a, const T *__restrict__ phi, 
     const int m = order ? order[t] : t;
     const double q = m < a.nel ? a.q0 : a.q1;
     const double L[3] = {a.box0, a.box1, a.box2};
+    const double KL[3] = {a.kl0, a.kl1, a.kl2};
     const int K[3] = {a.K1, a.K2, a.K3};
     T W[3][P], dW[3][P];
     int base[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const double u = (double)K[d] * (a.x[(size_t)d * a.n + m] + L[d] * .5) / L[d];
+        const double u = (a.x[(size_t)d * a.n + m] + L[d] * .5) * KL[d];
         spline_w<P, T>(u, W[d], dW[d]);
         base[d] = wrapi((int)trunc(u) - (P - 3), K[d]);    // first mesh index, wrapped once
     }
@@ -399,9 +403,9 @@ __global__ void spme_gather_kernel(const SpmeArgs a, const T *__restrict__ phi, 
         iz = iz + 1 == a.K3 ? 0 : iz + 1;
     }
     // F = -eps/(pi V) q (K_d/L_d) sum dW W W phi
-    frec[m] = -coef * q * (double)gx * ((double)a.K1 / a.box0);
-    frec[(size_t)a.n + m] = -coef * q * (double)gy * ((double)a.K2 / a.box1);
-    frec[2 * (size_t)a.n + m] = -coef * q * (double)gz * ((double)a.K3 / a.box2);
+    frec[m] = -coef * q * (double)gx * a.kl0;
+    frec[(size_t)a.n + m] = -coef * q * (double)gy * a.kl1;
+    frec[2 * (size_t)a.n + m] = -coef * q * (double)gz * a.kl2;
 }
 
 // FP32C influence multiply.  Energy terms are summed in FP32 per thread (a
@@ -651,6 +655,9 @@ static SpmeArgs spme_args(const tcp_ctx *c) {
     a.K1 = c->K1;
     a.K2 = c->K2;
     a.K3 = c->K3;
+    a.kl0 = (double)c->K1 / c->p.box[0];
+    a.kl1 = (double)c->K2 / c->p.box[1];
+    a.kl2 = (double)c->K3 / c->p.box[2];
     return a;
 }
 

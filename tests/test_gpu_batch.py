@@ -68,7 +68,7 @@ def test_batch_rejects_unsupported():
         T.Batch([p], [s.nel], [s.nion])
 
 
-@pytest.mark.parametrize("variant", list(range(8)))
+@pytest.mark.parametrize("variant", list(range(12)))
 def test_batch_pair_variants_match_oracle(monkeypatch, variant):
     """Every batched real-space variant (TCP_BATCH_VARIANT) against the oracle's
     total force and the energies."""
