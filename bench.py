@@ -515,10 +515,12 @@ def run_gpu(args, world, rank, local, dist):
         cr.md_steps(s.dt, args.warmup)
         tr = cr.time_steps(s.dt, args.steps, flush_l2=True)
         recip64_alone_ms = cr.time_component(1, 5)
+        r64_reserve, r64_reserve_ms = cr.overlap_report()
     r64_ms = tr["step"] / tr["nsteps"]
     recip_fp64 = {"ms_per_step": r64_ms, "value": pairs / (r64_ms * 1e-3),
                   "pair_kernel_ms": tr["pair"] / tr["nsteps"], "recip_concurrent_wall": tr["recip"] / tr["nsteps"],
                   "recip_alone_ms": recip64_alone_ms, "step_time_ratio_vs_fp32c_recip": r64_ms / step_ms,
+                  "grid_reserve": r64_reserve, "reserve_ms": {k: round(v, 4) for k, v in r64_reserve_ms.items()},
                   "note": "TCP_PREC_FP32C_R64: the FP32C real-space sum with the SPME spread, transforms, "
                           "influence multiply and gather in FP64, on the second stream beside the pair kernel"}
 

@@ -201,9 +201,9 @@ static int mark(tcp_ctx *c, int k) { return mark_on(c, k, c->stream); }
 
 // Phase marks ev[0..4] (event nodes in the graph): 0 step start, 1 after
 // the first half kick, 2 end of the reciprocal chain (on stream2, concurrent
-// with the pair kernel), 3 end of the real-space sum (the pair launch, the
-// reserved CTAs that rejoin it after the chain, and the chain itself), 4 step
-// end.
+// with the pair kernel), 3 end of the pair launch on the main stream (the
+// reserved CTAs that rejoin it after the chain drain the same chunk counter,
+// so they end within a chunk of it), 4 step end.
 static int step_chain(tcp_ctx *c, double dt, bool apply, int *pass) {
     int rc;
     if ((rc = mark(c, 0))) return rc;
@@ -216,8 +216,8 @@ static int step_chain(tcp_ctx *c, double dt, bool apply, int *pass) {
         return rc;
     }
     if ((rc = launch_pair(c, energy_on(c), (c->flags & TCP_FLAG_RDF) != 0))) return rc;
-    if ((rc = recip_join(c))) return rc;
     if ((rc = mark(c, 3))) return rc;
+    if ((rc = recip_join(c))) return rc;
     if ((rc = launch_force_finalize(c, c->p.reciprocal != TCP_RECIP_NONE))) return rc;
     if ((rc = launch_kick2(c, dt, true, apply, (c->flags & TCP_FLAG_VDF) != 0, pass))) return rc;
     if ((rc = launch_reduce(c, (energy_on(c) ? kRedUr : 0) | kRedMv2, *pass))) return rc;
@@ -906,9 +906,8 @@ int tcp_time_steps(tcp_ctx *c, double dt, int nsteps, int flush_l2, double *out)
         if (flush_l2) TCP_CUDA(cudaMemsetAsync(c->l2_flush, s & 0xff, c->l2_flush_bytes, c->stream));
         if ((rc = launch_step(c, dt))) return rc;
         TCP_CUDA(cudaEventSynchronize(c->ev[4]));
-        // step; first kick (0-1); reciprocal (1-2, stream2); pair (1-3: the pair
-        // launch with the reciprocal chain beside it, up to the join of both
-        // streams); epilogue (from the later of 2 and 3 to 4)
+        // step; first kick (0-1); reciprocal (1-2, stream2); pair (1-3, concurrent
+        // with the reciprocal chain); epilogue (from the later of 2 and 3 to 4)
         float t[5], e2, e3;
         cudaEventElapsedTime(&t[0], c->ev[0], c->ev[4]);
         cudaEventElapsedTime(&t[1], c->ev[0], c->ev[1]);
