@@ -218,21 +218,39 @@ struct N3Rdf {
 
 __device__ __forceinline__ int idiff_i(int a, int b) { return (int)((unsigned)a - (unsigned)b); }
 
-// r: FP32 distance (meaningless where the caller replaced r^2 by 1); r2: the
-// pair's FP32 r^2; ok: the FP32 cut-off and index mask; valid: the index mask
+// The bins of the two pairs of a packed step.  r: FP32 distances (meaningless
+// where the caller replaced r^2 by 1); r2: the pairs' FP32 r^2; ok: the FP32
+// cut-off and index masks; v: the index masks.  floor(r/dx) comes from packed
+// FP32 arithmetic without a float->int conversion: (tb - 1/2) + 1.5 2^23
+// rounds tb - 1/2 to an integer held in the low mantissa bits, which is
+// floor(tb) unless tb lies within rounding of an integer; there, and within
+// 2^-12 of any bin edge or of rc, the exact test of the fixed-point separation
+// decides (two conversions per pair on the slow pipe had cost more than the
+// pair's own arithmetic).
+constexpr float kRdfRound = 12582912.0f;   // 1.5 * 2^23
+constexpr int kRdfRoundBits = 0x4B400000;  // the bit pattern of kRdfRound
 template <bool RDF>
-__device__ __forceinline__ void rdf_add(const N3Rdf &h, float r, float r2, bool ok, bool valid, const int4 &xa,
-                                        const int4 &xj) {
+__device__ __forceinline__ void rdf_add2(const N3Rdf &h, float2 r, float2 r2, bool ok0, bool ok1, bool v0, bool v1,
+                                         const int4 &xa, const int4 &xb, const int4 &xj) {
     if (RDF) {
-        const float tb = r * h.inv_dx;
-        int bin = (int)tb;
-        if (valid && rdf_near_edge(tb, bin, r2, h.rc2)) {
-            if (!ok) bin = (int)(sqrtf(r2) * h.inv_dx);
-            bin = rdf_exact_bin<true>(idiff_i(xa.x, xj.x), idiff_i(xa.y, xj.y), idiff_i(xa.z, xj.z), h.E, h.pt,
-                                      nullptr, bin, ok);
+        const float2 tb = __fmul2_rn(r, make_float2(h.inv_dx, h.inv_dx));
+        const float2 m = __fadd2_rn(__fadd2_rn(tb, make_float2(-0.5f, -0.5f)), make_float2(kRdfRound, kRdfRound));
+        const float2 binf = __fadd2_rn(m, make_float2(-kRdfRound, -kRdfRound));
+        const float2 fr = __ffma2_rn(binf, make_float2(-1.0f, -1.0f), tb);   // tb - floor estimate, exact
+        int bin0 = __float_as_int(m.x) - kRdfRoundBits, bin1 = __float_as_int(m.y) - kRdfRoundBits;
+        if (v0 && rdf_near_fr(fr.x, r2.x, h.rc2)) {
+            if (!ok0) bin0 = (int)(sqrtf(r2.x) * h.inv_dx);
+            bin0 = rdf_exact_bin<true>(idiff_i(xa.x, xj.x), idiff_i(xa.y, xj.y), idiff_i(xa.z, xj.z), h.E, h.pt,
+                                       nullptr, bin0, ok0);
         }
-        const int idx = (ok && bin <= kNdist) ? h.hoff + bin : kRdfSpare + (int)(threadIdx.x & 31);
-        atomicAdd(&h.hist[idx], 2u);
+        if (v1 && rdf_near_fr(fr.y, r2.y, h.rc2)) {
+            if (!ok1) bin1 = (int)(sqrtf(r2.y) * h.inv_dx);
+            bin1 = rdf_exact_bin<true>(idiff_i(xb.x, xj.x), idiff_i(xb.y, xj.y), idiff_i(xb.z, xj.z), h.E, h.pt,
+                                       nullptr, bin1, ok1);
+        }
+        const int spare = kRdfSpare + (int)(threadIdx.x & 31);
+        atomicAdd(&h.hist[(ok0 && bin0 <= kNdist) ? h.hoff + bin0 : spare], 2u);
+        atomicAdd(&h.hist[(ok1 && bin1 <= kNdist) ? h.hoff + bin1 : spare], 2u);
     }
 }
 
@@ -249,10 +267,7 @@ __device__ __forceinline__ float2 n3_pair_x2(const PairConsts &c, float2 r2, boo
     const float2 rinv = make_float2(rsqrt_approx(r2s.x), rsqrt_approx(r2s.y));
     const float2 rinv_m = make_float2(ok0 ? rinv.x : 0.0f, ok1 ? rinv.y : 0.0f);
     const float2 r = __fmul2_rn(r2s, rinv);
-    if (RDF) {
-        rdf_add<RDF>(*h, r.x, r2.x, ok0, v0, *xa, *xj);
-        rdf_add<RDF>(*h, r.y, r2.y, ok1, v1, *xb, *xj);
-    }
+    if (RDF) rdf_add2<RDF>(*h, r, r2, ok0, ok1, v0, v1, *xa, *xb, *xj);
     const float2 ta = __ffma2_rn(f2(PD == kErfcH6 ? c.u_p_alpha : c.u_p_alpha5), r, f2(1.0f));
     const float2 t = make_float2(rcp_approx(ta.x), rcp_approx(ta.y));
     const float2 ea = __fmul2_rn(f2(c.u_c_exp), r2s);
