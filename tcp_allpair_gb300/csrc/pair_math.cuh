@@ -40,11 +40,6 @@ __device__ __forceinline__ bool rdf_near_edge(float tb, int bin, float r2, float
     return fr < kRdfEdge || fr > 1.0f - kRdfEdge || fabsf(r2 - rc2) < kRdfEdge * rc2;
 }
 
-// the same test from the fractional part fr = tb - floor(tb)
-__device__ __forceinline__ bool rdf_near_fr(float fr, float r2, float rc2) {
-    return fabsf(fr - 0.5f) > 0.5f - kRdfEdge || fabsf(r2 - rc2) < kRdfEdge * rc2;
-}
-
 // erfc(x) = exp(-x^2) t Q(t), t = 1/(1 + kErfcP x): the factor of the
 // reciprocal argument (host constants p_alpha = kErfcP alpha, p_lam = kErfcP/lambda).
 constexpr double kErfcP = 0.36;

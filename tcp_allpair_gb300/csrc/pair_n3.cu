@@ -202,7 +202,10 @@ __device__ __forceinline__ float2 erfc_poly2(float2 t) {
 // Branch-free on the common path: a pair that does not count adds to its
 // lane's spare slot (kRdfSpare + lane, never flushed), so every lane issues
 // the same atomic (a predicated atomic, skipping the ~half of the pairs past
-// rc = L/2, made the RDF step 10 % slower).  Pairs whose FP32 r/dx or r^2 lies
+// rc = L/2, made the RDF step 10 % slower).  Measured at N = 65,536: the
+// binning with its atomics costs 0.5 ms of a 2.6 ms step, the exact test of
+// the pairs near a bin edge (taken in ~2 % of the steps) 2.6 ms when inlined
+// behind a per-lane branch, 1.7 ms behind a warp vote, 1.1 ms out of line.  Pairs whose FP32 r/dx or r^2 lies
 // near a bin edge or rc take the exact test of the fixed-point separation
 // (rdf_exact_bin), so the counts equal those of exact arithmetic on the
 // fixed-point positions.
@@ -217,6 +220,19 @@ struct N3Rdf {
 };
 
 __device__ __forceinline__ int idiff_i(int a, int b) { return (int)((unsigned)a - (unsigned)b); }
+
+// The exact bin test of one pair, out of line: inlined, its 64-bit integer
+// arithmetic and table loops weighed on the register allocation and
+// scheduling of every rotation step although a step takes it rarely.  bin:
+// the FP32 estimate, or -1 when the pair lies past rc in FP32 (the estimate is
+// then taken from r2).  Returns bin << 1 | (r < rc exactly).
+__device__ __noinline__ int rdf_exact_call(int d0, int d1, int d2, const RdfEdges *E, int t, int bin, float r2,
+                                           float inv_dx) {
+    if (bin < 0) bin = (int)(sqrtf(r2) * inv_dx);
+    bool ok;
+    bin = rdf_exact_bin<true>(d0, d1, d2, E, t, nullptr, bin, ok);
+    return (bin << 1) | (ok ? 1 : 0);
+}
 
 // The bins of the two pairs of a packed step.  r: FP32 distances (meaningless
 // where the caller replaced r^2 by 1); r2: the pairs' FP32 r^2; ok: the FP32
@@ -238,15 +254,28 @@ __device__ __forceinline__ void rdf_add2(const N3Rdf &h, float2 r, float2 r2, bo
         const float2 binf = __fadd2_rn(m, make_float2(-kRdfRound, -kRdfRound));
         const float2 fr = __ffma2_rn(binf, make_float2(-1.0f, -1.0f), tb);   // tb - floor estimate, exact
         int bin0 = __float_as_int(m.x) - kRdfRoundBits, bin1 = __float_as_int(m.y) - kRdfRoundBits;
-        if (v0 && rdf_near_fr(fr.x, r2.x, h.rc2)) {
-            if (!ok0) bin0 = (int)(sqrtf(r2.x) * h.inv_dx);
-            bin0 = rdf_exact_bin<true>(idiff_i(xa.x, xj.x), idiff_i(xa.y, xj.y), idiff_i(xa.z, xj.z), h.E, h.pt,
-                                       nullptr, bin0, ok0);
-        }
-        if (v1 && rdf_near_fr(fr.y, r2.y, h.rc2)) {
-            if (!ok1) bin1 = (int)(sqrtf(r2.y) * h.inv_dx);
-            bin1 = rdf_exact_bin<true>(idiff_i(xb.x, xj.x), idiff_i(xb.y, xj.y), idiff_i(xb.z, xj.z), h.E, h.pt,
-                                       nullptr, bin1, ok1);
+        // the exact test where the estimate may be wrong: a bin edge within
+        // 2^-12 of a pair inside rc, or rc itself within 2^-12; a pair clearly
+        // past rc counts nothing whatever its bin
+        // (one warp vote per step: a per-lane branch in every rotation step,
+        // rarely taken, had cost as much as the pair arithmetic by breaking
+        // the step's straight-line code)
+        const float nrc = kRdfEdge * h.rc2;
+        const bool x0 = v0 && (fabsf(r2.x - h.rc2) < nrc || (ok0 && fabsf(fr.x - 0.5f) > 0.5f - kRdfEdge));
+        const bool x1 = v1 && (fabsf(r2.y - h.rc2) < nrc || (ok1 && fabsf(fr.y - 0.5f) > 0.5f - kRdfEdge));
+        if (__any_sync(0xffffffffu, x0 || x1)) {
+            if (x0) {
+                const int pk = rdf_exact_call(idiff_i(xa.x, xj.x), idiff_i(xa.y, xj.y), idiff_i(xa.z, xj.z), h.E,
+                                              h.pt, ok0 ? bin0 : -1, r2.x, h.inv_dx);
+                bin0 = pk >> 1;
+                ok0 = (pk & 1) != 0;
+            }
+            if (x1) {
+                const int pk = rdf_exact_call(idiff_i(xb.x, xj.x), idiff_i(xb.y, xj.y), idiff_i(xb.z, xj.z), h.E,
+                                              h.pt, ok1 ? bin1 : -1, r2.y, h.inv_dx);
+                bin1 = pk >> 1;
+                ok1 = (pk & 1) != 0;
+            }
         }
         const int spare = kRdfSpare + (int)(threadIdx.x & 31);
         atomicAdd(&h.hist[(ok0 && bin0 <= kNdist) ? h.hoff + bin0 : spare], 2u);
@@ -714,9 +743,10 @@ constexpr int kN3Variants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 // Forms that also accumulate the RDF histograms (steps with TCP_FLAG_RDF,
 // which the reference accumulates in every force call): the 2-warp form of
-// the variants above with the degree-5 (0) or degree-6 (1) erfc, and two
-// 8-warp forms, the second of which (3) is the default: RDF steps of 5.50 ms
-// at N = 65,536 against 5.55 (2) and 5.72 (0); TCP_RDF_VARIANT=k picks one.
+// the variants above with the degree-5 (0, the default where alpha rc allows
+// it) or degree-6 (1, the default otherwise) erfc, and two 8-warp forms: RDF
+// steps of 4.25 / 4.30 / 4.59 / 4.52 ms at N = 65,536; TCP_RDF_VARIANT=k picks
+// one.
 static const N3Variant kRdfVariants[] = {
     {pair_n3_kernel<true, 4, 2, 8, false, 1, 2, true, kErfcH5>,
      pair_n3_kernel<false, 4, 2, 8, false, 1, 2, true, kErfcH5>, 4, 2, "n3_r4_u2_w2b8_x2_p5_rdf", true},
@@ -824,7 +854,7 @@ static void n3_rejoin_set(N3Rejoin &r, const N3Args &a, int grid, int threads, c
 }
 
 int launch_pair_n3(tcp_ctx *c, bool energy, bool rdf) {
-    int rv = 3;   // the 8-warp 2-CTA form: the fastest RDF step measured, no spills
+    int rv = c->pc.erfc5_ok ? 0 : 1;   // the 2-warp forms: the fastest RDF steps measured
     if (const char *forced = getenv("TCP_RDF_VARIANT")) rv = std::min(std::max(atoi(forced), 0), kN3RdfVariants - 1);
     if (kRdfVariants[rv].erfc5 && !c->pc.erfc5_ok) rv = 1;
     const int v = std::min(std::max(c->pair_variant, 1), kN3Variants);
