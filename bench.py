@@ -405,6 +405,7 @@ def run_batch_leg(T, args, device):
         b.force()
         bvar, bms = b.autotune_report()
         bres, bres_ms = b.overlap_report()
+        bname = b.variant_name(bvar)
         b.md_steps(dt, args.warmup)
         ms_batch = b.time_steps(dt, args.steps)
     ctxs = []
@@ -424,13 +425,24 @@ def run_batch_leg(T, args, device):
     ms_loop = (time.perf_counter() - t0) * 1e3 / args.steps
     for c in ctxs:
         c.close()
+    # the batched pair launch against the FFMA peak (its variants use the degree-6 erfc)
+    peak = T.fp32_peak(device) * 1e12
+    pair_ms = float(bms[bvar])
+    roof = {"bound": "fp32", "kernel": f"pair_n3_kernel batched (variant {bvar}: {bname})",
+            "recipe": f"{RECIPE_N3} FP32/ALU-pipe ops + {RECIPE_SFU_OPS} SFU ops per unique pair",
+            "pair_kernel_alone_ms": pair_ms, "peak": peak / 1e12, "unit": "Top/s",
+            "achieved": RECIPE_N3 * pairs / (pair_ms * 1e-3) / 1e12,
+            "frac_alone": RECIPE_N3 * pairs / (pair_ms * 1e-3) / peak,
+            "note": "the autotuner's time of the batched pair launch alone (no chains beside it); "
+                    "replicas of 256-4096 particles per species have many masked diagonal items"}
     return {"metric": "aggregate pair-int/s, batched replicas", "workload": f"batch{len(ss)}_n512-8192",
             "value": pairs / (ms_batch * 1e-3), "unit": "pair-int/s", "ms_per_step": ms_batch,
             "loop_single_contexts": {"value": pairs / (ms_loop * 1e-3), "ms_per_step": ms_loop},
             "speedup_batch_over_loop": ms_loop / ms_batch, "replicas": len(ss),
             "particles": sum(s.n for s in ss), "steps": args.steps, "warmup": args.warmup,
             "batch_variant": int(bvar), "batch_variant_ms": [round(float(x), 4) for x in bms if x > 0],
-            "grid_reserve": bres, "reserve_ms": {k: round(v, 4) for k, v in bres_ms.items()}}
+            "grid_reserve": bres, "reserve_ms": {k: round(v, 4) for k, v in bres_ms.items()},
+            "roofline": roof}
 
 
 def run_gpu(args, world, rank, local, dist):

@@ -273,6 +273,9 @@ int tcp_batch_md_steps(tcp_batch *b, double dt, int nsteps, tcp_energies *e);
 /* The batched real-space kernel the batch autotuner picked (variant index) and
  * the per-candidate times in ms (0 when not timed), up to nmax entries. */
 int tcp_batch_autotune_report(tcp_batch *b, int *variant, double *ms, int nmax);
+/* Name of batched real-space variant `variant` (NULL past the last): "b_", i-particles per
+ * lane, unroll, warps and CTAs per SM, packed forms ("x2", "x2l"). */
+const char *tcp_batch_variant_name(int variant);
 /* The CTAs the batch autotuner left out of the persistent batched pair grid so
  * that the replicas' SPME chains, which run beside it, find room on the SMs
  * (they join the pair launch's work once the chains are done); the candidates

@@ -348,6 +348,11 @@ class Batch:
                   "tcp_batch_autotune_report")
         return v.value, ms
 
+    def variant_name(self, variant):
+        """Name of batched real-space variant `variant` (tcp_batch_variant_name)."""
+        n = self.lib.tcp_batch_variant_name(int(variant))
+        return n.decode() if n else None
+
     def overlap_report(self):
         """(CTAs left out of the batched pair grid for the SPME chains, {candidate: ms of the
         pair launch with the chains beside it})."""

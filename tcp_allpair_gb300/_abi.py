@@ -83,6 +83,7 @@ SIGNATURES = {
     "tcp_time_steps": (C.c_int, [_CTX, C.c_double, C.c_int, C.c_int, _P]),
     "tcp_autotune_report": (C.c_int, [_CTX, C.POINTER(C.c_int), _P, C.c_int]),
     "tcp_pair_variant_name": (C.c_char_p, [C.c_int]),
+    "tcp_batch_variant_name": (C.c_char_p, [C.c_int]),
     "tcp_overlap_report": (C.c_int, [_CTX, C.POINTER(C.c_int), C.POINTER(C.c_int), _P, C.c_int]),
     "tcp_launch_count": (C.c_int, [_CTX, C.POINTER(C.c_longlong)]),
     "tcp_fp32_peak": (C.c_int, [C.c_int, _P]),

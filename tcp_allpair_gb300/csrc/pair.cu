@@ -1100,6 +1100,12 @@ extern "C" const char *tcp_pair_variant_name(int variant) {
     return n3_variant_name(variant);
 }
 
+extern "C" const char *tcp_batch_variant_name(int variant) {
+    using namespace tcp;
+    if (variant < 0 || variant >= n3_batch_variant_count()) return nullptr;
+    return n3_batch_variant_name(variant);
+}
+
 extern "C" int tcp_autotune_report(tcp_ctx *c, int *variant, double *ms, int nmax) {
     using namespace tcp;
     if (!c) return set_error(TCP_ERR_BAD_PARAM, "ctx is NULL");

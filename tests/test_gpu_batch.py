@@ -81,8 +81,9 @@ def test_batch_pair_variants_match_oracle(monkeypatch, variant):
             b.upload(r, x=s.x, v=s.v)
         eb = b.force()
         chosen, _ = b.autotune_report()
+        name = b.variant_name(chosen)
         fb = [b.download(r, x=False, v=False)[2] for r in range(len(ss))]
-    assert chosen == variant
+    assert chosen == variant and name.startswith("b_r")
     for r, s in enumerate(ss):
         fo, uro, umo = oracle.Oracle.from_system(s, ei="kelbg").force_total(s.x)
         assert oracle.rms_rel(fb[r], fo) < 2e-6
