@@ -425,14 +425,15 @@ def run_batch_leg(T, args, device):
     ms_loop = (time.perf_counter() - t0) * 1e3 / args.steps
     for c in ctxs:
         c.close()
-    # the batched pair launch against the FFMA peak (its variants use the degree-6 erfc)
+    # the batched pair launch against the FFMA peak
     peak = T.fp32_peak(device) * 1e12
     pair_ms = float(bms[bvar])
+    recipe = RECIPE_N3_P5 if bname.endswith("_p5") else RECIPE_N3
     roof = {"bound": "fp32", "kernel": f"pair_n3_kernel batched (variant {bvar}: {bname})",
-            "recipe": f"{RECIPE_N3} FP32/ALU-pipe ops + {RECIPE_SFU_OPS} SFU ops per unique pair",
+            "recipe": f"{recipe} FP32/ALU-pipe ops + {RECIPE_SFU_OPS} SFU ops per unique pair",
             "pair_kernel_alone_ms": pair_ms, "peak": peak / 1e12, "unit": "Top/s",
-            "achieved": RECIPE_N3 * pairs / (pair_ms * 1e-3) / 1e12,
-            "frac_alone": RECIPE_N3 * pairs / (pair_ms * 1e-3) / peak,
+            "achieved": recipe * pairs / (pair_ms * 1e-3) / 1e12,
+            "frac_alone": recipe * pairs / (pair_ms * 1e-3) / peak,
             "note": "the autotuner's time of the batched pair launch alone (no chains beside it); "
                     "replicas of 256-4096 particles per species have many masked diagonal items"}
     return {"metric": "aggregate pair-int/s, batched replicas", "workload": f"batch{len(ss)}_n512-8192",

@@ -664,8 +664,12 @@ static int b_autotune(tcp_batch *b) {
     if (b->tuned) return TCP_OK;
     b->tuned = true;
     const int nv = n3_batch_variant_count();
+    bool erfc5_ok = true;   // the degree-5 erfc variants need it in every replica
+    for (const PairConsts &pc : b->pcs) erfc5_ok = erfc5_ok && pc.erfc5_ok;
     if (const char *forced = getenv("TCP_BATCH_VARIANT")) {
-        if (int rc = b_fill_n3(b, std::min(std::max(atoi(forced), 0), nv - 1))) return rc;
+        int v = std::min(std::max(atoi(forced), 0), nv - 1);
+        if (n3_batch_variant_erfc5(v) && !erfc5_ok) v = 0;
+        if (int rc = b_fill_n3(b, v)) return rc;
         return b_choose_reserve(b);
     }
     const BAcc A = acc_of(b);
@@ -677,6 +681,7 @@ static int b_autotune(tcp_batch *b) {
     double best = 1e300;
     int best_v = 0, rc = TCP_OK;
     for (int v = 0; v < nv && v < 16 && !rc; ++v) {
+        if (n3_batch_variant_erfc5(v) && !erfc5_ok) continue;   // ms stays 0: not timed
         if ((rc = b_fill_n3(b, v))) break;
         rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, b->n3_chunks, b->n3_nchunks, A.ur,
                                   b->status, b->counter, b->num_sms, true, v);

@@ -944,6 +944,7 @@ struct N3BatchVariant {
     N3Kernel energy, plain;
     int R, W;
     const char *name;
+    bool erfc5 = false;   // degree-5 Ewald erfc: only where every replica's alpha rc allows it
 };
 static const N3BatchVariant kBatchVariants[] = {
     {pair_n3_kernel<true, 2, 2, 2, true>, pair_n3_kernel<false, 2, 2, 2, true>, 2, 8, "b_r2_u2_b2"},
@@ -961,10 +962,16 @@ static const N3BatchVariant kBatchVariants[] = {
     {pair_n3_kernel<true, 2, 2, 12, true, 1, 2>, pair_n3_kernel<false, 2, 2, 12, true, 1, 2>, 2, 2,
      "b_r2_u2_w2b12_x2"},
     {pair_n3_kernel<true, 4, 2, 16, true, 1, 1>, pair_n3_kernel<false, 4, 2, 16, true, 1, 1>, 4, 1, "b_r4_u2_w1b16_x2"},
+    // the degree-5 Ewald erfc (every replica with alpha rc <= kErfc5Xmax)
+    {pair_n3_kernel<true, 2, 2, 12, true, 2, 2, false, kErfcH5>,
+     pair_n3_kernel<false, 2, 2, 12, true, 2, 2, false, kErfcH5>, 2, 2, "b_r2_u2_w2b12_x2l_p5", true},
+    {pair_n3_kernel<true, 4, 2, 8, true, 1, 2, false, kErfcH5>,
+     pair_n3_kernel<false, 4, 2, 8, true, 1, 2, false, kErfcH5>, 4, 2, "b_r4_u2_w2b8_x2_p5", true},
 };
 constexpr int kN3BatchVariants = sizeof(kBatchVariants) / sizeof(kBatchVariants[0]);
 
 int n3_batch_variant_count() { return kN3BatchVariants; }
+bool n3_batch_variant_erfc5(int v) { return kBatchVariants[std::min(std::max(v, 0), kN3BatchVariants - 1)].erfc5; }
 const char *n3_batch_variant_name(int v) { return kBatchVariants[std::min(std::max(v, 0), kN3BatchVariants - 1)].name; }
 int n3_batch_tile(int v) {
     const N3BatchVariant &k = kBatchVariants[std::min(std::max(v, 0), kN3BatchVariants - 1)];

@@ -280,6 +280,7 @@ void n3_free(tcp_ctx *c);
 int n3_rejoin_launch(N3Rejoin &r, cudaStream_t st, cudaEvent_t ready, long long *launches);
 void n3_rejoin_free(N3Rejoin &r);
 int n3_batch_variant_count();
+bool n3_batch_variant_erfc5(int v);   // the variant needs every replica's PairConsts::erfc5_ok
 const char *n3_batch_variant_name(int v);
 int n3_batch_tile(int variant);
 size_t n3_rep_bytes();

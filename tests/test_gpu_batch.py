@@ -68,7 +68,7 @@ def test_batch_rejects_unsupported():
         T.Batch([p], [s.nel], [s.nion])
 
 
-@pytest.mark.parametrize("variant", list(range(12)))
+@pytest.mark.parametrize("variant", list(range(14)))
 def test_batch_pair_variants_match_oracle(monkeypatch, variant):
     """Every batched real-space variant (TCP_BATCH_VARIANT) against the oracle's
     total force and the energies."""
@@ -86,6 +86,37 @@ def test_batch_pair_variants_match_oracle(monkeypatch, variant):
     assert chosen == variant and name.startswith("b_r")
     for r, s in enumerate(ss):
         fo, uro, umo = oracle.Oracle.from_system(s, ei="kelbg").force_total(s.x)
+        assert oracle.rms_rel(fb[r], fo) < 2e-6
+        assert eb[r]["Ur"] == pytest.approx(uro, rel=2e-5)
+
+
+def test_batch_degree5_erfc_needs_every_replica(monkeypatch):
+    """The degree-5 erfc variants are tuned and forced only when every
+    replica's alpha rc is within the fit's range; one replica beyond it keeps
+    the whole batch on the degree-6 variants."""
+    ss = systems()[:2]
+    ss.append(T.make_system(600, gamma=1.0, lam=0.5, seed=77, alpha_rc=3.8, K=16, order=4))
+    params = [T.params_for(s, precision="fp32c", ei="kelbg", recip="spme") for s in ss]
+
+    def run():
+        with T.Batch(params, [s.nel for s in ss], [s.nion for s in ss]) as b:
+            b.EWALD_SELF()
+            for r, s in enumerate(ss):
+                b.upload(r, x=s.x, v=s.v)
+            eb = b.force()
+            chosen, ms = b.autotune_report()
+            fb = [b.download(r, x=False, v=False)[2] for r in range(len(ss))]
+            return chosen, b.variant_name(chosen), ms, eb, fb
+
+    monkeypatch.delenv("TCP_BATCH_VARIANT", raising=False)
+    chosen, name, ms, _, _ = run()
+    assert not name.endswith("_p5")
+    assert ms[12] == 0 and ms[13] == 0 and all(m > 0 for m in ms[:12])
+    monkeypatch.setenv("TCP_BATCH_VARIANT", "13")
+    chosen, name, _, eb, fb = run()
+    assert chosen == 0
+    for r, s in enumerate(ss):
+        fo, uro, _ = oracle.Oracle.from_system(s, ei="kelbg").force_total(s.x)
         assert oracle.rms_rel(fb[r], fo) < 2e-6
         assert eb[r]["Ur"] == pytest.approx(uro, rel=2e-5)
 
