@@ -406,8 +406,11 @@ def run_batch_leg(T, args, device):
         bvar, bms = b.autotune_report()
         bres, bres_ms = b.overlap_report()
         bname = b.variant_name(bvar)
+        b_names = [b.variant_name(v) for v in range(len(bms))]
         b.md_steps(dt, args.warmup)
-        ms_batch = b.time_steps(dt, args.steps)
+        tb = b.time_steps(dt, args.steps, flush_l2=True)
+        ms_batch = tb["step"] / tb["nsteps"]
+        phases = {k: round(tb[k] / tb["nsteps"], 4) for k in ("vverlet1", "recip", "pair", "epilogue")}
     ctxs = []
     for p_, s in zip(params, ss):
         c = T.Context(p_, s.nel, s.nion, device=device)
@@ -441,7 +444,9 @@ def run_batch_leg(T, args, device):
             "loop_single_contexts": {"value": pairs / (ms_loop * 1e-3), "ms_per_step": ms_loop},
             "speedup_batch_over_loop": ms_loop / ms_batch, "replicas": len(ss),
             "particles": sum(s.n for s in ss), "steps": args.steps, "warmup": args.warmup,
-            "batch_variant": int(bvar), "batch_variant_ms": [round(float(x), 4) for x in bms if x > 0],
+            "l2": "flushed before each timed step", "phases_ms": phases,
+            "batch_variant": int(bvar),
+            "batch_variant_ms": {b_names[v]: round(float(x), 4) for v, x in enumerate(bms) if x > 0},
             "grid_reserve": bres, "reserve_ms": {k: round(v, 4) for k, v in bres_ms.items()},
             "roofline": roof}
 

@@ -283,8 +283,12 @@ const char *tcp_batch_variant_name(int variant);
  * the join (ms, 0 when not timed), up to nmax entries.  TCP_BATCH_RESERVE=k
  * forces k. */
 int tcp_batch_overlap_report(tcp_batch *b, int *reserve, int *candidates, double *ms, int nmax);
-/* Mean device time of one batched step over nsteps graph replays (CUDA events). */
-int tcp_batch_time_steps(tcp_batch *b, double dt, int nsteps, double *ms_per_step);
+/* Device time of nsteps batched steps, one graph replay each, with the L2
+ * cache overwritten before each when flush_l2 is set: out[6] = summed ms of
+ * the step, the first half kick, the SPME chains (beside the pair launch),
+ * the pair launch, the epilogue after the later of the two, and the step
+ * count (CUDA events recorded inside the step graph). */
+int tcp_batch_time_steps(tcp_batch *b, double dt, int nsteps, int flush_l2, double *out);
 
 /* ---- derivatives ---------------------------------------------------------
  * No counterpart in the reference (it computes no derivatives): the analytic

@@ -335,10 +335,14 @@ class Batch:
     def md_steps(self, dt, nsteps):
         return self._energies(self.lib.tcp_batch_md_steps, C.c_double(dt), C.c_int(nsteps))
 
-    def time_steps(self, dt, nsteps):
-        ms = C.c_double()
-        self._chk(self.lib.tcp_batch_time_steps(self.h, dt, nsteps, C.byref(ms)), "tcp_batch_time_steps")
-        return ms.value
+    def time_steps(self, dt, nsteps, flush_l2=True):
+        """Per-step CUDA-event timing of the batched step: dict of summed ms per phase
+        (the SPME chains run beside the pair launch)."""
+        out = np.zeros(6)
+        self._chk(self.lib.tcp_batch_time_steps(self.h, dt, nsteps, int(flush_l2),
+                                                out.ctypes.data_as(C.POINTER(C.c_double))), "tcp_batch_time_steps")
+        keys = ("step", "vverlet1", "recip", "pair", "epilogue", "nsteps")
+        return dict(zip(keys, out.tolist()))
 
     def autotune_report(self):
         """(chosen batched pair-kernel variant, per-variant ms measured by the batch autotuner)."""

@@ -404,6 +404,9 @@ struct tcp_batch {
     cudaStream_t stream2 = nullptr;     // the SPME chain of a step, beside the pair launch
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t ev_ready = nullptr;     // the pair launch's counter and accumulators are cleared
+    cudaEvent_t ev[5] = {};             // phase marks of a step (event nodes in the step graph)
+    void *l2_flush = nullptr;           // written between timed steps (tcp_batch_time_steps)
+    size_t l2_flush_bytes = 0;
     // CTAs of the persistent pair grid left to the SPME chains; they rejoin the
     // pair launch on stream2 once the chains are done (chosen by the autotuner)
     int pair_reserve = 0;
@@ -557,7 +560,23 @@ static int b_recip_fork(tcp_batch *b, const BAcc &A) {
     return TCP_OK;
 }
 
+// Phase mark k of a step: an event-record node while the stream is captured,
+// a plain record otherwise (the External flag is valid during capture only).
+// 0 step start, 1 after the first half kick, 2 end of the SPME chains (stream2),
+// 3 end of the pair launch on the main stream, 4 step end.
+static int b_mark(tcp_batch *b, int k, cudaStream_t s) {
+    if (!b->ev[k]) return TCP_OK;
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    TCP_CUDA(cudaStreamIsCapturing(s, &st));
+    if (st == cudaStreamCaptureStatusActive)
+        TCP_CUDA(cudaEventRecordWithFlags(b->ev[k], s, cudaEventRecordExternal));
+    else
+        TCP_CUDA(cudaEventRecord(b->ev[k], s));
+    return TCP_OK;
+}
+
 static int b_recip_join(tcp_batch *b) {
+    if (int rc = b_mark(b, 2, b->stream2)) return rc;
     if (int rc = n3_rejoin_launch(b->rejoin, b->stream2, b->ev_ready, &b->launches)) return rc;
     TCP_CUDA(cudaEventRecord(b->ev_join, b->stream2));
     TCP_CUDA(cudaStreamWaitEvent(b->stream, b->ev_join, 0));
@@ -568,13 +587,17 @@ static int b_recip_join(tcp_batch *b) {
 static int b_step(tcp_batch *b, double dt) {
     const BAcc A = acc_of(b);
     const int nb = (b->ntot + kBThreads - 1) / kBThreads;
+    int rc;
+    if ((rc = b_mark(b, 0, b->stream))) return rc;
     TCP_CUDA(cudaMemsetAsync(A.um, 0, sizeof(double) * 8 * (size_t)b->nrep, b->stream));   // um, mv0, mv1, fsum
     b_vverlet1_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), dt);
-    int rc = b_recip_fork(b, A);
+    if ((rc = b_mark(b, 1, b->stream))) return rc;
+    rc = b_recip_fork(b, A);
     if (!rc)
         rc = launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items, b->n3_chunks, b->n3_nchunks, A.ur,
                                   b->status, b->counter, b->num_sms, true, b->pair_variant, b->pair_reserve,
                                   &b->rejoin, b->ev_ready);
+    if (!rc) rc = b_mark(b, 3, b->stream);
     if (int jrc = b_recip_join(b)) return jrc;
     if (rc) return rc;
     b_finalize_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), A.fsum);
@@ -582,7 +605,7 @@ static int b_step(tcp_batch *b, double dt) {
     b_rescale_kernel<<<nb, kBThreads, 0, b->stream>>>(parts(b), dt, A.mv0, A.mv1);
     b->launches += 15;
     TCP_CUDA(cudaGetLastError());
-    return TCP_OK;
+    return b_mark(b, 4, b->stream);
 }
 
 // Newton-3 item table for variant v (its i-tile), uploaded on the stream
@@ -757,6 +780,9 @@ int tcp_batch_destroy(tcp_batch *b) {
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->ev_join) cudaEventDestroy(b->ev_join);
     if (b->ev_ready) cudaEventDestroy(b->ev_ready);
+    for (cudaEvent_t &e : b->ev)
+        if (e) cudaEventDestroy(e);
+    cudaFree(b->l2_flush);
     n3_rejoin_free(b->rejoin);
     if (b->stream2) {
         cudaStreamSynchronize(b->stream2);
@@ -821,7 +847,10 @@ int tcp_batch_create(const tcp_params *params, const int *nel, const int *nion, 
         cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&b->ev_ready, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&b->ev_ready, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&b->ev[0]) != cudaSuccess || cudaEventCreate(&b->ev[1]) != cudaSuccess ||
+        cudaEventCreate(&b->ev[2]) != cudaSuccess || cudaEventCreate(&b->ev[3]) != cudaSuccess ||
+        cudaEventCreate(&b->ev[4]) != cudaSuccess)
         return fail(cuda_check(cudaGetLastError(), "cudaStreamCreate"));
     TCP_BALLOC(b->x, sizeof(double) * 3 * n);
     TCP_BALLOC(b->v, sizeof(double) * 3 * n);
@@ -1118,27 +1147,36 @@ int tcp_batch_overlap_report(tcp_batch *b, int *reserve, int *candidates, double
     return TCP_OK;
 }
 
-int tcp_batch_time_steps(tcp_batch *b, double dt, int nsteps, double *ms_per_step) {
-    if (!b || !ms_per_step || nsteps <= 0) return set_error(TCP_ERR_BAD_PARAM, "bad arguments");
+int tcp_batch_time_steps(tcp_batch *b, double dt, int nsteps, int flush_l2, double *out) {
+    if (!b || !out || nsteps <= 0) return set_error(TCP_ERR_BAD_PARAM, "bad arguments");
     int rc = tcp_batch_md_steps(b, dt, 1, nullptr);   // builds the graph
     if (rc) return rc;
-    cudaEvent_t e0, e1;
-    TCP_CUDA(cudaEventCreate(&e0));
-    TCP_CUDA(cudaEventCreate(&e1));
-    cudaEventRecord(e0, b->stream);
+    if (flush_l2 && !b->l2_flush) {
+        int l2 = 0;
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, b->device);
+        b->l2_flush_bytes = 2 * (size_t)std::max(l2, 64 << 20);
+        TCP_CUDA(cudaMalloc(&b->l2_flush, b->l2_flush_bytes));
+    }
+    for (int k = 0; k < 6; ++k) out[k] = 0.0;
     for (int s = 0; s < nsteps; ++s) {
+        if (flush_l2) TCP_CUDA(cudaMemsetAsync(b->l2_flush, s & 0xff, b->l2_flush_bytes, b->stream));
         TCP_CUDA(cudaGraphLaunch(b->graph, b->stream));
         b->launches += b->graph_kernels;
+        TCP_CUDA(cudaEventSynchronize(b->ev[4]));
+        // step; first kick (0-1); SPME chains (1-2, stream2); pair launch (1-3,
+        // beside the chains); epilogue (from the later of 2 and 3 to 4)
+        float t[5], e2, e3;
+        cudaEventElapsedTime(&t[0], b->ev[0], b->ev[4]);
+        cudaEventElapsedTime(&t[1], b->ev[0], b->ev[1]);
+        cudaEventElapsedTime(&t[2], b->ev[1], b->ev[2]);
+        cudaEventElapsedTime(&t[3], b->ev[1], b->ev[3]);
+        cudaEventElapsedTime(&e2, b->ev[2], b->ev[4]);
+        cudaEventElapsedTime(&e3, b->ev[3], b->ev[4]);
+        t[4] = std::min(e2, e3);
+        for (int k = 0; k < 5; ++k) out[k] += t[k];
+        out[5] += 1.0;
     }
-    cudaEventRecord(e1, b->stream);
-    cudaEventSynchronize(e1);
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if ((rc = b_sync(b))) return rc;
-    *ms_per_step = (double)ms / nsteps;
-    return TCP_OK;
+    return b_sync(b);
 }
 
 }  // extern "C"

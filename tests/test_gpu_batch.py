@@ -153,3 +153,33 @@ def test_batch_grid_reserve_and_rejoin(monkeypatch):
             assert e[k]["Ur"] == pytest.approx(e0[k]["Ur"], rel=1e-6)
             assert e[k]["Um"] == pytest.approx(e0[k]["Um"], rel=1e-6)
             assert np.max(np.abs(x[k] - x0[k])) < 1e-6 * ss[k].box
+
+
+def test_batch_time_steps_phases():
+    """tcp_batch_time_steps: per-step event marks inside the step graph, with
+    and without the L2 flush; the phases nest inside the step and the state
+    advances by the steps timed."""
+    ss = systems()[:3]
+    params = [T.params_for(s, precision="fp32c", ei="kelbg", recip="spme") for s in ss]
+    with T.Batch(params, [s.nel for s in ss], [s.nion for s in ss]) as b:
+        b.EWALD_SELF()
+        for r, s in enumerate(ss):
+            b.upload(r, x=s.x, v=s.v)
+        b.force()
+        x0 = b.download(0, v=False, f=False)[0]
+        for flush in (True, False):
+            t = b.time_steps(ss[0].dt, 4, flush_l2=flush)
+            assert t["nsteps"] == 4
+            assert all(t[k] > 0 for k in ("step", "vverlet1", "recip", "pair", "epilogue"))
+            assert t["pair"] < t["step"] and t["recip"] < t["step"]
+            assert t["vverlet1"] + max(t["pair"], t["recip"]) + t["epilogue"] <= t["step"] * 1.001
+        x1 = b.download(0, v=False, f=False)[0]
+    with T.Batch(params, [s.nel for s in ss], [s.nion for s in ss]) as b:
+        b.EWALD_SELF()
+        for r, s in enumerate(ss):
+            b.upload(r, x=s.x, v=s.v)
+        b.force()
+        b.md_steps(ss[0].dt, 1 + 4 + 1 + 4)   # time_steps builds its graph with one step first
+        x2 = b.download(0, v=False, f=False)[0]
+    assert np.max(np.abs(x1 - x2)) < 1e-9 * ss[0].box
+    assert np.max(np.abs(x1 - x0)) > 0
