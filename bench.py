@@ -408,6 +408,8 @@ def run_batch_leg(T, args, device):
         bname = b.variant_name(bvar)
         b_names = [b.variant_name(v) for v in range(len(bms))]
         b.md_steps(dt, args.warmup)
+        chain_alone = b.time_component(1, 10)
+        pair_alone = b.time_component(0, 10)
         tb = b.time_steps(dt, args.steps, flush_l2=True)
         ms_batch = tb["step"] / tb["nsteps"]
         phases = {k: round(tb[k] / tb["nsteps"], 4) for k in ("vverlet1", "recip", "pair", "epilogue")}
@@ -445,6 +447,7 @@ def run_batch_leg(T, args, device):
             "speedup_batch_over_loop": ms_loop / ms_batch, "replicas": len(ss),
             "particles": sum(s.n for s in ss), "steps": args.steps, "warmup": args.warmup,
             "l2": "flushed before each timed step", "phases_ms": phases,
+            "alone_ms": {"pair": round(pair_alone, 4), "spme_chains": round(chain_alone, 4)},
             "batch_variant": int(bvar),
             "batch_variant_ms": {b_names[v]: round(float(x), 4) for v, x in enumerate(bms) if x > 0},
             "grid_reserve": bres, "reserve_ms": {k: round(v, 4) for k, v in bres_ms.items()},

@@ -283,6 +283,11 @@ const char *tcp_batch_variant_name(int variant);
  * the join (ms, 0 when not timed), up to nmax entries.  TCP_BATCH_RESERVE=k
  * forces k. */
 int tcp_batch_overlap_report(tcp_batch *b, int *reserve, int *candidates, double *ms, int nmax);
+/* Mean device time of one launch of a batch component over `reps` launches
+ * on the batch's stream (CUDA events), after one untimed launch: which 0 =
+ * the batched real-space pair launch alone, 1 = the SPME chains of every
+ * replica alone (forked onto the second stream and joined back). */
+int tcp_batch_time_component(tcp_batch *b, int which, int reps, double *ms_per_launch);
 /* Device time of nsteps batched steps, one graph replay each, with the L2
  * cache overwritten before each when flush_l2 is set: out[6] = summed ms of
  * the step, the first half kick, the SPME chains (beside the pair launch),

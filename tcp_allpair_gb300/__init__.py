@@ -344,6 +344,14 @@ class Batch:
         keys = ("step", "vverlet1", "recip", "pair", "epilogue", "nsteps")
         return dict(zip(keys, out.tolist()))
 
+    def time_component(self, which, reps):
+        """Mean ms of one launch of the batched pair kernel alone (which=0) or of the
+        SPME chains of every replica alone (which=1), tcp_batch_time_component."""
+        ms = C.c_double()
+        self._chk(self.lib.tcp_batch_time_component(self.h, int(which), int(reps), C.byref(ms)),
+                  "tcp_batch_time_component")
+        return ms.value
+
     def autotune_report(self):
         """(chosen batched pair-kernel variant, per-variant ms measured by the batch autotuner)."""
         v = C.c_int()

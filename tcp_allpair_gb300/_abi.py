@@ -100,6 +100,7 @@ SIGNATURES = {
     "tcp_batch_force": (C.c_int, [C.c_void_p, C.POINTER(TcpEnergies)]),
     "tcp_batch_md_steps": (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.POINTER(TcpEnergies)]),
     "tcp_batch_time_steps": (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.c_int, _P]),
+    "tcp_batch_time_component": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P]),
     "tcp_batch_autotune_report": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), _P, C.c_int]),
     "tcp_batch_overlap_report": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), _P, C.c_int]),
 }

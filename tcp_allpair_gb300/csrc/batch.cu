@@ -446,6 +446,10 @@ struct tcp_batch {
         cufftHandle fwd, inv;
     };
     std::vector<Group> groups;
+    // the transforms of mesh-size group k >= 1 run on gstream[k - 1] beside group 0's on stream2
+    std::vector<cudaStream_t> gstream;
+    cudaEvent_t ev_fft[2] = {};                 // forks: after the spread, after the influence multiply
+    std::vector<cudaEvent_t> ev_gdone[2];       // joins of groups 1.. (each direction)
     bool ready = false;
     cudaGraphExec_t graph = nullptr;
     double graph_dt = 0;
@@ -537,6 +541,36 @@ static void b_spme(tcp_batch *b, bool gather, cudaStream_t st) {
     }
 }
 
+// The batched R2C (dir 0) or C2R (dir 1) of every mesh-size group.  The groups
+// are independent and each transform leaves most of the GPU idle, so group 0
+// runs on stream2 and group k >= 1 on gstream[k - 1], forked from stream2 and
+// joined back into it.
+static int b_fft_groups(tcp_batch *b, int dir) {
+    const size_t ng = b->groups.size();
+    if (ng > 1) {
+        TCP_CUDA(cudaEventRecord(b->ev_fft[dir], b->stream2));
+        for (size_t k = 1; k < ng; ++k) TCP_CUDA(cudaStreamWaitEvent(b->gstream[k - 1], b->ev_fft[dir], 0));
+    }
+    for (size_t k = 0; k < ng; ++k) {
+        const auto &g = b->groups[k];
+        const cudaStream_t st = k ? b->gstream[k - 1] : b->stream2;
+        if (dir == 0) {
+            cufftSetStream(g.fwd, st);
+            if (cufftExecR2C(g.fwd, b->Qf + g.mesh_off, b->Qk + g.half_off) != CUFFT_SUCCESS)
+                return set_error(TCP_ERR_CUFFT, "batched cufftExecR2C failed");
+        } else {
+            cufftSetStream(g.inv, st);
+            if (cufftExecC2R(g.inv, b->Qk + g.half_off, b->Qf + g.mesh_off) != CUFFT_SUCCESS)
+                return set_error(TCP_ERR_CUFFT, "batched cufftExecC2R failed");
+        }
+    }
+    for (size_t k = 1; k < ng; ++k) {
+        TCP_CUDA(cudaEventRecord(b->ev_gdone[dir][k - 1], b->gstream[k - 1]));
+        TCP_CUDA(cudaStreamWaitEvent(b->stream2, b->ev_gdone[dir][k - 1], 0));
+    }
+    return TCP_OK;
+}
+
 // The SPME chain of every replica (spread, batched R2C per mesh size,
 // influence multiply + energy, C2R, gather into frec), forked onto stream2
 // after the work queued on the main stream, so that it runs beside the
@@ -545,17 +579,9 @@ static int b_recip_fork(tcp_batch *b, const BAcc &A) {
     TCP_CUDA(cudaEventRecord(b->ev_fork, b->stream));
     TCP_CUDA(cudaStreamWaitEvent(b->stream2, b->ev_fork, 0));
     b_spme(b, false, b->stream2);                       // atomic-free, every mesh point written
-    for (auto &g : b->groups) {
-        cufftSetStream(g.fwd, b->stream2);
-        if (cufftExecR2C(g.fwd, b->Qf + g.mesh_off, b->Qk + g.half_off) != CUFFT_SUCCESS)
-            return set_error(TCP_ERR_CUFFT, "batched cufftExecR2C failed");
-    }
+    if (int rc = b_fft_groups(b, 0)) return rc;
     b_influence_kernel<<<b->infl_blocks, 256, 0, b->stream2>>>(b->Qk, b->infl, b->reps, b->blk0, b->nrep, A.um);
-    for (auto &g : b->groups) {
-        cufftSetStream(g.inv, b->stream2);
-        if (cufftExecC2R(g.inv, b->Qk + g.half_off, b->Qf + g.mesh_off) != CUFFT_SUCCESS)
-            return set_error(TCP_ERR_CUFFT, "batched cufftExecC2R failed");
-    }
+    if (int rc = b_fft_groups(b, 1)) return rc;
     b_spme(b, true, b->stream2);
     return TCP_OK;
 }
@@ -784,6 +810,14 @@ int tcp_batch_destroy(tcp_batch *b) {
         if (e) cudaEventDestroy(e);
     cudaFree(b->l2_flush);
     n3_rejoin_free(b->rejoin);
+    for (cudaStream_t st : b->gstream) {
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+    }
+    for (int d = 0; d < 2; ++d) {
+        if (b->ev_fft[d]) cudaEventDestroy(b->ev_fft[d]);
+        for (cudaEvent_t e : b->ev_gdone[d]) cudaEventDestroy(e);
+    }
     if (b->stream2) {
         cudaStreamSynchronize(b->stream2);
         cudaStreamDestroy(b->stream2);
@@ -906,6 +940,21 @@ int tcp_batch_create(const tcp_params *params, const int *nel, const int *nion, 
         cufftSetStream(g.inv, b->stream);
         b->groups.push_back(g);
     }
+    for (size_t k = 1; k < b->groups.size(); ++k) {
+        cudaStream_t st = nullptr;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+            return fail(cuda_check(cudaGetLastError(), "cudaStreamCreate"));
+        b->gstream.push_back(st);
+        for (int d = 0; d < 2; ++d) {
+            cudaEvent_t e = nullptr;
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                return fail(cuda_check(cudaGetLastError(), "cudaEventCreate"));
+            b->ev_gdone[d].push_back(e);
+        }
+    }
+    for (int d = 0; d < 2 && b->groups.size() > 1; ++d)
+        if (cudaEventCreateWithFlags(&b->ev_fft[d], cudaEventDisableTiming) != cudaSuccess)
+            return fail(cuda_check(cudaGetLastError(), "cudaEventCreate"));
     TCP_BALLOC(b->Qf, sizeof(float) * (size_t)b->mesh_total);
     // spreading bins (K2 K3 per replica) and 8-row groups (ceil(K2/8) K3 per replica)
     for (int r = 0; r < nrep; ++r) {
@@ -1144,6 +1193,40 @@ int tcp_batch_overlap_report(tcp_batch *b, int *reserve, int *candidates, double
         if (candidates) candidates[k] = kBReserveCandidates[k];
         if (ms) ms[k] = b->reserve_ms[k];
     }
+    return TCP_OK;
+}
+
+int tcp_batch_time_component(tcp_batch *b, int which, int reps, double *ms_per_launch) {
+    if (!b || !b->ready) return set_error(TCP_ERR_STATE, "tcp_batch_ewald_self must be called first");
+    if (reps <= 0 || !ms_per_launch || which < 0 || which > 1) return set_error(TCP_ERR_BAD_PARAM, "bad arguments");
+    cudaSetDevice(b->device);
+    int rc;
+    if ((rc = b_autotune(b))) return rc;
+    const BAcc A = acc_of(b);
+    cudaEvent_t e0, e1;
+    TCP_CUDA(cudaEventCreate(&e0));
+    TCP_CUDA(cudaEventCreate(&e1));
+    auto one = [&]() -> int {
+        if (which == 0)   // clears its accumulators itself
+            return launch_pair_n3_batch(b->stream, b->xq, b->ntot, b->facc, b->n3reps, b->nrep, b->n3_items,
+                                        b->n3_chunks, b->n3_nchunks, A.ur, b->status, b->counter, b->num_sms, true,
+                                        b->pair_variant);
+        TCP_CUDA(cudaMemsetAsync(A.um, 0, sizeof(double) * (size_t)b->nrep, b->stream));
+        if (int r = b_recip_fork(b, A)) return r;
+        return b_recip_join(b);
+    };
+    rc = one();   // warm-up
+    cudaEventRecord(e0, b->stream);
+    for (int r = 0; r < reps && !rc; ++r) rc = one();
+    cudaEventRecord(e1, b->stream);
+    cudaEventSynchronize(e1);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if ((rc = b_sync(b))) return rc;
+    *ms_per_launch = (double)t / reps;
     return TCP_OK;
 }
 
