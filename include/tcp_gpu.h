@@ -280,8 +280,8 @@ const char *tcp_batch_variant_name(int variant);
  * that the replicas' SPME chains, which run beside it, find room on the SMs
  * (they join the pair launch's work once the chains are done); the candidates
  * and the time of the pair launch with the chains beside it for each, up to
- * the join (ms, 0 when not timed), up to nmax entries.  TCP_BATCH_RESERVE=k
- * forces k. */
+ * the join, replayed as one captured graph (ms, 0 when not timed), up to nmax
+ * entries.  TCP_BATCH_RESERVE=k forces k. */
 int tcp_batch_overlap_report(tcp_batch *b, int *reserve, int *candidates, double *ms, int nmax);
 /* Mean device time of one launch of a batch component over `reps` launches
  * on the batch's stream (CUDA events), after one untimed launch: which 0 =
@@ -352,8 +352,8 @@ const char *tcp_pair_variant_name(int variant);
  * so that the reciprocal chain, which runs beside the pair kernel in a step,
  * finds room on the SMs (they join the pair kernel's work once the chain is
  * done); the candidates and the time of the pair kernel with the chain
- * beside it for each, up to the join of both (ms, 0 when not timed), up to
- * nmax entries.  TCP_PAIR_RESERVE=k forces k. */
+ * beside it for each, up to the join of both, replayed as one captured graph
+ * (ms, 0 when not timed), up to nmax entries.  TCP_PAIR_RESERVE=k forces k. */
 int tcp_overlap_report(tcp_ctx *ctx, int *reserve, int *candidates, double *ms, int nmax);
 /* Kernel launches issued by the context so far (all kernels of this library). */
 int tcp_launch_count(tcp_ctx *ctx, long long *count);

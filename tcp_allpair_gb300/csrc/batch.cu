@@ -656,7 +656,7 @@ static int b_fill_n3(tcp_batch *b, int v) {
 // CTAs of the persistent pair grid left to the SPME chains, which run beside
 // it on stream2 and find no registers free otherwise; they rejoin the pair
 // launch once the chains are done.  Each candidate is timed as the chains and
-// the pair launch beside them, up to the join, over four launches; the
+// the pair launch beside them, up to the join, over four graph replays; the
 // smallest reserve within 0.3 % of the fastest is kept (TCP_BATCH_RESERVE
 // forces one).
 static constexpr int kBReserveCandidates[] = {0, 16, 32, 64, 128, 256, 512};
@@ -682,13 +682,33 @@ static int b_choose_reserve(tcp_batch *b) {
         if (int j = b_recip_join(b)) return j;
         return r;
     };
+    // each candidate captured as one graph and replayed, as it runs inside the
+    // step graph (launched one by one, the chains would run ahead on an idle
+    // GPU while the host is still issuing the pair launch)
+    auto graph_of = [&](cudaGraphExec_t *ge) -> int {
+        cudaGraph_t g = nullptr;
+        TCP_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        int r = once();
+        const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+        if (!r && ce != cudaSuccess) r = cuda_check(ce, "cudaStreamEndCapture");
+        if (!r) {
+            const cudaError_t ie = cudaGraphInstantiate(ge, g, 0);
+            if (ie != cudaSuccess) r = cuda_check(ie, "cudaGraphInstantiate");
+        }
+        if (g) cudaGraphDestroy(g);
+        return r;
+    };
     for (const int r : kBReserveCandidates) {
         b->pair_reserve = r;
-        rc = once();
+        cudaGraphExec_t ge = nullptr;
+        if ((rc = graph_of(&ge))) break;
+        cudaError_t le = cudaGraphLaunch(ge, b->stream);
         cudaEventRecord(e0, b->stream);
-        for (int t = 0; t < 4 && !rc; ++t) rc = once();
+        for (int t = 0; t < 4 && le == cudaSuccess; ++t) le = cudaGraphLaunch(ge, b->stream);
         cudaEventRecord(e1, b->stream);
         cudaEventSynchronize(e1);
+        cudaGraphExecDestroy(ge);
+        if (le != cudaSuccess) rc = cuda_check(le, "cudaGraphLaunch");
         if (rc) break;
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);

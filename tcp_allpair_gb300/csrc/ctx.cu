@@ -134,27 +134,40 @@ static int recip_join(tcp_ctx *c) {
 // Mean time of the real-space launch with the reciprocal chain beside it on
 // stream2, as inside a step (the autotuner's measure for the grid reserve).
 int time_pair_with_recip(tcp_ctx *c, int reps, double *ms) {
+    // The fork, the pair launch and the join are captured as one graph and
+    // replayed, as they run inside the step graph: both branches become ready
+    // together.  Launched one by one, the chain's kernels would run ahead on
+    // an idle GPU while the host is still issuing the rest.
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    TCP_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = recip_fork(c);
+    if (!rc) rc = launch_pair(c, energy_on(c), false);
+    const int jrc = recip_join(c);
+    const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    if (!rc) rc = jrc;
+    if (!rc && ce != cudaSuccess) rc = cuda_check(ce, "cudaStreamEndCapture");
+    if (!rc) {
+        const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+        if (ie != cudaSuccess) rc = cuda_check(ie, "cudaGraphInstantiate");
+    }
+    if (g) cudaGraphDestroy(g);
+    if (rc) return rc;
     cudaEvent_t e0, e1;
     TCP_CUDA(cudaEventCreate(&e0));
     TCP_CUDA(cudaEventCreate(&e1));
-    int rc = TCP_OK;
-    auto once = [&]() -> int {
-        int r = recip_fork(c);
-        if (!r) r = launch_pair(c, energy_on(c), false);
-        if (int j = recip_join(c)) return j;
-        return r;
-    };
-    rc = once();
+    cudaError_t le = cudaGraphLaunch(ge, c->stream);   // warm-up
     cudaEventRecord(e0, c->stream);
-    for (int r = 0; r < reps && !rc; ++r) rc = once();
+    for (int r = 0; r < reps && le == cudaSuccess; ++r) le = cudaGraphLaunch(ge, c->stream);
     cudaEventRecord(e1, c->stream);
     cudaEventSynchronize(e1);
     float t = 0.f;
     cudaEventElapsedTime(&t, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    cudaGraphExecDestroy(ge);
+    if (le != cudaSuccess) return cuda_check(le, "cudaGraphLaunch");
     *ms = t / std::max(reps, 1);
-    if (rc) return rc;
     TCP_CUDA(cudaGetLastError());
     return TCP_OK;
 }

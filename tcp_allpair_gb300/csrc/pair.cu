@@ -1031,7 +1031,8 @@ static int choose_variant(tcp_ctx *c, const char *cache, const std::string &key)
 // large reserve costs the pair kernel only while the chain runs: where the
 // chain is long against the pair kernel (small N, or the FP64 chain) it lets
 // the chain finish first.  Each candidate is timed as the pair kernel with the
-// chain beside it, up to the join of both (TCP_PAIR_RESERVE forces one).
+// chain beside it, up to the join of both, captured as one graph and replayed
+// (time_pair_with_recip; TCP_PAIR_RESERVE forces one).
 static constexpr int kReserveCandidates[] = {0, 16, 32, 64, 128, 256, 512};
 static int choose_reserve(tcp_ctx *c, const char *cache, const std::string &key) {
     c->pair_reserve = 0;
