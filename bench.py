@@ -696,7 +696,8 @@ def run_gpu(args, world, rank, local, dist):
 def run_pair_only(args):
     """Launch the real-space pair kernel alone on an N-particle version of the
     headline system (profiling target: `ncu --clock-control none -k regex:pair_
-    -c 1 ... python bench.py --pair-only N`)."""
+    -c 1 ... python bench.py --pair-only N`); with --rdf, the form that also
+    bins the RDF histograms."""
     import tcp_allpair_gb300 as T
     n = args.pair_only
     s = T.make_system(n, gamma=1.0, lam=0.5, seed=0, ewald_rel_err=1e-6, K=64, order=5)
@@ -704,10 +705,12 @@ def run_pair_only(args):
     with T.Context(p, s.nel, s.nion) as c:
         c.EWALD_SELF()
         c.upload(x=s.x, v=s.v)
+        if args.rdf:
+            c.set_flags(T.FLAG_ENERGY | T.FLAG_RDF)
         for _ in range(3):
             c.Force_direct_self()
         ms = c.time_component(0, 5)
-    print(json.dumps({"pair_only": n, "precision": args.precision, "pair_kernel_ms": ms}))
+    print(json.dumps({"pair_only": n, "precision": args.precision, "rdf": bool(args.rdf), "pair_kernel_ms": ms}))
     return 0
 
 
@@ -748,6 +751,7 @@ def main():
     ap.add_argument("--nve-fp64-steps", type=int, default=500, help="FP64 NVE energy-drift run (0: skip)")
     ap.add_argument("--c2-steps", type=int, default=1000, help="N = 16,384 isokinetic run (0: skip)")
     ap.add_argument("--pair-only", type=int, default=0, help="profile target: pair kernel alone at this N")
+    ap.add_argument("--rdf", action="store_true", help="with --pair-only: the form that bins the RDF histograms")
     ap.add_argument("--recip-only", type=int, default=0, help="profile target: SPME chain alone at this N")
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--config", default="n65536_spme128", help="named workload of --recip-only")

@@ -328,7 +328,8 @@ int tcp_reverse_md(tcp_ctx *ctx, double dt, int nsteps, int every, double *J, do
 /* ---- measurement hooks ---------------------------------------------------- */
 /* Runs `reps` launches of one component on the context's stream and returns
  * the mean device time per launch from CUDA events recorded on that stream.
- * which: 0 = real-space pair kernel, 1 = SPME chain, 2 = full md step. */
+ * which: 0 = real-space pair kernel (the RDF-binning form when the context's
+ * flags hold TCP_FLAG_RDF), 1 = SPME chain, 2 = full md step. */
 int tcp_time_component(tcp_ctx *ctx, int which, int reps, double dt, double *ms_per_launch);
 /* Times nsteps MD steps one by one with CUDA events recorded on the
  * context's stream (also inside the captured step graph), optionally writing

@@ -884,7 +884,7 @@ int tcp_time_component(tcp_ctx *c, int which, int reps, double dt, double *ms) {
     int rc = TCP_OK;
     if ((rc = autotune_pair(c))) return rc;
     auto one = [&]() -> int {
-        if (which == 0) return launch_pair(c, energy_on(c), false);
+        if (which == 0) return launch_pair(c, energy_on(c), (c->flags & TCP_FLAG_RDF) != 0);
         return recip_launch(c);
     };
     if (which == 2 && (rc = ensure_graph(c, dt))) return rc;
